@@ -1,0 +1,1097 @@
+// Batched bordered-banded factor and solves on the GPU (FP64 real and complex).
+//
+// A tau system is banded except for its r boundary ("border") rows. With the border rows moved to
+// the top (row permutation P), P A = B + U V^T where B equals P A with each border row i replaced by
+// s_i e_i (s_i = max |row i|, 1 for a zero row), U = [e_0 .. e_{r-1}] and V^T = border rows - diag(s).
+// B is factored by LU with partial pivoting inside the band (the LAPACK gbtf2 algorithm and pivot
+// rule), then W = B^{-1} U and the capacitance S = I + V^T W (LU, 1-norm condition). A solve is
+// y = B^{-1} P b, z = S^{-1} V^T y, x = y - W z (Woodbury). This is the algorithm of the reference's
+// core/include/conatus/banded.hpp:1-27,170-478 and of its GPU batch (core/src/cuda/banded.cu); the
+// kernels below are this library's own design.
+//
+// GPU layout (one handle = one batch of systems of equal n, common band kl/ku):
+//   ab   [batch][n][ldab]   LAPACK band storage per system, column j at ab + j*ldab, A(i,j) at row
+//                           kv + i - j (kv = kl + ku); LU factors after the factorization
+//   ipiv [batch][n]         0-based pivot rows
+//   vt   [batch][r][n]      V^T rows;  w [batch][r][n]  columns of W stored as rows
+//   slu  [batch][r][r]      LU of S (column-major), spiv [batch][r]
+// One warp owns one system in every kernel: the band recurrences are sequential along n and each
+// column's band entries are spread over the lanes; the working vector lives in shared memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "conatus_gb300.h"
+
+namespace cng {
+
+static constexpr int kWarpsPerBlock = 4;
+static constexpr size_t kMaxSolveSmem = 200 * 1024;   // bytes of shared memory for the y vectors
+
+template <class T>
+struct BandView {
+    int batch, n, r, kl, ku, ldab, pivot;
+    T* ab;
+    int* ipiv;
+    T* vt;
+    T* w;
+    T* slu;
+    int* spiv;
+    const int* perm;      // n entries, shared by the batch (border rows first)
+    int* info;            // per system: 0 ok, j+1 singular band pivot j, -1 singular capacitance,
+                          // -2 non-finite capacitance condition
+    double* cond;         // per system: 1-norm condition of S (1 when r = 0)
+    // transposed Woodbury data (built on demand)
+    T* wt;                // [batch][r][n]
+    T* stlu;              // [batch][r][r]
+    int* stpiv;           // [batch][r]
+};
+
+// ------------------------------------------------------------------------------------------------
+// device building blocks (one warp, lane = threadIdx.x & 31)
+
+template <class T>
+__device__ inline T band_at(const T* ab, int ldab, int kv, int i, int j) {
+    return ab[(size_t)j * ldab + (kv + i - j)];
+}
+
+// In-place LU of the band (LAPACK gbtf2 order). Returns 0 or j+1 of the first zero pivot.
+template <class T>
+__device__ int warp_gbtf2(T* ab, int* ipiv, int n, int kl, int ku, int ldab, int pivot) {
+    const int lane = threadIdx.x & 31;
+    const int kv = kl + ku;
+    int ju = 0, info = 0;
+    for (int j = 0; j < n; ++j) {
+        const int km = min(kl, n - 1 - j);
+        T* colj = ab + (size_t)j * ldab;
+        // pivot: largest |.|_1 among rows j..j+km, first index on ties (i?amax)
+        int jp = 0;
+        if (pivot) {
+            double best = -1.0;
+            int bi = 0;
+            for (int t = lane; t <= km; t += 32) {
+                double a = abs1(colj[kv + t]);
+                if (a > best) { best = a; bi = t; }
+            }
+            for (int m = 16; m > 0; m >>= 1) {
+                double ob = __shfl_xor_sync(0xffffffffu, best, m);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, m);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            jp = bi;
+        }
+        if (lane == 0) ipiv[j] = j + jp;
+        const T piv = colj[kv + jp];
+        if (!is_zero(piv)) {
+            ju = max(ju, min(j + ku + jp, n - 1));
+            if (jp != 0) {
+                for (int c = j + lane; c <= ju; c += 32) {
+                    T* cc = ab + (size_t)c * ldab;
+                    T a = cc[kv + j + jp - c], b = cc[kv + j - c];
+                    cc[kv + j + jp - c] = b;
+                    cc[kv + j - c] = a;
+                }
+                __syncwarp();
+            }
+            if (km > 0) {
+                const T rp = one<T>() / colj[kv];
+                for (int t = 1 + lane; t <= km; t += 32) colj[kv + t] = rp * colj[kv + t];
+                __syncwarp();
+                const int w = ju - j;
+                const int cnt = w * km;
+                for (int idx = lane; idx < cnt; idx += 32) {
+                    const int c = j + 1 + idx / km;
+                    const int t = 1 + idx % km;
+                    T* cc = ab + (size_t)c * ldab;
+                    const T u = cc[kv + j - c];
+                    cc[kv + j + t - c] = cc[kv + j + t - c] - colj[kv + t] * u;
+                }
+                __syncwarp();
+            }
+        } else if (info == 0) {
+            info = j + 1;
+        }
+    }
+    return info;
+}
+
+// y := B^{-1} y with the band LU (gbtrs 'N'); y in shared or global memory, one warp.
+template <class T>
+__device__ void warp_band_solve(const T* ab, const int* ipiv, T* y, int n, int kl, int ku, int ldab) {
+    const int lane = threadIdx.x & 31;
+    const int kv = kl + ku;
+    if (kl > 0) {
+        for (int j = 0; j < n - 1; ++j) {
+            const int lm = min(kl, n - 1 - j);
+            const int l = ipiv[j];
+            const T bj = y[l];
+            const T yj0 = y[j];
+            __syncwarp();
+            const T* colj = ab + (size_t)j * ldab + kv + 1;
+            for (int t = lane; t < lm; t += 32) {
+                const int i = j + 1 + t;
+                const T v = (i == l) ? yj0 : y[i];
+                y[i] = v - colj[t] * bj;
+            }
+            if (lane == 0) y[j] = bj;
+            __syncwarp();
+        }
+    }
+    for (int j = n - 1; j >= 0; --j) {
+        T yj = y[j];
+        if (is_zero(yj)) {
+            __syncwarp();
+            continue;
+        }
+        const T* colj = ab + (size_t)j * ldab;
+        yj = yj / colj[kv];
+        const int m = min(kv, j);
+        for (int t = lane; t < m; t += 32) {
+            const int i = j - 1 - t;
+            y[i] = y[i] - yj * colj[kv - 1 - t];
+        }
+        if (lane == 0) y[j] = yj;
+        __syncwarp();
+    }
+}
+
+// y := B^{-T} y (gbtrs 'T', plain transpose): U^T then L^T with the interchanges.
+template <class T>
+__device__ void warp_band_solve_T(const T* ab, const int* ipiv, T* y, int n, int kl, int ku, int ldab) {
+    const int lane = threadIdx.x & 31;
+    const int kv = kl + ku;
+    for (int j = 0; j < n; ++j) {
+        const T* colj = ab + (size_t)j * ldab;
+        const int i0 = max(0, j - kv);
+        T acc = T(0.0);
+        for (int i = i0 + lane; i < j; i += 32) acc = acc + colj[kv + i - j] * y[i];
+        acc = warp_sum(acc);
+        const T yj = (y[j] - acc) / colj[kv];
+        __syncwarp();
+        if (lane == 0) y[j] = yj;
+        __syncwarp();
+    }
+    if (kl > 0) {
+        for (int j = n - 2; j >= 0; --j) {
+            const int lm = min(kl, n - 1 - j);
+            const T* colj = ab + (size_t)j * ldab + kv + 1;
+            T acc = T(0.0);
+            for (int t = lane; t < lm; t += 32) acc = acc + colj[t] * y[j + 1 + t];
+            acc = warp_sum(acc);
+            const T yj = y[j] - acc;
+            const int l = ipiv[j];
+            const T yl = y[l];
+            __syncwarp();
+            if (lane == 0) {
+                if (l != j) {
+                    y[j] = yl;
+                    y[l] = yj;
+                } else {
+                    y[j] = yj;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// LU with partial pivoting of a small r x r column-major matrix by lane 0 (getrf semantics).
+// Returns 0 or k+1 of the first zero pivot.
+template <class T>
+__device__ int small_getrf(T* a, int* piv, int r) {
+    int info = 0;
+    for (int k = 0; k < r; ++k) {
+        int p = k;
+        double best = abs1(a[k * r + k]);
+        for (int i = k + 1; i < r; ++i) {
+            double v = abs1(a[k * r + i]);
+            if (v > best) { best = v; p = i; }
+        }
+        piv[k] = p;
+        if (is_zero(a[k * r + p])) {
+            if (info == 0) info = k + 1;
+            continue;
+        }
+        if (p != k)
+            for (int c = 0; c < r; ++c) {
+                T t = a[c * r + k];
+                a[c * r + k] = a[c * r + p];
+                a[c * r + p] = t;
+            }
+        const T rp = one<T>() / a[k * r + k];
+        for (int i = k + 1; i < r; ++i) a[k * r + i] = rp * a[k * r + i];
+        for (int c = k + 1; c < r; ++c) {
+            const T u = a[c * r + k];
+            for (int i = k + 1; i < r; ++i) a[c * r + i] = a[c * r + i] - a[k * r + i] * u;
+        }
+    }
+    return info;
+}
+
+// z := S^{-1} z with the small LU (getrs 'N'), lane 0.
+template <class T>
+__device__ void small_getrs(const T* a, const int* piv, T* z, int r) {
+    for (int k = 0; k < r; ++k) {
+        const int p = piv[k];
+        if (p != k) {
+            T t = z[k];
+            z[k] = z[p];
+            z[p] = t;
+        }
+    }
+    for (int k = 0; k < r; ++k)
+        for (int i = k + 1; i < r; ++i) z[i] = z[i] - a[k * r + i] * z[k];
+    for (int k = r - 1; k >= 0; --k) {
+        z[k] = z[k] / a[k * r + k];
+        for (int i = 0; i < k; ++i) z[i] = z[i] - a[k * r + i] * z[k];
+    }
+}
+
+// 1-norm of an r x r column-major matrix (NaN propagates as in the reference's norm1).
+template <class T>
+__device__ double small_norm1(const T* a, int r) {
+    double m = 0.0;
+    for (int c = 0; c < r; ++c) {
+        double s = 0.0;
+        for (int i = 0; i < r; ++i) s += absval(a[c * r + i]);
+        if (!(s <= m)) m = s;
+    }
+    return m;
+}
+
+// ------------------------------------------------------------------------------------------------
+// kernels
+
+// Factor: band LU, W = B^{-1} U, S = I + V^T W, LU of S and its 1-norm condition. Scratch for the
+// r x r work lives in the slu/w buffers of the system itself.
+template <class T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_factor(BandView<T> v) {
+    const int sys = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r, ldab = v.ldab;
+    T* ab = v.ab + (size_t)sys * n * ldab;
+    int* ipiv = v.ipiv + (size_t)sys * n;
+    int info = warp_gbtf2(ab, ipiv, n, v.kl, v.ku, ldab, v.pivot);
+    double cond = 1.0;
+    if (info == 0 && r > 0) {
+        T* w = v.w + (size_t)sys * r * n;
+        const T* vt = v.vt + (size_t)sys * r * n;
+        for (int k = 0; k < r; ++k) {
+            T* wk = w + (size_t)k * n;
+            for (int i = lane; i < n; i += 32) wk[i] = (i == k) ? one<T>() : T(0.0);
+            __syncwarp();
+            warp_band_solve(ab, ipiv, wk, n, v.kl, v.ku, ldab);
+            __syncwarp();
+        }
+        T* S = v.slu + (size_t)sys * r * r;
+        for (int a = 0; a < r; ++a)
+            for (int b = 0; b < r; ++b) {
+                const T* va = vt + (size_t)a * n;
+                const T* wb = w + (size_t)b * n;
+                T acc = T(0.0);
+                for (int i = lane; i < n; i += 32) acc = acc + va[i] * wb[i];
+                acc = warp_sum(acc);
+                if (lane == 0) S[b * r + a] = ((a == b) ? one<T>() : T(0.0)) + acc;
+            }
+        __syncwarp();
+        if (lane == 0) {
+            const double nS = small_norm1(S, r);
+            int* sp = v.spiv + (size_t)sys * r;
+            int sinfo = small_getrf(S, sp, r);
+            if (sinfo != 0) {
+                info = -1;
+            } else {
+                // ||S^{-1}||_1 column by column (r solves with unit vectors); r <= 64
+                double ninv = 0.0;
+                T z[64];
+                for (int c = 0; c < r; ++c) {
+                    for (int i = 0; i < r; ++i) z[i] = (i == c) ? one<T>() : T(0.0);
+                    small_getrs(S, sp, z, r);
+                    double s = 0.0;
+                    for (int i = 0; i < r; ++i) s += absval(z[i]);
+                    if (!(s <= ninv)) ninv = s;
+                }
+                cond = nS * ninv;
+                if (isnan(cond)) info = -2;
+            }
+        }
+        info = __shfl_sync(0xffffffffu, info, 0);
+    }
+    if (lane == 0) {
+        v.info[sys] = info;
+        v.cond[sys] = cond;
+    }
+}
+
+// Transposed Woodbury data: Wt = B^{-T} V (rows of V^T solved), St = I + U^T Wt, LU of St.
+template <class T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_prepare_T(BandView<T> v) {
+    const int sys = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r;
+    const T* ab = v.ab + (size_t)sys * n * v.ldab;
+    const int* ipiv = v.ipiv + (size_t)sys * n;
+    T* wt = v.wt + (size_t)sys * r * n;
+    const T* vt = v.vt + (size_t)sys * r * n;
+    for (int k = 0; k < r; ++k) {
+        T* wk = wt + (size_t)k * n;
+        for (int i = lane; i < n; i += 32) wk[i] = vt[(size_t)k * n + i];
+        __syncwarp();
+        warp_band_solve_T(ab, ipiv, wk, n, v.kl, v.ku, v.ldab);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        T* St = v.stlu + (size_t)sys * r * r;
+        for (int a = 0; a < r; ++a)
+            for (int b = 0; b < r; ++b)
+                St[b * r + a] = ((a == b) ? one<T>() : T(0.0)) + wt[(size_t)b * n + a];
+        small_getrf(St, v.stpiv + (size_t)sys * r, r);
+    }
+}
+
+// Woodbury correction y -= W S^{-1} V^T y (one warp; zbuf: r entries of shared memory).
+template <class T>
+__device__ void warp_woodbury(const T* vt, const T* w, const T* slu, const int* spiv, T* y, T* zbuf,
+                              int n, int r) {
+    const int lane = threadIdx.x & 31;
+    for (int a = 0; a < r; ++a) {
+        const T* va = vt + (size_t)a * n;
+        T acc = T(0.0);
+        for (int i = lane; i < n; i += 32) acc = acc + va[i] * y[i];
+        acc = warp_sum(acc);
+        if (lane == 0) zbuf[a] = acc;
+    }
+    __syncwarp();
+    if (lane == 0) small_getrs(slu, spiv, zbuf, r);
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+        T acc = y[i];
+        for (int k = 0; k < r; ++k) acc = acc - w[(size_t)k * n + i] * zbuf[k];
+        y[i] = acc;
+    }
+    __syncwarp();
+}
+
+// Input/output adapters of the solve kernel: plain in-place, mapped (int64 gather/scatter maps)
+// and split (complex system with real data: b = re[rows_c] + i re[rows_s]).
+enum IoKind { IO_PLAIN = 0, IO_MAPPED = 1, IO_SPLIT = 2 };
+
+struct SolveIo {
+    const void* rhs;
+    void* x;
+    const long long* rows;
+    const long long* cols;
+    const long long* rows_s;
+    const long long* cols_s;
+};
+
+template <class T, int IO>
+__device__ inline T io_load(const SolveIo& io, int sys, int n, int i) {
+    const size_t k = (size_t)sys * n + i;
+    if constexpr (IO == IO_PLAIN) {
+        return static_cast<const T*>(io.rhs)[k];
+    } else if constexpr (IO == IO_MAPPED) {
+        const T* rhs = static_cast<const T*>(io.rhs);
+        return rhs[io.rows ? io.rows[k] : (long long)k];
+    } else {
+        const double* re = static_cast<const double*>(io.rhs);
+        return T(zd(re[io.rows[k]], re[io.rows_s[k]]));
+    }
+}
+
+template <class T, int IO>
+__device__ inline void io_store(const SolveIo& io, int sys, int n, int i, T v) {
+    const size_t k = (size_t)sys * n + i;
+    if constexpr (IO == IO_PLAIN) {
+        static_cast<T*>(io.x)[k] = v;
+    } else if constexpr (IO == IO_MAPPED) {
+        static_cast<T*>(io.x)[io.cols ? io.cols[k] : (long long)k] = v;
+    } else {
+        double* x = static_cast<double*>(io.x);
+        const zd z = *reinterpret_cast<const zd*>(&v);
+        x[io.cols[k]] = z.re;
+        x[io.cols_s[k]] = z.im;
+    }
+}
+
+template <class T, int IO>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_solve(BandView<T> v, SolveIo io) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wib = threadIdx.x >> 5;
+    const int sys = blockIdx.x * kWarpsPerBlock + wib;
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r;
+    T* y = reinterpret_cast<T*>(smem_raw) + (size_t)wib * (n + 64);
+    T* zbuf = y + n;
+    for (int i = lane; i < n; i += 32) y[i] = io_load<T, IO>(io, sys, n, v.perm[i]);
+    __syncwarp();
+    warp_band_solve(v.ab + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, n, v.kl, v.ku, v.ldab);
+    if (r > 0)
+        warp_woodbury(v.vt + (size_t)sys * r * n, v.w + (size_t)sys * r * n, v.slu + (size_t)sys * r * r,
+                      v.spiv + (size_t)sys * r, y, zbuf, n, r);
+    for (int i = lane; i < n; i += 32) io_store<T, IO>(io, sys, n, i, y[i]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_solve_T(BandView<T> v, T* b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wib = threadIdx.x >> 5;
+    const int sys = blockIdx.x * kWarpsPerBlock + wib;
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r;
+    T* y = reinterpret_cast<T*>(smem_raw) + (size_t)wib * (n + 64);
+    T* zbuf = y + n;
+    T* bs = b + (size_t)sys * n;
+    for (int i = lane; i < n; i += 32) y[i] = bs[i];
+    __syncwarp();
+    warp_band_solve_T(v.ab + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, n, v.kl, v.ku, v.ldab);
+    if (r > 0) {
+        const T* wt = v.wt + (size_t)sys * r * n;
+        if (lane == 0) {
+            for (int k = 0; k < r; ++k) zbuf[k] = y[k];
+            small_getrs(v.stlu + (size_t)sys * r * r, v.stpiv + (size_t)sys * r, zbuf, r);
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            T acc = y[i];
+            for (int k = 0; k < r; ++k) acc = acc - wt[(size_t)k * n + i] * zbuf[k];
+            y[i] = acc;
+        }
+        __syncwarp();
+    }
+    for (int i = lane; i < n; i += 32) bs[v.perm[i]] = y[i];
+}
+
+
+// Device layout of a batch sharing one CSR pattern: values [batch][nnz] -> band of B and V^T.
+// bulk_dest[p] >= 0: band offset (j*ldab + kv + i - j) of bulk entry p, -1 for a border entry.
+// Border position i owns the entries bptr[i]..bptr[i+1]-1 of (bp: CSR position, bcol: column), in
+// CSR order: V^T row i accumulates them, s_i = max |entry| (1 if the row is zero) goes on the
+// diagonal of B and is subtracted from V^T(i, i) (banded.hpp:197-214).
+template <class T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_layout_shared(BandView<T> v, const T* values, int nnz, const long long* bulk_dest, const int* bptr,
+                const int* bp, const int* bcol) {
+    const int sys = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r, kv = v.kl + v.ku;
+    T* ab = v.ab + (size_t)sys * n * v.ldab;
+    T* vt = v.vt + (size_t)sys * r * n;
+    const T* val = values + (size_t)sys * nnz;
+    for (size_t i = lane; i < (size_t)n * v.ldab; i += 32) ab[i] = T(0.0);
+    for (size_t i = lane; i < (size_t)r * n; i += 32) vt[i] = T(0.0);
+    __syncwarp();
+    for (int p = lane; p < nnz; p += 32) {
+        const long long d = bulk_dest[p];
+        if (d >= 0) ab[d] = ab[d] + val[p];
+    }
+    for (int i = lane; i < r; i += 32) {
+        double s = 0.0;
+        T* row = vt + (size_t)i * n;
+        for (int q = bptr[i]; q < bptr[i + 1]; ++q) {
+            const T a = val[bp[q]];
+            s = fmax(s, absval(a));
+            row[bcol[q]] = row[bcol[q]] + a;
+        }
+        if (s == 0.0) s = 1.0;
+        ab[(size_t)i * v.ldab + kv] = T(s);
+        row[i] = row[i] - T(s);
+    }
+}
+
+// ================================================================================================
+// host side
+
+struct Banded {
+    int dtype = 0;                // 0 = float64, 1 = complex128
+    int batch = 0, n = 0, r = 0, kl = 0, ku = 0, ldab = 1, pivot = 1;
+    size_t esz = 8;
+    void* ab = nullptr;
+    int* ipiv = nullptr;
+    void* vt = nullptr;
+    void* w = nullptr;
+    void* slu = nullptr;
+    int* spiv = nullptr;
+    int* perm = nullptr;
+    int* info = nullptr;
+    double* cond = nullptr;
+    void* wt = nullptr;
+    void* stlu = nullptr;
+    int* stpiv = nullptr;
+    bool transposed_ready = false;
+    double factor_ms = 0.0;
+    double cond_max = 1.0;
+    std::vector<int> perm_host;
+    // shared-pattern refactorization data (create_shared)
+    int nnz = 0;
+    long long* bulk_dest = nullptr;
+    int* bptr = nullptr;
+    int* bp = nullptr;
+    int* bcol = nullptr;
+
+    ~Banded() {
+        for (void* p : {ab, (void*)ipiv, vt, w, slu, (void*)spiv, (void*)perm, (void*)info,
+                        (void*)cond, wt, stlu, (void*)stpiv, (void*)bulk_dest, (void*)bptr,
+                        (void*)bp, (void*)bcol})
+            if (p) cudaFree(p);
+    }
+
+    template <class T>
+    BandView<T> view() const {
+        BandView<T> v;
+        v.batch = batch; v.n = n; v.r = r; v.kl = kl; v.ku = ku; v.ldab = ldab; v.pivot = pivot;
+        v.ab = static_cast<T*>(ab); v.ipiv = ipiv; v.vt = static_cast<T*>(vt);
+        v.w = static_cast<T*>(w); v.slu = static_cast<T*>(slu); v.spiv = spiv; v.perm = perm;
+        v.info = info; v.cond = cond; v.wt = static_cast<T*>(wt); v.stlu = static_cast<T*>(stlu);
+        v.stpiv = stpiv;
+        return v;
+    }
+
+    size_t solve_smem() const {
+        return (size_t)kWarpsPerBlock * (size_t)(n + 64) * esz;
+    }
+};
+
+template <class P>
+static void dalloc(P** p, size_t count, size_t esz) {
+    void* q = nullptr;
+    size_t bytes = std::max<size_t>(count * esz, 16);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw CudaFailure(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes failed: " +
+                          cudaGetErrorString(e));
+    }
+    *p = static_cast<P*>(q);
+}
+
+static void alloc_handle(Banded& h) {
+    const size_t B = h.batch, n = h.n, r = h.r;
+    dalloc(&h.ab, B * n * h.ldab, h.esz);
+    dalloc(&h.ipiv, B * n, sizeof(int));
+    dalloc(&h.vt, B * r * n, h.esz);
+    dalloc(&h.w, B * r * n, h.esz);
+    dalloc(&h.slu, B * r * r, h.esz);
+    dalloc(&h.spiv, B * r, sizeof(int));
+    dalloc(&h.perm, n, sizeof(int));
+    dalloc(&h.info, B, sizeof(int));
+    dalloc(&h.cond, B, sizeof(double));
+}
+
+static std::vector<int> border_perm(int n, const int* border, int r) {
+    if (r < 0 || r > n) throw InvalidArgument("border row count out of range");
+    if (r > 64) throw InvalidArgument("at most 64 border rows are supported (capacitance size)");
+    std::vector<char> is_border(n, 0);
+    std::vector<int> perm;
+    perm.reserve(n);
+    for (int k = 0; k < r; ++k) {
+        int i = border[k];
+        if (i < 0 || i >= n) throw InvalidArgument("border row out of range");
+        if (is_border[i]) throw InvalidArgument("duplicate border row");
+        is_border[i] = 1;
+        perm.push_back(i);
+    }
+    for (int i = 0; i < n; ++i)
+        if (!is_border[i]) perm.push_back(i);
+    return perm;
+}
+
+static void check_csr(int n, const int* ip, const int* ix, long long nnz) {
+    if (ip[0] != 0 || ip[n] != nnz)
+        throw InvalidArgument("inconsistent CSR arrays (indptr[0] = 0, indptr[n] = nnz = "
+                              "len(indices) = len(data) required)");
+    for (int i = 0; i < n; ++i)
+        if (ip[i + 1] < ip[i])
+            throw InvalidArgument("CSR: indptr decreases at row " + std::to_string(i));
+    for (long long p = 0; p < nnz; ++p)
+        if (ix[p] < 0 || ix[p] >= n)
+            throw InvalidArgument("CSR: column index " + std::to_string(ix[p]) + " outside [0, " +
+                                  std::to_string(n) + ")");
+}
+
+template <class T>
+static void check_finite(int n, const int* ip, const int* ix, const T* d) {
+    for (int i = 0; i < n; ++i)
+        for (int p = ip[i]; p < ip[i + 1]; ++p)
+            if (!finite_val(d[p]))
+                throw InvalidArgument("BorderedBanded: non-finite matrix entry at (" + std::to_string(i) +
+                                      ", " + std::to_string(ix[p]) + "): the operator must be finite");
+}
+
+static void finish_factor(Banded& h, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1) {
+    CNG_CUDA(cudaEventRecord(e1, st));
+    CNG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    h.factor_ms = ms;
+    std::vector<int> info(h.batch);
+    std::vector<double> cond(h.batch);
+    CNG_CUDA(cudaMemcpy(info.data(), h.info, sizeof(int) * h.batch, cudaMemcpyDeviceToHost));
+    CNG_CUDA(cudaMemcpy(cond.data(), h.cond, sizeof(double) * h.batch, cudaMemcpyDeviceToHost));
+    h.cond_max = 1.0;
+    for (int k = 0; k < h.batch; ++k) {
+        if (info[k] > 0)
+            throw RuntimeFailure("BandedBatch: banded part of system " + std::to_string(k) +
+                                 " is singular at pivot " + std::to_string(info[k]) +
+                                 "; the non-border rows must form an invertible banded operator "
+                                 "(check the row/column ordering of the plan)");
+        if (info[k] == -1)
+            throw RuntimeFailure("BandedBatch: capacitance matrix of system " + std::to_string(k) +
+                                 " is singular: the boundary rows are not independent of the banded "
+                                 "operator (ill-posed or rank-deficient BCs)");
+        if (info[k] == -2)
+            throw RuntimeFailure("BandedBatch: capacitance condition number is NaN");
+        if (!(cond[k] <= h.cond_max)) h.cond_max = cond[k];
+    }
+}
+
+static void launch_factor(Banded& h, cudaStream_t st) {
+    const int blocks = ceil_div(h.batch, kWarpsPerBlock);
+    if (h.dtype == 0) k_factor<double><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(h.view<double>());
+    else k_factor<zd><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(h.view<zd>());
+    CNG_LAUNCH("k_factor");
+}
+
+// General path: one CSR matrix per system (host arrays), layout on the host (border rows first,
+// common band of the batch), then the factorization on the device.
+template <class T>
+static void build_csr(Banded& h, const int* indptr, const int* indices, const T* data,
+                      const long long* off, const int* border, cudaStream_t st) {
+    const int n = h.n, B = h.batch;
+    h.perm_host = border_perm(n, border, h.r);
+    std::vector<int> pos(n);
+    for (int i = 0; i < n; ++i) pos[h.perm_host[i]] = i;
+    // band of the bulk rows over the batch (explicit zeros do not count, banded.hpp:116-133)
+    int kl = 0, ku = 0;
+    for (int k = 0; k < B; ++k) {
+        const int* ip = indptr + (size_t)k * (n + 1);
+        const int* ix = indices + off[k];
+        const T* d = data + off[k];
+        check_csr(n, ip, ix, ip[n]);
+        check_finite(n, ip, ix, d);
+        for (int o = 0; o < n; ++o) {
+            const int i = pos[o];
+            if (i < h.r) continue;
+            for (int p = ip[o]; p < ip[o + 1]; ++p) {
+                if (is_zero(d[p])) continue;
+                kl = std::max(kl, i - ix[p]);
+                ku = std::max(ku, ix[p] - i);
+            }
+        }
+    }
+    h.kl = kl;
+    h.ku = ku;
+    const long long ldab = 2LL * kl + ku + 1;
+    if (ldab > 1 << 20) throw InvalidArgument("banded layout: band too wide");
+    h.ldab = static_cast<int>(ldab);
+    alloc_handle(h);
+    const int kv = kl + ku;
+    std::vector<T> ab((size_t)n * h.ldab), vt((size_t)h.r * n);
+    // staged in chunks of systems to bound host memory
+    const int chunk = std::max(1, (int)std::min<long long>(B, (64LL << 20) / std::max<long long>(1, (long long)n * h.ldab * sizeof(T))));
+    std::vector<T> stage_ab((size_t)chunk * n * h.ldab), stage_vt((size_t)chunk * h.r * n);
+    for (int k0 = 0; k0 < B; k0 += chunk) {
+        const int k1 = std::min(B, k0 + chunk);
+        for (int k = k0; k < k1; ++k) {
+            T* abk = stage_ab.data() + (size_t)(k - k0) * n * h.ldab;
+            T* vtk = stage_vt.data() + (size_t)(k - k0) * h.r * n;
+            std::fill(abk, abk + (size_t)n * h.ldab, T(0.0));
+            std::fill(vtk, vtk + (size_t)h.r * n, T(0.0));
+            const int* ip = indptr + (size_t)k * (n + 1);
+            const int* ix = indices + off[k];
+            const T* d = data + off[k];
+            for (int i = 0; i < n; ++i) {
+                const int o = h.perm_host[i];
+                if (i < h.r) {
+                    double s = 0.0;
+                    for (int p = ip[o]; p < ip[o + 1]; ++p) {
+                        s = std::max(s, absval(d[p]));
+                        vtk[(size_t)i * n + ix[p]] = vtk[(size_t)i * n + ix[p]] + d[p];
+                    }
+                    if (s == 0.0) s = 1.0;
+                    abk[(size_t)i * h.ldab + kv] = T(s);
+                    vtk[(size_t)i * n + i] = vtk[(size_t)i * n + i] - T(s);
+                } else {
+                    for (int p = ip[o]; p < ip[o + 1]; ++p) {
+                        if (is_zero(d[p])) continue;
+                        const int j = ix[p];
+                        T& slot = abk[(size_t)j * h.ldab + kv + i - j];
+                        slot = slot + d[p];
+                    }
+                }
+            }
+        }
+        CNG_CUDA(cudaMemcpyAsync(static_cast<T*>(h.ab) + (size_t)k0 * n * h.ldab, stage_ab.data(),
+                                 sizeof(T) * (size_t)(k1 - k0) * n * h.ldab, cudaMemcpyHostToDevice, st));
+        if (h.r)
+            CNG_CUDA(cudaMemcpyAsync(static_cast<T*>(h.vt) + (size_t)k0 * h.r * n, stage_vt.data(),
+                                     sizeof(T) * (size_t)(k1 - k0) * h.r * n, cudaMemcpyHostToDevice, st));
+        CNG_CUDA(cudaStreamSynchronize(st));   // the staging buffers are reused
+    }
+    CNG_CUDA(cudaMemcpyAsync(h.perm, h.perm_host.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+}
+
+// Shared-pattern path: structure analysed once on the host, values assembled on the device.
+static void build_shared_structure(Banded& h, const int* indptr, const int* indices, int nnz,
+                                   const int* border, cudaStream_t st) {
+    const int n = h.n;
+    check_csr(n, indptr, indices, nnz);
+    h.perm_host = border_perm(n, border, h.r);
+    std::vector<int> pos(n);
+    for (int i = 0; i < n; ++i) pos[h.perm_host[i]] = i;
+    int kl = 0, ku = 0;
+    for (int o = 0; o < n; ++o) {
+        const int i = pos[o];
+        if (i < h.r) continue;
+        for (int p = indptr[o]; p < indptr[o + 1]; ++p) {
+            kl = std::max(kl, i - indices[p]);
+            ku = std::max(ku, indices[p] - i);
+        }
+    }
+    h.kl = kl;
+    h.ku = ku;
+    h.ldab = 2 * kl + ku + 1;
+    h.nnz = nnz;
+    alloc_handle(h);
+    const int kv = kl + ku;
+    std::vector<long long> dest(std::max(nnz, 1), -1);
+    std::vector<int> bptr(h.r + 1, 0), bp, bcol;
+    for (int i = 0; i < n; ++i) {
+        const int o = h.perm_host[i];
+        for (int p = indptr[o]; p < indptr[o + 1]; ++p) {
+            const int j = indices[p];
+            if (i < h.r) {
+                bp.push_back(p);
+                bcol.push_back(j);
+            } else {
+                dest[p] = (long long)j * h.ldab + kv + i - j;
+            }
+        }
+        if (i < h.r) bptr[i + 1] = static_cast<int>(bp.size());
+    }
+    // duplicate (row, column) entries would land twice in one band slot: refused
+    {
+        std::vector<long long> d2;
+        for (long long d : dest) if (d >= 0) d2.push_back(d);
+        std::sort(d2.begin(), d2.end());
+        if (std::adjacent_find(d2.begin(), d2.end()) != d2.end())
+            throw InvalidArgument("shared CSR pattern has duplicate entries (sum them first)");
+    }
+    dalloc(&h.bulk_dest, dest.size(), sizeof(long long));
+    dalloc(&h.bptr, bptr.size(), sizeof(int));
+    dalloc(&h.bp, std::max<size_t>(bp.size(), 1), sizeof(int));
+    dalloc(&h.bcol, std::max<size_t>(bcol.size(), 1), sizeof(int));
+    CNG_CUDA(cudaMemcpyAsync(h.bulk_dest, dest.data(), sizeof(long long) * dest.size(), cudaMemcpyHostToDevice, st));
+    CNG_CUDA(cudaMemcpyAsync(h.bptr, bptr.data(), sizeof(int) * bptr.size(), cudaMemcpyHostToDevice, st));
+    if (!bp.empty()) {
+        CNG_CUDA(cudaMemcpyAsync(h.bp, bp.data(), sizeof(int) * bp.size(), cudaMemcpyHostToDevice, st));
+        CNG_CUDA(cudaMemcpyAsync(h.bcol, bcol.data(), sizeof(int) * bcol.size(), cudaMemcpyHostToDevice, st));
+    }
+    CNG_CUDA(cudaMemcpyAsync(h.perm, h.perm_host.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    CNG_CUDA(cudaStreamSynchronize(st));     // host vectors go out of scope
+}
+
+static void launch_layout_shared(Banded& h, const void* values, cudaStream_t st) {
+    const int blocks = ceil_div(h.batch, kWarpsPerBlock);
+    if (h.dtype == 0)
+        k_layout_shared<double><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(
+            h.view<double>(), static_cast<const double*>(values), h.nnz, h.bulk_dest, h.bptr, h.bp, h.bcol);
+    else
+        k_layout_shared<zd><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(
+            h.view<zd>(), static_cast<const zd*>(values), h.nnz, h.bulk_dest, h.bptr, h.bp, h.bcol);
+    CNG_LAUNCH("k_layout_shared");
+}
+
+static void check_smem(const Banded& h) {
+    if (h.solve_smem() > kMaxSolveSmem)
+        throw InvalidArgument("BandedBatch: n = " + std::to_string(h.n) +
+                              " is too large for the shared-memory solve (at most " +
+                              std::to_string(kMaxSolveSmem / kWarpsPerBlock / h.esz - 64) + ")");
+}
+
+template <class T, int IO>
+static void launch_solve_t(const Banded& h, const SolveIo& io, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve<T, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
+    });
+    const int blocks = ceil_div(h.batch, kWarpsPerBlock);
+    k_solve<T, IO><<<blocks, 32 * kWarpsPerBlock, h.solve_smem(), st>>>(h.view<T>(), io);
+    CNG_LAUNCH("k_solve");
+}
+
+static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st) {
+    if (h.dtype == 0) {
+        if (io_kind == IO_PLAIN) launch_solve_t<double, IO_PLAIN>(h, io, st);
+        else if (io_kind == IO_MAPPED) launch_solve_t<double, IO_MAPPED>(h, io, st);
+        else throw InvalidArgument("solve_split needs complex (complex128) factors");
+    } else {
+        if (io_kind == IO_PLAIN) launch_solve_t<zd, IO_PLAIN>(h, io, st);
+        else if (io_kind == IO_MAPPED) launch_solve_t<zd, IO_MAPPED>(h, io, st);
+        else launch_solve_t<zd, IO_SPLIT>(h, io, st);
+    }
+}
+
+static void prepare_transpose(Banded& h, cudaStream_t st) {
+    if (h.transposed_ready) return;
+    if (h.r > 0) {
+        if (!h.wt) dalloc(&h.wt, (size_t)h.batch * h.r * h.n, h.esz);
+        if (!h.stlu) dalloc(&h.stlu, (size_t)h.batch * h.r * h.r, h.esz);
+        if (!h.stpiv) dalloc(&h.stpiv, (size_t)h.batch * h.r, sizeof(int));
+        const int blocks = ceil_div(h.batch, kWarpsPerBlock);
+        if (h.dtype == 0) k_prepare_T<double><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(h.view<double>());
+        else k_prepare_T<zd><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(h.view<zd>());
+        CNG_LAUNCH("k_prepare_T");
+        CNG_CUDA(cudaStreamSynchronize(st));
+    }
+    h.transposed_ready = true;
+}
+
+template <class T>
+static void launch_solve_T_t(const Banded& h, void* b, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve_T<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
+    });
+    const int blocks = ceil_div(h.batch, kWarpsPerBlock);
+    k_solve_T<T><<<blocks, 32 * kWarpsPerBlock, h.solve_smem(), st>>>(h.view<T>(), static_cast<T*>(b));
+    CNG_LAUNCH("k_solve_T");
+}
+
+}  // namespace cng
+
+// ================================================================================================
+// C-ABI
+
+using namespace cng;
+
+static Banded* as_banded(cng_banded* h) {
+    if (!h) throw InvalidArgument("null BandedBatch handle");
+    return reinterpret_cast<Banded*>(h);
+}
+static const Banded* as_banded(const cng_banded* h) {
+    if (!h) throw InvalidArgument("null BandedBatch handle");
+    return reinterpret_cast<const Banded*>(h);
+}
+
+extern "C" {
+
+int cng_banded_create_csr(int dtype, int batch, int n, const int32_t* indptr, const int32_t* indices,
+                          const void* data, const int64_t* nnz_offsets, const int32_t* border, int r,
+                          int pivot, void* stream, cng_banded** out) {
+    CNG_TRY({
+        if (!out) throw InvalidArgument("null output handle");
+        *out = nullptr;
+        if (dtype != 0 && dtype != 1) throw InvalidArgument("dtype must be 0 (float64) or 1 (complex128)");
+        if (batch < 1) throw InvalidArgument("BandedBatch: no matrix given");
+        if (n < 1) throw InvalidArgument("BandedBatch: n must be >= 1");
+        if (!indptr || !indices || !data || !nnz_offsets || (r > 0 && !border))
+            throw InvalidArgument("null CSR array");
+        auto h = std::make_unique<Banded>();
+        h->dtype = dtype; h->batch = batch; h->n = n; h->r = r; h->pivot = pivot ? 1 : 0;
+        h->esz = dtype ? sizeof(zd) : sizeof(double);
+        check_smem(*h);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        cudaEvent_t e0, e1;
+        CNG_CUDA(cudaEventCreate(&e0));
+        CNG_CUDA(cudaEventCreate(&e1));
+        try {
+            if (dtype == 0)
+                build_csr<double>(*h, indptr, indices, static_cast<const double*>(data),
+                                  reinterpret_cast<const long long*>(nnz_offsets), border, st);
+            else
+                build_csr<zd>(*h, indptr, indices, static_cast<const zd*>(data),
+                              reinterpret_cast<const long long*>(nnz_offsets), border, st);
+            CNG_CUDA(cudaEventRecord(e0, st));
+            launch_factor(*h, st);
+            finish_factor(*h, st, e0, e1);
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *out = reinterpret_cast<cng_banded*>(h.release());
+    })
+}
+
+int cng_banded_create_shared(int dtype, int batch, int n, const int32_t* indptr, const int32_t* indices,
+                             int nnz, const void* values, const int32_t* border, int r, int pivot,
+                             void* stream, cng_banded** out) {
+    CNG_TRY({
+        if (!out) throw InvalidArgument("null output handle");
+        *out = nullptr;
+        if (dtype != 0 && dtype != 1) throw InvalidArgument("dtype must be 0 (float64) or 1 (complex128)");
+        if (batch < 1) throw InvalidArgument("BandedBatch: no matrix given");
+        if (n < 1 || nnz < 0) throw InvalidArgument("BandedBatch: n must be >= 1");
+        if (!indptr || (nnz > 0 && !indices) || !values || (r > 0 && !border))
+            throw InvalidArgument("null array");
+        auto h = std::make_unique<Banded>();
+        h->dtype = dtype; h->batch = batch; h->n = n; h->r = r; h->pivot = pivot ? 1 : 0;
+        h->esz = dtype ? sizeof(zd) : sizeof(double);
+        check_smem(*h);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        build_shared_structure(*h, indptr, indices, nnz, border, st);
+        cudaEvent_t e0, e1;
+        CNG_CUDA(cudaEventCreate(&e0));
+        CNG_CUDA(cudaEventCreate(&e1));
+        try {
+            CNG_CUDA(cudaEventRecord(e0, st));
+            launch_layout_shared(*h, values, st);
+            launch_factor(*h, st);
+            finish_factor(*h, st, e0, e1);
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *out = reinterpret_cast<cng_banded*>(h.release());
+    })
+}
+
+int cng_banded_destroy(cng_banded* h) {
+    CNG_TRY({ delete reinterpret_cast<Banded*>(h); })
+}
+
+int cng_banded_info(const cng_banded* hh, int32_t* dims, double* stats) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (dims) {
+            dims[0] = h->batch; dims[1] = h->n; dims[2] = h->r; dims[3] = h->kl;
+            dims[4] = h->ku; dims[5] = h->ldab; dims[6] = h->dtype; dims[7] = h->pivot;
+        }
+        if (stats) {
+            stats[0] = h->factor_ms;
+            stats[1] = h->cond_max;
+        }
+    })
+}
+
+int cng_banded_capacitance_cond(const cng_banded* hh, double* cond_host) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!cond_host) throw InvalidArgument("null output");
+        CNG_CUDA(cudaMemcpy(cond_host, h->cond, sizeof(double) * h->batch, cudaMemcpyDeviceToHost));
+    })
+}
+
+int cng_banded_solve(const cng_banded* hh, void* b, void* stream) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!b) throw InvalidArgument("BandedBatch.solve: null device pointer");
+        SolveIo io{b, b, nullptr, nullptr, nullptr, nullptr};
+        launch_solve(*h, IO_PLAIN, io, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_banded_solve_mapped(const cng_banded* hh, const void* rhs, const int64_t* rows, void* x,
+                            const int64_t* cols, void* stream) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!rhs || !x) throw InvalidArgument("BandedBatch.solve_mapped_ptr: null device pointer");
+        if (rhs == x) throw InvalidArgument("BandedBatch.solve_mapped_ptr: rhs and x must not alias");
+        SolveIo io{rhs, x, reinterpret_cast<const long long*>(rows), reinterpret_cast<const long long*>(cols),
+                   nullptr, nullptr};
+        launch_solve(*h, IO_MAPPED, io, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_banded_solve_split(const cng_banded* hh, const double* re, const int64_t* rows_c,
+                           const int64_t* rows_s, double* x, const int64_t* cols_c,
+                           const int64_t* cols_s, void* stream) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!re || !x || !rows_c || !rows_s || !cols_c || !cols_s)
+            throw InvalidArgument("BandedBatch.solve_split_ptr: null device pointer");
+        if (static_cast<const void*>(re) == static_cast<const void*>(x))
+            throw InvalidArgument("BandedBatch.solve_split_ptr: re and x must not alias");
+        SolveIo io{re, x, reinterpret_cast<const long long*>(rows_c), reinterpret_cast<const long long*>(cols_c),
+                   reinterpret_cast<const long long*>(rows_s), reinterpret_cast<const long long*>(cols_s)};
+        launch_solve(*h, IO_SPLIT, io, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_banded_prepare_transpose(cng_banded* hh, void* stream) {
+    CNG_TRY({ prepare_transpose(*as_banded(hh), static_cast<cudaStream_t>(stream)); })
+}
+
+int cng_banded_solve_transpose(const cng_banded* hh, void* b, void* stream) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!b) throw InvalidArgument("BandedBatch.solve_transpose_ptr: null device pointer");
+        if (!h->transposed_ready)
+            throw InvalidArgument("BandedBatch.solve_transpose_ptr: call prepare_transpose() first "
+                                  "(it allocates; never inside a graph capture)");
+        if (h->dtype == 0) launch_solve_T_t<double>(*h, b, static_cast<cudaStream_t>(stream));
+        else launch_solve_T_t<zd>(*h, b, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_banded_solve_host(cng_banded* hh, const void* b_host, void* x_host, int transpose) {
+    CNG_TRY({
+        Banded* h = as_banded(hh);
+        if (!b_host || !x_host) throw InvalidArgument("BorderedBandedBatch.solve: null host pointer");
+        const size_t bytes = h->esz * (size_t)h->batch * h->n;
+        void* d = nullptr;
+        cudaStream_t st = nullptr;
+        CNG_CUDA(cudaMalloc(&d, bytes));
+        try {
+            CNG_CUDA(cudaMemcpyAsync(d, b_host, bytes, cudaMemcpyHostToDevice, st));
+            if (transpose) {
+                prepare_transpose(*h, st);
+                if (h->dtype == 0) launch_solve_T_t<double>(*h, d, st);
+                else launch_solve_T_t<zd>(*h, d, st);
+            } else {
+                SolveIo io{d, d, nullptr, nullptr, nullptr, nullptr};
+                launch_solve(*h, IO_PLAIN, io, st);
+            }
+            CNG_CUDA(cudaMemcpyAsync(x_host, d, bytes, cudaMemcpyDeviceToHost, st));
+            CNG_CUDA(cudaStreamSynchronize(st));
+        } catch (...) {
+            cudaFree(d);
+            throw;
+        }
+        CNG_CUDA(cudaFree(d));
+    })
+}
+
+int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream) {
+    CNG_TRY({
+        Banded* h = as_banded(hh);
+        if (!h->bulk_dest) throw InvalidArgument("refactor_shared: handle was not created from a shared pattern");
+        if (!values) throw InvalidArgument("null values");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        cudaEvent_t e0, e1;
+        CNG_CUDA(cudaEventCreate(&e0));
+        CNG_CUDA(cudaEventCreate(&e1));
+        try {
+            CNG_CUDA(cudaEventRecord(e0, st));
+            launch_layout_shared(*h, values, st);
+            launch_factor(*h, st);
+            h->transposed_ready = false;
+            finish_factor(*h, st, e0, e1);
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    })
+}
+
+}  // extern "C"

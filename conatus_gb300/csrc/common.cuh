@@ -1,0 +1,122 @@
+// Shared helpers of the conatus_gb300 CUDA library: complex arithmetic, error reporting through a
+// thread-local message (the C-ABI returns an int status), launch checks.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace cng {
+
+// Status codes of the C-ABI (0 = success).
+enum Status : int {
+    CNG_OK = 0,
+    CNG_EINVAL = 1,      // invalid argument (ValueError on the Python side)
+    CNG_ERUNTIME = 2,    // numerical or runtime failure (RuntimeError), e.g. "singular"
+    CNG_ECUDA = 3,       // CUDA error
+    CNG_ENOMEM = 4,      // allocation failed
+};
+
+struct InvalidArgument : std::invalid_argument {
+    using std::invalid_argument::invalid_argument;
+};
+struct RuntimeFailure : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct CudaFailure : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void set_error(const std::string& msg);
+
+inline void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw CudaFailure(std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CNG_CUDA(call) ::cng::cuda_check((call), #call)
+#define CNG_LAUNCH(what) ::cng::cuda_check(cudaGetLastError(), what)
+
+// ---- complex double with explicit operations (no library dependency in device code) ----------
+struct alignas(16) zd {
+    double re, im;
+    __host__ __device__ zd() : re(0), im(0) {}
+    __host__ __device__ zd(double r) : re(r), im(0) {}
+    __host__ __device__ zd(double r, double i) : re(r), im(i) {}
+};
+__host__ __device__ inline zd operator+(zd a, zd b) { return zd(a.re + b.re, a.im + b.im); }
+__host__ __device__ inline zd operator-(zd a, zd b) { return zd(a.re - b.re, a.im - b.im); }
+__host__ __device__ inline zd operator-(zd a) { return zd(-a.re, -a.im); }
+__host__ __device__ inline zd operator*(zd a, zd b) {
+    return zd(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__host__ __device__ inline zd operator*(double s, zd a) { return zd(s * a.re, s * a.im); }
+// a / b by Smith's method (overflow-safe scaling of the denominator).
+__host__ __device__ inline zd operator/(zd a, zd b) {
+    if (fabs(b.re) >= fabs(b.im)) {
+        double r = b.im / b.re, d = b.re + b.im * r;
+        return zd((a.re + a.im * r) / d, (a.im - a.re * r) / d);
+    }
+    double r = b.re / b.im, d = b.im + b.re * r;
+    return zd((a.re * r + a.im) / d, (a.im * r - a.re) / d);
+}
+__host__ __device__ inline bool operator==(zd a, zd b) { return a.re == b.re && a.im == b.im; }
+__host__ __device__ inline bool operator!=(zd a, zd b) { return !(a == b); }
+
+// Magnitudes: |.| of LAPACK's pivot search (i?amax: |re| + |im| for complex) and the modulus.
+__host__ __device__ inline double abs1(double x) { return fabs(x); }
+__host__ __device__ inline double abs1(zd x) { return fabs(x.re) + fabs(x.im); }
+__host__ __device__ inline double absval(double x) { return fabs(x); }
+__host__ __device__ inline double absval(zd x) { return hypot(x.re, x.im); }
+__host__ __device__ inline bool is_zero(double x) { return x == 0.0; }
+__host__ __device__ inline bool is_zero(zd x) { return x.re == 0.0 && x.im == 0.0; }
+__host__ __device__ inline bool finite_val(double x) { return isfinite(x); }
+__host__ __device__ inline bool finite_val(zd x) { return isfinite(x.re) && isfinite(x.im); }
+
+template <class T> __host__ __device__ inline T one();
+template <> __host__ __device__ inline double one<double>() { return 1.0; }
+template <> __host__ __device__ inline zd one<zd>() { return zd(1.0, 0.0); }
+
+// Warp shuffle of either type.
+__device__ inline double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ inline zd shfl(zd v, int src) {
+    return zd(__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src));
+}
+__device__ inline double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ inline zd shfl_xor(zd v, int m) {
+    return zd(__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m));
+}
+template <class T>
+__device__ inline T warp_sum(T v) {
+    for (int m = 16; m > 0; m >>= 1) v = v + shfl_xor(v, m);
+    return v;
+}
+
+// Body of a C-ABI function: exceptions become a status code and the thread-local message.
+#define CNG_TRY(...)                                                                   \
+    try {                                                                              \
+        __VA_ARGS__;                                                                   \
+        return ::cng::CNG_OK;                                                          \
+    } catch (const ::cng::InvalidArgument& e) {                                        \
+        ::cng::set_error(e.what());                                                    \
+        return ::cng::CNG_EINVAL;                                                      \
+    } catch (const ::cng::RuntimeFailure& e) {                                         \
+        ::cng::set_error(e.what());                                                    \
+        return ::cng::CNG_ERUNTIME;                                                    \
+    } catch (const ::cng::CudaFailure& e) {                                            \
+        ::cng::set_error(e.what());                                                    \
+        return ::cng::CNG_ECUDA;                                                       \
+    } catch (const std::bad_alloc&) {                                                  \
+        ::cng::set_error("host allocation failed");                                    \
+        return ::cng::CNG_ENOMEM;                                                      \
+    } catch (const std::exception& e) {                                                \
+        ::cng::set_error(e.what());                                                    \
+        return ::cng::CNG_ERUNTIME;                                                    \
+    }
+
+inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+}  // namespace cng

@@ -1,0 +1,36 @@
+"""CPU: the C-ABI library builds, loads without a GPU, and exports every function that
+include/conatus_gb300.h declares (no compute calls)."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            names |= set(re.findall(r"\b(cng_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    from conatus_gb300 import build, _lib
+    path = build.build()
+    L = ctypes.CDLL(path)
+    missing = [n for n in declared() if not hasattr(L, n)]
+    assert not missing, missing
+    # the Python binding knows every declared symbol too
+    assert set(declared()) <= set(_lib.EXPORTS), sorted(set(declared()) - set(_lib.EXPORTS))
+
+
+def test_library_reports_no_device_on_cpu_host():
+    import torch
+    from conatus_gb300 import _lib
+    if not torch.cuda.is_available():
+        assert _lib.lib().cng_cuda_available() == 0
