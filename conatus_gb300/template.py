@@ -1,0 +1,247 @@
+"""Problem templates: the set-up data of a Fourier^d x Chebyshev IVP, independent of the Fourier
+resolution, in the layout the GB300 kernels use.
+
+The reference discretizes a model once (python/conatus/discretize/plan.py:851, ``GlobalSystem``
+in python/conatus/timestep/system.py:244-334): one system per Fourier group, its rows and columns
+permuted into solver order (border rows first, interleaved Chebyshev order), groups with one
+sparsity pattern batched into a "bucket", and RealFourier (cos, -sin) pairs solved as complex
+systems (``complexify=True``, system.py:600-726, exact). A template keeps, per bucket:
+
+* the sparsity pattern of ``a M + b L`` in solver order and the values of M and L as polynomials
+  in the signed wavenumbers (kx, kz) of the group -- the reference's group matrices are built
+  from derivative blocks ``(i k)^order`` (discretize/layout.py:48-56), so each entry is a
+  polynomial in k; the coefficients are recovered exactly from the reference's own assembly
+  evaluated at small integer wavenumbers (see ``conatus_gb300.reference_adapter``);
+* which (variable, component, Chebyshev index) each solver column holds, and which (equation,
+  component, Chebyshev index, ultraspherical level lambda) each row holds;
+* the rule that lists its systems at any Fourier resolution (which Fourier directions are nonzero,
+  and the sign s of the second direction for the complex modes exp(i(kx x + s kz z))).
+
+Plus the explicit right-hand side in polynomial form (``FusedRHS.factor_list/outputs`` of
+python/conatus/timestep/fused.py:524-537), the conversions T -> C^(lambda) of the equations
+(discretize/ultraspherical.py:43-66) and the constant part of F (boundary data, forcing).
+
+Device layout ("mode layout"): every system is one complex vector of length n in solver order; the
+state X, M X and F of a bucket are (nsys, n) complex arrays. A system of mode (jx, jz, s) holds the
+complex amplitudes C with f = w Re(C exp(i(kx x + s kz z))), w = 2^(1 - d_act) for d_act >= 1
+nonzero Fourier indices (1 for the mean mode), the reference's complex view of the real group.
+"""
+from __future__ import annotations
+
+import itertools
+import json
+from dataclasses import dataclass, field
+
+import numpy as np
+
+__all__ = ["Bucket", "ProblemTemplate", "Problem"]
+
+
+@dataclass
+class Bucket:
+    kind: str                     # "real" (all Fourier indices zero) or "complex"
+    n: int
+    r: int                        # border rows (first r rows in solver order)
+    active: tuple                 # per Fourier direction: nonzero index in this bucket
+    sign: int                     # s of the second Fourier direction (+1 / -1)
+    indptr: np.ndarray            # pattern of a M + b L in solver order
+    indices: np.ndarray
+    monos: np.ndarray             # (nmono, d) powers of the signed wavenumbers
+    Mc: np.ndarray                # (nmono, nnz) complex coefficients of M
+    Lc: np.ndarray                # (nmono, nnz) complex coefficients of L
+    col: np.ndarray               # (n, 3) int: variable, flat component, Chebyshev index (-1: none)
+    row: np.ndarray               # (n, 4) int: equation, flat component, Chebyshev index, lambda
+    fit_error: float = 0.0        # max relative error of the polynomial form on the source build
+    exact: tuple | None = None    # optional (M values, L values), each (nsys, nnz), of the systems
+                                  # of one resolution, taken bit for bit from the reference
+
+    @property
+    def nnz(self) -> int:
+        return int(self.indices.shape[0])
+
+    def coo_rows(self) -> np.ndarray:
+        return np.repeat(np.arange(self.n), np.diff(self.indptr))
+
+    def m_is_constant(self) -> bool:
+        """M does not depend on the wavenumbers (only the constant monomial is nonzero)."""
+        k0 = np.nonzero(np.all(self.monos == 0, axis=1))[0]
+        others = [t for t in range(self.monos.shape[0]) if t not in set(k0.tolist())]
+        return bool(not others or np.all(self.Mc[others] == 0))
+
+
+@dataclass
+class ProblemTemplate:
+    name: str
+    axes: list                    # per coordinate: {coord, kind, N, L, a, M}
+    cheb_axis: int                # index of the Chebyshev axis (-1: none)
+    fourier_axes: list            # indices of the RealFourier axes, in order
+    variables: list               # {name, ncomp, shape}
+    equations: list               # {ncomp, shape}
+    factors: list                 # (var, comp, orders per axis)
+    outputs: list                 # (eq, comp, [(coef, (factor ids))]) -- constant terms excluded
+    conv: dict                    # lambda -> (N, N) dense conversion T -> C^(lambda)
+    buckets: list
+    b0: list = field(default_factory=list)   # (bucket, mode tuple, position, value) of F(0)
+    params: dict = field(default_factory=dict)
+    source: dict = field(default_factory=dict)
+
+    # ---------------------------------------------------------------- persistence
+    def save(self, path: str) -> None:
+        meta = dict(name=self.name, axes=self.axes, cheb_axis=self.cheb_axis,
+                    fourier_axes=self.fourier_axes, variables=self.variables,
+                    equations=self.equations,
+                    factors=[[int(v), int(c), [int(o) for o in a]] for v, c, a in self.factors],
+                    outputs=[[int(e), int(c), [[_cplx_json(co), [int(f) for f in fs]] for co, fs in m]]
+                             for e, c, m in self.outputs],
+                    lams=sorted(int(k) for k in self.conv),
+                    buckets=[dict(kind=b.kind, n=b.n, r=b.r, active=list(map(bool, b.active)),
+                                  sign=int(b.sign), fit_error=float(b.fit_error))
+                             for b in self.buckets],
+                    b0=[[int(bi), [int(j) for j in mode], int(pos), _cplx_json(v)]
+                        for bi, mode, pos, v in self.b0],
+                    params=self.params, source=self.source)
+        arrays = {"meta": np.array(json.dumps(meta))}
+        for lam, C in self.conv.items():
+            arrays[f"conv_{lam}"] = C
+        for i, b in enumerate(self.buckets):
+            p = f"b{i}_"
+            arrays[p + "indptr"] = b.indptr.astype(np.int32)
+            arrays[p + "indices"] = b.indices.astype(np.int32)
+            arrays[p + "monos"] = b.monos.astype(np.int32)
+            arrays[p + "Mc"] = b.Mc
+            arrays[p + "Lc"] = b.Lc
+            arrays[p + "col"] = b.col.astype(np.int32)
+            arrays[p + "row"] = b.row.astype(np.int32)
+        np.savez_compressed(path, **arrays)
+
+    @classmethod
+    def load(cls, path: str) -> "ProblemTemplate":
+        z = np.load(path, allow_pickle=False)
+        meta = json.loads(str(z["meta"]))
+        buckets = []
+        for i, bm in enumerate(meta["buckets"]):
+            p = f"b{i}_"
+            buckets.append(Bucket(bm["kind"], int(bm["n"]), int(bm["r"]), tuple(bm["active"]),
+                                  int(bm["sign"]), z[p + "indptr"], z[p + "indices"], z[p + "monos"],
+                                  z[p + "Mc"], z[p + "Lc"], z[p + "col"], z[p + "row"],
+                                  float(bm.get("fit_error", 0.0))))
+        return cls(name=meta["name"], axes=meta["axes"], cheb_axis=int(meta["cheb_axis"]),
+                   fourier_axes=list(meta["fourier_axes"]), variables=meta["variables"],
+                   equations=meta["equations"],
+                   factors=[(v, c, tuple(a)) for v, c, a in meta["factors"]],
+                   outputs=[(e, c, [(_cplx_from(co), tuple(fs)) for co, fs in m])
+                            for e, c, m in meta["outputs"]],
+                   conv={int(l): z[f"conv_{l}"] for l in meta["lams"]},
+                   buckets=buckets,
+                   b0=[(bi, tuple(mode), pos, _cplx_from(v)) for bi, mode, pos, v in meta["b0"]],
+                   params=meta.get("params", {}), source=meta.get("source", {}))
+
+    # ---------------------------------------------------------------- derived
+    @property
+    def ncheb(self) -> int:
+        return self.axes[self.cheb_axis]["N"] if self.cheb_axis >= 0 else 1
+
+    def instantiate(self, fourier_sizes=None) -> "Problem":
+        """The systems of this template at the given RealFourier sizes (default: the template's)."""
+        return Problem(self, fourier_sizes)
+
+
+def _cplx_json(v):
+    v = complex(v)
+    return [v.real, v.imag]
+
+
+def _cplx_from(v):
+    if isinstance(v, (list, tuple)):
+        return complex(v[0], v[1])
+    return complex(v)
+
+
+class Problem:
+    """A template at a Fourier resolution: the systems (modes, wavenumbers) of every bucket."""
+
+    def __init__(self, tpl: ProblemTemplate, fourier_sizes=None):
+        self.tpl = tpl
+        d = len(tpl.fourier_axes)
+        if fourier_sizes is None:
+            fourier_sizes = [tpl.axes[a]["N"] for a in tpl.fourier_axes]
+        fourier_sizes = [int(s) for s in fourier_sizes]
+        if len(fourier_sizes) != d:
+            raise ValueError(f"{tpl.name}: {d} Fourier sizes expected, got {fourier_sizes}")
+        for s in fourier_sizes:
+            if s % 2 or s < 2:
+                raise ValueError("Fourier sizes must be even (Nyquist convention)")
+        self.fourier_sizes = fourier_sizes
+        self.K = [s // 2 for s in fourier_sizes]
+        self.lengths = [tpl.axes[a]["L"] for a in tpl.fourier_axes]
+        # grid sizes: the reference's dealiasing rule floor(N * 3/2) scaled from the template
+        self.modes, self.wavenumbers, self.offsets = [], [], []
+        off = 0
+        for b in tpl.buckets:
+            ranges = [range(1, K) if act else range(0, 1) for act, K in zip(b.active, self.K)]
+            modes = np.array(list(itertools.product(*ranges)), dtype=np.int64).reshape(-1, d) if d else \
+                np.zeros((1, 0), np.int64)
+            kw = np.zeros(modes.shape, dtype=np.float64)
+            for j in range(d):
+                kw[:, j] = 2 * np.pi * modes[:, j] / self.lengths[j]
+            if d >= 2:
+                kw[:, 1] *= b.sign
+            self.modes.append(modes)
+            self.wavenumbers.append(kw)
+            self.offsets.append(off)
+            off += modes.shape[0] * b.n
+        self.n_total = off           # complex unknowns of the mode layout
+
+    @property
+    def nsys(self):
+        return [m.shape[0] for m in self.modes]
+
+    def mono_values(self, bi: int) -> np.ndarray:
+        """(nsys, nmono) values of the wavenumber monomials of bucket bi."""
+        b = self.tpl.buckets[bi]
+        kw = self.wavenumbers[bi]
+        out = np.ones((kw.shape[0], b.monos.shape[0]), dtype=np.float64)
+        for t, powers in enumerate(b.monos):
+            for j, p in enumerate(powers):
+                if p:
+                    out[:, t] *= kw[:, j] ** int(p)
+        return out
+
+    def values(self, bi: int, which: str) -> np.ndarray:
+        """(nsys, nnz) values of M or L ('M' / 'L') of every system of bucket bi: the reference's
+        own values when the bucket carries them for this resolution, else the wavenumber
+        polynomial."""
+        b = self.tpl.buckets[bi]
+        if b.exact is not None and b.exact[0].shape[0] == self.nsys[bi]:
+            return np.array(b.exact[0] if which == "M" else b.exact[1], dtype=np.complex128)
+        C = b.Mc if which == "M" else b.Lc
+        return self.mono_values(bi).astype(np.complex128) @ C
+
+    def set_exact(self, values) -> None:
+        """Attach the reference's own (M, L) values per bucket, [(Mv, Lv)] with (nsys, nnz)."""
+        for b, (Mv, Lv), ns in zip(self.tpl.buckets, values, self.nsys):
+            if Mv.shape != (ns, b.nnz) or Lv.shape != (ns, b.nnz):
+                raise ValueError("exact values do not match the bucket (nsys, nnz)")
+            b.exact = (np.asarray(Mv), np.asarray(Lv))
+
+    def d_active(self, bi: int) -> int:
+        return int(sum(self.tpl.buckets[bi].active))
+
+    def real_unknowns(self) -> int:
+        """Unknowns of the reference's real global vector (N_u): complex systems count twice,
+        except the modes with 2 active directions, whose two sign views share 4 real entries."""
+        tot = 0
+        for bi, b in enumerate(self.tpl.buckets):
+            ns = self.nsys[bi]
+            tot += ns * b.n * (1 if b.kind == "real" else 2)
+        return tot
+
+    def b0_dense(self):
+        """Constant part of F in the mode layout: list per bucket of (nsys, n) complex arrays
+        (zero where the template has no entry; modes absent at this resolution are dropped)."""
+        out = [np.zeros((ns, b.n), np.complex128) for ns, b in zip(self.nsys, self.tpl.buckets)]
+        for bi, mode, pos, v in self.tpl.b0:
+            hit = np.nonzero(np.all(self.modes[bi] == np.asarray(mode, dtype=np.int64), axis=1))[0]
+            if hit.size:
+                out[bi][hit[0], pos] += v
+        return out

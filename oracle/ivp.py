@@ -1,0 +1,360 @@
+"""Oracle (test infrastructure only): CPU restatement of the reference's IMEX step on the mode
+layout of a problem template (``conatus_gb300.template``).
+
+Imported only by ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``. It
+follows, in NumPy/SciPy:
+
+* ``_to_arrays`` / ``_to_rows``: the reference's ``GlobalSystem.scatter`` / ``gather_rhs``
+  (python/conatus/timestep/system.py:876-931) composed with its complex views of RealFourier pairs
+  (system.py:600-726): a_p = 2^(1-d) sum_s Re(conj(w_s(p)) C_s), R_s = sum_p w_s(p) r_p,
+  w_s(p) = prod_j (i s_j)^p_j; the C^(lambda) conversion of each equation (``zconv``).
+* ``F``: ``FusedRHS.evaluate`` (python/conatus/timestep/fused.py:994-1085): factor derivatives in
+  coefficient space (``SpectralEvaluator._diff``, spectral.py:199-223: Fourier pair swap times k,
+  Chebyshev backward recurrence ``_cheb_diff_recurrence`` spectral.py:53-80 times 2/L), backward
+  transforms Chebyshev first, the product sums, forward transforms Fourier first; transforms with
+  the conventions of python/conatus/reference/transforms.py:103-187 (DCT-II/III on Gauss nodes,
+  rfft with (cos, -sin) pairs); plus the constant part F(0).
+* ``sbdf_step``: ``IVPSolver._sbdf_step`` (python/conatus/timestep/integrator.py:361-373) with
+  ``sbdf_coefficients`` (schemes.py:106-116) and ``sbdf_rhs`` (lincomb.py:146-162), solves by
+  the oracle bordered-banded restatement (oracle/banded.py), factorizations cached per (a, b).
+"""
+from __future__ import annotations
+
+import itertools
+from collections import deque
+
+import numpy as np
+import scipy.fft as sfft
+import scipy.sparse as sp
+
+from .banded import BorderedBandedBatch
+
+SBDF = {1: ([1, -1], [0, 1]),
+        2: ([1.5, -2, 0.5], [0, 2, -1]),
+        3: ([11 / 6, -3, 1.5, -1 / 3], [0, 3, -3, 1]),
+        4: ([25 / 12, -4, 3, -4 / 3, 0.25], [0, 4, -6, 4, -1])}
+
+
+# ------------------------------------------------------------------------------------------------
+# reference transforms (reference/transforms.py:103-187), along axis 0
+
+def cheb_forward(f, N):
+    M = f.shape[0]
+    y = sfft.dct(f, type=2, axis=0) / M
+    y[0] /= 2
+    sign = (-1.0) ** np.arange(M)
+    return (y * sign.reshape((M,) + (1,) * (f.ndim - 1)))[:N]
+
+
+def cheb_backward(c, M):
+    N = c.shape[0]
+    y = np.zeros((M,) + c.shape[1:], dtype=c.dtype)
+    sign = (-1.0) ** np.arange(N)
+    y[:N] = c * sign.reshape((N,) + (1,) * (c.ndim - 1))
+    y[0] *= 2
+    y *= M
+    return sfft.idct(y, type=2, axis=0)
+
+
+def rf_forward(f, N):
+    M = f.shape[0]
+    F = np.fft.rfft(f, axis=0) / M
+    K = N // 2
+    c = np.zeros((N,) + f.shape[1:])
+    c[0] = F[0].real
+    c[2:N:2] = 2 * F[1:K].real
+    c[3:N:2] = 2 * F[1:K].imag
+    return c
+
+
+def rf_backward(c, M):
+    N = c.shape[0]
+    K = N // 2
+    F = np.zeros((M // 2 + 1,) + c.shape[1:], dtype=complex)
+    F[0] = c[0]
+    F[1:K] = (c[2:N:2] + 1j * c[3:N:2]) / 2
+    F *= M
+    return np.fft.irfft(F, n=M, axis=0)
+
+
+def _along(fn, a, axis, *args):
+    a = np.moveaxis(a, axis, 0)
+    return np.moveaxis(fn(a, *args), 0, axis)
+
+
+def cheb_diff(c, length):
+    """Chebyshev derivative along axis 0 (spectral.py:53-80), times 2/L."""
+    N = c.shape[0]
+    out = np.zeros_like(c)
+    if N >= 2:
+        out[N - 2] = 2 * (N - 1) * c[N - 1]
+        for n in range(N - 3, -1, -1):
+            out[n] = out[n + 2] + 2 * (n + 1) * c[n + 1]
+        out[0] = out[0] / 2
+    return out * (2.0 / length)
+
+
+def rf_diff(c, length):
+    """RealFourier derivative along axis 0 on (cos, -sin) pairs (spectral.py:214-221)."""
+    N = c.shape[0]
+    k = 2 * np.pi * np.arange(N // 2) / length
+    kk = k.reshape((N // 2,) + (1,) * (c.ndim - 1))
+    out = np.zeros_like(c)
+    out[0::2] = -kk * c[1::2]
+    out[1::2] = kk * c[0::2]
+    return out
+
+
+# ------------------------------------------------------------------------------------------------
+
+class OracleProblem:
+    """A template instantiated on the CPU (``conatus_gb300.template.Problem``) with the maps
+    between the mode layout and the reference's coefficient arrays."""
+
+    def __init__(self, problem):
+        self.P = problem
+        self.tpl = tpl = problem.tpl
+        self.d = len(tpl.fourier_axes)
+        self.ax_sizes = []
+        for i, ax in enumerate(tpl.axes):
+            if ax["kind"] == "RealFourier":
+                self.ax_sizes.append(problem.fourier_sizes[tpl.fourier_axes.index(i)])
+            else:
+                self.ax_sizes.append(ax["N"])
+        # dealiased grids: floor(N * dealias) (the reference's Basis.grid_size)
+        self.grid_sizes = [int(np.floor(s * tpl.axes[i].get("dealias", tpl.axes[i]["M"] / tpl.axes[i]["N"])))
+                           for i, s in enumerate(self.ax_sizes)]
+        self._factors = {}
+
+    # ---- layout maps
+    def _pos_index(self, bi, m, p):
+        """Per-axis index into a coefficient array for Fourier positions p (cos 0 / msin 1) of
+        system m of bucket bi (Chebyshev entry left as None)."""
+        idx = []
+        mode = self.P.modes[bi][m]
+        for i, ax in enumerate(self.tpl.axes):
+            if ax["kind"] == "RealFourier":
+                j = self.tpl.fourier_axes.index(i)
+                idx.append(2 * int(mode[j]) + int(p[j]) if mode[j] > 0 else 0)
+            else:
+                idx.append(None)
+        return idx
+
+    def _weights(self, bi):
+        """[(p, w_s(p))] over the Fourier positions of bucket bi's active directions."""
+        b = self.tpl.buckets[bi]
+        act = [j for j in range(self.d) if b.active[j]]
+        out = []
+        for q in itertools.product((0, 1), repeat=len(act)):
+            p = [0] * self.d
+            w = 1.0 + 0j
+            for jj, j in enumerate(act):
+                p[j] = q[jj]
+                s = b.sign if j == 1 else 1
+                w *= (1j * s) ** q[jj]
+            out.append((tuple(p), w))
+        return out
+
+    def _shape(self, obj):
+        sh = list(obj["shape"])
+        rank = obj["rank"]
+        for i in range(len(self.tpl.axes)):
+            if sh[rank + i] > 1:
+                sh[rank + i] = self.ax_sizes[i]
+        return tuple(sh)
+
+    @staticmethod
+    def _index(shape, rank, comp, base, n):
+        """Index of (component, Fourier positions ``base``, Chebyshev index n) in an object's
+        coefficient array (size-1 axes: the object does not depend on that coordinate)."""
+        idx = list(comp)
+        for a, bpos in enumerate(base):
+            size = shape[rank + a]
+            if bpos is None:                      # Chebyshev axis
+                idx.append(n if (size > 1 and n >= 0) else 0)
+            else:
+                idx.append(bpos if size > 1 else 0)
+        return tuple(idx)
+
+    def to_arrays(self, C):
+        """Mode layout -> coefficient arrays of the variables (system.scatter)."""
+        tpl = self.tpl
+        arrs = [np.zeros(self._shape(v)) for v in tpl.variables]
+        for bi, b in enumerate(tpl.buckets):
+            da = self.P.d_active(bi)
+            scale = 2.0 ** (1 - da) if da >= 1 else 1.0
+            Cb = C[bi]
+            for p, w in self._weights(bi):
+                coef = scale * np.conj(w)
+                for m in range(Cb.shape[0]):
+                    base = self._pos_index(bi, m, p)
+                    for i in range(b.n):
+                        v, cf, n = b.col[i]
+                        var = tpl.variables[v]
+                        rank = var["rank"]
+                        comp = np.unravel_index(cf, tuple(var["shape"][:rank])) if rank else ()
+                        arrs[v][self._index(arrs[v].shape, rank, comp, base, n)] += (coef * Cb[m, i]).real
+        return arrs
+
+    def to_rows(self, eq_arrays):
+        """Equation coefficient arrays (Chebyshev T) -> mode-layout right-hand sides, each row
+        converted to its equation's C^(lambda) space (system.gather_rhs + complex view)."""
+        tpl = self.tpl
+        ca = tpl.cheb_axis
+        conv_cache = {}
+        out = []
+        for bi, b in enumerate(tpl.buckets):
+            R = np.zeros((self.P.nsys[bi], b.n), np.complex128)
+            wts = self._weights(bi)
+            for i in range(b.n):
+                e, cf, n, lam = b.row[i]
+                arr = eq_arrays[e]
+                if arr is None:
+                    continue
+                eqd = tpl.equations[e]
+                rank = eqd["rank"]
+                if lam > 0 and ca >= 0 and arr.shape[rank + ca] > 1:
+                    key = (e, lam)
+                    if key not in conv_cache:
+                        S = tpl.conv[int(lam)]
+                        conv_cache[key] = np.moveaxis(
+                            np.tensordot(S, np.moveaxis(arr, rank + ca, 0), axes=(1, 0)), 0, rank + ca)
+                    arr = conv_cache[key]
+                comp = np.unravel_index(cf, tuple(eqd["shape"][:rank])) if rank else ()
+                for m in range(R.shape[0]):
+                    acc = 0j
+                    for p, w in wts:
+                        acc += w * arr[self._index(arr.shape, rank, comp, self._pos_index(bi, m, p), n)]
+                    R[m, i] = acc
+            out.append(R)
+        return out
+
+    # ---- F
+    def factor_arrays(self, C):
+        tpl = self.tpl
+        arrs = self.to_arrays(C)
+        G = []
+        for v, cf, orders in tpl.factors:
+            var = tpl.variables[v]
+            a = arrs[v]
+            if var["rank"]:
+                a = a.reshape((-1,) + a.shape[var["rank"]:])[cf]
+            for ax, o in enumerate(orders):
+                for _ in range(o):
+                    if tpl.axes[ax]["kind"] == "Chebyshev":
+                        a = _along(cheb_diff, a, ax, tpl.axes[ax]["L"])
+                    else:
+                        a = _along(rf_diff, a, ax, tpl.axes[ax]["L"])
+            G.append(a)
+        return G
+
+    def F(self, C):
+        """Nonlinear part (polynomial form) + constant part F(0), mode layout."""
+        tpl = self.tpl
+        G = self.factor_arrays(C)
+        order = [i for i, ax in enumerate(tpl.axes) if ax["kind"] == "Chebyshev"] + \
+                [i for i, ax in enumerate(tpl.axes) if ax["kind"] != "Chebyshev"]
+        grids = []
+        for g in G:
+            for ax in order:
+                fn = cheb_backward if tpl.axes[ax]["kind"] == "Chebyshev" else rf_backward
+                g = _along(fn, g, ax, self.grid_sizes[ax])
+            grids.append(g)
+        eq_arrays = [None] * len(tpl.equations)
+        for e, cf, monos in tpl.outputs:
+            acc = np.zeros(grids[0].shape if grids else tuple(self.grid_sizes))
+            for c, fs in monos:
+                t = c.real if np.imag(c) == 0 else c
+                for j in fs:
+                    t = t * grids[j]
+                acc = acc + t
+            for ax in order[::-1]:
+                fn = cheb_forward if tpl.axes[ax]["kind"] == "Chebyshev" else rf_forward
+                acc = _along(fn, acc, ax, self.ax_sizes[ax])
+            eqd = tpl.equations[e]
+            if eq_arrays[e] is None:
+                eq_arrays[e] = np.zeros(self._shape(eqd))
+            rank = eqd["rank"]
+            if rank:
+                comp = np.unravel_index(cf, tuple(eqd["shape"][:rank]))
+                eq_arrays[e][comp] = acc
+            else:
+                eq_arrays[e][...] = acc
+        R = self.to_rows(eq_arrays)
+        b0 = self.P.b0_dense()
+        return [r + c for r, c in zip(R, b0)]
+
+    # ---- linear algebra
+    def csr(self, bi, which, m):
+        b = self.tpl.buckets[bi]
+        vals = self._vals(bi, which)[m]
+        return sp.csr_matrix((vals, b.indices, b.indptr), shape=(b.n, b.n))
+
+    def _vals(self, bi, which):
+        key = ("vals", bi, which)
+        if key not in self._factors:
+            self._factors[key] = self.P.values(bi, which)
+        return self._factors[key]
+
+    def MX(self, C):
+        out = []
+        for bi, b in enumerate(self.tpl.buckets):
+            V = self._vals(bi, "M")
+            rows = b.coo_rows()
+            Y = np.zeros_like(C[bi])
+            for m in range(C[bi].shape[0]):
+                np.add.at(Y[m], rows, V[m] * C[bi][m, b.indices])
+            out.append(Y)
+        return out
+
+    def factor(self, a, b_):
+        key = ("lu", float(a), float(b_))
+        if key not in self._factors:
+            fs = []
+            for bi, b in enumerate(self.tpl.buckets):
+                Vm, Vl = self._vals(bi, "M"), self._vals(bi, "L")
+                mats = []
+                for m in range(Vm.shape[0]):
+                    vals = a * Vm[m] + b_ * Vl[m]
+                    if b.kind == "real":
+                        vals = vals.real
+                    mats.append((b.n, b.indptr, b.indices, vals))
+                dt = np.float64 if b.kind == "real" else np.complex128
+                fs.append(BorderedBandedBatch(mats, list(range(b.r)), dtype=dt))
+            self._factors[key] = fs
+        return self._factors[key]
+
+    def solve(self, a, b_, rhs):
+        out = []
+        for bi, (B, r) in enumerate(zip(self.factor(a, b_), rhs)):
+            if self.tpl.buckets[bi].kind == "real":
+                out.append(B.solve(r.real).astype(np.complex128))
+            else:
+                out.append(B.solve(r))
+        return out
+
+
+class SBDFStepper:
+    """``IVPSolver`` SBDF-q stepping on the mode layout (integrator.py:361-373), lower-order
+    start-up (q = 1, 2, .. while the history fills)."""
+
+    def __init__(self, oproblem, order, dt):
+        self.op, self.order, self.dt = oproblem, int(order), float(dt)
+        self.MXh, self.Fh = deque(), deque()
+
+    def step(self, C):
+        op, dt = self.op, self.dt
+        self.MXh.appendleft(op.MX(C))
+        self.Fh.appendleft(op.F(C))
+        while len(self.MXh) > self.order:
+            self.MXh.pop()
+            self.Fh.pop()
+        q = min(self.order, len(self.MXh))
+        a, c = SBDF[q]
+        rhs = []
+        for bi in range(len(C)):
+            r = np.zeros_like(C[bi])
+            for j in range(1, q + 1):
+                r += c[j] * self.Fh[j - 1][bi] - (a[j] / dt) * self.MXh[j - 1][bi]
+            rhs.append(r)
+        return op.solve(a[0] / dt, 1.0, rhs)

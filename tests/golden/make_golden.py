@@ -132,10 +132,77 @@ def banded_fixtures(cn, out_dir, rng):
             arrays[p + "x"] = x
             arrays[p + "xt"] = xt
             arrays[p + "band"] = np.array([info["kl"], info["ku"]], np.int32)
+            arrays[p + "cond"] = np.array([np.linalg.cond(A.toarray()) for A in mats])
             labels.append(f"{label}|n={n}|r={nb}|kl={info['kl']}|ku={info['ku']}")
         arrays["labels"] = np.array(labels)
         np.savez_compressed(os.path.join(out_dir, f"banded_{name}.npz"), **arrays)
         print(name, labels)
+
+
+def step_fixtures(cn, out_dir, rng):
+    """Step fixtures (``step_<case>.npz``): the reference's IVPSolver (fused F, complexify=True)
+    from a seeded smooth state, a few start-up steps to fill the SBDF history, then one recorded
+    step: X_n, the M X and F history, F(X_n) and X_{n+1} (reference real layout), with the maps
+    between that layout and the mode layout of the problem template, and the reference's own M, L
+    values. ``Xn1_perturbed``: the reference's X_{n+1} from X_n perturbed by about one ulp (three
+    seeds) -- the spread of the reference's own arithmetic, the floor below which two correct
+    FP64 implementations cannot be told apart."""
+    from conatus_gb300.problems import make_problems as mp
+    from conatus_gb300.reference_adapter import reference_maps, scatter_state, template_from_solver
+    cases = [("burgers128", "burgers_n128"), ("rb32x16", "rb_nz16_32"), ("channel8x17x8", "channel_ny17_8")]
+    builds = {
+        "burgers128": ("burgers", dict(N=128, scheme="SBDF2", dt=1e-4), {}),
+        "rb32x16": ("rayleigh_benard", dict(N=(32, 16), scheme="SBDF2", dt=1e-4), dict(Ra=1e6, Pr=1.0)),
+        "channel8x17x8": ("channel", dict(N=(8, 17, 8), scheme="SBDF3", dt=5e-3), dict(Re=4000.0)),
+    }
+    for name, _ in cases:
+        fn, kw, params = builds[name]
+        sim = globals()[fn](cn, **params).simulate(complexify=True, f_backend="fused", **kw)
+        s = sim.solver
+        tpl = template_from_solver(s, name, params=params, exact_values=True)
+        maps = reference_maps(s)
+        P = tpl.instantiate()
+        # seeded smooth state in the mode layout: decay with the Chebyshev index
+        C = []
+        for bi, b in enumerate(tpl.buckets):
+            n_idx = np.maximum(b.col[:, 2], 0)
+            amp = 0.05 * np.exp(-0.35 * n_idx)
+            z = rng.standard_normal((P.nsys[bi], b.n)) + (0 if b.kind == "real" else 1j) * rng.standard_normal((P.nsys[bi], b.n))
+            C.append(z * amp)
+        X0 = scatter_state(C, maps, s.system.n)
+        s.X = X0.astype(s.system.dtype)
+        s.t, s.iteration = 0.0, 0
+        s._reset_history()
+        for _ in range(3):
+            s.step()
+        Xn = np.array(s.X)
+        MXh = [np.array(v) for v in s._MXh]
+        Fh = [np.array(v) for v in s._Fh]
+        Fn = np.array(s.F(s.X, s.t))
+        state = (np.array(s.X), s.t, s.iteration, list(s._MXh), list(s._Fh))
+        s.step()
+        Xn1 = np.array(s.X)
+        # the reference's own rounding floor: the same step from X_n perturbed by ~1 ulp
+        floors = []
+        for trial in range(3):
+            s.X = state[0] * (1 + 2.0 ** -52 * rng.standard_normal(state[0].shape))
+            s.t, s.iteration = state[1], state[2]
+            s._MXh.clear(); s._MXh.extend(state[3])
+            s._Fh.clear(); s._Fh.extend(state[4])
+            s.step()
+            floors.append(np.array(s.X))
+        arrays = dict(Xn=Xn, Xn1=Xn1, Fn=Fn, MXh=np.stack(MXh), Fh=np.stack(Fh), dt=kw["dt"],
+                      order=int(kw["scheme"][-1]), nb=len(maps), Xn1_perturbed=np.stack(floors))
+        for bi, m in enumerate(maps):
+            p = f"m{bi}_"
+            arrays[p + "cols"] = m["cols"].astype(np.int32)
+            arrays[p + "rows"] = m["rows"].astype(np.int32)
+            arrays[p + "wc"] = m["wc"]
+            arrays[p + "wr"] = m["wr"]
+            arrays[p + "dact"] = m["dact"]
+            arrays[p + "Mv"], arrays[p + "Lv"] = tpl.buckets[bi].exact
+        np.savez_compressed(os.path.join(out_dir, f"step_{name}.npz"), **arrays)
+        print(name, "N_u", s.system.n, "history", len(MXh))
 
 
 def main():
@@ -147,6 +214,8 @@ def main():
     rng = np.random.default_rng(20261203)
     if args.only in ("", "banded"):
         banded_fixtures(cn, HERE, rng)
+    if args.only in ("", "step"):
+        step_fixtures(cn, HERE, np.random.default_rng(7))
 
 
 if __name__ == "__main__":

