@@ -39,6 +39,19 @@ _SIGS = {
     "cng_banded_prepare_transpose": [P, P],
     "cng_banded_solve_transpose": [P, P, P],
     "cng_banded_solve_host": [P, P, P, c_int],
+    "cng_rhs_create": [P, P],
+    "cng_rhs_destroy": [P],
+    "cng_rhs_evaluate": [P, P, P, P],
+    "cng_rhs_workspace_bytes": [P, P],
+    "cng_cheb_transform": [c_int, P, P, ctypes.c_int64, c_int, c_int, P],
+    "cng_fft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],
+    "cng_rfft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],
+    "cng_csr_matvec": [c_int, c_int, P, P, P, c_int, P, P, P],
+    "cng_sbdf_rhs": [c_int, P, P, P, P, P, ctypes.c_int64, P],
+    "cng_graph_begin": [P],
+    "cng_graph_end": [P, P],
+    "cng_graph_launch": [P, P],
+    "cng_graph_destroy": [P],
 }
 _RESTYPES = {"cng_last_error": c_char_p, "cng_version": c_char_p}
 

@@ -53,4 +53,53 @@ int cng_mem_info(uint64_t* free_bytes, uint64_t* total_bytes) {
     return 0;
 }
 
+struct cng_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+int cng_graph_begin(void* stream) {
+    CNG_TRY({
+        if (!stream) throw cng::InvalidArgument("graph capture needs a non-default stream");
+        CNG_CUDA(cudaStreamBeginCapture(static_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal));
+    })
+}
+
+int cng_graph_end(void* stream, cng_graph** out) {
+    CNG_TRY({
+        if (!out) throw cng::InvalidArgument("null output");
+        *out = nullptr;
+        auto* g = new cng_graph();
+        cudaError_t e = cudaStreamEndCapture(static_cast<cudaStream_t>(stream), &g->graph);
+        if (e != cudaSuccess) {
+            delete g;
+            CNG_CUDA(e);
+        }
+        e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g->graph);
+            delete g;
+            CNG_CUDA(e);
+        }
+        *out = g;
+    })
+}
+
+int cng_graph_launch(cng_graph* g, void* stream) {
+    CNG_TRY({
+        if (!g) throw cng::InvalidArgument("null graph");
+        CNG_CUDA(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+    })
+}
+
+int cng_graph_destroy(cng_graph* g) {
+    CNG_TRY({
+        if (g) {
+            if (g->exec) cudaGraphExecDestroy(g->exec);
+            if (g->graph) cudaGraphDestroy(g->graph);
+            delete g;
+        }
+    })
+}
+
 }  // extern "C"

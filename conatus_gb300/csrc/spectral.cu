@@ -1,0 +1,893 @@
+// Pseudospectral explicit right-hand side F(X) on the mode layout, and the transform kernels.
+//
+// F is the reference's polynomial form (python/conatus/timestep/fused.py:524-537):
+// out_o = sum_m c_m prod_j f_j over the 3/2-dealiased grid, f_j = derivatives of state components,
+// then projected back (truncation) and converted to each equation's C^(lambda) rows
+// (system.py:910-931). Pipeline for Fourier (x[, z]) x Chebyshev (y):
+//
+//   unpack   state (mode layout) -> factor spectra S[f][jx][jz][n]: complex-view amplitudes scaled
+//            to FFT coefficients (1, 1/2, 1/4 for 0, 1, 2 nonzero Fourier indices), Fourier
+//            derivatives (i k)^o, Chebyshev derivative by the backward recurrence (as a suffix scan)
+//   cheb_bwd Chebyshev N -> My Gauss points along y (DCT-III by Makhoul's length-My FFT)
+//   fft_z    complex inverse FFT along z (compact fftfreq spectrum -> Mz points)     [2 directions]
+//   irfft_x  Hermitian half spectrum -> Mx real points along x (two columns per complex FFT)
+//   products out_o(x, z, y)
+//   rfft_x, fft_z (forward, truncation = dealias projection), cheb_fwd (DCT-II, My -> N)
+//   pack     rows: 2^d_act * C^(lambda) conversion of the output coefficients + constant part F(0)
+//
+// The Chebyshev grid My is any even size >= the reference's floor(3N/2): Gauss quadrature on My
+// points is exact for the degree of the dealiased products, so the projected coefficients are the
+// reference's (to rounding) and My can be FFT-friendly (193 -> 200 for N = 129).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "conatus_gb300.h"
+#include "fft.cuh"
+
+namespace cng {
+
+static constexpr int kFftThreads = 256;
+static constexpr size_t kFftSmemMax = 200 * 1024;
+
+FftPlan make_plan(int L) {
+    FftPlan p;
+    p.L = L;
+    p.nstages = 0;
+    int r = L;
+    const int order[] = {8, 4, 2, 3, 5};
+    for (int rad : order) {
+        while (r % rad == 0) {
+            if (p.nstages >= 12) throw InvalidArgument("FFT length has too many factors");
+            p.radix[p.nstages++] = rad;
+            r /= rad;
+        }
+    }
+    if (r != 1 || L < 1)
+        throw InvalidArgument("FFT length " + std::to_string(L) + " must be 2^a 3^b 5^c");
+    return p;
+}
+
+// ---- twiddle tables (host double precision, uploaded once per length and precision) ----------
+// kind 0: exp(-2 pi i q / L), q < L (FFT twiddles); kind 1: exp(-i pi k / (2L)), k < L (the
+// Makhoul post-twiddles of the Chebyshev transforms). Angles reduced in long double.
+template <class R>
+struct TwiddleCache {
+    std::mutex mu;
+    std::vector<std::pair<long long, c2<R>*>> tables;
+    const c2<R>* get(int L, int kind = 0) {
+        std::lock_guard<std::mutex> lock(mu);
+        const long long key = (long long)L * 2 + kind;
+        for (auto& t : tables)
+            if (t.first == key) return t.second;
+        std::vector<c2<R>> h(L);
+        const long double pi = 3.14159265358979323846264338327950288L;
+        for (int q = 0; q < L; ++q) {
+            const long double ang = kind == 0 ? -2.0L * pi * q / L : -pi * q / (2.0L * L);
+            h[q].x = static_cast<R>(cosl(ang));
+            h[q].y = static_cast<R>(sinl(ang));
+        }
+        c2<R>* d = nullptr;
+        CNG_CUDA(cudaMalloc(&d, sizeof(c2<R>) * L));
+        CNG_CUDA(cudaMemcpy(d, h.data(), sizeof(c2<R>) * L, cudaMemcpyHostToDevice));
+        tables.push_back({key, d});
+        return d;
+    }
+};
+template <class R>
+TwiddleCache<R>& twiddles() {
+    static TwiddleCache<R> c;
+    return c;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Chebyshev transforms of contiguous complex columns (Makhoul; conventions of the reference's
+// reference/transforms.py:117-121,158-164: Gauss nodes t_j = -cos(pi (j + 1/2) / M)).
+
+// backward: c[0..N) -> f[0..M): f_j = sum_n c_n T_n(t_j).
+template <class R>
+__global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
+                           FftPlan plan, int B, const c2<R>* __restrict__ tw_g,
+                           const c2<R>* __restrict__ tq_g) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int M = plan.L;
+    c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
+    c2<R>* tq = tw + M;
+    c2<R>* b0 = tq + M;
+    c2<R>* b1 = b0 + (size_t)B * M;
+    c2<R>* a = b1 + (size_t)B * M;     // staging of the coefficients (B x (M + 1))
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int q = tid; q < M; q += nt) {
+        tw[q] = tw_g[q];
+        tq[q] = tq_g[q];
+    }
+    const long long col0 = (long long)blockIdx.x * B;
+    for (int e = tid; e < B * (M + 1); e += nt) {
+        const int t = e / (M + 1), k = e - t * (M + 1);
+        const long long col = col0 + t;
+        c2<R> v = mk<R>(0, 0);
+        if (col < ncols && k < N) {
+            v = in[col * N + k];
+            if (k & 1) v = mk<R>(-v.x, -v.y);          // a_k = c_k (-1)^k
+        }
+        a[e] = v;
+    }
+    __syncthreads();
+    // Z_k = 1/2 e^{i pi k / (2M)} (a_k - i a_{M-k}), Z_0 = a_0
+    for (int e = tid; e < B * M; e += nt) {
+        const int t = e / M, k = e - t * M;
+        const c2<R>* at = a + (size_t)t * (M + 1);
+        c2<R> z;
+        if (k == 0) {
+            z = at[0];
+        } else {
+            c2<R> u = at[k], w = at[M - k];
+            c2<R> d = mk<R>(u.x + w.y, u.y - w.x);     // a_k - i a_{M-k}
+            z = scl<R>(R(0.5), mul<R>(conjg<R>(tq[k]), d));   // e^{+i pi k / (2M)}
+        }
+        b0[e] = z;
+    }
+    __syncthreads();
+    c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, +1);
+    // f_{2j} = z_j, f_{2j+1} = z_{M-1-j}
+    for (int e = tid; e < B * M; e += nt) {
+        const int t = e / M, j = e - t * M;
+        const long long col = col0 + t;
+        if (col >= ncols) continue;
+        const int src = (j & 1) ? (M - 1 - (j >> 1)) : (j >> 1);
+        out[col * M + j] = r[(size_t)t * M + src];
+    }
+}
+
+// forward: f[0..M) -> c[0..N): c_k = (2/M) sum_j f_j T_k(t_j), halved at k = 0 (DCT-II / M).
+template <class R>
+__global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
+                           FftPlan plan, int B, const c2<R>* __restrict__ tw_g,
+                           const c2<R>* __restrict__ tq_g) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int M = plan.L;
+    c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
+    c2<R>* tq = tw + M;
+    c2<R>* b0 = tq + M;
+    c2<R>* b1 = b0 + (size_t)B * M;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int q = tid; q < M; q += nt) {
+        tw[q] = tw_g[q];
+        tq[q] = tq_g[q];
+    }
+    const long long col0 = (long long)blockIdx.x * B;
+    // v_j = f_{2j}, v_{M-1-j} = f_{2j+1}
+    for (int e = tid; e < B * M; e += nt) {
+        const int t = e / M, i = e - t * M;
+        const long long col = col0 + t;
+        c2<R> v = mk<R>(0, 0);
+        if (col < ncols) v = in[col * M + i];
+        const int dst = (i & 1) ? (M - 1 - (i >> 1)) : (i >> 1);
+        b0[(size_t)t * M + dst] = v;
+    }
+    __syncthreads();
+    c2<R>* Z = smem_fft<R>(b0, b1, plan, B, tw, -1);
+    const R invM = R(1) / R(M);
+    for (int e = tid; e < B * N; e += nt) {
+        const int t = e / N, k = e - t * N;
+        const long long col = col0 + t;
+        if (col >= ncols) continue;
+        const c2<R>* Zt = Z + (size_t)t * M;
+        c2<R> zk = Zt[k], zm = conjg<R>(Zt[k == 0 ? 0 : M - k]);
+        const c2<R> w = tq[k];                         // e^{-i pi k / (2M)}
+        R re = mul<R>(w, add<R>(zk, zm)).x;
+        R im = mul<R>(w, sub<R>(zk, zm)).y;
+        R sg = (k & 1) ? -invM : invM;
+        if (k == 0) sg *= R(0.5);
+        out[col * N + k] = mk<R>(re * sg, im * sg);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// complex FFT along a strided axis: data [outer][len][inner]. Backward: compact spectrum of Nc
+// entries (fftfreq order, Nyquist entry Nc/2 ignored) -> L grid points, unnormalized inverse.
+// Forward: L points -> compact Nc (|k| < Nc/2, Nyquist set to 0), scaled 1/L.
+template <class R>
+__global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long outer, int inner,
+                           int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int L = plan.L;
+    c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
+    c2<R>* b0 = tw + L;
+    c2<R>* b1 = b0 + (size_t)B * L;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
+    const int chunks = (inner + B - 1) / B;
+    const long long o = blockIdx.x / chunks;
+    const int i0 = (blockIdx.x - o * chunks) * B;
+    const int K = Nc / 2;
+    const int lin = forward ? L : Nc;
+    const int lout = forward ? Nc : L;
+    const c2<R>* src = in + o * (long long)lin * inner;
+    c2<R>* dst = out + o * (long long)lout * inner;
+    if (!forward) {
+        for (int e = tid; e < B * L; e += nt) b0[e] = mk<R>(0, 0);
+        __syncthreads();
+        for (int e = tid; e < B * Nc; e += nt) {
+            const int k = e / B, t = e - k * B;
+            if (i0 + t >= inner || k == K) continue;
+            const int slot = k < K ? k : L - (Nc - k);
+            b0[(size_t)t * L + slot] = src[(long long)k * inner + i0 + t];
+        }
+    } else {
+        for (int e = tid; e < B * L; e += nt) {
+            const int k = e / B, t = e - k * B;
+            b0[(size_t)t * L + k] = (i0 + t < inner) ? src[(long long)k * inner + i0 + t] : mk<R>(0, 0);
+        }
+    }
+    __syncthreads();
+    c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, forward ? -1 : +1);
+    if (!forward) {
+        for (int e = tid; e < B * L; e += nt) {
+            const int k = e / B, t = e - k * B;
+            if (i0 + t < inner) dst[(long long)k * inner + i0 + t] = r[(size_t)t * L + k];
+        }
+    } else {
+        const R invL = R(1) / R(L);
+        for (int e = tid; e < B * Nc; e += nt) {
+            const int k = e / B, t = e - k * B;
+            if (i0 + t >= inner) continue;
+            c2<R> v = mk<R>(0, 0);
+            if (k != K) v = scl<R>(invL, r[(size_t)t * L + (k < K ? k : L - (Nc - k))]);
+            dst[(long long)k * inner + i0 + t] = v;
+        }
+    }
+}
+
+// Real FFT along the outer axis of [outer][len][inner] (inner even): two adjacent inner columns
+// per complex FFT. Backward (c2r): half spectrum [outer][K][inner] complex (modes 0..K-1,
+// Hermitian continuation, zero padding) -> [outer][L][inner] real, unnormalized. Forward (r2c):
+// real -> modes 0..K-1, scaled 1/L.
+template <class R>
+__global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out_, long long outer, int inner,
+                            int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int L = plan.L;
+    c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
+    c2<R>* b0 = tw + L;
+    c2<R>* b1 = b0 + (size_t)B * L;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
+    const int pairs = inner / 2;
+    const int chunks = (pairs + B - 1) / B;
+    const long long o = blockIdx.x / chunks;
+    const int p0 = (blockIdx.x - o * chunks) * B;     // first pair
+    if (!forward) {
+        const c2<R>* src = static_cast<const c2<R>*>(in_) + o * (long long)K * inner;
+        R* dst = static_cast<R*>(out_) + o * (long long)L * inner;
+        for (int e = tid; e < B * L; e += nt) b0[e] = mk<R>(0, 0);
+        __syncthreads();
+        // Z_k = A_k + i B_k, Z_{L-k} = conj(A_k) + i conj(B_k)
+        for (int e = tid; e < B * K; e += nt) {
+            const int k = e / B, t = e - k * B;
+            const int p = p0 + t;
+            if (p >= pairs) continue;
+            c2<R> A = src[(long long)k * inner + 2 * p];
+            c2<R> Bv = src[(long long)k * inner + 2 * p + 1];
+            if (k == 0) {
+                b0[(size_t)t * L] = mk<R>(A.x - Bv.y, A.y + Bv.x);
+            } else {
+                b0[(size_t)t * L + k] = mk<R>(A.x - Bv.y, A.y + Bv.x);
+                b0[(size_t)t * L + L - k] = mk<R>(A.x + Bv.y, -A.y + Bv.x);
+            }
+        }
+        __syncthreads();
+        c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, +1);
+        for (int e = tid; e < B * L; e += nt) {
+            const int j = e / B, t = e - j * B;
+            const int p = p0 + t;
+            if (p >= pairs) continue;
+            c2<R> z = r[(size_t)t * L + j];
+            R* d = dst + (long long)j * inner + 2 * p;
+            d[0] = z.x;
+            d[1] = z.y;
+        }
+    } else {
+        const R* src = static_cast<const R*>(in_) + o * (long long)L * inner;
+        c2<R>* dst = static_cast<c2<R>*>(out_) + o * (long long)K * inner;
+        for (int e = tid; e < B * L; e += nt) {
+            const int j = e / B, t = e - j * B;
+            const int p = p0 + t;
+            c2<R> z = mk<R>(0, 0);
+            if (p < pairs) {
+                const R* s = src + (long long)j * inner + 2 * p;
+                z = mk<R>(s[0], s[1]);
+            }
+            b0[(size_t)t * L + j] = z;
+        }
+        __syncthreads();
+        c2<R>* Z = smem_fft<R>(b0, b1, plan, B, tw, -1);
+        const R h = R(0.5) / R(L);
+        for (int e = tid; e < B * K; e += nt) {
+            const int k = e / B, t = e - k * B;
+            const int p = p0 + t;
+            if (p >= pairs) continue;
+            c2<R> zk = Z[(size_t)t * L + k];
+            c2<R> zm = conjg<R>(Z[(size_t)t * L + (k == 0 ? 0 : L - k)]);
+            c2<R> A = scl<R>(h, add<R>(zk, zm));
+            c2<R> d = sub<R>(zk, zm);                      // B = d / (2i)
+            c2<R> Bv = mk<R>(h * d.y, -h * d.x);
+            dst[(long long)k * inner + 2 * p] = A;
+            dst[(long long)k * inner + 2 * p + 1] = Bv;
+        }
+    }
+}
+
+
+// ------------------------------------------------------------------------------------------------
+// F pipeline: descriptors on the device
+
+struct RhsDev {
+    int ndir, Kx, Nzc, Ny, nfactors, noutputs, nbuckets;
+    double lx, lz, ly;
+    const int* factors;        // nfactors x 5: var, comp, ox, oy, oz
+    const int* out_lam;        // noutputs: lambda (0: no conversion)
+    const int* out_mono_ptr;   // noutputs + 1
+    const double* mono_coef;   // per monomial
+    const int* mono_fac;       // per monomial: 4 factor ids (-1 pad)
+    const double* conv;        // per lambda 1..: (Ny x Ny) dense, conv + (lam - 1) Ny Ny
+    const int* conv_bw;        // per lambda: upper bandwidth of the conversion
+};
+
+struct BucketDev {
+    int nsys, n, dact, sign, real;
+    long long offset;          // complex elements into the state / rows
+    const int* modes;          // nsys x 2
+    const int* colpos;         // nfactors x Ny
+    const int* rowmap;         // n x 2: output index (-1: none), Chebyshev index
+};
+
+// Spectral slot of mode (jx, jz, sign) along the compact z axis.
+__device__ __forceinline__ int zslot(int jz, int sign, int Nzc) {
+    return (jz == 0 || sign > 0) ? jz : Nzc - jz;
+}
+
+// one warp per system: state -> factor spectra (with derivatives), complex<R> output
+template <class R>
+__global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ state, c2<R>* __restrict__ S) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    const int m = blockIdx.x * nw + wib;
+    if (m >= b.nsys) return;
+    const int Ny = d.Ny;
+    double2* x = reinterpret_cast<double2*>(sm) + (size_t)wib * (b.n + 2 * Ny);
+    double2* col = x + b.n;
+    double2* der = col + Ny;
+    const double2* src = state + b.offset + (long long)m * b.n;
+    for (int i = lane; i < b.n; i += 32) x[i] = src[i];
+    __syncwarp();
+    const int jx = b.modes[2 * m], jz = b.modes[2 * m + 1];
+    const double kx = 6.283185307179586476925286766559 * jx / d.lx;
+    const double kz = b.sign * 6.283185307179586476925286766559 * jz / d.lz;
+    const double w = b.dact == 0 ? 1.0 : (b.dact == 1 ? 0.5 : 0.25);
+    const int slot = zslot(jz, b.sign, d.Nzc);
+    for (int f = 0; f < d.nfactors; ++f) {
+        const int* fd = d.factors + 5 * f;
+        const int ox = fd[2], oy = fd[3], oz = fd[4];
+        const int* cp = b.colpos + (size_t)f * Ny;
+        for (int nn = lane; nn < Ny; nn += 32) {
+            const int pos = cp[nn];
+            col[nn] = pos >= 0 ? x[pos] : make_double2(0.0, 0.0);
+        }
+        __syncwarp();
+        // Chebyshev derivative oy times: out[n] = out[n+2] + 2 (n+1) c[n+1], out[0] /= 2, x 2/L
+        for (int rep = 0; rep < oy; ++rep) {
+            if (lane < 2) {
+                const int par = lane;                 // chain of entries n with n % 2 == par
+                int start = Ny - 2;
+                if ((start & 1) != par) start -= 1;
+                double2 acc = make_double2(0.0, 0.0);
+                if (Ny - 1 >= 0 && ((Ny - 1) & 1) == par) der[Ny - 1] = make_double2(0.0, 0.0);
+                for (int nn = start; nn >= 0; nn -= 2) {
+                    const double t = 2.0 * (nn + 1);
+                    acc.x = acc.x + t * col[nn + 1].x;
+                    acc.y = acc.y + t * col[nn + 1].y;
+                    der[nn] = acc;
+                }
+            }
+            __syncwarp();
+            const double sc = 2.0 / d.ly;
+            for (int nn = lane; nn < Ny; nn += 32) {
+                double2 v = der[nn];
+                if (nn == 0) { v.x = v.x / 2; v.y = v.y / 2; }
+                col[nn] = make_double2(v.x * sc, v.y * sc);
+            }
+            __syncwarp();
+        }
+        // Fourier derivatives and the amplitude scale: w (i kx)^ox (i kz)^oz
+        double fr = w, fi = 0.0;
+        for (int q = 0; q < ox; ++q) { double t = fr; fr = -fi * kx; fi = t * kx; }
+        for (int q = 0; q < oz; ++q) { double t = fr; fr = -fi * kz; fi = t * kz; }
+        c2<R>* dst;
+        c2<R>* dstc = nullptr;
+        if (d.ndir == 2) {
+            dst = S + (((long long)f * d.Kx + jx) * d.Nzc + slot) * Ny;
+            if (jx == 0 && jz > 0) dstc = S + (((long long)f * d.Kx) * d.Nzc + (d.Nzc - jz)) * Ny;
+        } else if (d.ndir == 1) {
+            dst = S + ((long long)f * d.Kx + jx) * Ny;
+        } else {
+            dst = S + (long long)f * Ny;
+        }
+        for (int nn = lane; nn < Ny; nn += 32) {
+            const double2 c = col[nn];
+            double vr = fr * c.x - fi * c.y, vi = fr * c.y + fi * c.x;
+            if (b.real) vi = 0.0;
+            dst[nn] = mk<R>(R(vr), R(vi));
+            if (dstc) dstc[nn] = mk<R>(R(vr), R(-vi));
+        }
+        __syncwarp();
+    }
+}
+
+// products on the grid: out_o = sum_m c_m prod_j G_j
+template <class R>
+__global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P;
+         p += (long long)gridDim.x * blockDim.x) {
+        R g[16];
+        for (int f = 0; f < d.nfactors && f < 16; ++f) g[f] = G[(long long)f * P + p];
+        for (int o = 0; o < d.noutputs; ++o) {
+            R acc = R(0);
+            for (int mi = d.out_mono_ptr[o]; mi < d.out_mono_ptr[o + 1]; ++mi) {
+                R t = R(d.mono_coef[mi]);
+                const int* fs = d.mono_fac + 4 * mi;
+                for (int q = 0; q < 4; ++q)
+                    if (fs[q] >= 0) t = t * g[fs[q]];
+                acc = acc + t;
+            }
+            O[(long long)o * P + p] = acc;
+        }
+    }
+}
+
+// one warp per system: output spectra -> rows (C^(lambda) conversion, 2^d_act, real buckets real)
+template <class R>
+__global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, double2* __restrict__ rows) {
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    const int m = blockIdx.x * nw + wib;
+    if (m >= b.nsys) return;
+    const int Ny = d.Ny;
+    const int jx = b.modes[2 * m], jz = b.modes[2 * m + 1];
+    const int slot = zslot(jz, b.sign, d.Nzc);
+    const double sc = (double)(1 << b.dact);
+    double2* dst = rows + b.offset + (long long)m * b.n;
+    for (int i = lane; i < b.n; i += 32) {
+        const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
+        double2 v = make_double2(0.0, 0.0);
+        if (o >= 0) {
+            const c2<R>* h;
+            if (d.ndir == 2) h = H + (((long long)o * d.Kx + jx) * d.Nzc + slot) * Ny;
+            else if (d.ndir == 1) h = H + ((long long)o * d.Kx + jx) * Ny;
+            else h = H + (long long)o * Ny;
+            const int lam = d.out_lam[o];
+            if (lam <= 0) {
+                v = make_double2((double)h[nn].x, (double)h[nn].y);
+            } else {
+                const double* cv = d.conv + (size_t)(lam - 1) * Ny * Ny + (size_t)nn * Ny;
+                const int hi = min(Ny - 1, nn + d.conv_bw[lam - 1]);
+                double ar = 0.0, ai = 0.0;
+                for (int k = nn; k <= hi; ++k) {
+                    ar += cv[k] * (double)h[k].x;
+                    ai += cv[k] * (double)h[k].y;
+                }
+                v = make_double2(ar, ai);
+            }
+            v.x *= sc;
+            v.y *= sc;
+            if (b.real) v.y = 0.0;
+        }
+        dst[i] = v;
+    }
+}
+
+// constant part of F: rows[idx] += value
+__global__ void k_add_sparse(double2* rows, const long long* idx, const double2* val, long long n) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        double2 r = rows[idx[q]];
+        rows[idx[q]] = make_double2(r.x + val[q].x, r.y + val[q].y);
+    }
+}
+
+template <class R>
+__global__ void k_realpart(const c2<R>* __restrict__ in, R* __restrict__ out, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[i].x;
+}
+template <class R>
+__global__ void k_complexify(const R* __restrict__ in, c2<R>* __restrict__ out, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = mk<R>(in[i], R(0));
+}
+template <class R>
+void realpart_kernel_launch(const c2<R>* in, R* out, long long n, cudaStream_t st) {
+    k_realpart<R><<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(in, out, n);
+    CNG_LAUNCH("k_realpart");
+}
+template <class R>
+void complexify_kernel_launch(const R* in, void* out, long long n, cudaStream_t st) {
+    k_complexify<R><<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(in, static_cast<c2<R>*>(out), n);
+    CNG_LAUNCH("k_complexify");
+}
+
+// ------------------------------------------------------------------------------------------------
+// host: transform launchers
+
+template <class R>
+static void set_smem_attr(const void* fn) {
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax);
+}
+
+template <class R>
+static int pick_B(int L, int extra_per_col, int maxB) {
+    const size_t per = sizeof(c2<R>) * (size_t)(2 * L + extra_per_col);
+    int B = (int)std::max<size_t>(1, (kFftSmemMax - sizeof(c2<R>) * 2 * (size_t)L) / per);
+    return std::max(1, std::min(B, maxB));
+}
+
+template <class R>
+void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st) {
+    if (ncols <= 0) return;
+    static std::once_flag f1, f2;
+    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_cheb_bwd<R>); });
+    std::call_once(f2, [] { set_smem_attr<R>((const void*)k_cheb_fwd<R>); });
+    if (M % 2) throw InvalidArgument("Chebyshev grid size must be even");
+    FftPlan plan = make_plan(M);
+    const c2<R>* tw = twiddles<R>().get(M, 0);
+    const c2<R>* tq = twiddles<R>().get(M, 1);
+    const int B = pick_B<R>(M, forward ? 0 : M + 1, 16);
+    const size_t smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
+    const long long blocks = (ncols + B - 1) / B;
+    if (forward) k_cheb_fwd<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
+    else k_cheb_bwd<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
+    CNG_LAUNCH("k_cheb");
+}
+
+template <class R>
+void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, int Nc, int L, bool forward,
+                     cudaStream_t st) {
+    if (outer <= 0 || inner <= 0) return;
+    static std::once_flag f1;
+    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_fft_axis<R>); });
+    FftPlan plan = make_plan(L);
+    const c2<R>* tw = twiddles<R>().get(L, 0);
+    const int B = pick_B<R>(L, 0, 16);
+    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * L);
+    const long long blocks = outer * ((inner + B - 1) / B);
+    k_fft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
+    CNG_LAUNCH("k_fft_axis");
+}
+
+template <class R>
+void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int K, int L, bool forward,
+                      cudaStream_t st) {
+    if (outer <= 0 || inner <= 0) return;
+    if (inner % 2) throw InvalidArgument("real FFT along the outer axis needs an even inner size");
+    static std::once_flag f1;
+    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
+    FftPlan plan = make_plan(L);
+    const c2<R>* tw = twiddles<R>().get(L, 0);
+    const int B = pick_B<R>(L, 0, 16);
+    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * L);
+    const long long blocks = outer * ((inner / 2 + B - 1) / B);
+    k_rfft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
+    CNG_LAUNCH("k_rfft_axis");
+}
+
+// ------------------------------------------------------------------------------------------------
+// the F pipeline object
+
+template <class P>
+static P* upload(const P* h, size_t n) {
+    P* d = nullptr;
+    CNG_CUDA(cudaMalloc(&d, std::max<size_t>(sizeof(P) * n, 16)));
+    if (n) CNG_CUDA(cudaMemcpy(d, h, sizeof(P) * n, cudaMemcpyHostToDevice));
+    return d;
+}
+
+struct Rhs {
+    int precision = 0;         // 0 = FP64 transforms and products, 1 = FP32
+    int ndir = 0, nx = 0, nz = 0, mx = 1, mz = 1, ny = 1, my = 1;
+    int Kx = 1, Nzc = 1;
+    double lx = 1, lz = 1, ly = 2;
+    int nfactors = 0, noutputs = 0;
+    RhsDev dev{};
+    std::vector<BucketDev> buckets;
+    std::vector<void*> owned;
+    long long nb0 = 0;
+    long long* b0_idx = nullptr;
+    double2* b0_val = nullptr;
+    // work buffers
+    void* S = nullptr;     // factor spectra after unpack / output spectra before pack
+    void* W1 = nullptr;
+    void* W2 = nullptr;
+    size_t S_bytes = 0, W_bytes = 0;
+
+    ~Rhs() {
+        for (void* p : owned) cudaFree(p);
+    }
+    template <class P> P* keep(P* p) { owned.push_back((void*)p); return p; }
+
+    long long spec_cols(int nfields) const {      // Chebyshev columns of the spectral arrays
+        return (long long)nfields * (ndir >= 1 ? Kx : 1) * (ndir == 2 ? Nzc : 1);
+    }
+    long long grid_points() const { return (long long)(ndir >= 1 ? mx : 1) * (ndir == 2 ? mz : 1) * my; }
+
+    template <class R>
+    void run(const double2* state, double2* rows, cudaStream_t st);
+};
+
+template <class R>
+void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
+    using C = c2<R>;
+    const int nf = nfactors, no = noutputs;
+    C* Sp = static_cast<C*>(S);
+    // 1. unpack (one warp per system)
+    for (const auto& b : buckets) {
+        if (b.nsys == 0) continue;
+        const int nw = 4;
+        const size_t smem = (size_t)nw * (b.n + 2 * ny) * sizeof(double2);
+        k_unpack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, state, Sp);
+        CNG_LAUNCH("k_unpack");
+    }
+    // 2. Chebyshev backward along y: S [cols][ny] -> W1 [cols][my]
+    C* A = static_cast<C*>(W1);
+    C* Bf = static_cast<C*>(W2);
+    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st);
+    C* cur = A;
+    C* other = Bf;
+    // 3. z backward: [nf Kx][Nzc][my] -> [nf Kx][mz][my]
+    if (ndir == 2) {
+        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st);
+        std::swap(cur, other);
+    }
+    // 4. x backward (c2r): [nf][Kx][inner] -> [nf][mx][inner] real
+    const long long inner = (long long)(ndir == 2 ? mz : 1) * my;
+    R* G = reinterpret_cast<R*>(cur);
+    if (ndir >= 1) {
+        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st);
+        G = reinterpret_cast<R*>(other);
+        std::swap(cur, other);
+    } else {
+        // no Fourier direction: the grid values are complex with zero imaginary part; compact them
+        // to reals in place of the c2r step (real buckets only, so the imaginary part is zero)
+        G = reinterpret_cast<R*>(cur);
+    }
+    // 5. products: G [nf][P] -> O [no][P] (real)
+    const long long P = grid_points();
+    R* O = reinterpret_cast<R*>(other);
+    if (ndir == 0) {
+        // complex grid values -> real: O_tmp holds reals of the factors
+        R* Gr = reinterpret_cast<R*>(S);
+        const long long n = (long long)nf * P;
+        realpart_kernel_launch<R>(reinterpret_cast<const C*>(G), Gr, n, st);
+        G = Gr;
+    }
+    {
+        const int threads = 256;
+        const long long blocks = std::min<long long>((P + threads - 1) / threads, 152LL * 16);
+        k_products<R><<<(unsigned)blocks, threads, 0, st>>>(dev, G, O, P);
+        CNG_LAUNCH("k_products");
+    }
+    std::swap(cur, other);           // cur = O
+    // 6. x forward (r2c): [no][mx][inner] -> [no][Kx][inner]
+    if (ndir >= 1) {
+        launch_rfft_axis<R>(cur, other, no, (int)inner, Kx, mx, true, st);
+        std::swap(cur, other);
+    } else {
+        complexify_kernel_launch<R>(reinterpret_cast<const R*>(cur), other, (long long)no * P, st);
+        std::swap(cur, other);
+    }
+    // 7. z forward: [no Kx][mz][my] -> [no Kx][Nzc][my]
+    if (ndir == 2) {
+        launch_fft_axis<R>(cur, other, (long long)no * Kx, my, Nzc, mz, true, st);
+        std::swap(cur, other);
+    }
+    // 8. Chebyshev forward: [cols][my] -> S [cols][ny]
+    launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st);
+    // 9. pack rows and add the constant part
+    for (const auto& b : buckets) {
+        if (b.nsys == 0) continue;
+        const int nw = 4;
+        k_pack<R><<<ceil_div(b.nsys, nw), 32 * nw, 0, st>>>(dev, b, Sp, rows);
+        CNG_LAUNCH("k_pack");
+    }
+    if (nb0) {
+        k_add_sparse<<<ceil_div(nb0, 256), 256, 0, st>>>(rows, b0_idx, b0_val, nb0);
+        CNG_LAUNCH("k_add_sparse");
+    }
+}
+
+}  // namespace cng
+
+// ================================================================================================
+// C-ABI
+
+using namespace cng;
+
+static Rhs* build_rhs(const cng_rhs_desc* D) {
+    if (!D) throw InvalidArgument("null descriptor");
+    auto h = std::make_unique<Rhs>();
+    h->precision = D->precision;
+    if (D->precision != 0 && D->precision != 1) throw InvalidArgument("precision must be 0 (FP64) or 1 (FP32)");
+    h->ndir = D->ndir;
+    if (D->ndir < 0 || D->ndir > 2) throw InvalidArgument("0, 1 or 2 Fourier directions");
+    h->nx = D->nx; h->nz = D->nz; h->mx = D->mx; h->mz = D->mz; h->ny = D->ny; h->my = D->my;
+    h->lx = D->lx; h->lz = D->lz; h->ly = D->ly;
+    if (h->ny < 1 || h->my < h->ny || h->my % 2) throw InvalidArgument("Chebyshev grid my must be even and >= ny");
+    if (h->ndir >= 1) {
+        if (h->nx % 2 || h->mx < h->nx) throw InvalidArgument("Fourier sizes: nx even, mx >= nx");
+        h->Kx = h->nx / 2;
+        make_plan(h->mx);
+    }
+    if (h->ndir == 2) {
+        if (h->nz % 2 || h->mz < h->nz) throw InvalidArgument("Fourier sizes: nz even, mz >= nz");
+        h->Nzc = h->nz;
+        make_plan(h->mz);
+    }
+    make_plan(h->my);
+    h->nfactors = D->nfactors;
+    h->noutputs = D->noutputs;
+    if (h->nfactors < 1 || h->nfactors > 16) throw InvalidArgument("1 to 16 factors");
+    if (h->noutputs < 1) throw InvalidArgument("at least one output");
+    RhsDev& dv = h->dev;
+    dv.ndir = h->ndir; dv.Kx = h->Kx; dv.Nzc = h->Nzc; dv.Ny = h->ny;
+    dv.nfactors = h->nfactors; dv.noutputs = h->noutputs; dv.nbuckets = D->nbuckets;
+    dv.lx = h->lx; dv.lz = h->lz; dv.ly = h->ly;
+    dv.factors = h->keep(upload(D->factors, (size_t)5 * h->nfactors));
+    dv.out_lam = h->keep(upload(D->out_lam, (size_t)h->noutputs));
+    dv.out_mono_ptr = h->keep(upload(D->out_mono_ptr, (size_t)h->noutputs + 1));
+    const int nmono = D->out_mono_ptr[h->noutputs];
+    for (int mi = 0; mi < 4 * nmono; ++mi)
+        if (D->mono_factors[mi] >= h->nfactors) throw InvalidArgument("monomial factor id out of range");
+    dv.mono_coef = h->keep(upload(D->mono_coef, (size_t)nmono));
+    dv.mono_fac = h->keep(upload(D->mono_factors, (size_t)4 * nmono));
+    int maxlam = 0;
+    for (int o = 0; o < h->noutputs; ++o) maxlam = std::max(maxlam, D->out_lam[o]);
+    if (maxlam > D->nlam) throw InvalidArgument("output lambda without a conversion matrix");
+    std::vector<int> bw(std::max(1, D->nlam), 0);
+    for (int l = 0; l < D->nlam; ++l) {
+        const double* cv = D->conv + (size_t)l * h->ny * h->ny;
+        for (int i = 0; i < h->ny; ++i)
+            for (int k = 0; k < h->ny; ++k)
+                if (cv[(size_t)i * h->ny + k] != 0.0) {
+                    if (k < i) throw InvalidArgument("conversion matrices must be upper triangular");
+                    bw[l] = std::max(bw[l], k - i);
+                }
+    }
+    dv.conv = h->keep(upload(D->conv, (size_t)std::max(1, D->nlam) * h->ny * h->ny * (D->nlam ? 1 : 0)));
+    dv.conv_bw = h->keep(upload(bw.data(), bw.size()));
+    for (int bi = 0; bi < D->nbuckets; ++bi) {
+        const int* bd = D->buckets + 5 * bi;
+        BucketDev b{};
+        b.nsys = bd[0]; b.n = bd[1]; b.dact = bd[2]; b.sign = bd[3]; b.real = bd[4];
+        b.offset = D->bucket_offset[bi];
+        for (int m = 0; m < b.nsys; ++m) {
+            const int jx = D->modes[bi][2 * m], jz = D->modes[bi][2 * m + 1];
+            if (jx < 0 || (h->ndir >= 1 && jx >= h->Kx) || jz < 0 || (h->ndir == 2 && jz >= h->Nzc / 2))
+                throw InvalidArgument("mode index out of range");
+        }
+        for (int q = 0; q < h->nfactors * h->ny; ++q)
+            if (D->colpos[bi][q] >= b.n) throw InvalidArgument("column position out of range");
+        for (int i = 0; i < b.n; ++i)
+            if (D->rowmap[bi][2 * i] >= h->noutputs || D->rowmap[bi][2 * i + 1] >= h->ny)
+                throw InvalidArgument("row map out of range");
+        b.modes = h->keep(upload(D->modes[bi], (size_t)2 * b.nsys));
+        b.colpos = h->keep(upload(D->colpos[bi], (size_t)h->nfactors * h->ny));
+        b.rowmap = h->keep(upload(D->rowmap[bi], (size_t)2 * b.n));
+        h->buckets.push_back(b);
+    }
+    h->nb0 = D->nb0;
+    if (h->nb0) {
+        h->b0_idx = h->keep(upload(reinterpret_cast<const long long*>(D->b0_index), (size_t)h->nb0));
+        h->b0_val = h->keep(upload(reinterpret_cast<const double2*>(D->b0_value), (size_t)h->nb0));
+    }
+    // work buffers
+    const size_t cs = h->precision ? sizeof(float2) : sizeof(double2);
+    const size_t rs = cs / 2;
+    const int nfo = std::max(h->nfactors, h->noutputs);
+    const long long Kx = h->ndir >= 1 ? h->Kx : 1, Nzc = h->ndir == 2 ? h->Nzc : 1;
+    const long long mx = h->ndir >= 1 ? h->mx : 1, mz = h->ndir == 2 ? h->mz : 1;
+    const long long P = h->grid_points();
+    h->S_bytes = std::max<size_t>(cs * nfo * Kx * Nzc * h->ny, rs * h->nfactors * P);
+    size_t w = 0;
+    w = std::max<size_t>(w, cs * nfo * Kx * Nzc * h->my);
+    w = std::max<size_t>(w, cs * nfo * Kx * mz * h->my);
+    w = std::max<size_t>(w, rs * nfo * mx * mz * h->my);
+    w = std::max<size_t>(w, cs * nfo * P);
+    h->W_bytes = w;
+    CNG_CUDA(cudaMalloc(&h->S, h->S_bytes));
+    h->keep(h->S);
+    CNG_CUDA(cudaMalloc(&h->W1, w));
+    h->keep(h->W1);
+    CNG_CUDA(cudaMalloc(&h->W2, w));
+    h->keep(h->W2);
+    // the Nyquist and padding slots of the spectra are never written: zero them once
+    CNG_CUDA(cudaMemset(h->S, 0, h->S_bytes));
+    CNG_CUDA(cudaMemset(h->W1, 0, w));
+    CNG_CUDA(cudaMemset(h->W2, 0, w));
+    static std::once_flag f;
+    std::call_once(f, [] {
+        cudaFuncSetAttribute(k_unpack<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_unpack<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    return h.release();
+}
+
+extern "C" {
+
+int cng_rhs_create(const cng_rhs_desc* desc, cng_rhs** out) {
+    CNG_TRY({
+        if (!out) throw InvalidArgument("null output handle");
+        *out = nullptr;
+        *out = reinterpret_cast<cng_rhs*>(build_rhs(desc));
+    })
+}
+
+int cng_rhs_destroy(cng_rhs* h) {
+    CNG_TRY({ delete reinterpret_cast<Rhs*>(h); })
+}
+
+int cng_rhs_evaluate(cng_rhs* hh, const void* state, void* rows, void* stream) {
+    CNG_TRY({
+        Rhs* h = reinterpret_cast<Rhs*>(hh);
+        if (!h) throw InvalidArgument("null RHS handle");
+        if (!state || !rows) throw InvalidArgument("null device pointer");
+        if (state == rows) throw InvalidArgument("state and rows must not alias");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (h->precision == 0) h->run<double>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
+        else h->run<float>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
+    })
+}
+
+int cng_rhs_workspace_bytes(const cng_rhs* hh, uint64_t* bytes) {
+    CNG_TRY({
+        const Rhs* h = reinterpret_cast<const Rhs*>(hh);
+        if (!h || !bytes) throw InvalidArgument("null argument");
+        *bytes = h->S_bytes + 2 * h->W_bytes;
+    })
+}
+
+// Standalone transforms on caller-owned device memory (complex128 columns / axes).
+int cng_cheb_transform(int forward, const void* in, void* out, int64_t ncols, int n, int m, void* stream) {
+    CNG_TRY({
+        if (!in || !out) throw InvalidArgument("null device pointer");
+        if (n < 1 || m < n) throw InvalidArgument("need 1 <= n <= m");
+        launch_cheb<double>(static_cast<const double2*>(in), static_cast<double2*>(out), ncols, n, m,
+                            forward != 0, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_fft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int ncompact, int length,
+                 void* stream) {
+    CNG_TRY({
+        if (!in || !out) throw InvalidArgument("null device pointer");
+        if (ncompact % 2 || ncompact > length) throw InvalidArgument("compact size must be even and <= length");
+        launch_fft_axis<double>(static_cast<const double2*>(in), static_cast<double2*>(out), outer, inner,
+                                ncompact, length, forward != 0, static_cast<cudaStream_t>(stream));
+    })
+}
+
+int cng_rfft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int nmodes, int length,
+                  void* stream) {
+    CNG_TRY({
+        if (!in || !out) throw InvalidArgument("null device pointer");
+        if (nmodes < 1 || 2 * (nmodes - 1) >= length) throw InvalidArgument("need 2 (nmodes - 1) < length");
+        launch_rfft_axis<double>(in, out, outer, inner, nmodes, length, forward != 0,
+                                 static_cast<cudaStream_t>(stream));
+    })
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// Pieces of the IMEX step on the mode layout: M X per bucket and the SBDF right-hand side.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "conatus_gb300.h"
+
+namespace cng {
+
+// one warp per (system, row chunk): y[m][i] = sum_p M[i, p] x[m][col p]
+__global__ void k_csr_matvec(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
+                             const double2* __restrict__ val, int per_sys, const double2* __restrict__ x,
+                             double2* __restrict__ y) {
+    const long long total = (long long)nsys * n;
+    const int nnz = ip[n];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long m = t / n;
+        const int i = (int)(t - m * n);
+        const double2* xm = x + m * n;
+        const double2* v = val + (per_sys ? m * nnz : 0);
+        double ar = 0.0, ai = 0.0;
+        for (int p = ip[i]; p < ip[i + 1]; ++p) {
+            const double2 a = v[p], b = xm[ix[p]];
+            ar += a.x * b.x - a.y * b.y;
+            ai += a.x * b.y + a.y * b.x;
+        }
+        y[t] = make_double2(ar, ai);
+    }
+}
+
+struct SbdfArgs {
+    int q;
+    double c[4], d[4];
+    const double* F[4];
+    const double* MX[4];
+};
+
+// rhs = sum_j (c_j F_j - d_j MX_j) on real and imaginary parts, explicit roundings in the order of
+// the reference's sbdf_rhs (a = 0; a = a + (c F - d MX)).
+__global__ void k_sbdf_rhs(SbdfArgs a, double* __restrict__ rhs, long long count) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int j = 0; j < a.q; ++j)
+            acc = __dadd_rn(acc, __dsub_rn(__dmul_rn(a.c[j], a.F[j][t]), __dmul_rn(a.d[j], a.MX[j][t])));
+        rhs[t] = acc;
+    }
+}
+
+}  // namespace cng
+
+using namespace cng;
+
+extern "C" {
+
+int cng_csr_matvec(int nsys, int n, const int32_t* indptr, const int32_t* indices, const void* values,
+                   int values_per_system, const void* x, void* y, void* stream) {
+    CNG_TRY({
+        if (!indptr || !indices || !values || !x || !y) throw InvalidArgument("null device pointer");
+        if (x == y) throw InvalidArgument("x and y must not alias");
+        if (nsys <= 0 || n <= 0) return CNG_OK;
+        const long long total = (long long)nsys * n;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+        k_csr_matvec<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            nsys, n, indptr, indices, static_cast<const double2*>(values), values_per_system,
+            static_cast<const double2*>(x), static_cast<double2*>(y));
+        CNG_LAUNCH("k_csr_matvec");
+    })
+}
+
+int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
+                 void* rhs, int64_t count, void* stream) {
+    CNG_TRY({
+        if (q < 1 || q > 4) throw InvalidArgument("SBDF order must be 1..4");
+        if (!c || !d || !F || !MX || !rhs) throw InvalidArgument("null argument");
+        SbdfArgs a{};
+        a.q = q;
+        for (int j = 0; j < q; ++j) {
+            a.c[j] = c[j];
+            a.d[j] = d[j];
+            a.F[j] = static_cast<const double*>(F[j]);
+            a.MX[j] = static_cast<const double*>(MX[j]);
+            if (!a.F[j] || !a.MX[j]) throw InvalidArgument("null history vector");
+        }
+        const long long n = 2 * count;      // complex entries -> doubles
+        const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 32);
+        k_sbdf_rhs<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<double*>(rhs), n);
+        CNG_LAUNCH("k_sbdf_rhs");
+    })
+}
+
+}  // extern "C"

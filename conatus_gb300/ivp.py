@@ -1,0 +1,436 @@
+"""IMEX time stepping on the GB300: the reference's ``IVPSolver`` SBDF path on the mode layout.
+
+``DeviceProblem`` places a problem (``template.Problem``) on the device: the explicit right-hand
+side F as one ``cng_rhs`` evaluator, M of every bucket for ``M X``, and the factorizations of
+``a M + b L`` (one ``cng_banded`` handle per bucket and per (a, b), assembled on the device from the
+wavenumber polynomials, or from the reference's own values when the problem carries them).
+
+``IVPSolver`` mirrors python/conatus/timestep/integrator.py:129-771 for the SBDF family:
+``step()`` is ``_sbdf_step`` (integrator.py:361-373) -- M X and F(X) of the current state pushed
+on the history, ``rhs = sum_j c_j F_j - (a_j/dt) M X_j`` (lincomb.py:146-162) with the
+lower-order start-up of ``startup="lower_order"``, then ``(a_0/dt M + L) X = rhs`` -- and
+``run_graph(n)`` replays whole steps as CUDA graphs (integrator.py:781-920). State, history and
+factors stay resident in HBM; nothing is copied to the host inside a step.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+from .core import _Handle
+from .errors import CudaError
+
+SBDF = {1: ([1, -1], [0, 1]),
+        2: ([1.5, -2, 0.5], [0, 2, -1]),
+        3: ([11 / 6, -3, 1.5, -1 / 3], [0, 3, -3, 1]),
+        4: ([25 / 12, -4, 3, -4 / 3, 0.25], [0, 4, -6, 4, -1])}
+
+P32 = ctypes.POINTER(ctypes.c_int32)
+
+
+def smooth_size(m: int, even: bool = False) -> int:
+    """Smallest n >= m whose prime factors are 2, 3 and 5 (even if requested)."""
+    n = max(1, int(m))
+    while True:
+        k = n
+        for p in (2, 3, 5):
+            while k % p == 0:
+                k //= p
+        if k == 1 and (not even or n % 2 == 0):
+            return n
+        n += 1
+
+
+class RhsDesc(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("ndir", ctypes.c_int32), ("nx", ctypes.c_int32),
+                ("nz", ctypes.c_int32), ("mx", ctypes.c_int32), ("mz", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("my", ctypes.c_int32),
+                ("lx", ctypes.c_double), ("lz", ctypes.c_double), ("ly", ctypes.c_double),
+                ("nfactors", ctypes.c_int32), ("noutputs", ctypes.c_int32),
+                ("factors", ctypes.c_void_p), ("out_lam", ctypes.c_void_p),
+                ("out_mono_ptr", ctypes.c_void_p), ("mono_coef", ctypes.c_void_p),
+                ("mono_factors", ctypes.c_void_p), ("nbuckets", ctypes.c_int32),
+                ("buckets", ctypes.c_void_p), ("bucket_offset", ctypes.c_void_p),
+                ("modes", ctypes.c_void_p), ("colpos", ctypes.c_void_p), ("rowmap", ctypes.c_void_p),
+                ("nlam", ctypes.c_int32), ("conv", ctypes.c_void_p), ("nb0", ctypes.c_int64),
+                ("b0_index", ctypes.c_void_p), ("b0_value", ctypes.c_void_p)]
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise CudaError("conatus_gb300 needs a CUDA device (there is no CPU fallback)")
+    return torch
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        return _torch().cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class DeviceProblem:
+    """A problem instance resident on the device (see module docstring)."""
+
+    def __init__(self, problem, precision: str = "fp64", device: str = "cuda"):
+        torch = _torch()
+        _lib.lib()
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.P = problem
+        self.tpl = tpl = problem.tpl
+        self.precision = precision
+        self.device = torch.device(device)
+        self.d = len(tpl.fourier_axes)
+        self.nsys = list(problem.nsys)
+        self.offsets = []
+        off = 0
+        for b, ns in zip(tpl.buckets, self.nsys):
+            self.offsets.append(off)
+            off += ns * b.n
+        self.n_total = off
+        self._build_rhs()
+        # M of every bucket (constant across the bucket when it does not depend on k)
+        self._M, self._pat = [], []
+        for bi, b in enumerate(tpl.buckets):
+            ip = torch.as_tensor(b.indptr.astype(np.int32), device=self.device)
+            ix = torch.as_tensor(b.indices.astype(np.int32), device=self.device)
+            self._pat.append((ip, ix))
+            if b.m_is_constant() and b.exact is None:
+                t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
+                self._M.append((torch.as_tensor(b.Mc[t0].astype(np.complex128), device=self.device), 0))
+            else:
+                self._M.append((torch.as_tensor(problem.values(bi, "M"), device=self.device).contiguous(), 1))
+        self._L = [None] * len(tpl.buckets)
+        self._factors = {}
+
+    # ------------------------------------------------------------------ F
+    def _build_rhs(self):
+        tpl, P = self.tpl, self.P
+        d = self.d
+        ax = tpl.axes
+        fa = tpl.fourier_axes
+        ca = tpl.cheb_axis
+        desc = RhsDesc()
+        desc.precision = 0 if self.precision == "fp64" else 1
+        desc.ndir = d
+        keep = []
+
+        def arr(a, dtype):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a.ctypes.data
+
+        if d >= 1:
+            desc.nx = P.fourier_sizes[0]
+            desc.mx = smooth_size(int(math.floor(P.fourier_sizes[0] * ax[fa[0]].get("dealias", 1.5))))
+            desc.lx = ax[fa[0]]["L"]
+        if d >= 2:
+            desc.nz = P.fourier_sizes[1]
+            desc.mz = smooth_size(int(math.floor(P.fourier_sizes[1] * ax[fa[1]].get("dealias", 1.5))))
+            desc.lz = ax[fa[1]]["L"]
+        if ca >= 0:
+            desc.ny = ax[ca]["N"]
+            desc.my = smooth_size(ax[ca]["M"], even=True)
+            desc.ly = ax[ca]["L"]
+        else:
+            desc.ny, desc.my, desc.ly = 1, 1, 1.0
+        self.grid = dict(mx=desc.mx, mz=desc.mz, my=desc.my)
+
+        def axis_orders(orders):
+            ox = orders[fa[0]] if d >= 1 else 0
+            oz = orders[fa[1]] if d >= 2 else 0
+            oy = orders[ca] if ca >= 0 else 0
+            return ox, oy, oz
+
+        facs = np.array([[v, c, *axis_orders(a)] for v, c, a in tpl.factors], np.int32).reshape(-1, 5)
+        desc.nfactors = facs.shape[0]
+        desc.factors = arr(facs, np.int32)
+        # outputs: lambda from the rows of their equation
+        lam_of = {}
+        for b in tpl.buckets:
+            for e, c, n, lam in b.row:
+                if n >= 0:
+                    lam_of[(int(e), int(c))] = max(int(lam), 0)
+        outs = tpl.outputs
+        desc.noutputs = len(outs)
+        desc.out_lam = arr([lam_of.get((e, c), 0) for e, c, _ in outs], np.int32)
+        ptr, coef, mf = [0], [], []
+        for e, c, monos in outs:
+            for co, fs in monos:
+                if len(fs) > 4:
+                    raise NotImplementedError("monomials of more than 4 factors")
+                if complex(co).imag != 0:
+                    raise NotImplementedError("complex monomial coefficients")
+                coef.append(complex(co).real)
+                mf.append(list(fs) + [-1] * (4 - len(fs)))
+            ptr.append(len(coef))
+        desc.out_mono_ptr = arr(ptr, np.int32)
+        desc.mono_coef = arr(coef if coef else [0.0], np.float64)
+        desc.mono_factors = arr(mf if mf else [[-1] * 4], np.int32)
+        out_index = {(e, c): o for o, (e, c, _) in enumerate(outs)}
+        nb = len(tpl.buckets)
+        desc.nbuckets = nb
+        bd, modes_p, col_p, row_p = [], [], [], []
+        ny = desc.ny
+        for bi, b in enumerate(tpl.buckets):
+            bd.append([P.nsys[bi], b.n, P.d_active(bi), b.sign, 1 if b.kind == "real" else 0])
+            md = np.zeros((P.nsys[bi], 2), np.int32)
+            if d >= 1:
+                md[:, 0] = P.modes[bi][:, 0]
+            if d >= 2:
+                md[:, 1] = P.modes[bi][:, 1]
+            modes_p.append(arr(md, np.int32))
+            cp = -np.ones((facs.shape[0], ny), np.int32)
+            for f, (v, c, *_o) in enumerate(facs):
+                for i, (cv, cc, cn) in enumerate(b.col):
+                    if cv == v and cc == c and cn >= 0:
+                        cp[f, cn] = i
+            col_p.append(arr(cp, np.int32))
+            rm = -np.ones((b.n, 2), np.int32)
+            for i, (e, c, n, lam) in enumerate(b.row):
+                o = out_index.get((int(e), int(c)))
+                if o is not None and n >= 0:
+                    rm[i] = (o, n)
+                else:
+                    rm[i] = (-1, 0)
+            row_p.append(arr(rm, np.int32))
+        desc.buckets = arr(bd, np.int32)
+        desc.bucket_offset = arr(self.offsets, np.int64)
+        ptrs = [(ctypes.c_void_p * nb)(*modes_p), (ctypes.c_void_p * nb)(*col_p), (ctypes.c_void_p * nb)(*row_p)]
+        keep.extend(ptrs)
+        desc.modes, desc.colpos, desc.rowmap = (ctypes.cast(p, ctypes.c_void_p).value for p in ptrs)
+        lams = sorted(tpl.conv)
+        if lams and lams != list(range(1, len(lams) + 1)):
+            raise NotImplementedError("conversion levels must be 1..n")
+        desc.nlam = len(lams)
+        desc.conv = arr(np.stack([tpl.conv[l] for l in lams]) if lams else np.zeros(1), np.float64)
+        b0 = P.b0_dense()
+        idx, val = [], []
+        for bi, B0 in enumerate(b0):
+            m, i = np.nonzero(B0)
+            for mm, ii in zip(m, i):
+                idx.append(self.offsets[bi] + mm * tpl.buckets[bi].n + ii)
+                val.append([B0[mm, ii].real, B0[mm, ii].imag])
+        desc.nb0 = len(idx)
+        desc.b0_index = arr(idx if idx else [0], np.int64)
+        desc.b0_value = arr(val if val else [[0.0, 0.0]], np.float64)
+        h = ctypes.c_void_p()
+        call("cng_rhs_create", ctypes.byref(desc), ctypes.byref(h))
+        self._rhs = h
+
+    def F(self, X, out, stream=None) -> None:
+        """out = F(X) (mode layout, complex128 device tensors)."""
+        call("cng_rhs_evaluate", self._rhs, X.data_ptr(), out.data_ptr(), _stream_handle(stream))
+
+    def workspace_bytes(self) -> int:
+        v = ctypes.c_uint64()
+        call("cng_rhs_workspace_bytes", self._rhs, ctypes.byref(v))
+        return int(v.value)
+
+    # ------------------------------------------------------------------ linear algebra
+    def bucket(self, X, bi):
+        b = self.tpl.buckets[bi]
+        o = self.offsets[bi]
+        return X[o:o + self.nsys[bi] * b.n]
+
+    def MX(self, X, out, stream=None) -> None:
+        s = _stream_handle(stream)
+        for bi, b in enumerate(self.tpl.buckets):
+            ip, ix = self._pat[bi]
+            vals, per = self._M[bi]
+            call("cng_csr_matvec", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), vals.data_ptr(), per,
+                 self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
+
+    def _Lvals(self, bi):
+        torch = _torch()
+        if self._L[bi] is None:
+            self._L[bi] = torch.as_tensor(self.P.values(bi, "L"), device=self.device).contiguous()
+        return self._L[bi]
+
+    def factor(self, a: float, b_: float, stream=None):
+        """Factorizations of a M + b L for every bucket (cached per (a, b), as the reference's
+        FactorCache, system.py:58-82)."""
+        key = (float(a), float(b_))
+        f = self._factors.get(key)
+        if f is None:
+            torch = _torch()
+            torch.cuda.synchronize(self.device)    # values below come from torch's stream
+            f = []
+            for bi, b in enumerate(self.tpl.buckets):
+                Mv, per = self._M[bi]
+                Lv = self._Lvals(bi)
+                vals = (a * (Mv if per else Mv.unsqueeze(0)) + b_ * Lv).contiguous()
+                f.append(_Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
+                                        list(range(b.r)), pivot=True, stream=_stream_handle(stream)))
+            self._factors[key] = f
+        return f
+
+    def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
+        """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias)."""
+        s = _stream_handle(stream)
+        for bi, h in enumerate(self.factor(a, b_, stream)):
+            call("cng_banded_solve_mapped", h.h, self.bucket(rhs, bi).data_ptr(), None,
+                 self.bucket(out, bi).data_ptr(), None, s)
+
+    def zeros(self):
+        torch = _torch()
+        return torch.zeros(self.n_total, dtype=torch.complex128, device=self.device)
+
+    # ------------------------------------------------------------------ layout helpers
+    def to_device(self, C_list):
+        torch = _torch()
+        flat = np.concatenate([np.asarray(c, np.complex128).ravel() for c in C_list])
+        return torch.as_tensor(flat, device=self.device)
+
+    def to_host(self, X):
+        x = X.detach().cpu().numpy()
+        return [x[o:o + ns * b.n].reshape(ns, b.n) for o, ns, b in zip(self.offsets, self.nsys, self.tpl.buckets)]
+
+    def __del__(self):
+        h = getattr(self, "_rhs", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().cng_rhs_destroy(h)
+            except Exception:
+                pass
+
+
+class _Graph:
+    def __init__(self, h):
+        self.h = h
+
+    def launch(self, stream):
+        call("cng_graph_launch", self.h, stream)
+
+    def __del__(self):
+        if self.h is not None and self.h.value:
+            try:
+                _lib.lib().cng_graph_destroy(self.h)
+            except Exception:
+                pass
+
+
+class IVPSolver:
+    """SBDF-q time stepper on the device (see module docstring)."""
+
+    def __init__(self, problem, scheme: str = "SBDF2", dt: float = 1e-3, precision: str = "fp64",
+                 device_problem: DeviceProblem | None = None):
+        if scheme not in ("SBDF1", "SBDF2", "SBDF3", "SBDF4"):
+            raise ValueError(f"scheme {scheme!r}: SBDF1..SBDF4")
+        self.scheme, self.dt = scheme, float(dt)
+        self.order = int(scheme[-1])
+        self.dev = device_problem or DeviceProblem(problem, precision)
+        z = self.dev.zeros
+        self.X, self.R = z(), z()
+        self.MXh = [z() for _ in range(self.order)]
+        self.Fh = [z() for _ in range(self.order)]
+        self.filled, self.head = 0, self.order - 1
+        self.t, self.iteration = 0.0, 0
+        self._graphs = {}
+        torch = _torch()
+        self.stream = torch.cuda.Stream()
+
+    def set_state(self, X, t: float = 0.0) -> None:
+        """Initial state (mode layout tensor or list of per-bucket arrays); resets the history."""
+        if isinstance(X, (list, tuple)):
+            X = self.dev.to_device(X)
+        self.X.copy_(X)
+        self.t, self.iteration = float(t), 0
+        self.filled, self.head = 0, self.order - 1
+
+    def set_history(self, MX_list, F_list) -> None:
+        """History of M X and F (newest first), e.g. to continue from another solver's state."""
+        self.filled = len(MX_list)
+        for j, (mx, f) in enumerate(zip(MX_list, F_list)):
+            slot = (self.head - j) % self.order
+            self.MXh[slot].copy_(mx)
+            self.Fh[slot].copy_(f)
+
+    def _push(self, s):
+        self.head = (self.head + 1) % self.order
+        self.dev.MX(self.X, self.MXh[self.head], s)
+        self.dev.F(self.X, self.Fh[self.head], s)
+        self.filled = min(self.filled + 1, self.order)
+
+    def _combine_solve(self, s):
+        q = min(self.order, self.filled)
+        a, c = SBDF[q]
+        slots = [(self.head - j) % self.order for j in range(q)]
+        cs = (ctypes.c_double * q)(*[c[j + 1] for j in range(q)])
+        ds = (ctypes.c_double * q)(*[a[j + 1] / self.dt for j in range(q)])
+        Fp = (ctypes.c_void_p * q)(*[self.Fh[k].data_ptr() for k in slots])
+        Mp = (ctypes.c_void_p * q)(*[self.MXh[k].data_ptr() for k in slots])
+        call("cng_sbdf_rhs", q, cs, ds, Fp, Mp, self.R.data_ptr(), self.dev.n_total, s)
+        self.dev.solve(a[0] / self.dt, 1.0, self.R, self.X, s)
+
+    def _enter(self):
+        torch = _torch()
+        self.stream.wait_stream(torch.cuda.current_stream())
+
+    def _leave(self):
+        torch = _torch()
+        torch.cuda.current_stream().wait_stream(self.stream)
+
+    def step(self) -> None:
+        self._enter()
+        self._step()
+        self._leave()
+
+    def _step(self) -> None:
+        s = _stream_handle(self.stream)
+        q = min(self.order, self.filled + 1)
+        a, _ = SBDF[q]
+        self.dev.factor(a[0] / self.dt, 1.0, s)         # outside the timed/captured work
+        self._push(s)
+        self._combine_solve(s)
+        self.t += self.dt
+        self.iteration += 1
+
+    def run(self, steps: int) -> None:
+        self._enter()
+        for _ in range(int(steps)):
+            self._step()
+        self._leave()
+
+    def run_graph(self, steps: int) -> None:
+        """``steps`` steps; once the history is full, each step is one CUDA graph launch (one graph
+        per position of the history ring, captured on first use)."""
+        s = _stream_handle(self.stream)
+        steps = int(steps)
+        self._enter()
+        while steps > 0 and self.filled < self.order:
+            self._step()
+            steps -= 1
+        if steps <= 0:
+            self._leave()
+            return
+        a, _ = SBDF[self.order]
+        self.dev.factor(a[0] / self.dt, 1.0, s)
+        for _ in range(steps):
+            nxt = (self.head + 1) % self.order
+            g = self._graphs.get(nxt)
+            if g is None:
+                self.stream.synchronize()
+                call("cng_graph_begin", s)
+                head0, filled0 = self.head, self.filled
+                try:
+                    self._push(s)
+                    self._combine_solve(s)
+                finally:
+                    h = ctypes.c_void_p()
+                    call("cng_graph_end", s, ctypes.byref(h))
+                g = self._graphs[nxt] = _Graph(h)
+                self.head, self.filled = head0, filled0     # captured, not run
+            g.launch(s)
+            self.head = nxt
+            self.t += self.dt
+            self.iteration += 1
+        self._leave()
+
+    def synchronize(self) -> None:
+        self.stream.synchronize()

@@ -95,6 +95,98 @@ int cng_banded_solve_transpose(const cng_banded* h, void* b, void* stream);
  * Replaces _core.BorderedBandedBatch{D,Z}.solve (core/bindings/module.cpp:184-206). */
 int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int transpose);
 
+/* ---- pseudospectral explicit right-hand side F(X) ------------------------------------------ */
+
+typedef struct cng_rhs cng_rhs;
+
+/* Description of F in polynomial form on the mode layout (host arrays, copied at creation).
+ * Directions: ndir Fourier directions (0, 1 or 2; sizes nx, nz even, grids mx, mz >= 3/2 of them,
+ * lengths lx, lz) and one Chebyshev direction (ny coefficients, even grid my >= the reference's
+ * floor(3 ny / 2), length ly; without a Chebyshev direction ny = my = 1).
+ * factors[5 f]: variable, component, derivative orders (x, y, z); out_lam[o]: conversion level
+ * lambda of output o (0 = none); out_mono_ptr[o]..out_mono_ptr[o+1]-1: its monomials with
+ * mono_coef[m] and mono_factors[4 m] (factor ids, -1 padded). buckets[5 b]: nsys, n, number of
+ * nonzero Fourier indices, sign of the second direction, real flag; bucket_offset[b]: offset of the
+ * bucket in the state (complex elements); modes[b][2 m]: (jx, jz) of system m; colpos[b][f ny + k]:
+ * solver position of Chebyshev coefficient k of factor f's component (-1: absent);
+ * rowmap[b][2 i]: (output, Chebyshev index) of row i (output -1: no explicit term). conv: nlam
+ * dense ny x ny conversions T -> C^(lambda), lambda = 1..nlam. b0: constant part, nb0 entries
+ * (state index, re, im). precision 0: FP64 transforms and products; 1: FP32. */
+typedef struct {
+    int32_t precision, ndir, nx, nz, mx, mz, ny, my;
+    double lx, lz, ly;
+    int32_t nfactors, noutputs;
+    const int32_t* factors;
+    const int32_t* out_lam;
+    const int32_t* out_mono_ptr;
+    const double* mono_coef;
+    const int32_t* mono_factors;
+    int32_t nbuckets;
+    const int32_t* buckets;
+    const int64_t* bucket_offset;
+    const int32_t* const* modes;
+    const int32_t* const* colpos;
+    const int32_t* const* rowmap;
+    int32_t nlam;
+    const double* conv;
+    int64_t nb0;
+    const int64_t* b0_index;
+    const double* b0_value;
+} cng_rhs_desc;
+
+/* Build the F evaluator (allocates its work buffers). Replaces the reference's compiled F
+ * (FusedRHS, python/conatus/timestep/fused.py:280-343; the GPU 2D pipeline
+ * FourierChebyshev2DRHS, python/conatus/timestep/fc2d.py:433-643). */
+int cng_rhs_create(const cng_rhs_desc* desc, cng_rhs** out);
+int cng_rhs_destroy(cng_rhs* h);
+/* rows = F(state) on the mode layout (complex128 device arrays; must not alias). Capturable.
+ * Replaces IVPSolver.F (python/conatus/timestep/integrator.py:308-348). */
+int cng_rhs_evaluate(cng_rhs* h, const void* state, void* rows, void* stream);
+/* Device bytes of the evaluator's work buffers (admission by footprint). */
+int cng_rhs_workspace_bytes(const cng_rhs* h, uint64_t* bytes);
+
+/* Chebyshev transforms of ncols contiguous complex128 columns on Gauss-Chebyshev nodes:
+ * forward (m grid values -> n coefficients, DCT-II) or backward (n -> m, DCT-III); m even.
+ * Replaces cuda.cheb_forward / cheb_backward (core/bindings/module.cpp:228-239,
+ * core/src/cuda/transforms.cu:79-143). */
+int cng_cheb_transform(int forward, const void* in, void* out, int64_t ncols, int n, int m, void* stream);
+/* Complex FFT along the middle axis of [outer][len][inner] complex128: backward maps a compact
+ * fftfreq-ordered spectrum of ncompact entries to length points (zero padding, unnormalized);
+ * forward maps length points to ncompact coefficients (truncation, 1/length). Replaces
+ * cuda.complexfourier_forward / backward (module.cpp:478-489). */
+int cng_fft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int ncompact,
+                 int length, void* stream);
+/* Real FFT along the middle axis: backward maps nmodes Hermitian half-spectrum modes (complex128)
+ * to length real points; forward maps length real points to nmodes modes (1/length). inner even.
+ * Replaces cuda.rfft / irfft and realfourier_forward / backward (module.cpp:456-477). */
+int cng_rfft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int nmodes,
+                  int length, void* stream);
+
+/* ---- IMEX step pieces ------------------------------------------------------------------------ */
+
+/* y = M x per system of a bucket sharing one CSR pattern (indptr/indices device int32, n rows):
+ * values_per_system = 0 -> one value array shared by every system, else values[m nnz + p].
+ * x, y: (nsys, n) complex128. Replaces system.M @ X (python/conatus/timestep/device.py:78-105). */
+int cng_csr_matvec(int nsys, int n, const int32_t* indptr, const int32_t* indices, const void* values,
+                   int values_per_system, const void* x, void* y, void* stream);
+
+/* rhs = sum_j (c_j F_j - d_j MX_j), j < q, on count complex128 entries (explicit roundings, no
+ * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */
+int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
+                 void* rhs, int64_t count, void* stream);
+
+/* ---- CUDA graphs of whole steps ------------------------------------------------------------- */
+
+typedef struct cng_graph cng_graph;
+
+/* Begin capturing the work launched on `stream` (thread-local capture mode). */
+int cng_graph_begin(void* stream);
+/* End the capture and instantiate it. Replaces the reference's CuPy graph capture of a step
+ * (IVPSolver.run_graph / _capture_graph, python/conatus/timestep/integrator.py:781-920). */
+int cng_graph_end(void* stream, cng_graph** out);
+int cng_graph_launch(cng_graph* g, void* stream);
+int cng_graph_destroy(cng_graph* g);
+
 #ifdef __cplusplus
 }
 #endif
