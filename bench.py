@@ -1,0 +1,291 @@
+"""Benchmark of the IMEX step (the reference's IVPSolver SBDF path) on the GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--config channel|rayleigh_benard|burgers] [--precision fp64|fp32]
+
+Default workload: the 3D plane channel 192 x 129 x 192 (Lx = 4 pi, Lz = 2 pi, Re = 4000), SBDF3,
+dt = 5e-3, FP64, seeded divergence-free initial perturbation (conatus_gb300.workloads). A step is
+one IMEX step of every Fourier mode: M X, the dealiased pseudospectral F, the SBDF right-hand side
+and the batched bordered-banded solves. ``value`` is steps/s of the whole job with the state
+resident in HBM (CUDA events on the stepping stream, max over ranks); ``e2e`` is the same metric
+through the public API with the state copied in from pinned host memory and back out every step.
+N > 1 (torchrun): independent replicas, one per GPU (weak scaling, no collective on the path).
+
+``--impl reference`` times the reference algorithm on the host cores instead: the CPU restatement
+of the reference's IVPSolver step (oracle/ivp.py), on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = {
+    "channel": "IMEX steps/s (3D channel 192x129x192, SBDF3)",
+    "rayleigh_benard": "IMEX steps/s (2D Rayleigh-Benard 256x64, SBDF2)",
+    "burgers": "IMEX steps/s (1D Burgers N=128, SBDF2)",
+}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while active."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows, self.proc, self.gpu = [], None, gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def solve_bytes(dev):
+    """Algorithmic bytes of one solve over every bucket: band LU (ldab n), pivots, V^T and W
+    (2 r n), right-hand side in and solution out (2 n), complex128, per system."""
+    tot = 0
+    a, _ = dev_factor_key(dev)
+    for bi, h in enumerate(dev.factor(*dev_factor_key(dev))):
+        ns, n, r, ldab = h.batch, h.n, h.rank, h.ldab
+        tot += ns * (16 * (ldab * n + 2 * r * n + 2 * n + r * r) + 4 * n)
+    return tot
+
+
+def dev_factor_key(dev):
+    return next(iter(dev._factors))
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ivp import IVPSolver
+    cfg = W.CONFIGS[args.config]
+    P = W.problem(args.config)
+    C0 = W.initial_state(args.config, P, seed=rank)
+    solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=args.precision)
+    dev = solver.dev
+    solver.set_state(C0)
+    solver.run_graph(max(args.warmup, solver.order))            # start-up, capture, warm-up
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- timed region: K steps, state resident in HBM
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(solver.stream)
+        solver.run_graph(args.steps)
+        e1.record(solver.stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * args.steps / (ms / 1e3)
+    finite = bool(torch.isfinite(torch.view_as_real(solver.X)).all().item())
+
+    # ---- per-kernel timing of the dominant pieces (same stream, CUDA events)
+    s = solver.stream
+    reps = 5
+    a0 = dev_factor_key(dev)
+    R = dev.zeros()
+    R.copy_(solver.X)
+    X2 = dev.zeros()
+    torch.cuda.synchronize()
+    ts = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ts[0].record(s)
+    for _ in range(reps):
+        dev.solve(a0[0], a0[1], R, X2, s)
+    ts[1].record(s)
+    for _ in range(reps):
+        dev.F(solver.X, R, s)
+    ts[2].record(s)
+    torch.cuda.synchronize()
+    solve_ms = ts[0].elapsed_time(ts[1]) / reps
+    f_ms = ts[1].elapsed_time(ts[2]) / reps
+    hbm_peak, peak_kind = measured_peaks()
+    sb = solve_bytes(dev)
+    roof = {"kernel": "k_solve (bordered-banded solves of all buckets, one launch per bucket)",
+            "bound": "hbm", "achieved": sb / (solve_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+            "frac": sb / (solve_ms / 1e3) / 1e9 / hbm_peak, "traffic": None,
+            "algorithmic_bytes": sb, "launch_ms": solve_ms, "peak_kind": peak_kind,
+            "F_ms": f_ms}
+
+    # ---- end to end through the public API: host state in and out every step
+    import torch as _t
+    host_in = _t.empty(dev.n_total, dtype=_t.complex128, pin_memory=True)
+    host_out = _t.empty(dev.n_total, dtype=_t.complex128, pin_memory=True)
+    host_in.copy_(solver.X.cpu())
+    ke = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        solver.step_host(host_in, host_out)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ke
+    nbytes = dev.n_total * 16
+    out = {
+        "metric": METRIC[args.config] + (" FP32 form" if args.precision == "fp32" else " plain FP64"),
+        "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded initial state of the configuration, conatus_gb300.workloads)",
+        "config": {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
+                   "real_unknowns": P.real_unknowns(), "systems": int(sum(P.nsys)),
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (state, history and factors are GBs)",
+                   "grid": dev.grid, "state_finite": finite},
+        "mode_updates_per_s": value * P.real_unknowns(),
+        "roofline": roof,
+        "e2e": {"value": ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": solver.launches_per_step() * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, P, C0)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, P, C0, steps=1):
+    """The oracle (CPU restatement of the reference's step) on a bounded sample of the workload:
+    the full F, M X and right-hand side, and the banded solves of a subset of the systems of every
+    bucket (scaled to all systems); factorizations outside the timing."""
+    from oracle.ivp import SampledStepper
+    import multiprocessing
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else multiprocessing.cpu_count()
+    cfg = args.cfg
+    st = SampledStepper(P, int(cfg["scheme"][-1]), cfg["dt"], sample_systems=args.cpu_sample_systems,
+                        workers=cores)
+    t_step, desc = st.time_steps(C0, steps)
+    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": desc}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    from conatus_gb300 import workloads as W
+    P = W.problem(args.config)
+    C0 = W.initial_state(args.config, P, seed=0)
+    from oracle.ivp import SampledStepper
+    import multiprocessing
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else multiprocessing.cpu_count()
+    cfg = args.cfg
+    st = SampledStepper(P, int(cfg["scheme"][-1]), cfg["dt"], sample_systems=args.cpu_sample_systems,
+                        workers=cores)
+    t_step, desc = st.time_steps(C0, max(1, min(args.steps, 2)), warmup=min(args.warmup, 1))
+    value = 1.0 / t_step
+    out = {"impl": "reference", "metric": METRIC[args.config] + " plain FP64", "value": value,
+           "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded initial state of the configuration)",
+           "config": {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
+                      "real_unknowns": P.real_unknowns()},
+           "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": desc},
+           "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="channel", choices=list(METRIC))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--cpu-sample-systems", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from conatus_gb300 import workloads as W
+    args.cfg = W.CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -204,11 +204,11 @@ class DeviceProblem:
         ptrs = [(ctypes.c_void_p * nb)(*modes_p), (ctypes.c_void_p * nb)(*col_p), (ctypes.c_void_p * nb)(*row_p)]
         keep.extend(ptrs)
         desc.modes, desc.colpos, desc.rowmap = (ctypes.cast(p, ctypes.c_void_p).value for p in ptrs)
-        lams = sorted(tpl.conv)
-        if lams and lams != list(range(1, len(lams) + 1)):
-            raise NotImplementedError("conversion levels must be 1..n")
-        desc.nlam = len(lams)
-        desc.conv = arr(np.stack([tpl.conv[l] for l in lams]) if lams else np.zeros(1), np.float64)
+        # conversions T -> C^(lambda) for lambda = 1..max (levels no row uses: identity, unused)
+        nlam = max(tpl.conv) if tpl.conv else 0
+        desc.nlam = nlam
+        desc.conv = arr(np.stack([tpl.conv.get(l, np.eye(ny)) for l in range(1, nlam + 1)])
+                        if nlam else np.zeros(1), np.float64)
         b0 = P.b0_dense()
         idx, val = [], []
         for bi, B0 in enumerate(b0):
@@ -217,6 +217,7 @@ class DeviceProblem:
                 idx.append(self.offsets[bi] + mm * tpl.buckets[bi].n + ii)
                 val.append([B0[mm, ii].real, B0[mm, ii].imag])
         desc.nb0 = len(idx)
+        self.has_b0 = len(idx) > 0
         desc.b0_index = arr(idx if idx else [0], np.int64)
         desc.b0_value = arr(val if val else [[0.0, 0.0]], np.float64)
         h = ctypes.c_void_p()
@@ -431,6 +432,34 @@ class IVPSolver:
             self.t += self.dt
             self.iteration += 1
         self._leave()
+
+    def step_host(self, host_in, host_out) -> None:
+        """One step through host buffers: the state is copied in from ``host_in`` (pinned, mode
+        layout), stepped (history kept), and copied out to ``host_out``."""
+        self._enter()
+        with _torch().cuda.stream(self.stream):
+            self.X.copy_(host_in, non_blocking=True)
+        if self.filled >= self.order:
+            self.run_graph(1)
+        else:
+            self._step()
+        with _torch().cuda.stream(self.stream):
+            host_out.copy_(self.X, non_blocking=True)
+        self.stream.synchronize()
+        self._leave()
+
+    def state_to_host(self):
+        self.stream.synchronize()
+        return self.dev.to_host(self.X)
+
+    def launches_per_step(self) -> int:
+        """Kernels of this library launched by one step: M X (one per bucket), F (unpack and pack
+        per bucket, 2 Chebyshev transforms, 2 or 4 Fourier transforms, products, constant part),
+        the right-hand side combination, one solve per bucket."""
+        nb = len(self.dev.tpl.buckets)
+        d = self.dev.d
+        f = 2 * nb + 2 + (2 if d >= 1 else 2) + (2 if d >= 2 else 0) + 1 + (1 if self.dev.has_b0 else 0)
+        return nb + f + 1 + nb
 
     def synchronize(self) -> None:
         self.stream.synchronize()

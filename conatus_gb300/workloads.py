@@ -1,0 +1,189 @@
+"""The benchmark workloads: problems and seeded initial states on the mode layout.
+
+* ``channel``: plane channel 192 x 129 x 192 (Lx = 4 pi, Lz = 2 pi, Re = 4000), SBDF3, dt = 5e-3;
+  U = 1 - y^2 plus 0.05 u', u' = curl(psi) with psi = (psi_x, 0, psi_z), each component a seeded
+  random amplitude ~ |k|^-2 (0 < |k| <= 16) times (1 - y^2)^2 q(y) (q a seeded quadratic), so u'
+  is divergence-free and vanishes at the walls; normalized to max |u'| = 1 on a sample grid.
+* ``rayleigh_benard``: 2D RB 256 x 64 (Lx = 2 pi/3.117, z in [0, 1], Ra = 1e6, Pr = 1), SBDF2,
+  dt = 1e-4; T = 1 - z + eps(x, z) z (1 - z), eps ~ N(0, 1e-3^2) per grid point, u = 0.
+* ``burgers``: N = 128, SBDF2, dt = 1e-4, u0 = -sin(pi x).
+
+The states are built in coefficient space (Chebyshev T_n on the wall-normal axis, complex mode
+amplitudes C with f = w Re(C exp(i(kx x + s kz z))), see conatus_gb300.template).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+from numpy.polynomial import chebyshev as npc
+
+from .template import ProblemTemplate
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PROBLEMS = os.path.join(HERE, "problems")
+
+CONFIGS = {
+    "channel": dict(template="channel_ny129", fourier=[192, 192], scheme="SBDF3", dt=5e-3),
+    "rayleigh_benard": dict(template="rb_nz64", fourier=[256], scheme="SBDF2", dt=1e-4),
+    "burgers": dict(template="burgers_n128", fourier=[], scheme="SBDF2", dt=1e-4),
+}
+
+
+def load_template(name: str) -> ProblemTemplate:
+    return ProblemTemplate.load(os.path.join(PROBLEMS, name + ".npz"))
+
+
+def problem(config: str, fourier=None):
+    c = CONFIGS[config]
+    return load_template(c["template"]).instantiate(fourier if fourier is not None else (c["fourier"] or None))
+
+
+def _positions(b, var, comp):
+    """Solver positions of Chebyshev coefficients n = 0.. of (variable, component) in bucket b."""
+    pos = {}
+    for i, (v, c, n) in enumerate(b.col):
+        if v == var and c == comp and n >= 0:
+            pos[int(n)] = i
+    return np.array([pos[n] for n in range(len(pos))], dtype=np.int64)
+
+
+def _var_index(tpl, name):
+    return [v["name"] for v in tpl.variables].index(name)
+
+
+def channel_state(P, seed: int = 0, amplitude: float = 0.05, kmax: float = 16.0):
+    tpl = P.tpl
+    rng = np.random.default_rng(seed)
+    ny = tpl.axes[tpl.cheb_axis]["N"]
+    u = _var_index(tpl, "u")
+    wall = npc.chebmul(npc.chebmul([0.5, 0, -0.5], [0.5, 0, -0.5]), [1.0])   # (1 - y^2)^2
+    C = [np.zeros((ns, b.n), np.complex128) for ns, b in zip(P.nsys, tpl.buckets)]
+    pert = []
+    for bi, b in enumerate(tpl.buckets):
+        kw = P.wavenumbers[bi]
+        Cp = np.zeros((P.nsys[bi], b.n), np.complex128)
+        px = [_positions(b, u, c) for c in range(3)]
+        for m in range(P.nsys[bi]):
+            kx, kz = kw[m]
+            k = np.hypot(kx, kz)
+            if not (0 < k <= kmax):
+                continue
+            amp = k ** -2
+            coef = []
+            for _ in range(2):
+                q = rng.standard_normal(3)
+                a = (rng.standard_normal() + 1j * rng.standard_normal()) * amp
+                coef.append(a * npc.chebmul(wall, q))
+            psx, psz = coef
+            ux = npc.chebder(psz)
+            uy = 1j * kz * psx - 1j * kx * psz
+            uz = -npc.chebder(psx)
+            for c, arr in enumerate((ux, uy, uz)):
+                arr = np.asarray(arr)[:ny]
+                Cp[m, px[c][:arr.size]] = arr
+        pert.append(Cp)
+    # max |u'| on a sample grid (Chebyshev Gauss points, the dealiased Fourier grids)
+    vmax = _max_abs(P, pert, u)
+    scale = amplitude / vmax if vmax > 0 else 0.0
+    for bi in range(len(C)):
+        C[bi] += scale * pert[bi]
+    # base flow U = 1 - y^2 in the mean mode
+    for bi, b in enumerate(tpl.buckets):
+        if b.kind == "real":
+            pos = _positions(b, u, 0)
+            C[bi][0, pos[0]] += 0.5
+            C[bi][0, pos[2]] += -0.5
+    return C
+
+
+def _max_abs(P, C, var, ny_sample=33):
+    """max over components of |f| on Gauss-Chebyshev sample points and the Fourier grid."""
+    tpl = P.tpl
+    d = len(tpl.fourier_axes)
+    ny = tpl.axes[tpl.cheb_axis]["N"]
+    t = -np.cos(np.pi * (np.arange(ny_sample) + 0.5) / ny_sample)
+    T = npc.chebvander(t, ny - 1)                           # (ny_sample, ny)
+    Kx = P.K[0]
+    Nz = P.fourier_sizes[1] if d >= 2 else 1
+    best = 0.0
+    for comp in range(tpl.variables[var]["ncomp"]):
+        spec = np.zeros((Kx, Nz, ny_sample), np.complex128)
+        for bi, b in enumerate(tpl.buckets):
+            pos = _positions(b, var, comp)
+            if pos.size == 0:
+                continue
+            da = P.d_active(bi)
+            w = 1.0 if da == 0 else (0.5 if da == 1 else 0.25)
+            vals = (C[bi][:, pos] @ T.T) * w                 # (nsys, ny_sample)
+            for m in range(P.nsys[bi]):
+                jx, jz = P.modes[bi][m]
+                slot = jz if (jz == 0 or tpl.buckets[bi].sign > 0) else Nz - jz
+                spec[jx, slot] += vals[m]
+                if jx == 0 and jz > 0:
+                    spec[0, Nz - jz] += np.conj(vals[m])
+        mx = 3 * P.fourier_sizes[0] // 2
+        full = np.zeros((mx, Nz, ny_sample), np.complex128)
+        full[:Kx] = spec
+        full[mx - Kx + 1:] = np.conj(spec[1:][::-1][:, (-np.arange(Nz)) % Nz])
+        g = np.fft.ifft(np.fft.ifft(full, axis=0), axis=1) * mx * Nz
+        best = max(best, float(np.abs(g.real).max()))
+    return best
+
+
+def rayleigh_benard_state(P, seed: int = 0, noise: float = 1e-3):
+    """T = 1 - z + eps z (1 - z), eps ~ N(0, noise^2) per grid point; u = 0 (z in [0, 1])."""
+    tpl = P.tpl
+    rng = np.random.default_rng(seed)
+    nz_c = tpl.axes[tpl.cheb_axis]["N"]
+    Nx = P.fourier_sizes[0]
+    Mx, Mz = 3 * Nx // 2, tpl.axes[tpl.cheb_axis]["M"]
+    zt = -np.cos(np.pi * (np.arange(Mz) + 0.5) / Mz)        # Gauss points on [-1, 1]
+    z = (zt + 1) / 2
+    eps = rng.standard_normal((Mx, Mz)) * noise
+    g = eps * (z * (1 - z))[None, :]
+    # forward transforms with the reference conventions: rfft / Mx in x, DCT-II on Gauss points in z
+    F = np.fft.rfft(g, axis=0) / Mx                          # (Mx/2+1, Mz)
+    V = npc.chebvander(zt, nz_c - 1)                          # (Mz, nz)
+    W = (2.0 / Mz) * V                                        # Gauss-Chebyshev quadrature
+    W[:, 0] *= 0.5
+    coef = F @ W                                              # (Mx/2+1, nz): complex half spectrum
+    T_idx = _var_index(tpl, "T")
+    C = [np.zeros((ns, b.n), np.complex128) for ns, b in zip(P.nsys, tpl.buckets)]
+    for bi, b in enumerate(tpl.buckets):
+        pos = _positions(b, T_idx, 0)
+        for m in range(P.nsys[bi]):
+            jx = int(P.modes[bi][m][0])
+            c = coef[jx].copy()
+            if jx == 0:
+                c = c.real.astype(np.complex128)
+                c[0] += 0.5
+                c[1] += -0.5                                  # 1 - z = (T0 - T1)/2 on t = 2z - 1
+                C[bi][m, pos] = c
+            else:
+                C[bi][m, pos] = 2 * c                         # C = 2 F_hat for one direction
+    return C
+
+
+def burgers_state(P):
+    """u0 = -sin(pi x) on [-1, 1] in Chebyshev coefficients (Jacobi-Anger: odd Bessel terms)."""
+    from scipy.special import jv
+    tpl = P.tpl
+    n = tpl.axes[tpl.cheb_axis]["N"]
+    c = np.zeros(n)
+    for k in range(1, n, 2):
+        c[k] = -2 * jv(k, np.pi) * (-1) ** ((k - 1) // 2)
+    b = tpl.buckets[0]
+    C = [np.zeros((1, b.n), np.complex128)]
+    C[0][0, _positions(b, 0, 0)] = c
+    return C
+
+
+def initial_state(config: str, P, seed: int = 0):
+    if config == "channel":
+        return channel_state(P, seed)
+    if config == "rayleigh_benard":
+        return rayleigh_benard_state(P, seed)
+    if config == "burgers":
+        return burgers_state(P)
+    raise KeyError(config)

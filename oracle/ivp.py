@@ -40,7 +40,7 @@ SBDF = {1: ([1, -1], [0, 1]),
 
 def cheb_forward(f, N):
     M = f.shape[0]
-    y = sfft.dct(f, type=2, axis=0) / M
+    y = sfft.dct(f, type=2, axis=0, workers=WORKERS) / M
     y[0] /= 2
     sign = (-1.0) ** np.arange(M)
     return (y * sign.reshape((M,) + (1,) * (f.ndim - 1)))[:N]
@@ -53,12 +53,23 @@ def cheb_backward(c, M):
     y[:N] = c * sign.reshape((N,) + (1,) * (c.ndim - 1))
     y[0] *= 2
     y *= M
-    return sfft.idct(y, type=2, axis=0)
+    return sfft.idct(y, type=2, axis=0, workers=WORKERS)
+
+
+WORKERS = None      # scipy.fft worker threads for the CPU baseline (None: NumPy's transforms)
+
+
+def _rfft(f):
+    return np.fft.rfft(f, axis=0) if WORKERS is None else sfft.rfft(f, axis=0, workers=WORKERS)
+
+
+def _irfft(F, n):
+    return np.fft.irfft(F, n=n, axis=0) if WORKERS is None else sfft.irfft(F, n=n, axis=0, workers=WORKERS)
 
 
 def rf_forward(f, N):
     M = f.shape[0]
-    F = np.fft.rfft(f, axis=0) / M
+    F = _rfft(f) / M
     K = N // 2
     c = np.zeros((N,) + f.shape[1:])
     c[0] = F[0].real
@@ -74,7 +85,7 @@ def rf_backward(c, M):
     F[0] = c[0]
     F[1:K] = (c[2:N:2] + 1j * c[3:N:2]) / 2
     F *= M
-    return np.fft.irfft(F, n=M, axis=0)
+    return _irfft(F, M)
 
 
 def _along(fn, a, axis, *args):
@@ -176,24 +187,62 @@ class OracleProblem:
                 idx.append(bpos if size > 1 else 0)
         return tuple(idx)
 
+    def _flat_maps(self, bi, kind):
+        """Cached per bucket: for each Fourier position p (weight w) and each object k, the
+        positions of the bucket's columns (kind "col") or rows ("row") that belong to k and their
+        flat indices (nsys, count) into k's coefficient array."""
+        key = ("maps", kind, bi)
+        if key in self._factors:
+            return self._factors[key]
+        tpl = self.tpl
+        b = tpl.buckets[bi]
+        modes = self.P.modes[bi]
+        ns = modes.shape[0]
+        desc = b.col if kind == "col" else b.row
+        objs = tpl.variables if kind == "col" else tpl.equations
+        out = []
+        for p, w in self._weights(bi):
+            per = {}
+            for k in np.unique(desc[:, 0]):
+                k = int(k)
+                obj = objs[k]
+                rank = obj["rank"]
+                shape = self._shape(obj)
+                sel = np.nonzero(desc[:, 0] == k)[0]
+                idx = []
+                comp = [np.unravel_index(int(cf), tuple(obj["shape"][:rank])) if rank else ()
+                        for cf in desc[sel, 1]]
+                for r in range(rank):
+                    idx.append(np.broadcast_to(np.array([c[r] for c in comp])[None, :], (ns, sel.size)))
+                for a, axd in enumerate(tpl.axes):
+                    size = shape[rank + a]
+                    if axd["kind"] == "RealFourier":
+                        j = tpl.fourier_axes.index(a)
+                        base = np.where(modes[:, j] > 0, 2 * modes[:, j] + p[j], 0)
+                        ia = base[:, None] if size > 1 else np.zeros((ns, 1), int)
+                        idx.append(np.broadcast_to(ia, (ns, sel.size)))
+                    else:
+                        nn = desc[sel, 2]
+                        ia = np.where((nn >= 0) & (size > 1), nn, 0)
+                        idx.append(np.broadcast_to(ia[None, :], (ns, sel.size)))
+                flat = np.ravel_multi_index(tuple(np.asarray(i) for i in idx), shape)
+                per[k] = (sel, flat)
+            out.append((p, w, per))
+        self._factors[key] = out
+        return out
+
     def to_arrays(self, C):
         """Mode layout -> coefficient arrays of the variables (system.scatter)."""
         tpl = self.tpl
         arrs = [np.zeros(self._shape(v)) for v in tpl.variables]
-        for bi, b in enumerate(tpl.buckets):
+        for bi in range(len(tpl.buckets)):
             da = self.P.d_active(bi)
             scale = 2.0 ** (1 - da) if da >= 1 else 1.0
-            Cb = C[bi]
-            for p, w in self._weights(bi):
+            Cb = np.asarray(C[bi])
+            for p, w, per in self._flat_maps(bi, "col"):
                 coef = scale * np.conj(w)
-                for m in range(Cb.shape[0]):
-                    base = self._pos_index(bi, m, p)
-                    for i in range(b.n):
-                        v, cf, n = b.col[i]
-                        var = tpl.variables[v]
-                        rank = var["rank"]
-                        comp = np.unravel_index(cf, tuple(var["shape"][:rank])) if rank else ()
-                        arrs[v][self._index(arrs[v].shape, rank, comp, base, n)] += (coef * Cb[m, i]).real
+                for v, (sel, flat) in per.items():
+                    np.add.at(arrs[v].reshape(-1), flat.ravel(), (coef * Cb[:, sel]).real.ravel())
         return arrs
 
     def to_rows(self, eq_arrays):
@@ -205,27 +254,24 @@ class OracleProblem:
         out = []
         for bi, b in enumerate(tpl.buckets):
             R = np.zeros((self.P.nsys[bi], b.n), np.complex128)
-            wts = self._weights(bi)
-            for i in range(b.n):
-                e, cf, n, lam = b.row[i]
-                arr = eq_arrays[e]
-                if arr is None:
-                    continue
-                eqd = tpl.equations[e]
-                rank = eqd["rank"]
-                if lam > 0 and ca >= 0 and arr.shape[rank + ca] > 1:
-                    key = (e, lam)
-                    if key not in conv_cache:
-                        S = tpl.conv[int(lam)]
-                        conv_cache[key] = np.moveaxis(
-                            np.tensordot(S, np.moveaxis(arr, rank + ca, 0), axes=(1, 0)), 0, rank + ca)
-                    arr = conv_cache[key]
-                comp = np.unravel_index(cf, tuple(eqd["shape"][:rank])) if rank else ()
-                for m in range(R.shape[0]):
-                    acc = 0j
-                    for p, w in wts:
-                        acc += w * arr[self._index(arr.shape, rank, comp, self._pos_index(bi, m, p), n)]
-                    R[m, i] = acc
+            for p, w, per in self._flat_maps(bi, "row"):
+                for e, (sel, flat) in per.items():
+                    arr = eq_arrays[e]
+                    if arr is None:
+                        continue
+                    rank = tpl.equations[e]["rank"]
+                    lams = np.unique(b.row[sel, 3])
+                    for lam in lams:
+                        sub = b.row[sel, 3] == lam
+                        a = arr
+                        if lam > 0 and ca >= 0 and arr.shape[rank + ca] > 1:
+                            key = (e, int(lam))
+                            if key not in conv_cache:
+                                S = tpl.conv[int(lam)]
+                                conv_cache[key] = np.moveaxis(
+                                    np.tensordot(S, np.moveaxis(arr, rank + ca, 0), axes=(1, 0)), 0, rank + ca)
+                            a = conv_cache[key]
+                        R[:, sel[sub]] += w * a.reshape(-1)[flat[:, sub]]
             out.append(R)
         return out
 
@@ -358,3 +404,81 @@ class SBDFStepper:
                 r += c[j] * self.Fh[j - 1][bi] - (a[j] / dt) * self.MXh[j - 1][bi]
             rhs.append(r)
         return op.solve(a[0] / dt, 1.0, rhs)
+
+
+class SampledStepper:
+    """Timing of the oracle step on a bounded sample of a large workload (the CPU baseline): the
+    full F, M X and SBDF right-hand side, and the banded solves of ``sample_systems`` systems
+    spread over the buckets, scaled to every system. Factorizations happen before the timing (the
+    reference times steps after a warm-up that includes them)."""
+
+    def __init__(self, problem, order, dt, sample_systems=256, workers=None):
+        global WORKERS
+        WORKERS = workers
+        self.op = OracleProblem(problem)
+        self.P = problem
+        self.order, self.dt = int(order), float(dt)
+        tot = sum(problem.nsys)
+        frac = min(1.0, sample_systems / max(tot, 1))
+        self.sample = [np.arange(min(ns, max(1, int(np.ceil(frac * ns))))) for ns in problem.nsys]
+        self.scale = [ns / max(len(s), 1) for ns, s in zip(problem.nsys, self.sample)]
+        a0 = SBDF[self.order][0][0] / self.dt
+        self._lu = []
+        for bi, b in enumerate(problem.tpl.buckets):
+            Vm, Vl = self.op._vals(bi, "M"), self.op._vals(bi, "L")
+            mats = [(b.n, b.indptr, b.indices, a0 * Vm[m] + Vl[m]) for m in self.sample[bi]]
+            self._lu.append(BorderedBandedBatch(mats, list(range(b.r)), dtype=np.complex128))
+        self._Mcsr = []
+        for bi, b in enumerate(problem.tpl.buckets):
+            V = self.op._vals(bi, "M")
+            self._Mcsr.append(V)
+
+    def _mx(self, C):
+        out = []
+        for bi, b in enumerate(self.P.tpl.buckets):
+            V = self._Mcsr[bi]
+            if np.all(V == V[:1]):
+                A = sp.csr_matrix((V[0], b.indices, b.indptr), shape=(b.n, b.n))
+                out.append(np.asarray(C[bi] @ A.T))
+            else:
+                out.append(self.op.MX([C[bi]])[0] if len(self.P.tpl.buckets) == 1 else self.op.MX(C)[bi])
+        return out
+
+    def time_steps(self, C0, steps=1, warmup=0):
+        import time
+        C = [np.asarray(c) for c in C0]
+        hist_f, hist_mx = deque(), deque()
+        a, c = SBDF[self.order]
+        times = []
+        for it in range(warmup + steps):
+            t0 = time.perf_counter()
+            F = self.op.F(C)
+            MX = self._mx(C)
+            hist_f.appendleft(F)
+            hist_mx.appendleft(MX)
+            while len(hist_f) > self.order:
+                hist_f.pop()
+                hist_mx.pop()
+            q = len(hist_f)
+            rhs = []
+            for bi in range(len(C)):
+                r = np.zeros_like(C[bi])
+                for j in range(q):
+                    r += c[j + 1] * hist_f[j][bi] - (a[j + 1] / self.dt) * hist_mx[j][bi]
+                rhs.append(r)
+            t1 = time.perf_counter()
+            t_solve = 0.0
+            newC = [x.copy() for x in C]
+            for bi, B in enumerate(self._lu):
+                ts = time.perf_counter()
+                xs = B.solve(rhs[bi][self.sample[bi]])
+                t_solve += (time.perf_counter() - ts) * self.scale[bi]
+                newC[bi][self.sample[bi]] = xs
+            C = newC
+            if it >= warmup:
+                times.append((t1 - t0) + t_solve)
+        nsamp = int(sum(len(s) for s in self.sample))
+        desc = (f"{steps} step(s): full F, M X and right-hand side on {self.P.real_unknowns()} unknowns; "
+                f"banded solves of {nsamp} of {sum(self.P.nsys)} systems scaled to all; "
+                f"factorizations untimed; scipy.fft workers={WORKERS}")
+        return float(np.mean(times)), desc

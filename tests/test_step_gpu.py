@@ -64,7 +64,7 @@ def _smooth_state(P, rng, amp=0.05):
     C = []
     for bi, b in enumerate(P.tpl.buckets):
         n_idx = np.maximum(b.col[:, 2], 0)
-        z = rng.standard_normal((P.nsys[bi], b.n))
+        z = rng.standard_normal((P.nsys[bi], b.n)).astype(np.complex128)
         if b.kind != "real":
             z = z + 1j * rng.standard_normal((P.nsys[bi], b.n))
         C.append(z * amp * np.exp(-0.35 * n_idx))
