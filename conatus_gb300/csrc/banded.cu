@@ -473,6 +473,49 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_solve_T(BandView<T> v, 
 }
 
 
+// Mixed precision: FP32 factors (demoted from the FP64 factorization), complex128 right-hand side
+// and result. accumulate = 0: x = A32^{-1} b; 1: x += A32^{-1} b (the refinement update in FP64).
+struct MixedView {
+    int batch, n, r, kl, ku, ldab;
+    const zf* ab;
+    const int* ipiv;
+    const zf* vt;
+    const zf* w;
+    const zf* slu;
+    const int* spiv;
+    const int* perm;
+};
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_solve_mixed(MixedView v, const zd* __restrict__ b, zd* __restrict__ x, int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wib = threadIdx.x >> 5;
+    const int sys = blockIdx.x * kWarpsPerBlock + wib;
+    if (sys >= v.batch) return;
+    const int lane = threadIdx.x & 31;
+    const int n = v.n, r = v.r;
+    zf* y = reinterpret_cast<zf*>(smem_raw) + (size_t)wib * (n + 64);
+    zf* zbuf = y + n;
+    const zd* bs = b + (size_t)sys * n;
+    for (int i = lane; i < n; i += 32) y[i] = to_zf(bs[v.perm[i]]);
+    __syncwarp();
+    warp_band_solve<zf>(const_cast<zf*>(v.ab) + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, n,
+                        v.kl, v.ku, v.ldab);
+    if (r > 0)
+        warp_woodbury<zf>(v.vt + (size_t)sys * r * n, v.w + (size_t)sys * r * n, v.slu + (size_t)sys * r * r,
+                          v.spiv + (size_t)sys * r, y, zbuf, n, r);
+    zd* xs = x + (size_t)sys * n;
+    for (int i = lane; i < n; i += 32) {
+        const zd d(y[i].re, y[i].im);
+        xs[i] = accumulate ? xs[i] + d : d;
+    }
+}
+
+__global__ void k_demote(const zd* __restrict__ a, zf* __restrict__ b, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = to_zf(a[i]);
+}
+
 // Device layout of a batch sharing one CSR pattern: values [batch][nnz] -> band of B and V^T.
 // bulk_dest[p] >= 0: band offset (j*ldab + kv + i - j) of bulk entry p, -1 for a border entry.
 // Border position i owns the entries bptr[i]..bptr[i+1]-1 of (bp: CSR position, bcol: column), in
@@ -533,6 +576,12 @@ struct Banded {
     double factor_ms = 0.0;
     double cond_max = 1.0;
     std::vector<int> perm_host;
+    // FP32 copies of the factors (mixed-precision solves)
+    zf* ab32 = nullptr;
+    zf* vt32 = nullptr;
+    zf* w32 = nullptr;
+    zf* slu32 = nullptr;
+    bool fp32_ready = false;
     // shared-pattern refactorization data (create_shared)
     int nnz = 0;
     long long* bulk_dest = nullptr;
@@ -543,7 +592,7 @@ struct Banded {
     ~Banded() {
         for (void* p : {ab, (void*)ipiv, vt, w, slu, (void*)spiv, (void*)perm, (void*)info,
                         (void*)cond, wt, stlu, (void*)stpiv, (void*)bulk_dest, (void*)bptr,
-                        (void*)bp, (void*)bcol})
+                        (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32})
             if (p) cudaFree(p);
     }
 
@@ -843,6 +892,27 @@ static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaSt
     }
 }
 
+static void make_fp32(Banded& h, cudaStream_t st) {
+    if (h.dtype != 1) throw InvalidArgument("FP32 factors need complex128 factors (complex bucket)");
+    const size_t B = h.batch, n = h.n, r = h.r;
+    if (!h.ab32) dalloc(&h.ab32, B * n * h.ldab, sizeof(zf));
+    if (!h.vt32) dalloc(&h.vt32, B * r * n, sizeof(zf));
+    if (!h.w32) dalloc(&h.w32, B * r * n, sizeof(zf));
+    if (!h.slu32) dalloc(&h.slu32, B * r * r, sizeof(zf));
+    auto dem = [&](const void* a, zf* b, long long cnt) {
+        if (cnt <= 0) return;
+        k_demote<<<(int)std::min<long long>((cnt + 255) / 256, 152LL * 32), 256, 0, st>>>(
+            static_cast<const zd*>(a), b, cnt);
+        CNG_LAUNCH("k_demote");
+    };
+    dem(h.ab, h.ab32, (long long)(B * n * h.ldab));
+    dem(h.vt, h.vt32, (long long)(B * r * n));
+    dem(h.w, h.w32, (long long)(B * r * n));
+    dem(h.slu, h.slu32, (long long)(B * r * r));
+    CNG_CUDA(cudaStreamSynchronize(st));
+    h.fp32_ready = true;
+}
+
 static void prepare_transpose(Banded& h, cudaStream_t st) {
     if (h.transposed_ready) return;
     if (h.r > 0) {
@@ -1069,6 +1139,30 @@ int cng_banded_solve_host(cng_banded* hh, const void* b_host, void* x_host, int 
     })
 }
 
+int cng_banded_make_fp32(cng_banded* hh, void* stream) {
+    CNG_TRY({ make_fp32(*as_banded(hh), static_cast<cudaStream_t>(stream)); })
+}
+
+int cng_banded_solve_fp32(const cng_banded* hh, const void* b, void* x, int accumulate, void* stream) {
+    CNG_TRY({
+        const Banded* h = as_banded(hh);
+        if (!h->fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first (it allocates)");
+        if (!b || !x) throw InvalidArgument("null device pointer");
+        if (b == x) throw InvalidArgument("b and x must not alias");
+        static std::once_flag once;
+        std::call_once(once, [] {
+            cudaFuncSetAttribute(k_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
+        });
+        MixedView v{h->batch, h->n, h->r, h->kl, h->ku, h->ldab, h->ab32, h->ipiv, h->vt32, h->w32,
+                    h->slu32, h->spiv, h->perm};
+        const size_t smem = (size_t)kWarpsPerBlock * (h->n + 64) * sizeof(zf);
+        k_solve_mixed<<<ceil_div(h->batch, kWarpsPerBlock), 32 * kWarpsPerBlock, smem,
+                        static_cast<cudaStream_t>(stream)>>>(v, static_cast<const zd*>(b), static_cast<zd*>(x),
+                                                             accumulate);
+        CNG_LAUNCH("k_solve_mixed");
+    })
+}
+
 int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream) {
     CNG_TRY({
         Banded* h = as_banded(hh);
@@ -1084,6 +1178,7 @@ int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream)
             launch_factor(*h, st);
             h->transposed_ready = false;
             finish_factor(*h, st, e0, e1);
+            if (h->fp32_ready) make_fp32(*h, st);
         } catch (...) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);

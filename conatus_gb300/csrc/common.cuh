@@ -66,6 +66,33 @@ __host__ __device__ inline zd operator/(zd a, zd b) {
 __host__ __device__ inline bool operator==(zd a, zd b) { return a.re == b.re && a.im == b.im; }
 __host__ __device__ inline bool operator!=(zd a, zd b) { return !(a == b); }
 
+// ---- complex float (FP32 factors of the mixed-precision solve) --------------------------------
+struct alignas(8) zf {
+    float re, im;
+    __host__ __device__ zf() : re(0), im(0) {}
+    __host__ __device__ zf(float r) : re(r), im(0) {}
+    __host__ __device__ zf(double r) : re((float)r), im(0) {}
+    __host__ __device__ zf(float r, float i) : re(r), im(i) {}
+};
+__host__ __device__ inline zf operator+(zf a, zf b) { return zf(a.re + b.re, a.im + b.im); }
+__host__ __device__ inline zf operator-(zf a, zf b) { return zf(a.re - b.re, a.im - b.im); }
+__host__ __device__ inline zf operator*(zf a, zf b) {
+    return zf(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__host__ __device__ inline zf operator/(zf a, zf b) {
+    if (fabsf(b.re) >= fabsf(b.im)) {
+        float r = b.im / b.re, d = b.re + b.im * r;
+        return zf((a.re + a.im * r) / d, (a.im - a.re * r) / d);
+    }
+    float r = b.re / b.im, d = b.im + b.re * r;
+    return zf((a.re * r + a.im) / d, (a.im * r - a.re) / d);
+}
+__host__ __device__ inline bool is_zero(zf x) { return x.re == 0.0f && x.im == 0.0f; }
+__device__ inline zf shfl_xor(zf v, int m) {
+    return zf(__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m));
+}
+__host__ __device__ inline zf to_zf(zd a) { return zf((float)a.re, (float)a.im); }
+
 // Magnitudes: |.| of LAPACK's pivot search (i?amax: |re| + |im| for complex) and the modulus.
 __host__ __device__ inline double abs1(double x) { return fabs(x); }
 __host__ __device__ inline double abs1(zd x) { return fabs(x.re) + fabs(x.im); }
@@ -79,6 +106,7 @@ __host__ __device__ inline bool finite_val(zd x) { return isfinite(x.re) && isfi
 template <class T> __host__ __device__ inline T one();
 template <> __host__ __device__ inline double one<double>() { return 1.0; }
 template <> __host__ __device__ inline zd one<zd>() { return zd(1.0, 0.0); }
+template <> __host__ __device__ inline zf one<zf>() { return zf(1.0f, 0.0f); }
 
 // Warp shuffle of either type.
 __device__ inline double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }

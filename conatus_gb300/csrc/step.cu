@@ -47,6 +47,38 @@ __global__ void k_sbdf_rhs(SbdfArgs a, double* __restrict__ rhs, long long count
     }
 }
 
+// r = b - (a M + c sum_t mono[m][t] L_t) x per system, FP64 (the refinement residual). M values
+// shared by the bucket (nnz), L_t coefficient rows (nmono x nnz), mono (nsys x nmono).
+__global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
+                                const double2* __restrict__ mval, const double2* __restrict__ lcoef,
+                                const double* __restrict__ mono, int nmono, double a, double c,
+                                const double2* __restrict__ x, const double2* __restrict__ b,
+                                double2* __restrict__ r) {
+    const long long total = (long long)nsys * n;
+    const int nnz = ip[n];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long m = t / n;
+        const int i = (int)(t - m * n);
+        const double2* xm = x + m * n;
+        const double* mv = mono + m * nmono;
+        double ar = 0.0, ai = 0.0;
+        for (int p = ip[i]; p < ip[i + 1]; ++p) {
+            double vr = a * mval[p].x, vi = a * mval[p].y;
+            for (int q = 0; q < nmono; ++q) {
+                const double2 l = lcoef[(long long)q * nnz + p];
+                vr += c * mv[q] * l.x;
+                vi += c * mv[q] * l.y;
+            }
+            const double2 xv = xm[ix[p]];
+            ar += vr * xv.x - vi * xv.y;
+            ai += vr * xv.y + vi * xv.x;
+        }
+        const double2 bv = b[t];
+        r[t] = make_double2(bv.x - ar, bv.y - ai);
+    }
+}
+
 }  // namespace cng
 
 using namespace cng;
@@ -65,6 +97,24 @@ int cng_csr_matvec(int nsys, int n, const int32_t* indptr, const int32_t* indice
             nsys, n, indptr, indices, static_cast<const double2*>(values), values_per_system,
             static_cast<const double2*>(x), static_cast<double2*>(y));
         CNG_LAUNCH("k_csr_matvec");
+    })
+}
+
+int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* indices, const void* mval,
+                      const void* lcoef, const double* mono, int nmono, double a, double c, const void* x,
+                      const void* b, void* r, void* stream) {
+    CNG_TRY({
+        if (!indptr || !indices || !mval || (nmono > 0 && (!lcoef || !mono)) || !x || !b || !r)
+            throw InvalidArgument("null device pointer");
+        if (r == x || r == b) throw InvalidArgument("r must not alias x or b");
+        if (nsys <= 0 || n <= 0) return CNG_OK;
+        const long long total = (long long)nsys * n;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+        k_poly_residual<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            nsys, n, indptr, indices, static_cast<const double2*>(mval), static_cast<const double2*>(lcoef),
+            mono, nmono, a, c, static_cast<const double2*>(x), static_cast<const double2*>(b),
+            static_cast<double2*>(r));
+        CNG_LAUNCH("k_poly_residual");
     })
 }
 

@@ -107,6 +107,8 @@ class DeviceProblem:
                 self._M.append((torch.as_tensor(problem.values(bi, "M"), device=self.device).contiguous(), 1))
         self._L = [None] * len(tpl.buckets)
         self._factors = {}
+        self._resid = [None] * len(tpl.buckets)
+        self._R2 = None
 
     # ------------------------------------------------------------------ F
     def _build_rhs(self):
@@ -266,17 +268,85 @@ class DeviceProblem:
                 Mv, per = self._M[bi]
                 Lv = self._Lvals(bi)
                 vals = (a * (Mv if per else Mv.unsqueeze(0)) + b_ * Lv).contiguous()
-                f.append(_Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
-                                        list(range(b.r)), pivot=True, stream=_stream_handle(stream)))
+                h = _Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
+                                   list(range(b.r)), pivot=True, stream=_stream_handle(stream))
+                if self.precision == "fp32":
+                    call("cng_banded_make_fp32", h.h, _stream_handle(stream))
+                f.append(h)
             self._factors[key] = f
         return f
 
-    def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
-        """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias)."""
+    def _residual_data(self, bi):
+        """Device data of the FP64 refinement residual of bucket bi: shared M values and the active
+        wavenumber-monomial rows of L with their per-system values; or, for buckets carrying the
+        reference's own values, per-system A values per (a, b)."""
+        if self._resid[bi] is None:
+            torch = _torch()
+            b = self.tpl.buckets[bi]
+            if b.exact is not None or not b.m_is_constant():
+                self._resid[bi] = ("values", {})
+            else:
+                t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
+                act = [t for t in range(b.monos.shape[0]) if np.any(b.Lc[t] != 0)]
+                mv = self.P.mono_values(bi)[:, act] if act else np.zeros((self.nsys[bi], 1))
+                lc = b.Lc[act] if act else np.zeros((1, b.nnz), np.complex128)
+                self._resid[bi] = ("poly", (torch.as_tensor(b.Mc[t0].astype(np.complex128), device=self.device),
+                                            torch.as_tensor(np.ascontiguousarray(lc), device=self.device),
+                                            torch.as_tensor(np.ascontiguousarray(mv), device=self.device),
+                                            len(act)))
+        return self._resid[bi]
+
+    def residual(self, a, b_, x, rhs, out, stream=None) -> None:
+        """out = rhs - (a M + b L) x per bucket, FP64."""
         s = _stream_handle(stream)
-        for bi, h in enumerate(self.factor(a, b_, stream)):
-            call("cng_banded_solve_mapped", h.h, self.bucket(rhs, bi).data_ptr(), None,
-                 self.bucket(out, bi).data_ptr(), None, s)
+        for bi, b in enumerate(self.tpl.buckets):
+            kind, data = self._residual_data(bi)
+            ip, ix = self._pat[bi]
+            xb, rb, ob = self.bucket(x, bi), self.bucket(rhs, bi), self.bucket(out, bi)
+            if kind == "poly":
+                mval, lc, mv, nm = data
+                call("cng_poly_residual", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), mval.data_ptr(),
+                     lc.data_ptr(), mv.data_ptr(), nm, float(a), float(b_), xb.data_ptr(), rb.data_ptr(),
+                     ob.data_ptr(), s)
+            else:
+                key = (float(a), float(b_))
+                if key not in data:
+                    torch = _torch()
+                    Mv, per = self._M[bi]
+                    data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
+                                 b_ * self._Lvals(bi)).contiguous()
+                zero = _torch().zeros(1, dtype=_torch().float64, device=self.device)
+                call("cng_poly_residual", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(),
+                     data[key].data_ptr(), None, None, 0, 1.0, 0.0, xb.data_ptr(), rb.data_ptr(), ob.data_ptr(), s) \
+                    if self.nsys[bi] == 1 else self._values_residual(bi, data[key], xb, rb, ob, s)
+
+    def _values_residual(self, bi, A, xb, rb, ob, s):
+        """Per-system A values: out = rhs - A x with one CSR matvec per system."""
+        b = self.tpl.buckets[bi]
+        ip, ix = self._pat[bi]
+        for m in range(self.nsys[bi]):
+            call("cng_poly_residual", 1, b.n, ip.data_ptr(), ix.data_ptr(), A[m].data_ptr(), None, None, 0,
+                 1.0, 0.0, xb[m * b.n:(m + 1) * b.n].data_ptr(), rb[m * b.n:(m + 1) * b.n].data_ptr(),
+                 ob[m * b.n:(m + 1) * b.n].data_ptr(), s)
+
+    def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
+        """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias). FP32 form: FP32
+        solve, FP64 residual, FP32 correction added in FP64 (one refinement step)."""
+        s = _stream_handle(stream)
+        fs = self.factor(a, b_, stream)
+        if self.precision == "fp64":
+            for bi, h in enumerate(fs):
+                call("cng_banded_solve_mapped", h.h, self.bucket(rhs, bi).data_ptr(), None,
+                     self.bucket(out, bi).data_ptr(), None, s)
+            return
+        if self._R2 is None:
+            self._R2 = self.zeros()
+        for bi, h in enumerate(fs):
+            call("cng_banded_solve_fp32", h.h, self.bucket(rhs, bi).data_ptr(), self.bucket(out, bi).data_ptr(), 0, s)
+        self.residual(a, b_, out, rhs, self._R2, s)
+        for bi, h in enumerate(fs):
+            call("cng_banded_solve_fp32", h.h, self.bucket(self._R2, bi).data_ptr(),
+                 self.bucket(out, bi).data_ptr(), 1, s)
 
     def zeros(self):
         torch = _torch()
@@ -459,7 +529,8 @@ class IVPSolver:
         nb = len(self.dev.tpl.buckets)
         d = self.dev.d
         f = 2 * nb + 2 + (2 if d >= 1 else 2) + (2 if d >= 2 else 0) + 1 + (1 if self.dev.has_b0 else 0)
-        return nb + f + 1 + nb
+        solve = nb if self.dev.precision == "fp64" else 3 * nb
+        return nb + f + 1 + solve
 
     def synchronize(self) -> None:
         self.stream.synchronize()

@@ -91,6 +91,13 @@ int cng_banded_prepare_transpose(cng_banded* h, void* stream);
  * cuda.BandedBatch.solve_transpose_ptr (module.cpp:420-426). */
 int cng_banded_solve_transpose(const cng_banded* h, void* b, void* stream);
 
+/* Mixed precision: keep FP32 (complex64) copies of the FP64 factors (allocates; refreshed by
+ * refactor_shared). No reference counterpart: the FP32 + FP64-refinement form of the solve. */
+int cng_banded_make_fp32(cng_banded* h, void* stream);
+/* x = A^{-1} b with the FP32 factors, b and x complex128 (accumulate != 0: x += A^{-1} b). One
+ * refinement step is solve, residual in FP64 (cng_poly_residual), solve with accumulate. */
+int cng_banded_solve_fp32(const cng_banded* h, const void* b, void* x, int accumulate, void* stream);
+
 /* Host buffers: x = A^{-1} b (or A^{-T} b) with the copies inside the call, (batch, n) C-order.
  * Replaces _core.BorderedBandedBatch{D,Z}.solve (core/bindings/module.cpp:184-206). */
 int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int transpose);
@@ -169,6 +176,13 @@ int cng_rfft_axis(int forward, const void* in, void* out, int64_t outer, int inn
  * x, y: (nsys, n) complex128. Replaces system.M @ X (python/conatus/timestep/device.py:78-105). */
 int cng_csr_matvec(int nsys, int n, const int32_t* indptr, const int32_t* indices, const void* values,
                    int values_per_system, const void* x, void* y, void* stream);
+
+/* r = b - (a M + c L(k_m)) x for every system m of a bucket, FP64: M values mval (nnz, shared),
+ * L(k) = sum_t mono[m nmono + t] lcoef[t nnz + p] (wavenumber polynomial), shared CSR pattern.
+ * The residual of the mixed-precision refinement (the reference solves in FP64 only). */
+int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* indices, const void* mval,
+                      const void* lcoef, const double* mono, int nmono, double a, double c, const void* x,
+                      const void* b, void* r, void* stream);
 
 /* rhs = sum_j (c_j F_j - d_j MX_j), j < q, on count complex128 entries (explicit roundings, no
  * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */
