@@ -380,6 +380,130 @@ __device__ void warp_woodbury(const T* vt, const T* w, const T* slu, const int* 
     __syncwarp();
 }
 
+// ---- staged solve ---------------------------------------------------------------------------
+// The sweeps of warp_band_solve wait on two dependent global loads per column (the pivot index and
+// the column entries). The staged solve streams the band into shared memory CH columns ahead with
+// cp.async (two buffers, hardware wait_group, no spin), and keeps the pivots of the current and the
+// next chunk in registers (lane t holds ipiv[chunk + t], broadcast by shuffle).
+template <class T>
+__device__ __forceinline__ void cp_async_el(T* s, const T* g) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(s));
+    if constexpr (sizeof(T) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+constexpr int kChunk = 16;
+
+// forward chunk c: columns j = c CH .. min(c CH + CH, n - 1) - 1, L entries rows kv+1 .. kv+lm
+template <class T>
+__device__ __forceinline__ void issue_fwd(const T* ab, T* buf, int c, int n, int kl, int kv, int ldab) {
+    const int lane = threadIdx.x & 31;
+    const int j0 = c * kChunk, j1 = min(j0 + kChunk, n - 1);
+    const int cnt = (j1 - j0) * kl;
+    for (int e = lane; e < cnt; e += 32) {
+        const int jj = e / kl, t = e - jj * kl;
+        const int j = j0 + jj;
+        if (t < n - 1 - j) cp_async_el(buf + jj * kl + t, ab + (size_t)j * ldab + kv + 1 + t);
+    }
+    cp_async_commit();
+}
+
+// backward chunk c: columns j = n-1 - (c CH + jj), rows max(0, kv - j) .. kv
+template <class T>
+__device__ __forceinline__ void issue_bwd(const T* ab, T* buf, int c, int n, int kv, int ldab) {
+    const int lane = threadIdx.x & 31;
+    const int w = kv + 1;
+    const int jj1 = min(kChunk, n - c * kChunk);
+    const int cnt = jj1 * w;
+    for (int e = lane; e < cnt; e += 32) {
+        const int jj = e / w, q = e - jj * w;
+        const int j = n - 1 - (c * kChunk + jj);
+        if (q >= kv - j) cp_async_el(buf + jj * w + q, ab + (size_t)j * ldab + q);
+    }
+    cp_async_commit();
+}
+
+template <class T>
+__device__ void warp_band_solve_staged(const T* __restrict__ ab, const int* __restrict__ ipiv, T* y, T* stage,
+                                       int n, int kl, int ku, int ldab) {
+    const int lane = threadIdx.x & 31;
+    const int kv = kl + ku;
+    const int sw = max(kl, kv + 1) * kChunk;          // elements per stage buffer
+    if (kl > 0 && n > 1) {
+        const int nch = (n - 1 + kChunk - 1) / kChunk;
+        issue_fwd(ab, stage, 0, n, kl, kv, ldab);
+        int ip_cur = lane < kChunk && lane < n - 1 ? ipiv[lane] : 0;
+        for (int c = 0; c < nch; ++c) {
+            const int nxt = (c + 1) * kChunk + lane;
+            int ip_nxt = 0;
+            if (c + 1 < nch) {
+                issue_fwd(ab, stage + ((c + 1) & 1) * sw, c + 1, n, kl, kv, ldab);
+                ip_nxt = lane < kChunk && nxt < n - 1 ? ipiv[nxt] : 0;
+                cp_async_wait1();
+            } else {
+                cp_async_wait0();
+            }
+            __syncwarp();
+            const T* buf = stage + (c & 1) * sw;
+            const int j0 = c * kChunk, j1 = min(j0 + kChunk, n - 1);
+            for (int j = j0; j < j1; ++j) {
+                const int jj = j - j0;
+                const int lm = min(kl, n - 1 - j);
+                const int l = __shfl_sync(0xffffffffu, ip_cur, jj);
+                const T bj = y[l];
+                const T yj0 = y[j];
+                __syncwarp();
+                for (int t = lane; t < lm; t += 32) {
+                    const int i = j + 1 + t;
+                    const T v = (i == l) ? yj0 : y[i];
+                    y[i] = v - buf[jj * kl + t] * bj;
+                }
+                if (lane == 0) y[j] = bj;
+                __syncwarp();
+            }
+            ip_cur = ip_nxt;
+        }
+    }
+    {
+        const int w = kv + 1;
+        const int nch = (n + kChunk - 1) / kChunk;
+        issue_bwd(ab, stage, 0, n, kv, ldab);
+        for (int c = 0; c < nch; ++c) {
+            if (c + 1 < nch) {
+                issue_bwd(ab, stage + ((c + 1) & 1) * sw, c + 1, n, kv, ldab);
+                cp_async_wait1();
+            } else {
+                cp_async_wait0();
+            }
+            __syncwarp();
+            const T* buf = stage + (c & 1) * sw;
+            const int jj1 = min(kChunk, n - c * kChunk);
+            for (int jj = 0; jj < jj1; ++jj) {
+                const int j = n - 1 - (c * kChunk + jj);
+                T yj = y[j];
+                if (is_zero(yj)) {
+                    __syncwarp();
+                    continue;
+                }
+                const T* col = buf + jj * w;
+                yj = yj / col[kv];
+                const int m = min(kv, j);
+                for (int t = lane; t < m; t += 32) {
+                    const int i = j - 1 - t;
+                    y[i] = y[i] - yj * col[kv - 1 - t];
+                }
+                if (lane == 0) y[j] = yj;
+                __syncwarp();
+            }
+        }
+    }
+}
+
 // Input/output adapters of the solve kernel: plain in-place, mapped (int64 gather/scatter maps)
 // and split (complex system with real data: b = re[rows_c] + i re[rows_s]).
 enum IoKind { IO_PLAIN = 0, IO_MAPPED = 1, IO_SPLIT = 2 };
@@ -430,11 +554,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_solve(BandView<T> v, So
     if (sys >= v.batch) return;
     const int lane = threadIdx.x & 31;
     const int n = v.n, r = v.r;
-    T* y = reinterpret_cast<T*>(smem_raw) + (size_t)wib * (n + 64);
+    const int per = n + 64 + 2 * max(v.kl, v.kl + v.ku + 1) * kChunk;
+    T* y = reinterpret_cast<T*>(smem_raw) + (size_t)wib * per;
     T* zbuf = y + n;
+    T* stage = zbuf + 64;
     for (int i = lane; i < n; i += 32) y[i] = io_load<T, IO>(io, sys, n, v.perm[i]);
     __syncwarp();
-    warp_band_solve(v.ab + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, n, v.kl, v.ku, v.ldab);
+    warp_band_solve_staged(v.ab + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, stage, n, v.kl, v.ku,
+                           v.ldab);
     if (r > 0)
         warp_woodbury(v.vt + (size_t)sys * r * n, v.w + (size_t)sys * r * n, v.slu + (size_t)sys * r * r,
                       v.spiv + (size_t)sys * r, y, zbuf, n, r);
@@ -494,13 +621,15 @@ k_solve_mixed(MixedView v, const zd* __restrict__ b, zd* __restrict__ x, int acc
     if (sys >= v.batch) return;
     const int lane = threadIdx.x & 31;
     const int n = v.n, r = v.r;
-    zf* y = reinterpret_cast<zf*>(smem_raw) + (size_t)wib * (n + 64);
+    const int per = n + 64 + 2 * max(v.kl, v.kl + v.ku + 1) * kChunk;
+    zf* y = reinterpret_cast<zf*>(smem_raw) + (size_t)wib * per;
     zf* zbuf = y + n;
+    zf* stage = zbuf + 64;
     const zd* bs = b + (size_t)sys * n;
     for (int i = lane; i < n; i += 32) y[i] = to_zf(bs[v.perm[i]]);
     __syncwarp();
-    warp_band_solve<zf>(const_cast<zf*>(v.ab) + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, n,
-                        v.kl, v.ku, v.ldab);
+    warp_band_solve_staged<zf>(v.ab + (size_t)sys * n * v.ldab, v.ipiv + (size_t)sys * n, y, stage, n,
+                               v.kl, v.ku, v.ldab);
     if (r > 0)
         warp_woodbury<zf>(v.vt + (size_t)sys * r * n, v.w + (size_t)sys * r * n, v.slu + (size_t)sys * r * r,
                           v.spiv + (size_t)sys * r, y, zbuf, n, r);
@@ -607,8 +736,9 @@ struct Banded {
         return v;
     }
 
-    size_t solve_smem() const {
-        return (size_t)kWarpsPerBlock * (size_t)(n + 64) * esz;
+    size_t solve_smem(size_t elem = 0) const {
+        const size_t e = elem ? elem : esz;
+        return (size_t)kWarpsPerBlock * (size_t)(n + 64 + 2 * std::max(kl, kl + ku + 1) * kChunk) * e;
     }
 };
 
@@ -864,9 +994,9 @@ static void launch_layout_shared(Banded& h, const void* values, cudaStream_t st)
 
 static void check_smem(const Banded& h) {
     if (h.solve_smem() > kMaxSolveSmem)
-        throw InvalidArgument("BandedBatch: n = " + std::to_string(h.n) +
-                              " is too large for the shared-memory solve (at most " +
-                              std::to_string(kMaxSolveSmem / kWarpsPerBlock / h.esz - 64) + ")");
+        throw InvalidArgument("BandedBatch: n = " + std::to_string(h.n) + " with band kl = " +
+                              std::to_string(h.kl) + ", ku = " + std::to_string(h.ku) +
+                              " is too large for the shared-memory solve");
 }
 
 template <class T, int IO>
@@ -935,7 +1065,8 @@ static void launch_solve_T_t(const Banded& h, void* b, cudaStream_t st) {
         cudaFuncSetAttribute(k_solve_T<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
     });
     const int blocks = ceil_div(h.batch, kWarpsPerBlock);
-    k_solve_T<T><<<blocks, 32 * kWarpsPerBlock, h.solve_smem(), st>>>(h.view<T>(), static_cast<T*>(b));
+    k_solve_T<T><<<blocks, 32 * kWarpsPerBlock, (size_t)kWarpsPerBlock * (h.n + 64) * sizeof(T), st>>>(
+        h.view<T>(), static_cast<T*>(b));
     CNG_LAUNCH("k_solve_T");
 }
 
@@ -971,7 +1102,6 @@ int cng_banded_create_csr(int dtype, int batch, int n, const int32_t* indptr, co
         auto h = std::make_unique<Banded>();
         h->dtype = dtype; h->batch = batch; h->n = n; h->r = r; h->pivot = pivot ? 1 : 0;
         h->esz = dtype ? sizeof(zd) : sizeof(double);
-        check_smem(*h);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         cudaEvent_t e0, e1;
         CNG_CUDA(cudaEventCreate(&e0));
@@ -983,6 +1113,7 @@ int cng_banded_create_csr(int dtype, int batch, int n, const int32_t* indptr, co
             else
                 build_csr<zd>(*h, indptr, indices, static_cast<const zd*>(data),
                               reinterpret_cast<const long long*>(nnz_offsets), border, st);
+            check_smem(*h);
             CNG_CUDA(cudaEventRecord(e0, st));
             launch_factor(*h, st);
             finish_factor(*h, st, e0, e1);
@@ -1011,9 +1142,9 @@ int cng_banded_create_shared(int dtype, int batch, int n, const int32_t* indptr,
         auto h = std::make_unique<Banded>();
         h->dtype = dtype; h->batch = batch; h->n = n; h->r = r; h->pivot = pivot ? 1 : 0;
         h->esz = dtype ? sizeof(zd) : sizeof(double);
-        check_smem(*h);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         build_shared_structure(*h, indptr, indices, nnz, border, st);
+        check_smem(*h);
         cudaEvent_t e0, e1;
         CNG_CUDA(cudaEventCreate(&e0));
         CNG_CUDA(cudaEventCreate(&e1));
@@ -1155,7 +1286,7 @@ int cng_banded_solve_fp32(const cng_banded* hh, const void* b, void* x, int accu
         });
         MixedView v{h->batch, h->n, h->r, h->kl, h->ku, h->ldab, h->ab32, h->ipiv, h->vt32, h->w32,
                     h->slu32, h->spiv, h->perm};
-        const size_t smem = (size_t)kWarpsPerBlock * (h->n + 64) * sizeof(zf);
+        const size_t smem = h->solve_smem(sizeof(zf));
         k_solve_mixed<<<ceil_div(h->batch, kWarpsPerBlock), 32 * kWarpsPerBlock, smem,
                         static_cast<cudaStream_t>(stream)>>>(v, static_cast<const zd*>(b), static_cast<zd*>(x),
                                                              accumulate);
