@@ -150,7 +150,7 @@ __device__ void warp_band_solve(const T* ab, const int* ipiv, T* y, int n, int k
             continue;
         }
         const T* colj = ab + (size_t)j * ldab;
-        yj = yj / colj[kv];
+        yj = yj * colj[kv];                          // the diagonal holds 1 / u_jj
         const int m = min(kv, j);
         for (int t = lane; t < m; t += 32) {
             const int i = j - 1 - t;
@@ -172,7 +172,7 @@ __device__ void warp_band_solve_T(const T* ab, const int* ipiv, T* y, int n, int
         T acc = T(0.0);
         for (int i = i0 + lane; i < j; i += 32) acc = acc + colj[kv + i - j] * y[i];
         acc = warp_sum(acc);
-        const T yj = (y[j] - acc) / colj[kv];
+        const T yj = (y[j] - acc) * colj[kv];          // the diagonal holds 1 / u_jj
         __syncwarp();
         if (lane == 0) y[j] = yj;
         __syncwarp();
@@ -231,6 +231,9 @@ __device__ int small_getrf(T* a, int* piv, int r) {
             for (int i = k + 1; i < r; ++i) a[c * r + i] = a[c * r + i] - a[k * r + i] * u;
         }
     }
+    // the factored form keeps 1 / u_kk on the diagonal (solves multiply; no division per solve)
+    if (info == 0)
+        for (int k = 0; k < r; ++k) a[k * r + k] = one<T>() / a[k * r + k];
     return info;
 }
 
@@ -248,7 +251,7 @@ __device__ void small_getrs(const T* a, const int* piv, T* z, int r) {
     for (int k = 0; k < r; ++k)
         for (int i = k + 1; i < r; ++i) z[i] = z[i] - a[k * r + i] * z[k];
     for (int k = r - 1; k >= 0; --k) {
-        z[k] = z[k] / a[k * r + k];
+        z[k] = z[k] * a[k * r + k];
         for (int i = 0; i < k; ++i) z[i] = z[i] - a[k * r + i] * z[k];
     }
 }
@@ -279,6 +282,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_factor(BandView<T> v) {
     T* ab = v.ab + (size_t)sys * n * ldab;
     int* ipiv = v.ipiv + (size_t)sys * n;
     int info = warp_gbtf2(ab, ipiv, n, v.kl, v.ku, ldab, v.pivot);
+    if (info == 0) {
+        // factored form: 1 / u_jj on the band diagonal, so that every sweep multiplies
+        const int kv = v.kl + v.ku;
+        for (int j = lane; j < n; j += 32) ab[(size_t)j * ldab + kv] = one<T>() / ab[(size_t)j * ldab + kv];
+        __syncwarp();
+    }
     double cond = 1.0;
     if (info == 0 && r > 0) {
         T* w = v.w + (size_t)sys * r * n;
@@ -491,7 +500,7 @@ __device__ void warp_band_solve_staged(const T* __restrict__ ab, const int* __re
                     continue;
                 }
                 const T* col = buf + jj * w;
-                yj = yj / col[kv];
+                yj = yj * col[kv];                   // the diagonal holds 1 / u_jj
                 const int m = min(kv, j);
                 for (int t = lane; t < m; t += 32) {
                     const int i = j - 1 - t;
