@@ -515,7 +515,7 @@ __device__ void warp_band_solve_staged(const T* __restrict__ ab, const int* __re
 
 // Input/output adapters of the solve kernel: plain in-place, mapped (int64 gather/scatter maps)
 // and split (complex system with real data: b = re[rows_c] + i re[rows_s]).
-enum IoKind { IO_PLAIN = 0, IO_MAPPED = 1, IO_SPLIT = 2 };
+enum IoKind { IO_PLAIN = 0, IO_MAPPED = 1, IO_SPLIT = 2, IO_MIXED = 3 };
 
 struct SolveIo {
     const void* rhs;
@@ -524,6 +524,7 @@ struct SolveIo {
     const long long* cols;
     const long long* rows_s;
     const long long* cols_s;
+    int accumulate = 0;
 };
 
 template <class T, int IO>
@@ -714,6 +715,23 @@ struct Banded {
     double factor_ms = 0.0;
     double cond_max = 1.0;
     std::vector<int> perm_host;
+    // compact bucket-union form (built by compact())
+    bool compact_ready = false;
+    int cL = 0, cU = 0, cV = 0, cMaxL = 0, cMaxU = 0, cWg = 0;
+    int* c_offL = nullptr;
+    unsigned char* c_Lrow = nullptr;
+    unsigned* c_Lmask = nullptr;
+    int* c_offU = nullptr;
+    unsigned char* c_Udist = nullptr;
+    int* c_offV = nullptr;
+    int* c_Vcol = nullptr;
+    void* c_L = nullptr;
+    void* c_U = nullptr;
+    void* c_V = nullptr;
+    int* c_piv = nullptr;
+    zf* c_L32 = nullptr;
+    zf* c_U32 = nullptr;
+    zf* c_V32 = nullptr;
     // FP32 copies of the factors (mixed-precision solves)
     zf* ab32 = nullptr;
     zf* vt32 = nullptr;
@@ -730,7 +748,10 @@ struct Banded {
     ~Banded() {
         for (void* p : {ab, (void*)ipiv, vt, w, slu, (void*)spiv, (void*)perm, (void*)info,
                         (void*)cond, wt, stlu, (void*)stpiv, (void*)bulk_dest, (void*)bptr,
-                        (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32})
+                        (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32,
+                        (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
+                        (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
+                        (void*)c_U32, (void*)c_V32})
             if (p) cudaFree(p);
     }
 
@@ -1019,7 +1040,10 @@ static void launch_solve_t(const Banded& h, const SolveIo& io, cudaStream_t st) 
     CNG_LAUNCH("k_solve");
 }
 
+static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st);
+
 static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st) {
+    if (h.compact_ready && launch_solve_compact(h, io_kind, io, st)) return;
     if (h.dtype == 0) {
         if (io_kind == IO_PLAIN) launch_solve_t<double, IO_PLAIN>(h, io, st);
         else if (io_kind == IO_MAPPED) launch_solve_t<double, IO_MAPPED>(h, io, st);
@@ -1293,6 +1317,11 @@ int cng_banded_solve_fp32(const cng_banded* hh, const void* b, void* x, int accu
         std::call_once(once, [] {
             cudaFuncSetAttribute(k_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
         });
+        if (h->compact_ready) {
+            SolveIo io{b, x, nullptr, nullptr, nullptr, nullptr, accumulate};
+            launch_solve_compact(*h, IO_MIXED, io, static_cast<cudaStream_t>(stream));
+            return CNG_OK;
+        }
         MixedView v{h->batch, h->n, h->r, h->kl, h->ku, h->ldab, h->ab32, h->ipiv, h->vt32, h->w32,
                     h->slu32, h->spiv, h->perm};
         const size_t smem = h->solve_smem(sizeof(zf));
@@ -1327,6 +1356,441 @@ int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream)
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     })
+}
+
+}  // extern "C"
+
+// ================================================================================================
+// Compact bucket-union solve.
+//
+// All systems of a bucket share one sparsity pattern, so the union over the bucket of the nonzero
+// slots of their LU factors (pivoting differs per system) is a fixed pattern: about 40% of the L
+// band and 20% of the U band for the channel. The compact solve keeps only those slots, packed for
+// kGroup systems per warp that sweep in lockstep (the pattern, hence the control flow, is shared):
+//   L stream  [wg][e][G]  e = forward entries, columns ascending (offL)
+//   U stream  [wg][e][G]  per column j, descending: 1/u_jj, then the U entries (offU in sweep order)
+//   pivots    [wg][j][G]
+//   V^T       [wg][e][G]  the union nonzeros of the border rows (offV, Vcol)
+//   W         [sys][r][n] dense (as before)
+// with wg = warp group of kGroup consecutive systems (the last one padded with identity systems).
+// The band index lists live in shared memory; the streams are staged chunk by chunk with cp.async.
+namespace cng {
+
+constexpr int kGroup = 4;
+constexpr int kLanesPer = 32 / kGroup;
+constexpr int kCChunk = 16;             // columns per staged chunk
+
+struct CompactIdx {
+    int n, r, kl, kv, nL, nU, nV, wgroups, batch;
+    int maxLc, maxUc;                   // largest chunk of the L / U streams (entries)
+    const int* offL;                    // n + 1
+    const unsigned char* Lrow;          // nL: t (row kv + 1 + t of the column)
+    const unsigned* Lmask;              // n: bit t set if row t is in the union
+    const int* offU;                    // n + 1, sweep order s = n - 1 - j, entries incl. diagonal
+    const unsigned char* Udist;         // per U stream entry: distance d >= 1 above the diagonal (0 = diagonal)
+    const int* offV;                    // r + 1
+    const int* Vcol;                    // nV
+};
+
+template <class TF>
+struct CompactData {
+    const TF* L;
+    const TF* U;
+    const int* piv;
+    const TF* V;
+    const TF* W;        // [sys][r][n]
+    const TF* slu;      // [sys][r][r] (1/u_kk on the diagonal)
+    const int* spiv;    // [sys][r]
+    const int* perm;    // n
+};
+
+template <class T>
+__device__ __forceinline__ void cp_async_bytes(void* s, const void* g, int bytes) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(s));
+    if (bytes == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+    else if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(g) : "memory");
+}
+
+// copy cnt elements of T from global to shared with cp.async (one warp), commit as one group
+template <class T>
+__device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
+    const int lane = threadIdx.x & 31;
+    for (int e = lane; e < cnt; e += 32) cp_async_bytes<T>(dst + e, src + e, (int)sizeof(T));
+}
+
+// The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
+template <class TF, class TD, int IO>
+__global__ void __launch_bounds__(32)
+k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int lane = threadIdx.x & 31;
+    const int g = lane / kLanesPer, lg = lane % kLanesPer;
+    const int wg = blockIdx.x;
+    const int sys = wg * kGroup + g;
+    const bool live = sys < ix.batch;
+    const int n = ix.n, r = ix.r;
+    // shared memory: index lists, then y[G][n + 64], then the staging buffers
+    int* s_offL = reinterpret_cast<int*>(sm);
+    int* s_offU = s_offL + (n + 1);
+    unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
+    unsigned char* s_Lrow = reinterpret_cast<unsigned char*>(s_Lmask + n);
+    unsigned char* s_Udist = s_Lrow + ix.nL;
+    size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
+    off = (off + 15) & ~(size_t)15;
+    TF* y0 = reinterpret_cast<TF*>(sm + off);
+    TF* y = y0 + (size_t)g * (n + 64);
+    TF* zb = y + n;
+    TF* Lb = y0 + (size_t)kGroup * (n + 64);
+    TF* Ub = Lb + 2 * (size_t)ix.maxLc * kGroup;
+    int* Pb = reinterpret_cast<int*>(Ub + 2 * (size_t)ix.maxUc * kGroup);
+    for (int i = lane; i <= n; i += 32) {
+        s_offL[i] = ix.offL[i];
+        s_offU[i] = ix.offU[i];
+    }
+    for (int i = lane; i < n; i += 32) s_Lmask[i] = ix.Lmask[i];
+    for (int i = lane; i < ix.nL; i += 32) s_Lrow[i] = ix.Lrow[i];
+    for (int i = lane; i < ix.nU; i += 32) s_Udist[i] = ix.Udist[i];
+    // gather the right-hand side (permuted rows first)
+    for (int i = lg; i < n; i += kLanesPer) {
+        TF v = TF(0.0);
+        if (live) {
+            if constexpr (IO == IO_MIXED) {
+                const zd b = static_cast<const zd*>(io.rhs)[(size_t)sys * n + cd.perm[i]];
+                v = to_zf(b);
+            } else {
+                v = io_load<TF, IO>(io, sys, n, cd.perm[i]);
+            }
+        }
+        y[i] = v;
+    }
+    __syncwarp();
+    const TF* Lg = cd.L + (size_t)wg * ix.nL * kGroup;
+    const TF* Ug = cd.U + (size_t)wg * (ix.nU) * kGroup;
+    const int* Pg = cd.piv + (size_t)wg * n * kGroup;
+    // ---------------- forward: L with the row interchanges
+    if (ix.kl > 0 && n > 1) {
+        const int nch = (n - 1 + kCChunk - 1) / kCChunk;
+        auto issue = [&](int c, int buf) {
+            const int j0 = c * kCChunk, j1 = min(j0 + kCChunk, n - 1);
+            warp_stage(Lb + (size_t)buf * ix.maxLc * kGroup, Lg + (size_t)s_offL[j0] * kGroup,
+                       (s_offL[j1] - s_offL[j0]) * kGroup);
+            warp_stage(Pb + (size_t)buf * kCChunk * kGroup, Pg + (size_t)j0 * kGroup, (j1 - j0) * kGroup);
+            cp_async_commit();
+        };
+        issue(0, 0);
+        for (int c = 0; c < nch; ++c) {
+            if (c + 1 < nch) {
+                issue(c + 1, (c + 1) & 1);
+                cp_async_wait1();
+            } else {
+                cp_async_wait0();
+            }
+            __syncwarp();
+            const TF* Lc = Lb + (size_t)(c & 1) * ix.maxLc * kGroup;
+            const int* Pc = Pb + (size_t)(c & 1) * kCChunk * kGroup;
+            const int j0 = c * kCChunk, j1 = min(j0 + kCChunk, n - 1);
+            const int base = s_offL[j0];
+            for (int j = j0; j < j1; ++j) {
+                const int l = Pc[(j - j0) * kGroup + g];
+                const TF bj = y[l];
+                const TF yj0 = y[j];
+                __syncwarp();
+                const int e0 = s_offL[j], e1 = s_offL[j + 1];
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
+                    const int i = j + 1 + s_Lrow[e];
+                    const TF v = (i == l) ? yj0 : y[i];
+                    y[i] = v - Lc[(e - base) * kGroup + g] * bj;
+                }
+                if (lg == 0) {
+                    y[j] = bj;
+                    if (l != j && !((s_Lmask[j] >> (l - j - 1)) & 1u)) y[l] = yj0;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    // ---------------- backward: U (diagonal holds 1/u_jj)
+    {
+        const int nch = (n + kCChunk - 1) / kCChunk;
+        auto issue = [&](int c, int buf) {
+            const int s0 = c * kCChunk, s1 = min(s0 + kCChunk, n);
+            warp_stage(Ub + (size_t)buf * ix.maxUc * kGroup, Ug + (size_t)s_offU[s0] * kGroup,
+                       (s_offU[s1] - s_offU[s0]) * kGroup);
+            cp_async_commit();
+        };
+        issue(0, 0);
+        for (int c = 0; c < nch; ++c) {
+            if (c + 1 < nch) {
+                issue(c + 1, (c + 1) & 1);
+                cp_async_wait1();
+            } else {
+                cp_async_wait0();
+            }
+            __syncwarp();
+            const TF* Uc = Ub + (size_t)(c & 1) * ix.maxUc * kGroup;
+            const int s0 = c * kCChunk, s1 = min(s0 + kCChunk, n);
+            const int base = s_offU[s0];
+            for (int s = s0; s < s1; ++s) {
+                const int j = n - 1 - s;
+                const int e0 = s_offU[s], e1 = s_offU[s + 1];
+                const TF yj = y[j] * Uc[(e0 - base) * kGroup + g];
+                __syncwarp();
+                for (int e = e0 + 1 + lg; e < e1; e += kLanesPer) {
+                    const int i = j - s_Udist[e];
+                    y[i] = y[i] - Uc[(e - base) * kGroup + g] * yj;
+                }
+                if (lg == 0) y[j] = yj;
+                __syncwarp();
+            }
+        }
+    }
+    // ---------------- Woodbury: z = S^{-1} V^T y, y -= W z
+    if (r > 0) {
+        const TF* Vg = cd.V + (size_t)wg * ix.nV * kGroup;
+        for (int a = 0; a < r; ++a) {
+            TF acc = TF(0.0);
+            for (int e = ix.offV[a] + lg; e < ix.offV[a + 1]; e += kLanesPer)
+                acc = acc + Vg[(size_t)e * kGroup + g] * y[ix.Vcol[e]];
+            for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
+            if (lg == 0) zb[a] = acc;
+        }
+        __syncwarp();
+        if (lg == 0 && live) small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        __syncwarp();
+        if (live) {
+            const TF* Ws = cd.W + (size_t)sys * r * n;
+            for (int i = lg; i < n; i += kLanesPer) {
+                TF acc = y[i];
+                for (int k = 0; k < r; ++k) acc = acc - Ws[(size_t)k * n + i] * zb[k];
+                y[i] = acc;
+            }
+        }
+        __syncwarp();
+    }
+    if (!live) return;
+    for (int i = lg; i < n; i += kLanesPer) {
+        if constexpr (IO == IO_MIXED) {
+            zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
+            const zd d(y[i].re, y[i].im);
+            xs[i] = io.accumulate ? xs[i] + d : d;
+        } else {
+            io_store<TF, IO>(io, sys, n, i, y[i]);
+        }
+    }
+}
+
+}  // namespace cng
+
+namespace cng {
+
+template <class T>
+__global__ void k_union_mask(const T* __restrict__ a, long long stride, int batch, long long count,
+                             unsigned char* __restrict__ mask) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
+         q += (long long)gridDim.x * blockDim.x) {
+        unsigned char any = 0;
+        for (int k = 0; k < batch && !any; ++k)
+            if (!is_zero(a[(size_t)k * stride + q])) any = 1;
+        mask[q] = any;
+    }
+}
+
+// one warp per system: band LU, pivots and V^T into the interleaved compact streams
+template <class T>
+__global__ void k_pack_compact(BandView<T> v, CompactIdx ix, T* __restrict__ L, T* __restrict__ U,
+                               T* __restrict__ V, int* __restrict__ piv, int total_sys) {
+    const int sys = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (sys >= total_sys) return;
+    const int lane = threadIdx.x & 31;
+    const int wg = sys / kGroup, g = sys % kGroup;
+    const bool live = sys < v.batch;
+    const int n = v.n, kv = v.kl + v.ku;
+    const T* ab = v.ab + (size_t)(live ? sys : 0) * n * v.ldab;
+    T* Lw = L + (size_t)wg * ix.nL * kGroup;
+    T* Uw = U + (size_t)wg * ix.nU * kGroup;
+    for (int j = lane; j < n - 1; j += 32)
+        for (int e = ix.offL[j]; e < ix.offL[j + 1]; ++e)
+            Lw[(size_t)e * kGroup + g] = live ? ab[(size_t)j * v.ldab + kv + 1 + ix.Lrow[e]] : T(0.0);
+    for (int s = lane; s < n; s += 32) {
+        const int j = n - 1 - s;
+        for (int e = ix.offU[s]; e < ix.offU[s + 1]; ++e) {
+            const int d = ix.Udist[e];
+            Uw[(size_t)e * kGroup + g] = live ? ab[(size_t)j * v.ldab + kv - d] : T(0.0);
+        }
+    }
+    int* Pw = piv + (size_t)wg * n * kGroup;
+    for (int j = lane; j < n; j += 32) Pw[(size_t)j * kGroup + g] = live ? v.ipiv[(size_t)sys * n + j] : j;
+    if (v.r > 0) {
+        T* Vw = V + (size_t)wg * ix.nV * kGroup;
+        const T* vt = v.vt + (size_t)(live ? sys : 0) * v.r * n;
+        for (int a = 0; a < v.r; ++a)
+            for (int e = ix.offV[a] + lane; e < ix.offV[a + 1]; e += 32)
+                Vw[(size_t)e * kGroup + g] = live ? vt[(size_t)a * n + ix.Vcol[e]] : T(0.0);
+    }
+}
+
+__global__ void k_demote_n(const zd* __restrict__ a, zf* __restrict__ b, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = to_zf(a[i]);
+}
+
+static CompactIdx compact_idx(const Banded& h) {
+    CompactIdx ix;
+    ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
+    ix.wgroups = h.cWg; ix.batch = h.batch; ix.maxLc = h.cMaxL; ix.maxUc = h.cMaxU;
+    ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
+    ix.offV = h.c_offV; ix.Vcol = h.c_Vcol;
+    return ix;
+}
+
+static void compact(Banded& h, cudaStream_t st) {
+    if (h.dtype != 1) throw InvalidArgument("the compact solve is built for complex128 buckets");
+    const int n = h.n, kv = h.kl + h.ku, r = h.r;
+    if (kv > 255 || h.kl > 31) throw InvalidArgument("compact solve: band too wide (kl <= 31, kl + ku <= 255)");
+    // 1. union masks over the batch
+    std::vector<unsigned char> mab((size_t)n * h.ldab), mvt((size_t)std::max(1, r) * n);
+    unsigned char* dm = nullptr;
+    dalloc(&dm, std::max(mab.size(), mvt.size()), 1);
+    try {
+        const long long cnt = (long long)n * h.ldab;
+        k_union_mask<zd><<<ceil_div(cnt, 256), 256, 0, st>>>(static_cast<const zd*>(h.ab), cnt, h.batch, cnt, dm);
+        CNG_LAUNCH("k_union_mask");
+        CNG_CUDA(cudaMemcpyAsync(mab.data(), dm, mab.size(), cudaMemcpyDeviceToHost, st));
+        if (r > 0) {
+            const long long c2 = (long long)r * n;
+            CNG_CUDA(cudaStreamSynchronize(st));
+            k_union_mask<zd><<<ceil_div(c2, 256), 256, 0, st>>>(static_cast<const zd*>(h.vt), c2, h.batch, c2, dm);
+            CNG_LAUNCH("k_union_mask");
+            CNG_CUDA(cudaMemcpyAsync(mvt.data(), dm, (size_t)r * n, cudaMemcpyDeviceToHost, st));
+        }
+        CNG_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        cudaFree(dm);
+        throw;
+    }
+    cudaFree(dm);
+    // 2. index lists
+    std::vector<int> offL(n + 1, 0), offU(n + 1, 0), offV(r + 1, 0), Vcol;
+    std::vector<unsigned char> Lrow, Udist;
+    std::vector<unsigned> Lmask(n, 0u);
+    for (int j = 0; j < n; ++j) {
+        if (j < n - 1) {
+            const int lm = std::min(h.kl, n - 1 - j);
+            for (int t = 0; t < lm; ++t)
+                if (mab[(size_t)j * h.ldab + kv + 1 + t]) {
+                    Lrow.push_back((unsigned char)t);
+                    Lmask[j] |= 1u << t;
+                }
+        }
+        offL[j + 1] = (int)Lrow.size();
+    }
+    for (int s2 = 0; s2 < n; ++s2) {
+        const int j = n - 1 - s2;
+        Udist.push_back(0);                                  // 1 / u_jj
+        for (int d = 1; d <= std::min(kv, j); ++d)
+            if (mab[(size_t)j * h.ldab + kv - d]) Udist.push_back((unsigned char)d);
+        offU[s2 + 1] = (int)Udist.size();
+    }
+    for (int a = 0; a < r; ++a) {
+        for (int i = 0; i < n; ++i)
+            if (mvt[(size_t)a * n + i]) Vcol.push_back(i);
+        offV[a + 1] = (int)Vcol.size();
+    }
+    int maxL = 1, maxU = 1;
+    for (int j0 = 0; j0 < n - 1; j0 += kCChunk) maxL = std::max(maxL, offL[std::min(j0 + kCChunk, n - 1)] - offL[j0]);
+    for (int s0 = 0; s0 < n; s0 += kCChunk) maxU = std::max(maxU, offU[std::min(s0 + kCChunk, n)] - offU[s0]);
+    h.cL = (int)Lrow.size();
+    h.cU = (int)Udist.size();
+    h.cV = (int)Vcol.size();
+    h.cMaxL = maxL;
+    h.cMaxU = maxU;
+    h.cWg = (h.batch + kGroup - 1) / kGroup;
+    auto up = [&](auto** d, const auto& v) {
+        using E = std::remove_reference_t<decltype(v[0])>;
+        dalloc(d, std::max<size_t>(v.size(), 1), sizeof(E));
+        if (!v.empty()) CNG_CUDA(cudaMemcpyAsync(*d, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, st));
+    };
+    if (!h.c_offL) {
+        up(&h.c_offL, offL); up(&h.c_Lrow, Lrow); up(&h.c_Lmask, Lmask); up(&h.c_offU, offU);
+        up(&h.c_Udist, Udist); up(&h.c_offV, offV); up(&h.c_Vcol, Vcol);
+        const size_t G = kGroup, W = h.cWg;
+        dalloc(&h.c_L, W * std::max(h.cL, 1) * G, sizeof(zd));
+        dalloc(&h.c_U, W * std::max(h.cU, 1) * G, sizeof(zd));
+        dalloc(&h.c_V, W * std::max(h.cV, 1) * G, sizeof(zd));
+        dalloc(&h.c_piv, W * n * G, sizeof(int));
+    } else {
+        // refactorization: the pattern of the new factors must fit the stored union
+        throw InvalidArgument("compact(): already built; refactor into a new handle");
+    }
+    CNG_CUDA(cudaStreamSynchronize(st));
+    // 3. pack
+    const int total = h.cWg * kGroup;
+    k_pack_compact<zd><<<ceil_div(total, 4), 128, 0, st>>>(h.view<zd>(), compact_idx(h), static_cast<zd*>(h.c_L),
+                                                           static_cast<zd*>(h.c_U), static_cast<zd*>(h.c_V), h.c_piv, total);
+    CNG_LAUNCH("k_pack_compact");
+    if (h.fp32_ready || true) {
+        const size_t G = kGroup, W = h.cWg;
+        if (!h.c_L32) {
+            dalloc(&h.c_L32, W * std::max(h.cL, 1) * G, sizeof(zf));
+            dalloc(&h.c_U32, W * std::max(h.cU, 1) * G, sizeof(zf));
+            dalloc(&h.c_V32, W * std::max(h.cV, 1) * G, sizeof(zf));
+        }
+        auto dem = [&](const void* a, zf* b, long long c) {
+            k_demote_n<<<(int)std::min<long long>((c + 255) / 256, 152LL * 32), 256, 0, st>>>(static_cast<const zd*>(a), b, c);
+            CNG_LAUNCH("k_demote_n");
+        };
+        dem(h.c_L, h.c_L32, (long long)(W * std::max(h.cL, 1) * G));
+        dem(h.c_U, h.c_U32, (long long)(W * std::max(h.cU, 1) * G));
+        dem(h.c_V, h.c_V32, (long long)(W * std::max(h.cV, 1) * G));
+    }
+    CNG_CUDA(cudaStreamSynchronize(st));
+    h.compact_ready = true;
+}
+
+template <class TF>
+static size_t compact_smem(const Banded& h) {
+    size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
+    off = (off + 15) & ~(size_t)15;
+    return off + sizeof(TF) * ((size_t)kGroup * (h.n + 64) + 2 * (size_t)(h.cMaxL + h.cMaxU) * kGroup) +
+           2 * (size_t)kCChunk * kGroup * sizeof(int);
+}
+
+template <class TF, class TD, int IO>
+static void launch_compact(const Banded& h, const CompactData<TF>& cd, const SolveIo& io, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve_compact<TF, TD, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    });
+    const size_t smem = compact_smem<TF>(h);
+    if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
+    k_solve_compact<TF, TD, IO><<<h.cWg, 32, smem, st>>>(compact_idx(h), cd, io);
+    CNG_LAUNCH("k_solve_compact");
+}
+
+static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st) {
+    if (h.dtype != 1) return false;
+    if (io_kind == IO_MIXED) {
+        if (!h.fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first");
+        CompactData<zf> cd{h.c_L32, h.c_U32, h.c_piv, h.c_V32, h.w32, h.slu32, h.spiv, h.perm};
+        launch_compact<zf, zd, IO_MIXED>(h, cd, io, st);
+        return true;
+    }
+    CompactData<zd> cd{static_cast<const zd*>(h.c_L), static_cast<const zd*>(h.c_U), h.c_piv,
+                       static_cast<const zd*>(h.c_V), static_cast<const zd*>(h.w), static_cast<const zd*>(h.slu),
+                       h.spiv, h.perm};
+    if (io_kind == IO_PLAIN) launch_compact<zd, zd, IO_PLAIN>(h, cd, io, st);
+    else if (io_kind == IO_MAPPED) launch_compact<zd, zd, IO_MAPPED>(h, cd, io, st);
+    else launch_compact<zd, zd, IO_SPLIT>(h, cd, io, st);
+    return true;
+}
+
+}  // namespace cng
+
+extern "C" {
+
+int cng_banded_compact(cng_banded* hh, void* stream) {
+    CNG_TRY({ cng::compact(*reinterpret_cast<cng::Banded*>(hh), static_cast<cudaStream_t>(stream)); })
 }
 
 }  // extern "C"

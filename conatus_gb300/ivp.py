@@ -76,7 +76,7 @@ def _stream_handle(stream) -> int:
 class DeviceProblem:
     """A problem instance resident on the device (see module docstring)."""
 
-    def __init__(self, problem, precision: str = "fp64", device: str = "cuda"):
+    def __init__(self, problem, precision: str = "fp64", device: str = "cuda", compact: bool = True):
         torch = _torch()
         _lib.lib()
         if precision not in ("fp64", "fp32"):
@@ -84,6 +84,7 @@ class DeviceProblem:
         self.P = problem
         self.tpl = tpl = problem.tpl
         self.precision = precision
+        self.compact = bool(compact)
         self.device = torch.device(device)
         self.d = len(tpl.fourier_axes)
         self.nsys = list(problem.nsys)
@@ -272,6 +273,8 @@ class DeviceProblem:
                                    list(range(b.r)), pivot=True, stream=_stream_handle(stream))
                 if self.precision == "fp32":
                     call("cng_banded_make_fp32", h.h, _stream_handle(stream))
+                if self.compact:
+                    call("cng_banded_compact", h.h, _stream_handle(stream))
                 f.append(h)
             self._factors[key] = f
         return f

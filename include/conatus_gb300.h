@@ -91,6 +91,13 @@ int cng_banded_prepare_transpose(cng_banded* h, void* stream);
  * cuda.BandedBatch.solve_transpose_ptr (module.cpp:420-426). */
 int cng_banded_solve_transpose(const cng_banded* h, void* b, void* stream);
 
+/* Build the compact bucket-union form of the factors (complex128 handles): the union over the
+ * batch of the nonzero slots of the LU factors and of V^T, packed for lockstep solves of 4 systems
+ * per warp; later solves (all variants, FP64 and FP32) use it. Allocates and synchronizes. The
+ * reference's GPU path drops the zeros of the factors per system instead (level-scheduled streams,
+ * core/src/cuda/banded.cu:824-1121). */
+int cng_banded_compact(cng_banded* h, void* stream);
+
 /* Mixed precision: keep FP32 (complex64) copies of the FP64 factors (allocates; refreshed by
  * refactor_shared). No reference counterpart: the FP32 + FP64-refinement form of the solve. */
 int cng_banded_make_fp32(cng_banded* h, void* stream);

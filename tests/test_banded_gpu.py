@@ -155,3 +155,30 @@ def test_errors(cuda_lib):
     B = core.BandedBatchD([(n, A.indptr, A.indices, A.data)], [0])
     with pytest.raises(ValueError, match="matching the factorization"):
         B.solve_ptr(12345, 2, n)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_compact_solve_matches_dense(case, cuda_lib):
+    """The compact bucket-union solve (4 systems per warp, union pattern of the factors) against
+    the dense band solve of the same factors: same arithmetic up to the order of the sums."""
+    import torch
+    from conatus_gb300 import core
+    from conatus_gb300._lib import call
+    for label, dtype, mats, border, rhs, x, xt, band in buckets(case):
+        if np.dtype(dtype).kind != "c":
+            continue
+        B = core.BandedBatchZ(mats, border)
+        b = _t(rhs.astype(dtype))
+        B.solve_ptr(b.data_ptr(), b.shape[0], b.shape[1])
+        call("cng_banded_compact", B._h.h, None)
+        b2 = _t(rhs.astype(dtype))
+        B.solve_ptr(b2.data_ptr(), b2.shape[0], b2.shape[1])
+        torch.cuda.synchronize()
+        assert rel(b2.cpu().numpy(), b.cpu().numpy()) < 1e-13, label
+        assert rel(b2.cpu().numpy(), x) < tol_vs_reference(case, label), label
+        # FP32 copies + refinement-free solve: FP32 accuracy against the FP64 solution
+        call("cng_banded_make_fp32", B._h.h, None)
+        out = torch.zeros_like(b2)
+        call("cng_banded_solve_fp32", B._h.h, _t(rhs.astype(dtype)).data_ptr(), out.data_ptr(), 0, None)
+        torch.cuda.synchronize()
+        assert rel(out.cpu().numpy(), x) < 1e-2, label

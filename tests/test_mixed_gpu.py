@@ -23,6 +23,16 @@ def _state(P, rng):
     return C
 
 
+def _workload_state(tname, P, rng):
+    """The configurations' own initial states (conatus_gb300.workloads) at test resolutions."""
+    from conatus_gb300 import workloads as W
+    if tname.startswith("channel"):
+        return W.channel_state(P, 0)
+    if tname.startswith("rb"):
+        return W.rayleigh_benard_state(P, 0)
+    return W.burgers_state(P)
+
+
 @pytest.mark.parametrize("tname,sizes,scheme,dt", [("rb_nz16", [32], "SBDF2", 1e-4),
                                                    ("channel_ny17", [16, 12], "SBDF3", 5e-3),
                                                    ("burgers_n128", None, "SBDF2", 1e-4)])
@@ -30,7 +40,7 @@ def test_mixed_matches_fp64(tname, sizes, scheme, dt, rng, cuda_lib):
     import torch
     from conatus_gb300.ivp import IVPSolver
     P = template(tname).instantiate(sizes)
-    C0 = _state(P, rng)
+    C0 = _workload_state(tname, P, rng)
     out = {}
     for prec in ("fp64", "fp32"):
         s = IVPSolver(P, scheme=scheme, dt=dt, precision=prec)
@@ -41,3 +51,22 @@ def test_mixed_matches_fp64(tname, sizes, scheme, dt, rng, cuda_lib):
     errs = field_errors(P, out["fp32"], out["fp64"])
     phys = {k: v for k, v in errs.items() if not k.startswith("tau")}
     assert max(phys.values()) < 1e-6, errs
+
+
+@pytest.mark.parametrize("tname,sizes", [("channel_ny17", [16, 12]), ("rb_nz16", [32])])
+def test_fp32_F_error(tname, sizes, rng, cuda_lib):
+    """F in FP32 against F in FP64 on the configuration's state: relative L2 per bucket below 1e-5
+    (FP32 transforms and products)."""
+    import torch
+    from conatus_gb300.ivp import DeviceProblem
+    P = template(tname).instantiate(sizes)
+    C0 = _workload_state(tname, P, rng)
+    outs = {}
+    for prec in ("fp64", "fp32"):
+        d = DeviceProblem(P, precision=prec)
+        o = d.zeros()
+        d.F(d.to_device(C0), o)
+        torch.cuda.synchronize()
+        outs[prec] = o.cpu().numpy()
+    err = np.linalg.norm(outs["fp32"] - outs["fp64"]) / np.linalg.norm(outs["fp64"])
+    assert err < 1e-5, err
