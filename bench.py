@@ -125,7 +125,7 @@ def run_gpu(args):
     from conatus_gb300 import workloads as W
     from conatus_gb300.ivp import IVPSolver
     cfg = W.CONFIGS[args.config]
-    P = W.problem(args.config)
+    P = W.problem(args.config, args.fourier)
     C0 = W.initial_state(args.config, P, seed=rank)
     solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=args.precision)
     dev = solver.dev
@@ -216,6 +216,8 @@ def run_gpu(args):
         "gpu_launches": solver.launches_per_step() * args.steps,
         "clocks": clk.summary(),
     }
+    if args.precision == "fp32" and rank == 0:
+        out["error_vs_fp64"] = mixed_error(P, C0, cfg, args.error_steps)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, P, C0)
     if rank == 0:
@@ -223,6 +225,33 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def mixed_error(P, C0, cfg, steps):
+    """Relative L2 error per field of the mixed form against the plain FP64 form (which matches the
+    reference's FP64 CPU path step by step) after ``steps`` steps from the same state."""
+    import torch
+    from conatus_gb300.ivp import IVPSolver
+    res = {}
+    for prec in ("fp64", "fp32"):
+        s = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=prec)
+        s.set_state(C0)
+        s.run_graph(steps)
+        torch.cuda.synchronize()
+        res[prec] = s.dev.to_host(s.X)
+        del s
+        torch.cuda.empty_cache()
+    errs = {}
+    for v, var in enumerate(P.tpl.variables):
+        if var["name"].startswith("tau"):
+            continue
+        num = den = 0.0
+        for bi, b in enumerate(P.tpl.buckets):
+            sel = b.col[:, 0] == v
+            num += float(np.sum(np.abs(res["fp32"][bi][:, sel] - res["fp64"][bi][:, sel]) ** 2))
+            den += float(np.sum(np.abs(res["fp64"][bi][:, sel]) ** 2))
+        errs[var["name"]] = (num / den) ** 0.5 if den else 0.0
+    return {"steps": steps, "relative_l2": errs, "max": max(errs.values()) if errs else 0.0}
 
 
 def cpu_baseline(args, P, C0, steps=1):
@@ -276,6 +305,9 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--cpu-sample-systems", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--error-steps", type=int, default=50)
+    ap.add_argument("--fourier", type=int, nargs="*", default=None,
+                    help="Fourier sizes overriding the configuration's (small cases for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
