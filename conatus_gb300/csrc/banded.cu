@@ -1378,7 +1378,7 @@ namespace cng {
 
 constexpr int kGroup = 4;
 constexpr int kLanesPer = 32 / kGroup;
-constexpr int kCChunk = 16;             // columns per staged chunk
+constexpr int kCChunk = 8;              // columns per staged chunk
 
 struct CompactIdx {
     int n, r, kl, kv, nL, nU, nV, wgroups, batch;
@@ -1421,14 +1421,16 @@ __device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
 
 // The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
 template <class TF, class TD, int IO>
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(256)
 k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int g = lane / kLanesPer, lg = lane % kLanesPer;
-    const int wg = blockIdx.x;
+    const int wg = blockIdx.x * nw + wib;
     const int sys = wg * kGroup + g;
     const bool live = sys < ix.batch;
+    const bool wlive = wg < ix.wgroups;
     const int n = ix.n, r = ix.r;
     // shared memory: index lists, then y[G][n + 64], then the staging buffers
     int* s_offL = reinterpret_cast<int*>(sm);
@@ -1438,19 +1440,23 @@ k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
     unsigned char* s_Udist = s_Lrow + ix.nL;
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
-    TF* y0 = reinterpret_cast<TF*>(sm + off);
+    const size_t per_warp = (size_t)kGroup * (n + 64) + 2 * (size_t)(ix.maxLc + ix.maxUc) * kGroup +
+                            (2 * (size_t)kCChunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
     TF* y = y0 + (size_t)g * (n + 64);
     TF* zb = y + n;
     TF* Lb = y0 + (size_t)kGroup * (n + 64);
     TF* Ub = Lb + 2 * (size_t)ix.maxLc * kGroup;
     int* Pb = reinterpret_cast<int*>(Ub + 2 * (size_t)ix.maxUc * kGroup);
-    for (int i = lane; i <= n; i += 32) {
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) {
         s_offL[i] = ix.offL[i];
         s_offU[i] = ix.offU[i];
     }
-    for (int i = lane; i < n; i += 32) s_Lmask[i] = ix.Lmask[i];
-    for (int i = lane; i < ix.nL; i += 32) s_Lrow[i] = ix.Lrow[i];
-    for (int i = lane; i < ix.nU; i += 32) s_Udist[i] = ix.Udist[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_Lmask[i] = ix.Lmask[i];
+    for (int i = threadIdx.x; i < ix.nL; i += blockDim.x) s_Lrow[i] = ix.Lrow[i];
+    for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) s_Udist[i] = ix.Udist[i];
+    __syncthreads();
+    if (!wlive) return;
     // gather the right-hand side (permuted rows first)
     for (int i = lg; i < n; i += kLanesPer) {
         TF v = TF(0.0);
@@ -1534,13 +1540,13 @@ k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
             for (int s = s0; s < s1; ++s) {
                 const int j = n - 1 - s;
                 const int e0 = s_offU[s], e1 = s_offU[s + 1];
-                const TF yj = y[j] * Uc[(e0 - base) * kGroup + g];
+                const TF yj = y[j];                       // entries hold u_ij / u_jj
                 __syncwarp();
                 for (int e = e0 + 1 + lg; e < e1; e += kLanesPer) {
                     const int i = j - s_Udist[e];
                     y[i] = y[i] - Uc[(e - base) * kGroup + g] * yj;
                 }
-                if (lg == 0) y[j] = yj;
+                if (lg == 0) y[j] = yj * Uc[(e0 - base) * kGroup + g];
                 __syncwarp();
             }
         }
@@ -1614,9 +1620,11 @@ __global__ void k_pack_compact(BandView<T> v, CompactIdx ix, T* __restrict__ L, 
             Lw[(size_t)e * kGroup + g] = live ? ab[(size_t)j * v.ldab + kv + 1 + ix.Lrow[e]] : T(0.0);
     for (int s = lane; s < n; s += 32) {
         const int j = n - 1 - s;
+        const T dinv = live ? ab[(size_t)j * v.ldab + kv] : T(0.0);     // 1 / u_jj
         for (int e = ix.offU[s]; e < ix.offU[s + 1]; ++e) {
             const int d = ix.Udist[e];
-            Uw[(size_t)e * kGroup + g] = live ? ab[(size_t)j * v.ldab + kv - d] : T(0.0);
+            // the diagonal entry keeps 1 / u_jj; the others are pre-scaled: u_ij / u_jj
+            Uw[(size_t)e * kGroup + g] = !live ? T(0.0) : (d == 0 ? dinv : ab[(size_t)j * v.ldab + kv - d] * dinv);
         }
     }
     int* Pw = piv + (size_t)wg * n * kGroup;
@@ -1749,11 +1757,12 @@ static void compact(Banded& h, cudaStream_t st) {
 }
 
 template <class TF>
-static size_t compact_smem(const Banded& h) {
+static size_t compact_smem(const Banded& h, int nwarps) {
     size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
     off = (off + 15) & ~(size_t)15;
-    return off + sizeof(TF) * ((size_t)kGroup * (h.n + 64) + 2 * (size_t)(h.cMaxL + h.cMaxU) * kGroup) +
-           2 * (size_t)kCChunk * kGroup * sizeof(int);
+    const size_t per_warp = (size_t)kGroup * (h.n + 64) + 2 * (size_t)(h.cMaxL + h.cMaxU) * kGroup +
+                            (2 * (size_t)kCChunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    return off + sizeof(TF) * per_warp * nwarps;
 }
 
 template <class TF, class TD, int IO>
@@ -1762,9 +1771,12 @@ static void launch_compact(const Banded& h, const CompactData<TF>& cd, const Sol
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_solve_compact<TF, TD, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     });
-    const size_t smem = compact_smem<TF>(h);
+    int nw = 8;
+    while (nw > 1 && compact_smem<TF>(h, nw) > 220 * 1024) --nw;
+    nw = std::min(nw, h.cWg);
+    const size_t smem = compact_smem<TF>(h, nw);
     if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
-    k_solve_compact<TF, TD, IO><<<h.cWg, 32, smem, st>>>(compact_idx(h), cd, io);
+    k_solve_compact<TF, TD, IO><<<ceil_div(h.cWg, nw), 32 * nw, smem, st>>>(compact_idx(h), cd, io);
     CNG_LAUNCH("k_solve_compact");
 }
 

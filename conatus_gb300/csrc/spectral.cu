@@ -431,20 +431,20 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     }
 }
 
-// products on the grid: out_o = sum_m c_m prod_j G_j
+// products on the grid: out_o = sum_m c_m prod_j G_j (factor values read through the L1 cache:
+// each grid point's factors are shared by several monomials)
 template <class R>
 __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P;
          p += (long long)gridDim.x * blockDim.x) {
-        R g[16];
-        for (int f = 0; f < d.nfactors && f < 16; ++f) g[f] = G[(long long)f * P + p];
         for (int o = 0; o < d.noutputs; ++o) {
             R acc = R(0);
             for (int mi = d.out_mono_ptr[o]; mi < d.out_mono_ptr[o + 1]; ++mi) {
                 R t = R(d.mono_coef[mi]);
                 const int* fs = d.mono_fac + 4 * mi;
+#pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (fs[q] >= 0) t = t * g[fs[q]];
+                    if (fs[q] >= 0) t = t * __ldg(G + (long long)fs[q] * P + p);
                 acc = acc + t;
             }
             O[(long long)o * P + p] = acc;

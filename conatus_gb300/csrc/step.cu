@@ -79,6 +79,42 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
     }
 }
 
+// r = b - (a M + c sum_t mono[m][t] L_t) x, FP64, with the operator stored as one real-coefficient
+// entry list per row: entry e of row i has column col[e], real value val[e] and a code
+// code[e] = 2 t + imag (t = monomial index, -1 for M: code -2 / -1; imag: the entry is i val).
+// Every coefficient of M and of each L_t is purely real or purely imaginary (derivatives
+// contribute (i k)^p), so an entry costs two real multiply-adds.
+__global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                 const double* __restrict__ val, const signed char* __restrict__ code,
+                                 const double* __restrict__ mono, int nmono, double a, double c,
+                                 const double2* __restrict__ x, const double2* __restrict__ b,
+                                 double2* __restrict__ r) {
+    const long long total = (long long)nsys * n;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long m = t / n;
+        const int i = (int)(t - m * n);
+        const double2* xm = x + m * n;
+        const double* mv = mono + m * nmono;
+        double ar = 0.0, ai = 0.0;
+        for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+            const int cd = code[e];
+            const int tt = cd >> 1;                         // -1: M
+            const double s = val[e] * (tt < 0 ? a : c * mv[tt]);
+            const double2 xv = xm[col[e]];
+            if (cd & 1) {                                   // i s x
+                ar -= s * xv.y;
+                ai += s * xv.x;
+            } else {
+                ar += s * xv.x;
+                ai += s * xv.y;
+            }
+        }
+        const double2 bv = b[t];
+        r[t] = make_double2(bv.x - ar, bv.y - ai);
+    }
+}
+
 }  // namespace cng
 
 using namespace cng;
@@ -115,6 +151,23 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
             mono, nmono, a, c, static_cast<const double2*>(x), static_cast<const double2*>(b),
             static_cast<double2*>(r));
         CNG_LAUNCH("k_poly_residual");
+    })
+}
+
+int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
+                       const int8_t* code, const double* mono, int nmono, double a, double c, const void* x,
+                       const void* b, void* r, void* stream) {
+    CNG_TRY({
+        if (!ptr || !col || !val || !code || (nmono > 0 && !mono) || !x || !b || !r)
+            throw InvalidArgument("null device pointer");
+        if (r == x || r == b) throw InvalidArgument("r must not alias x or b");
+        if (nsys <= 0 || n <= 0) return CNG_OK;
+        const long long total = (long long)nsys * n;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+        k_split_residual<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            nsys, n, ptr, col, val, reinterpret_cast<const signed char*>(code), mono, nmono, a, c,
+            static_cast<const double2*>(x), static_cast<const double2*>(b), static_cast<double2*>(r));
+        CNG_LAUNCH("k_split_residual");
     })
 }
 

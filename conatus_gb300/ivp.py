@@ -280,57 +280,78 @@ class DeviceProblem:
         return f
 
     def _residual_data(self, bi):
-        """Device data of the FP64 refinement residual of bucket bi: shared M values and the active
-        wavenumber-monomial rows of L with their per-system values; or, for buckets carrying the
-        reference's own values, per-system A values per (a, b)."""
+        """Device data of the FP64 refinement residual of bucket bi: M and every wavenumber monomial
+        of L as one real-coefficient entry list per row (each coefficient is purely real or purely
+        imaginary), with the per-system monomial values; or, for buckets carrying the reference's
+        own values, per-system A values per (a, b)."""
         if self._resid[bi] is None:
             torch = _torch()
             b = self.tpl.buckets[bi]
-            if b.exact is not None or not b.m_is_constant():
+            split = None
+            if b.exact is None and b.m_is_constant():
+                split = self._split_operator(b)
+            if split is None:
                 self._resid[bi] = ("values", {})
             else:
-                t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
-                act = [t for t in range(b.monos.shape[0]) if np.any(b.Lc[t] != 0)]
+                ptr, col, val, code, act = split
                 mv = self.P.mono_values(bi)[:, act] if act else np.zeros((self.nsys[bi], 1))
-                lc = b.Lc[act] if act else np.zeros((1, b.nnz), np.complex128)
-                self._resid[bi] = ("poly", (torch.as_tensor(b.Mc[t0].astype(np.complex128), device=self.device),
-                                            torch.as_tensor(np.ascontiguousarray(lc), device=self.device),
-                                            torch.as_tensor(np.ascontiguousarray(mv), device=self.device),
-                                            len(act)))
+                dv = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt), device=self.device)
+                self._resid[bi] = ("split", (dv(ptr, np.int32), dv(col, np.int32), dv(val, np.float64),
+                                             dv(code, np.int8), dv(mv, np.float64), len(act)))
         return self._resid[bi]
+
+    @staticmethod
+    def _split_operator(b):
+        """Row lists (ptr, col, val, code, active monomials) of M and the L_t, or None when some
+        coefficient is neither purely real nor purely imaginary."""
+        t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
+        act = [t for t in range(b.monos.shape[0]) if np.any(b.Lc[t] != 0)]
+        rows = b.coo_rows()
+        ent = [[] for _ in range(b.n)]
+        terms = [(-1, b.Mc[t0])] + [(k, b.Lc[t]) for k, t in enumerate(act)]
+        for k, C in terms:
+            nz = np.nonzero(C)[0]
+            for p in nz:
+                v = complex(C[p])
+                if v.imag == 0:
+                    ent[rows[p]].append((int(b.indices[p]), v.real, 2 * k))
+                elif v.real == 0:
+                    ent[rows[p]].append((int(b.indices[p]), v.imag, 2 * k + 1))
+                else:
+                    return None
+        ptr = np.zeros(b.n + 1, np.int64)
+        col, val, code = [], [], []
+        for i in range(b.n):
+            for c_, v_, cd in ent[i]:
+                col.append(c_)
+                val.append(v_)
+                code.append(cd)
+            ptr[i + 1] = len(col)
+        return ptr, np.array(col), np.array(val), np.array(code), act
 
     def residual(self, a, b_, x, rhs, out, stream=None) -> None:
         """out = rhs - (a M + b L) x per bucket, FP64."""
         s = _stream_handle(stream)
         for bi, b in enumerate(self.tpl.buckets):
             kind, data = self._residual_data(bi)
-            ip, ix = self._pat[bi]
             xb, rb, ob = self.bucket(x, bi), self.bucket(rhs, bi), self.bucket(out, bi)
-            if kind == "poly":
-                mval, lc, mv, nm = data
-                call("cng_poly_residual", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), mval.data_ptr(),
-                     lc.data_ptr(), mv.data_ptr(), nm, float(a), float(b_), xb.data_ptr(), rb.data_ptr(),
+            if kind == "split":
+                ptr, col, val, code, mv, nm = data
+                call("cng_split_residual", self.nsys[bi], b.n, ptr.data_ptr(), col.data_ptr(), val.data_ptr(),
+                     code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_), xb.data_ptr(), rb.data_ptr(),
                      ob.data_ptr(), s)
-            else:
-                key = (float(a), float(b_))
-                if key not in data:
-                    torch = _torch()
-                    Mv, per = self._M[bi]
-                    data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
-                                 b_ * self._Lvals(bi)).contiguous()
-                zero = _torch().zeros(1, dtype=_torch().float64, device=self.device)
-                call("cng_poly_residual", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(),
-                     data[key].data_ptr(), None, None, 0, 1.0, 0.0, xb.data_ptr(), rb.data_ptr(), ob.data_ptr(), s) \
-                    if self.nsys[bi] == 1 else self._values_residual(bi, data[key], xb, rb, ob, s)
-
-    def _values_residual(self, bi, A, xb, rb, ob, s):
-        """Per-system A values: out = rhs - A x with one CSR matvec per system."""
-        b = self.tpl.buckets[bi]
-        ip, ix = self._pat[bi]
-        for m in range(self.nsys[bi]):
-            call("cng_poly_residual", 1, b.n, ip.data_ptr(), ix.data_ptr(), A[m].data_ptr(), None, None, 0,
-                 1.0, 0.0, xb[m * b.n:(m + 1) * b.n].data_ptr(), rb[m * b.n:(m + 1) * b.n].data_ptr(),
-                 ob[m * b.n:(m + 1) * b.n].data_ptr(), s)
+                continue
+            key = (float(a), float(b_))
+            if key not in data:
+                Mv, per = self._M[bi]
+                data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
+                             b_ * self._Lvals(bi)).contiguous()
+            ip, ix = self._pat[bi]
+            A = data[key]
+            for m in range(self.nsys[bi]):
+                sl = slice(m * b.n, (m + 1) * b.n)
+                call("cng_poly_residual", 1, b.n, ip.data_ptr(), ix.data_ptr(), A[m].data_ptr(), None, None, 0,
+                     1.0, 0.0, xb[sl].data_ptr(), rb[sl].data_ptr(), ob[sl].data_ptr(), s)
 
     def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
         """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias). FP32 form: FP32

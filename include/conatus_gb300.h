@@ -191,6 +191,13 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
                       const void* lcoef, const double* mono, int nmono, double a, double c, const void* x,
                       const void* b, void* r, void* stream);
 
+/* The same residual with the operator split per wavenumber monomial into real coefficients:
+ * row i has entries ptr[i]..ptr[i+1]-1 with column col[e], real val[e] and code[e] = 2 t + imag
+ * (t = monomial index, -1 for M; imag = 1 when the coefficient is i val). */
+int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
+                       const int8_t* code, const double* mono, int nmono, double a, double c, const void* x,
+                       const void* b, void* r, void* stream);
+
 /* rhs = sum_j (c_j F_j - d_j MX_j), j < q, on count complex128 entries (explicit roundings, no
  * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */
 int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
