@@ -1421,13 +1421,13 @@ __device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
 
 // The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
 template <class TF, class TD, int IO>
-__global__ void __launch_bounds__(256)
-k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
+__device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const CompactData<TF>& cd,
+                                                   const SolveIo& io, int block) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int g = lane / kLanesPer, lg = lane % kLanesPer;
-    const int wg = blockIdx.x * nw + wib;
+    const int wg = block * nw + wib;
     const int sys = wg * kGroup + g;
     const bool live = sys < ix.batch;
     const bool wlive = wg < ix.wgroups;
@@ -1584,6 +1584,32 @@ k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
             io_store<TF, IO>(io, sys, n, i, y[i]);
         }
     }
+}
+
+template <class TF, class TD, int IO>
+__global__ void __launch_bounds__(256)
+k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
+    solve_compact_body<TF, TD, IO>(ix, cd, io, blockIdx.x);
+}
+
+// One launch for several buckets (the systems of a whole step): blocks block_start[b] ..
+// block_start[b+1]-1 solve bucket b, so small buckets run beside the large ones.
+constexpr int kMaxMulti = 8;
+template <class TF>
+struct MultiSolve {
+    int nb;
+    int block_start[kMaxMulti + 1];
+    CompactIdx ix[kMaxMulti];
+    CompactData<TF> cd[kMaxMulti];
+    SolveIo io[kMaxMulti];
+};
+
+template <class TF, class TD, int IO>
+__global__ void __launch_bounds__(256)
+k_solve_compact_multi(MultiSolve<TF> ms) {
+    int b = 0;
+    while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
+    solve_compact_body<TF, TD, IO>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
 }
 
 }  // namespace cng
@@ -1799,7 +1825,79 @@ static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io
 
 }  // namespace cng
 
+namespace cng {
+
+template <class TF, class TD, int IO>
+static void launch_multi(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
+                         const std::vector<SolveIo>& ios, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024);
+    });
+    // one warp count for all blocks: the largest that fits every bucket
+    int nw = 8;
+    for (const Banded* h : hs)
+        while (nw > 1 && compact_smem<TF>(*h, nw) > 220 * 1024) --nw;
+    size_t smem = 0;
+    for (const Banded* h : hs) smem = std::max(smem, compact_smem<TF>(*h, nw));
+    if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
+    MultiSolve<TF> ms{};
+    ms.nb = (int)hs.size();
+    // largest buckets first: their long tails start earliest
+    std::vector<int> order(hs.size());
+    for (size_t i = 0; i < hs.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->cWg > hs[b]->cWg; });
+    int blocks = 0;
+    for (int k = 0; k < ms.nb; ++k) {
+        const int i = order[k];
+        ms.block_start[k] = blocks;
+        ms.ix[k] = compact_idx(*hs[i]);
+        ms.cd[k] = cds[i];
+        ms.io[k] = ios[i];
+        blocks += ceil_div(hs[i]->cWg, nw);
+    }
+    ms.block_start[ms.nb] = blocks;
+    k_solve_compact_multi<TF, TD, IO><<<blocks, 32 * nw, smem, st>>>(ms);
+    CNG_LAUNCH("k_solve_compact_multi");
+}
+
+}  // namespace cng
+
 extern "C" {
+
+int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, void* const* x, int fp32,
+                           int accumulate, void* stream) {
+    CNG_TRY({
+        if (nh < 1 || nh > kMaxMulti) throw InvalidArgument("1 to 8 handles per batched solve");
+        if (!hh || !b || !x) throw InvalidArgument("null argument");
+        std::vector<const Banded*> hs;
+        std::vector<SolveIo> ios;
+        for (int k = 0; k < nh; ++k) {
+            const Banded* h = reinterpret_cast<const Banded*>(hh[k]);
+            if (!h || !h->compact_ready || h->dtype != 1)
+                throw InvalidArgument("batched solve needs complex128 handles in compact form");
+            if (fp32 && !h->fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first");
+            if (!b[k] || !x[k] || b[k] == x[k]) throw InvalidArgument("b and x: device pointers, not aliased");
+            hs.push_back(h);
+            ios.push_back(SolveIo{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate});
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (fp32) {
+            std::vector<CompactData<zf>> cds;
+            for (const Banded* h : hs)
+                cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm});
+            launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, st);
+        } else {
+            std::vector<CompactData<zd>> cds;
+            for (const Banded* h : hs)
+                cds.push_back(CompactData<zd>{static_cast<const zd*>(h->c_L), static_cast<const zd*>(h->c_U), h->c_piv,
+                                              static_cast<const zd*>(h->c_V), static_cast<const zd*>(h->w),
+                                              static_cast<const zd*>(h->slu), h->spiv, h->perm});
+            launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, st);
+        }
+    })
+}
 
 int cng_banded_compact(cng_banded* hh, void* stream) {
     CNG_TRY({ cng::compact(*reinterpret_cast<cng::Banded*>(hh), static_cast<cudaStream_t>(stream)); })

@@ -114,15 +114,15 @@ __device__ __forceinline__ void dft8(c2<R>* v, int sign) {
 }
 
 template <class R, int RAD>
-__device__ __forceinline__ void stage(const c2<R>* __restrict__ a, c2<R>* __restrict__ b, int L, int Ns,
+__device__ __forceinline__ void stage(const c2<R>* __restrict__ a, c2<R>* __restrict__ b, int L, int LS, int Ns,
                                       int B, const c2<R>* tw, int sign, int tid, int nthreads) {
     const int Lr = L / RAD;
     const int tstep = L / (Ns * RAD);
     for (int idx = tid; idx < B * Lr; idx += nthreads) {
         const int bt = idx / Lr;
         const int j = idx - bt * Lr;
-        const c2<R>* ab = a + bt * L;
-        c2<R>* bb = b + bt * L;
+        const c2<R>* ab = a + bt * LS;
+        c2<R>* bb = b + bt * LS;
         const int k = j % Ns;
         c2<R> v[RAD];
 #pragma unroll
@@ -145,11 +145,12 @@ __device__ __forceinline__ void stage(const c2<R>* __restrict__ a, c2<R>* __rest
     }
 }
 
-// Transform B sequences in buf0 (length L each, contiguous); result in buf0 or buf1 (returned).
-// tw: L twiddles exp(-2 pi i q / L) in shared memory. Caller synchronizes before the call.
+// Transform B sequences in buf0 (length L each, row stride LS >= L: rows padded against bank
+// conflicts); result in buf0 or buf1 (returned). tw: L twiddles exp(-2 pi i q / L) in shared memory.
+// Caller synchronizes before the call.
 template <class R>
 __device__ c2<R>* smem_fft(c2<R>* buf0, c2<R>* buf1, const FftPlan& p, int B, const c2<R>* tw,
-                           int sign) {
+                           int sign, int LS) {
     const int tid = threadIdx.x, nt = blockDim.x;
     c2<R>* a = buf0;
     c2<R>* b = buf1;
@@ -157,11 +158,11 @@ __device__ c2<R>* smem_fft(c2<R>* buf0, c2<R>* buf1, const FftPlan& p, int B, co
     for (int s = 0; s < p.nstages; ++s) {
         const int rad = p.radix[s];
         switch (rad) {
-            case 2: stage<R, 2>(a, b, p.L, Ns, B, tw, sign, tid, nt); break;
-            case 3: stage<R, 3>(a, b, p.L, Ns, B, tw, sign, tid, nt); break;
-            case 4: stage<R, 4>(a, b, p.L, Ns, B, tw, sign, tid, nt); break;
-            case 5: stage<R, 5>(a, b, p.L, Ns, B, tw, sign, tid, nt); break;
-            default: stage<R, 8>(a, b, p.L, Ns, B, tw, sign, tid, nt); break;
+            case 2: stage<R, 2>(a, b, p.L, LS, Ns, B, tw, sign, tid, nt); break;
+            case 3: stage<R, 3>(a, b, p.L, LS, Ns, B, tw, sign, tid, nt); break;
+            case 4: stage<R, 4>(a, b, p.L, LS, Ns, B, tw, sign, tid, nt); break;
+            case 5: stage<R, 5>(a, b, p.L, LS, Ns, B, tw, sign, tid, nt); break;
+            default: stage<R, 8>(a, b, p.L, LS, Ns, B, tw, sign, tid, nt); break;
         }
         __syncthreads();
         Ns *= rad;
@@ -170,6 +171,76 @@ __device__ c2<R>* smem_fft(c2<R>* buf0, c2<R>* buf1, const FftPlan& p, int B, co
         b = t;
     }
     return a;
+}
+
+// ---- compile-time plans: the same Stockham stages with L, Ns and the radix known at compile time
+template <class R, int L, int Ns, int RAD>
+__device__ __forceinline__ void stage_ct(const c2<R>* __restrict__ a, c2<R>* __restrict__ b, int B,
+                                         const c2<R>* tw, int sign, int LS) {
+    constexpr int Lr = L / RAD;
+    constexpr int tstep = L / (Ns * RAD);
+    const int total = B * Lr;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int bt = idx / Lr;
+        const int j = idx - bt * Lr;
+        const int k = j % Ns;
+        const c2<R>* ab = a + bt * LS;
+        c2<R>* bb = b + bt * LS;
+        c2<R> v[RAD];
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) v[t] = ab[j + t * Lr];
+        if (Ns > 1) {
+#pragma unroll
+            for (int t = 1; t < RAD; ++t) {
+                c2<R> w = tw[t * k * tstep];
+                if (sign > 0) w.y = -w.y;
+                v[t] = mul<R>(v[t], w);
+            }
+        }
+        if constexpr (RAD == 2) dft2<R>(v);
+        else if constexpr (RAD == 3) dft3<R>(v, sign);
+        else if constexpr (RAD == 4) dft4<R>(v, sign);
+        else if constexpr (RAD == 5) dft5<R>(v, sign);
+        else dft8<R>(v, sign);
+        const int d = (j / Ns) * Ns * RAD + k;
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) bb[d + t * Ns] = v[t];
+    }
+}
+
+template <class R, int L, int Ns, int RAD, int... REST>
+__device__ __forceinline__ c2<R>* run_ct(c2<R>* a, c2<R>* b, int B, const c2<R>* tw, int sign, int LS) {
+    stage_ct<R, L, Ns, RAD>(a, b, B, tw, sign, LS);
+    __syncthreads();
+    if constexpr (sizeof...(REST) == 0) {
+        return b;
+    } else {
+        return run_ct<R, L, Ns * RAD, REST...>(b, a, B, tw, sign, LS);
+    }
+}
+
+// Lengths of the benchmark configurations get compile-time plans; others take the runtime plan.
+template <class R>
+__device__ c2<R>* smem_fft_fast(c2<R>* b0, c2<R>* b1, const FftPlan& p, int B, const c2<R>* tw, int sign,
+                                int LS) {
+    switch (p.L) {
+        case 12: return run_ct<R, 12, 1, 4, 3>(b0, b1, B, tw, sign, LS);
+        case 24: return run_ct<R, 24, 1, 8, 3>(b0, b1, B, tw, sign, LS);
+        case 30: return run_ct<R, 30, 1, 2, 3, 5>(b0, b1, B, tw, sign, LS);
+        case 32: return run_ct<R, 32, 1, 8, 4>(b0, b1, B, tw, sign, LS);
+        case 48: return run_ct<R, 48, 1, 4, 4, 3>(b0, b1, B, tw, sign, LS);
+        case 64: return run_ct<R, 64, 1, 8, 8>(b0, b1, B, tw, sign, LS);
+        case 72: return run_ct<R, 72, 1, 8, 3, 3>(b0, b1, B, tw, sign, LS);
+        case 96: return run_ct<R, 96, 1, 8, 4, 3>(b0, b1, B, tw, sign, LS);
+        case 128: return run_ct<R, 128, 1, 8, 4, 4>(b0, b1, B, tw, sign, LS);
+        case 144: return run_ct<R, 144, 1, 4, 4, 3, 3>(b0, b1, B, tw, sign, LS);
+        case 192: return run_ct<R, 192, 1, 8, 8, 3>(b0, b1, B, tw, sign, LS);
+        case 200: return run_ct<R, 200, 1, 8, 5, 5>(b0, b1, B, tw, sign, LS);
+        case 256: return run_ct<R, 256, 1, 8, 8, 4>(b0, b1, B, tw, sign, LS);
+        case 288: return run_ct<R, 288, 1, 8, 4, 3, 3>(b0, b1, B, tw, sign, LS);
+        case 384: return run_ct<R, 384, 1, 8, 4, 4, 3>(b0, b1, B, tw, sign, LS);
+        default: return smem_fft<R>(b0, b1, p, B, tw, sign, LS);
+    }
 }
 
 }  // namespace cng

@@ -134,7 +134,7 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         b0[e] = z;
     }
     __syncthreads();
-    c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, +1);
+    c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, +1, M);
     // f_{2j} = z_j, f_{2j+1} = z_{M-1-j}
     for (int e = tid; e < B * M; e += nt) {
         const int t = e / M, j = e - t * M;
@@ -172,7 +172,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         b0[(size_t)t * M + dst] = v;
     }
     __syncthreads();
-    c2<R>* Z = smem_fft<R>(b0, b1, plan, B, tw, -1);
+    c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, M);
     const R invM = R(1) / R(M);
     for (int e = tid; e < B * N; e += nt) {
         const int t = e / N, k = e - t * N;
@@ -197,10 +197,10 @@ template <class R>
 __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long outer, int inner,
                            int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
     extern __shared__ __align__(16) unsigned char sm[];
-    const int L = plan.L;
+    const int L = plan.L, LS = L + 1;        // padded rows: the column-wise staging is conflict-free
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
     c2<R>* b0 = tw + L;
-    c2<R>* b1 = b0 + (size_t)B * L;
+    c2<R>* b1 = b0 + (size_t)B * LS;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int chunks = (inner + B - 1) / B;
@@ -212,26 +212,26 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     const c2<R>* src = in + o * (long long)lin * inner;
     c2<R>* dst = out + o * (long long)lout * inner;
     if (!forward) {
-        for (int e = tid; e < B * L; e += nt) b0[e] = mk<R>(0, 0);
+        for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
         __syncthreads();
         for (int e = tid; e < B * Nc; e += nt) {
             const int k = e / B, t = e - k * B;
             if (i0 + t >= inner || k == K) continue;
             const int slot = k < K ? k : L - (Nc - k);
-            b0[(size_t)t * L + slot] = src[(long long)k * inner + i0 + t];
+            b0[(size_t)t * LS + slot] = src[(long long)k * inner + i0 + t];
         }
     } else {
         for (int e = tid; e < B * L; e += nt) {
             const int k = e / B, t = e - k * B;
-            b0[(size_t)t * L + k] = (i0 + t < inner) ? src[(long long)k * inner + i0 + t] : mk<R>(0, 0);
+            b0[(size_t)t * LS + k] = (i0 + t < inner) ? src[(long long)k * inner + i0 + t] : mk<R>(0, 0);
         }
     }
     __syncthreads();
-    c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, forward ? -1 : +1);
+    c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, forward ? -1 : +1, LS);
     if (!forward) {
         for (int e = tid; e < B * L; e += nt) {
             const int k = e / B, t = e - k * B;
-            if (i0 + t < inner) dst[(long long)k * inner + i0 + t] = r[(size_t)t * L + k];
+            if (i0 + t < inner) dst[(long long)k * inner + i0 + t] = r[(size_t)t * LS + k];
         }
     } else {
         const R invL = R(1) / R(L);
@@ -239,7 +239,7 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
             const int k = e / B, t = e - k * B;
             if (i0 + t >= inner) continue;
             c2<R> v = mk<R>(0, 0);
-            if (k != K) v = scl<R>(invL, r[(size_t)t * L + (k < K ? k : L - (Nc - k))]);
+            if (k != K) v = scl<R>(invL, r[(size_t)t * LS + (k < K ? k : L - (Nc - k))]);
             dst[(long long)k * inner + i0 + t] = v;
         }
     }
@@ -253,10 +253,10 @@ template <class R>
 __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out_, long long outer, int inner,
                             int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
     extern __shared__ __align__(16) unsigned char sm[];
-    const int L = plan.L;
+    const int L = plan.L, LS = L + 1;
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
     c2<R>* b0 = tw + L;
-    c2<R>* b1 = b0 + (size_t)B * L;
+    c2<R>* b1 = b0 + (size_t)B * LS;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int pairs = inner / 2;
@@ -266,7 +266,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     if (!forward) {
         const c2<R>* src = static_cast<const c2<R>*>(in_) + o * (long long)K * inner;
         R* dst = static_cast<R*>(out_) + o * (long long)L * inner;
-        for (int e = tid; e < B * L; e += nt) b0[e] = mk<R>(0, 0);
+        for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
         __syncthreads();
         // Z_k = A_k + i B_k, Z_{L-k} = conj(A_k) + i conj(B_k)
         for (int e = tid; e < B * K; e += nt) {
@@ -276,19 +276,19 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             c2<R> A = src[(long long)k * inner + 2 * p];
             c2<R> Bv = src[(long long)k * inner + 2 * p + 1];
             if (k == 0) {
-                b0[(size_t)t * L] = mk<R>(A.x - Bv.y, A.y + Bv.x);
+                b0[(size_t)t * LS] = mk<R>(A.x - Bv.y, A.y + Bv.x);
             } else {
-                b0[(size_t)t * L + k] = mk<R>(A.x - Bv.y, A.y + Bv.x);
-                b0[(size_t)t * L + L - k] = mk<R>(A.x + Bv.y, -A.y + Bv.x);
+                b0[(size_t)t * LS + k] = mk<R>(A.x - Bv.y, A.y + Bv.x);
+                b0[(size_t)t * LS + L - k] = mk<R>(A.x + Bv.y, -A.y + Bv.x);
             }
         }
         __syncthreads();
-        c2<R>* r = smem_fft<R>(b0, b1, plan, B, tw, +1);
+        c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, +1, LS);
         for (int e = tid; e < B * L; e += nt) {
             const int j = e / B, t = e - j * B;
             const int p = p0 + t;
             if (p >= pairs) continue;
-            c2<R> z = r[(size_t)t * L + j];
+            c2<R> z = r[(size_t)t * LS + j];
             R* d = dst + (long long)j * inner + 2 * p;
             d[0] = z.x;
             d[1] = z.y;
@@ -304,17 +304,17 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
                 const R* s = src + (long long)j * inner + 2 * p;
                 z = mk<R>(s[0], s[1]);
             }
-            b0[(size_t)t * L + j] = z;
+            b0[(size_t)t * LS + j] = z;
         }
         __syncthreads();
-        c2<R>* Z = smem_fft<R>(b0, b1, plan, B, tw, -1);
+        c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, LS);
         const R h = R(0.5) / R(L);
         for (int e = tid; e < B * K; e += nt) {
             const int k = e / B, t = e - k * B;
             const int p = p0 + t;
             if (p >= pairs) continue;
-            c2<R> zk = Z[(size_t)t * L + k];
-            c2<R> zm = conjg<R>(Z[(size_t)t * L + (k == 0 ? 0 : L - k)]);
+            c2<R> zk = Z[(size_t)t * LS + k];
+            c2<R> zm = conjg<R>(Z[(size_t)t * LS + (k == 0 ? 0 : L - k)]);
             c2<R> A = scl<R>(h, add<R>(zk, zm));
             c2<R> d = sub<R>(zk, zm);                      // B = d / (2i)
             c2<R> Bv = mk<R>(h * d.y, -h * d.x);
@@ -563,8 +563,8 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_fft_axis<R>); });
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L, 0, 16);
-    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * L);
+    const int B = pick_B<R>(L + 1, 0, 16);
+    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * ((inner + B - 1) / B);
     k_fft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
     CNG_LAUNCH("k_fft_axis");
@@ -579,8 +579,8 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L, 0, 16);
-    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * L);
+    const int B = pick_B<R>(L + 1, 0, 16);
+    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * ((inner / 2 + B - 1) / B);
     k_rfft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
     CNG_LAUNCH("k_rfft_axis");

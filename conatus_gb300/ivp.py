@@ -354,23 +354,32 @@ class DeviceProblem:
                      1.0, 0.0, xb[sl].data_ptr(), rb[sl].data_ptr(), ob[sl].data_ptr(), s)
 
     def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
-        """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias). FP32 form: FP32
-        solve, FP64 residual, FP32 correction added in FP64 (one refinement step)."""
+        """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias), every bucket in one
+        launch. FP32 form: FP32 solve, FP64 residual, FP32 correction added in FP64 (one
+        refinement step)."""
         s = _stream_handle(stream)
         fs = self.factor(a, b_, stream)
-        if self.precision == "fp64":
+        if not self.compact:
             for bi, h in enumerate(fs):
-                call("cng_banded_solve_mapped", h.h, self.bucket(rhs, bi).data_ptr(), None,
-                     self.bucket(out, bi).data_ptr(), None, s)
+                if self.precision == "fp64":
+                    call("cng_banded_solve_mapped", h.h, self.bucket(rhs, bi).data_ptr(), None,
+                         self.bucket(out, bi).data_ptr(), None, s)
+                else:
+                    raise ValueError("the FP32 form needs the compact solve")
+            return
+        nb = len(fs)
+        hs = (ctypes.c_void_p * nb)(*[h.h.value for h in fs])
+        bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in range(nb)])
+        xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in range(nb)])
+        if self.precision == "fp64":
+            call("cng_banded_solve_batch", nb, hs, bp, xp, 0, 0, s)
             return
         if self._R2 is None:
             self._R2 = self.zeros()
-        for bi, h in enumerate(fs):
-            call("cng_banded_solve_fp32", h.h, self.bucket(rhs, bi).data_ptr(), self.bucket(out, bi).data_ptr(), 0, s)
+        call("cng_banded_solve_batch", nb, hs, bp, xp, 1, 0, s)
         self.residual(a, b_, out, rhs, self._R2, s)
-        for bi, h in enumerate(fs):
-            call("cng_banded_solve_fp32", h.h, self.bucket(self._R2, bi).data_ptr(),
-                 self.bucket(out, bi).data_ptr(), 1, s)
+        rp = (ctypes.c_void_p * nb)(*[self.bucket(self._R2, bi).data_ptr() for bi in range(nb)])
+        call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
 
     def zeros(self):
         torch = _torch()
@@ -553,7 +562,10 @@ class IVPSolver:
         nb = len(self.dev.tpl.buckets)
         d = self.dev.d
         f = 2 * nb + 2 + (2 if d >= 1 else 2) + (2 if d >= 2 else 0) + 1 + (1 if self.dev.has_b0 else 0)
-        solve = nb if self.dev.precision == "fp64" else 3 * nb
+        if self.dev.compact:
+            solve = 1 if self.dev.precision == "fp64" else 2 + nb
+        else:
+            solve = nb
         return nb + f + 1 + solve
 
     def synchronize(self) -> None:

@@ -98,6 +98,12 @@ int cng_banded_solve_transpose(const cng_banded* h, void* b, void* stream);
  * core/src/cuda/banded.cu:824-1121). */
 int cng_banded_compact(cng_banded* h, void* stream);
 
+/* One launch solving nh (<= 8) compact complex128 handles: x[k] = A_k^{-1} b[k] (fp32: with the FP32
+ * factors, accumulate: x += ...). The buckets of a whole step in one launch, large ones first,
+ * so that the latency of small buckets hides behind the large ones. */
+int cng_banded_solve_batch(int nh, cng_banded* const* h, const void* const* b, void* const* x, int fp32,
+                           int accumulate, void* stream);
+
 /* Mixed precision: keep FP32 (complex64) copies of the FP64 factors (allocates; refreshed by
  * refactor_shared). No reference counterpart: the FP32 + FP64-refinement form of the solve. */
 int cng_banded_make_fp32(cng_banded* h, void* stream);

@@ -33,8 +33,8 @@ def _workload_state(tname, P, rng):
     return W.burgers_state(P)
 
 
-@pytest.mark.parametrize("tname,sizes,scheme,dt", [("rb_nz16", [32], "SBDF2", 1e-4),
-                                                   ("channel_ny17", [16, 12], "SBDF3", 5e-3),
+@pytest.mark.parametrize("tname,sizes,scheme,dt", [("rb_nz64", [64], "SBDF2", 1e-4),
+                                                   ("channel_ny129", [24, 24], "SBDF3", 5e-3),
                                                    ("burgers_n128", None, "SBDF2", 1e-4)])
 def test_mixed_matches_fp64(tname, sizes, scheme, dt, rng, cuda_lib):
     import torch
