@@ -44,6 +44,8 @@ _SIGS = {
     "cng_banded_solve_batch": [c_int, P, P, P, c_int, c_int, P],
     "cng_banded_solve_fp32": [P, P, P, c_int, P],
     "cng_poly_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P],
+    "cng_twiddle_table": [c_int, c_int, P],
+    "cng_fourier_ensemble_step": [P, P, P, P, c_int, P, P, c_double, P],
     "cng_rhs_create": [P, P],
     "cng_rhs_destroy": [P],
     "cng_rhs_evaluate": [P, P, P, P],
@@ -52,6 +54,7 @@ _SIGS = {
     "cng_fft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],
     "cng_rfft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],
     "cng_csr_matvec": [c_int, c_int, P, P, P, c_int, P, P, P],
+    "cng_csr_matvec_real": [c_int, c_int, P, P, P, P, P, P],
     "cng_sbdf_rhs": [c_int, P, P, P, P, P, ctypes.c_int64, P],
     "cng_split_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P],
     "cng_graph_begin": [P],

@@ -383,18 +383,19 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         }
         __syncwarp();
         // Chebyshev derivative oy times: out[n] = out[n+2] + 2 (n+1) c[n+1], out[0] /= 2, x 2/L
+        // (in the transform precision R: the recurrence is part of F)
         for (int rep = 0; rep < oy; ++rep) {
             if (lane < 2) {
                 const int par = lane;                 // chain of entries n with n % 2 == par
                 int start = Ny - 2;
                 if ((start & 1) != par) start -= 1;
-                double2 acc = make_double2(0.0, 0.0);
-                if (Ny - 1 >= 0 && ((Ny - 1) & 1) == par) der[Ny - 1] = make_double2(0.0, 0.0);
+                R accx = R(0), accy = R(0);
+                if (((Ny - 1) & 1) == par) der[Ny - 1] = make_double2(0.0, 0.0);
                 for (int nn = start; nn >= 0; nn -= 2) {
-                    const double t = 2.0 * (nn + 1);
-                    acc.x = acc.x + t * col[nn + 1].x;
-                    acc.y = acc.y + t * col[nn + 1].y;
-                    der[nn] = acc;
+                    const R t = R(2 * (nn + 1));
+                    accx = accx + t * R(col[nn + 1].x);
+                    accy = accy + t * R(col[nn + 1].y);
+                    der[nn] = make_double2((double)accx, (double)accy);
                 }
             }
             __syncwarp();
@@ -540,6 +541,10 @@ static int pick_B(int L, int extra_per_col, int maxB) {
 template <class R>
 void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st) {
     if (ncols <= 0) return;
+    if (N == 1 && M == 1) {        // no Chebyshev direction: the single coefficient is the value
+        CNG_CUDA(cudaMemcpyAsync(out, in, sizeof(c2<R>) * (size_t)ncols, cudaMemcpyDeviceToDevice, st));
+        return;
+    }
     static std::once_flag f1, f2;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_cheb_bwd<R>); });
     std::call_once(f2, [] { set_smem_attr<R>((const void*)k_cheb_fwd<R>); });
@@ -726,7 +731,8 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     if (D->ndir < 0 || D->ndir > 2) throw InvalidArgument("0, 1 or 2 Fourier directions");
     h->nx = D->nx; h->nz = D->nz; h->mx = D->mx; h->mz = D->mz; h->ny = D->ny; h->my = D->my;
     h->lx = D->lx; h->lz = D->lz; h->ly = D->ly;
-    if (h->ny < 1 || h->my < h->ny || h->my % 2) throw InvalidArgument("Chebyshev grid my must be even and >= ny");
+    if (!(h->ny == 1 && h->my == 1) && (h->ny < 1 || h->my < h->ny || h->my % 2))
+        throw InvalidArgument("Chebyshev grid my must be even and >= ny (ny = my = 1: no Chebyshev direction)");
     if (h->ndir >= 1) {
         if (h->nx % 2 || h->mx < h->nx) throw InvalidArgument("Fourier sizes: nx even, mx >= nx");
         h->Kx = h->nx / 2;
@@ -833,6 +839,15 @@ int cng_rhs_create(const cng_rhs_desc* desc, cng_rhs** out) {
         if (!out) throw InvalidArgument("null output handle");
         *out = nullptr;
         *out = reinterpret_cast<cng_rhs*>(build_rhs(desc));
+    })
+}
+
+int cng_twiddle_table(int length, int precision, const void** table) {
+    CNG_TRY({
+        if (!table) throw InvalidArgument("null output");
+        make_plan(length);
+        *table = precision ? static_cast<const void*>(twiddles<float>().get(length, 0))
+                           : static_cast<const void*>(twiddles<double>().get(length, 0));
     })
 }
 

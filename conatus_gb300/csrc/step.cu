@@ -28,6 +28,39 @@ __global__ void k_csr_matvec(int nsys, int n, const int* __restrict__ ip, const 
     }
 }
 
+// y = M x with real M values (M of the tau systems is real: conversions between Chebyshev and
+// ultraspherical bases); two rows per thread and two partial sums per row for independent FP64
+// chains (FP64 latency is long on this part).
+__global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
+                                  const double* __restrict__ val, const double2* __restrict__ x,
+                                  double2* __restrict__ y) {
+    const long long total = (long long)nsys * n;
+    const long long half = (total + 1) / 2;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < half;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long rows[2] = {t, t + half};
+        double ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const long long r = rows[u];
+            if (r >= total) continue;
+            const long long m = r / n;
+            const int i = (int)(r - m * n);
+            const double2* xm = x + m * n;
+            int q = 0;
+            for (int p = ip[i]; p < ip[i + 1]; ++p, q ^= 1) {
+                const double a = val[p];
+                const double2 b = xm[ix[p]];
+                ar[u][q] += a * b.x;
+                ai[u][q] += a * b.y;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+            if (rows[u] < total) y[rows[u]] = make_double2(ar[u][0] + ar[u][1], ai[u][0] + ai[u][1]);
+    }
+}
+
 struct SbdfArgs {
     int q;
     double c[4], d[4];
@@ -96,22 +129,24 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
         const int i = (int)(t - m * n);
         const double2* xm = x + m * n;
         const double* mv = mono + m * nmono;
-        double ar = 0.0, ai = 0.0;
-        for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+        double ar[2] = {0.0, 0.0}, ai[2] = {0.0, 0.0};
+        int q = 0;
+        for (int e = ptr[i]; e < ptr[i + 1]; ++e, q ^= 1) {
             const int cd = code[e];
             const int tt = cd >> 1;                         // -1: M
             const double s = val[e] * (tt < 0 ? a : c * mv[tt]);
             const double2 xv = xm[col[e]];
             if (cd & 1) {                                   // i s x
-                ar -= s * xv.y;
-                ai += s * xv.x;
+                ar[q] -= s * xv.y;
+                ai[q] += s * xv.x;
             } else {
-                ar += s * xv.x;
-                ai += s * xv.y;
+                ar[q] += s * xv.x;
+                ai[q] += s * xv.y;
             }
         }
+        const double arr = ar[0] + ar[1], aii = ai[0] + ai[1];
         const double2 bv = b[t];
-        r[t] = make_double2(bv.x - ar, bv.y - ai);
+        r[t] = make_double2(bv.x - arr, bv.y - aii);
     }
 }
 
@@ -133,6 +168,20 @@ int cng_csr_matvec(int nsys, int n, const int32_t* indptr, const int32_t* indice
             nsys, n, indptr, indices, static_cast<const double2*>(values), values_per_system,
             static_cast<const double2*>(x), static_cast<double2*>(y));
         CNG_LAUNCH("k_csr_matvec");
+    })
+}
+
+int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* indices, const double* values,
+                        const void* x, void* y, void* stream) {
+    CNG_TRY({
+        if (!indptr || !indices || !values || !x || !y) throw InvalidArgument("null device pointer");
+        if (x == y) throw InvalidArgument("x and y must not alias");
+        if (nsys <= 0 || n <= 0) return CNG_OK;
+        const long long half = ((long long)nsys * n + 1) / 2;
+        const int blocks = (int)std::min<long long>((half + 255) / 256, 152LL * 32);
+        k_csr_matvec_real<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            nsys, n, indptr, indices, values, static_cast<const double2*>(x), static_cast<double2*>(y));
+        CNG_LAUNCH("k_csr_matvec_real");
     })
 }
 

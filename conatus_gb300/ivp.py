@@ -103,7 +103,12 @@ class DeviceProblem:
             self._pat.append((ip, ix))
             if b.m_is_constant() and b.exact is None:
                 t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
-                self._M.append((torch.as_tensor(b.Mc[t0].astype(np.complex128), device=self.device), 0))
+                mc = b.Mc[t0].astype(np.complex128)
+                if np.all(mc.imag == 0):       # real mass matrix: the real-valued kernel
+                    self._M.append((torch.as_tensor(mc, device=self.device),
+                                    torch.as_tensor(np.ascontiguousarray(mc.real), device=self.device)))
+                else:
+                    self._M.append((torch.as_tensor(mc, device=self.device), 0))
             else:
                 self._M.append((torch.as_tensor(problem.values(bi, "M"), device=self.device).contiguous(), 1))
         self._L = [None] * len(tpl.buckets)
@@ -131,11 +136,11 @@ class DeviceProblem:
         if d >= 1:
             desc.nx = P.fourier_sizes[0]
             desc.mx = smooth_size(int(math.floor(P.fourier_sizes[0] * ax[fa[0]].get("dealias", 1.5))))
-            desc.lx = ax[fa[0]]["L"]
+            desc.lx = P.lengths[0]
         if d >= 2:
             desc.nz = P.fourier_sizes[1]
             desc.mz = smooth_size(int(math.floor(P.fourier_sizes[1] * ax[fa[1]].get("dealias", 1.5))))
-            desc.lz = ax[fa[1]]["L"]
+            desc.lz = P.lengths[1]
         if ca >= 0:
             desc.ny = ax[ca]["N"]
             desc.my = smooth_size(ax[ca]["M"], even=True)
@@ -247,6 +252,10 @@ class DeviceProblem:
         for bi, b in enumerate(self.tpl.buckets):
             ip, ix = self._pat[bi]
             vals, per = self._M[bi]
+            if not isinstance(per, int):                 # shared real values
+                call("cng_csr_matvec_real", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), per.data_ptr(),
+                     self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
+                continue
             call("cng_csr_matvec", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), vals.data_ptr(), per,
                  self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
 
@@ -267,6 +276,7 @@ class DeviceProblem:
             f = []
             for bi, b in enumerate(self.tpl.buckets):
                 Mv, per = self._M[bi]
+                per = per if isinstance(per, int) else 0
                 Lv = self._Lvals(bi)
                 vals = (a * (Mv if per else Mv.unsqueeze(0)) + b_ * Lv).contiguous()
                 h = _Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
@@ -344,6 +354,7 @@ class DeviceProblem:
             key = (float(a), float(b_))
             if key not in data:
                 Mv, per = self._M[bi]
+                per = per if isinstance(per, int) else 0
                 data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
                              b_ * self._Lvals(bi)).contiguous()
             ip, ix = self._pat[bi]

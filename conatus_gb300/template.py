@@ -141,9 +141,11 @@ class ProblemTemplate:
     def ncheb(self) -> int:
         return self.axes[self.cheb_axis]["N"] if self.cheb_axis >= 0 else 1
 
-    def instantiate(self, fourier_sizes=None) -> "Problem":
-        """The systems of this template at the given RealFourier sizes (default: the template's)."""
-        return Problem(self, fourier_sizes)
+    def instantiate(self, fourier_sizes=None, lengths=None) -> "Problem":
+        """The systems of this template at the given RealFourier sizes (default: the template's) and,
+        optionally, other periods of the Fourier directions (the operators are polynomials in the
+        wavenumbers 2 pi j / L, so the period is a free parameter)."""
+        return Problem(self, fourier_sizes, lengths)
 
 
 def _cplx_json(v):
@@ -160,7 +162,7 @@ def _cplx_from(v):
 class Problem:
     """A template at a Fourier resolution: the systems (modes, wavenumbers) of every bucket."""
 
-    def __init__(self, tpl: ProblemTemplate, fourier_sizes=None):
+    def __init__(self, tpl: ProblemTemplate, fourier_sizes=None, lengths=None):
         self.tpl = tpl
         d = len(tpl.fourier_axes)
         if fourier_sizes is None:
@@ -173,7 +175,10 @@ class Problem:
                 raise ValueError("Fourier sizes must be even (Nyquist convention)")
         self.fourier_sizes = fourier_sizes
         self.K = [s // 2 for s in fourier_sizes]
-        self.lengths = [tpl.axes[a]["L"] for a in tpl.fourier_axes]
+        self.lengths = [float(x) for x in lengths] if lengths is not None else \
+            [tpl.axes[a]["L"] for a in tpl.fourier_axes]
+        if len(self.lengths) != d:
+            raise ValueError(f"{tpl.name}: {d} periods expected")
         # grid sizes: the reference's dealiasing rule floor(N * 3/2) scaled from the template
         self.modes, self.wavenumbers, self.offsets = [], [], []
         off = 0
@@ -191,6 +196,12 @@ class Problem:
             self.offsets.append(off)
             off += modes.shape[0] * b.n
         self.n_total = off           # complex unknowns of the mode layout
+
+    def axis_length(self, ax: int) -> float:
+        """Length of coordinate axis ``ax`` of this instance."""
+        if ax in self.tpl.fourier_axes:
+            return self.lengths[self.tpl.fourier_axes.index(ax)]
+        return self.tpl.axes[ax]["L"]
 
     @property
     def nsys(self):

@@ -182,6 +182,43 @@ int cng_fft_axis(int forward, const void* in, void* out, int64_t outer, int inne
 int cng_rfft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int nmodes,
                   int length, void* stream);
 
+/* Device table exp(-2 pi i q / length), q < length (complex128, or complex64 when precision = 1),
+ * owned by the library (one per length and precision, kept until exit). */
+int cng_twiddle_table(int length, int precision, const void** table);
+
+/* ---- ensembles of one-dimensional periodic problems ------------------------------------------ */
+
+/* Members of different sizes and periods advanced by one launch per step (one CTA per member).
+ * Per member (device arrays): N (even), grid M (3/2 dealiased, 2^a 3^b 5^c), offset of its N/2
+ * complex mode amplitudes in the ensemble state, period, index of its grid size in plan_sizes.
+ * The right-hand side is a polynomial in up to 4 factors (i k)^order u of one field; M(k), L(k)
+ * are polynomials of degree <= 4 in k (coefficients as re, im pairs) for k > 0, m_mean/l_mean the
+ * mean mode. precision 0: FFTs and products in FP64; 1: in FP32 (state, history, solve FP64). */
+typedef struct {
+    int32_t nmem, precision, nfactors, nmono, nplans;
+    const int32_t* size_dev;
+    const int32_t* grid_dev;
+    const int64_t* offset_dev;
+    const double* length_dev;
+    const int32_t* plan_dev;
+    int32_t plan_sizes[4];
+    const void* twiddles64[4];
+    const void* twiddles32[4];
+    int32_t factor_order[4];
+    double mono_coef[4];
+    int32_t mono_factors[16];
+    double m_poly[10], l_poly[10];
+    double m_mean[2], l_mean[2];
+} cng_fourier_ensemble_desc;
+
+/* One SBDF-q step of every member: MXh[0], Fh[0] receive M C and F of the current state (the
+ * newest history slot), MXh[j], Fh[j] (j < q) hold the older ones; c[j], d[j] the weights of F_j and
+ * M C_j (d includes 1/dt), a0dt = a_0/dt. X is advanced in place. The reference advances ensemble
+ * members through batched GlobalSystem solves (python/conatus/ensembles/batched.py:442-613, one
+ * discretization per ensemble); here the sizes may differ within one launch. */
+int cng_fourier_ensemble_step(const cng_fourier_ensemble_desc* desc, void* X, void* const* MXh, void* const* Fh,
+                              int q, const double* c, const double* d, double a0dt, void* stream);
+
 /* ---- IMEX step pieces ------------------------------------------------------------------------ */
 
 /* y = M x per system of a bucket sharing one CSR pattern (indptr/indices device int32, n rows):
@@ -203,6 +240,11 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
 int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
                        const int8_t* code, const double* mono, int nmono, double a, double c, const void* x,
                        const void* b, void* r, void* stream);
+
+/* y = M x with one real value array shared by every system of the bucket (the mass matrices of the
+ * tau systems are real). */
+int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* indices, const double* values,
+                        const void* x, void* y, void* stream);
 
 /* rhs = sum_j (c_j F_j - d_j MX_j), j < q, on count complex128 entries (explicit roundings, no
  * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */

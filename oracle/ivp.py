@@ -288,9 +288,9 @@ class OracleProblem:
             for ax, o in enumerate(orders):
                 for _ in range(o):
                     if tpl.axes[ax]["kind"] == "Chebyshev":
-                        a = _along(cheb_diff, a, ax, tpl.axes[ax]["L"])
+                        a = _along(cheb_diff, a, ax, self.P.axis_length(ax))
                     else:
-                        a = _along(rf_diff, a, ax, tpl.axes[ax]["L"])
+                        a = _along(rf_diff, a, ax, self.P.axis_length(ax))
             G.append(a)
         return G
 

@@ -13,7 +13,10 @@ STEP_CASES = {
     "step_burgers128.npz": ("burgers_n128", []),
     "step_rb32x16.npz": ("rb_nz16", [32]),
     "step_channel8x17x8.npz": ("channel_ny17", [8, 8]),
+    "step_ks64.npz": ("ks", [64]),
 }
+# periods of the fixtures whose period differs from the template's
+STEP_LENGTHS = {"step_ks64.npz": [37.0]}
 
 
 def template(name):
@@ -26,7 +29,7 @@ def load_step(fixture, exact=True):
     reference's own M and L values recorded in the fixture (the drop-in case); else the
     template's wavenumber polynomials."""
     tname, sizes = STEP_CASES[fixture]
-    P = template(tname).instantiate(sizes or None)
+    P = template(tname).instantiate(sizes or None, STEP_LENGTHS.get(fixture))
     g = golden(fixture)
     maps = []
     for bi in range(int(g["nb"])):

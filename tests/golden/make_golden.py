@@ -149,11 +149,13 @@ def step_fixtures(cn, out_dir, rng):
     FP64 implementations cannot be told apart."""
     from conatus_gb300.problems import make_problems as mp
     from conatus_gb300.reference_adapter import reference_maps, scatter_state, template_from_solver
-    cases = [("burgers128", "burgers_n128"), ("rb32x16", "rb_nz16_32"), ("channel8x17x8", "channel_ny17_8")]
+    cases = [("burgers128", "burgers_n128"), ("rb32x16", "rb_nz16_32"), ("channel8x17x8", "channel_ny17_8"),
+             ("ks64", "ks")]
     builds = {
         "burgers128": ("burgers", dict(N=128, scheme="SBDF2", dt=1e-4), {}),
         "rb32x16": ("rayleigh_benard", dict(N=(32, 16), scheme="SBDF2", dt=1e-4), dict(Ra=1e6, Pr=1.0)),
         "channel8x17x8": ("channel", dict(N=(8, 17, 8), scheme="SBDF3", dt=5e-3), dict(Re=4000.0)),
+        "ks64": ("kuramoto_sivashinsky", dict(N=64, scheme="SBDF2", dt=1e-2), dict(L=37.0)),
     }
     for name, _ in cases:
         fn, kw, params = builds[name]
