@@ -259,7 +259,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     c2<R>* b1 = b0 + (size_t)B * LS;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
-    const int pairs = inner / 2;
+    const int pairs = (inner + 1) / 2;             // an odd last column is paired with zero
     const int chunks = (pairs + B - 1) / B;
     const long long o = blockIdx.x / chunks;
     const int p0 = (blockIdx.x - o * chunks) * B;     // first pair
@@ -274,7 +274,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             const int p = p0 + t;
             if (p >= pairs) continue;
             c2<R> A = src[(long long)k * inner + 2 * p];
-            c2<R> Bv = src[(long long)k * inner + 2 * p + 1];
+            c2<R> Bv = 2 * p + 1 < inner ? src[(long long)k * inner + 2 * p + 1] : mk<R>(0, 0);
             if (k == 0) {
                 b0[(size_t)t * LS] = mk<R>(A.x - Bv.y, A.y + Bv.x);
             } else {
@@ -291,7 +291,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             c2<R> z = r[(size_t)t * LS + j];
             R* d = dst + (long long)j * inner + 2 * p;
             d[0] = z.x;
-            d[1] = z.y;
+            if (2 * p + 1 < inner) d[1] = z.y;
         }
     } else {
         const R* src = static_cast<const R*>(in_) + o * (long long)L * inner;
@@ -302,7 +302,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             c2<R> z = mk<R>(0, 0);
             if (p < pairs) {
                 const R* s = src + (long long)j * inner + 2 * p;
-                z = mk<R>(s[0], s[1]);
+                z = mk<R>(s[0], 2 * p + 1 < inner ? s[1] : R(0));
             }
             b0[(size_t)t * LS + j] = z;
         }
@@ -319,7 +319,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             c2<R> d = sub<R>(zk, zm);                      // B = d / (2i)
             c2<R> Bv = mk<R>(h * d.y, -h * d.x);
             dst[(long long)k * inner + 2 * p] = A;
-            dst[(long long)k * inner + 2 * p + 1] = Bv;
+            if (2 * p + 1 < inner) dst[(long long)k * inner + 2 * p + 1] = Bv;
         }
     }
 }
@@ -579,14 +579,13 @@ template <class R>
 void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int K, int L, bool forward,
                       cudaStream_t st) {
     if (outer <= 0 || inner <= 0) return;
-    if (inner % 2) throw InvalidArgument("real FFT along the outer axis needs an even inner size");
     static std::once_flag f1;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
     const int B = pick_B<R>(L + 1, 0, 16);
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
-    const long long blocks = outer * ((inner / 2 + B - 1) / B);
+    const long long blocks = outer * (((inner + 1) / 2 + B - 1) / B);
     k_rfft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
     CNG_LAUNCH("k_rfft_axis");
 }

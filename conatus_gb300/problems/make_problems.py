@@ -35,6 +35,12 @@ SPECS = {
     "channel_ny129": ("channel", dict(N=(8, 129, 8), scheme="SBDF3", dt=5e-3), dict(Re=4000.0)),
     "ks": ("kuramoto_sivashinsky", dict(N=16, scheme="SBDF2", dt=1e-2), dict(L=22.0)),
 }
+# serving mix: Burgers at N = 64, 96, .. 512 with L linear in nu; RB at Nz = 32 .. 96 with L linear in Ra
+LINEAR = {}
+for _n in range(64, 513, 32):
+    LINEAR[f"burgers_n{_n}_nu"] = ("burgers", dict(N=_n, scheme="SBDF2", dt=1e-4), "nu", {})
+for _nz in (32, 48, 64, 80, 96):
+    LINEAR[f"rb_nz{_nz}_ra"] = ("rayleigh_benard", dict(N=(16, _nz), scheme="SBDF2", dt=1e-4), "Ra", dict(Pr=1.0))
 
 
 def main():
@@ -46,6 +52,31 @@ def main():
     import make_golden as mg
     cn = mg.import_reference(args.ref)
     from conatus_gb300.reference_adapter import template_from_solver
+    for name, (fn, kw, pname, fixed) in LINEAR.items():
+        if args.only and name != args.only and args.only != "linear":
+            continue
+        t0 = time.time()
+        # L(theta) = L(1) + (theta - 1) (L(2) - L(1)): the parameter's terms are linear in it, so
+        # both differences are exact; the template stores L_0 = L(1) - dL and dL
+        tps = []
+        for val in (1.0, 2.0):
+            model = getattr(mg, fn)(cn, **dict(fixed, **{pname: val}))
+            sim = model.simulate(complexify=True, f_backend="fused", **kw)
+            tps.append(template_from_solver(sim.solver, name, params=dict(fixed, **{pname: val})))
+        t1, t2 = tps
+        for b1, b2 in zip(t1.buckets, t2.buckets):
+            if not (np.array_equal(b1.indices, b2.indices) and np.array_equal(b1.Mc, b2.Mc)):
+                raise ValueError(f"{name}: M or the pattern depends on {pname}")
+            b1.dL = {pname: b2.Lc - b1.Lc}
+            b1.Lc = b1.Lc - b1.dL[pname]
+        t1.linear_params = [pname]
+        t1.params = dict(fixed, **{pname: 1.0})
+        t1.source = dict(reference="conatus 0.5.0", model=fn, build=dict(kw, complexify=True),
+                         linear=f"L({pname}) = L0 + {pname} dL")
+        t1.save(os.path.join(HERE, f"{name}.npz"))
+        print(f"{name}: {len(t1.buckets)} buckets, {time.time() - t0:.1f}s")
+    if args.only == "linear":
+        return
     for name, (fn, kw, params) in SPECS.items():
         if args.only and name != args.only:
             continue

@@ -54,6 +54,7 @@ class Bucket:
     fit_error: float = 0.0        # max relative error of the polynomial form on the source build
     exact: tuple | None = None    # optional (M values, L values), each (nsys, nnz), of the systems
                                   # of one resolution, taken bit for bit from the reference
+    dL: dict = field(default_factory=dict)   # parameter name -> (nmono, nnz): L = Lc + sum_p theta_p dL[p]
 
     @property
     def nnz(self) -> int:
@@ -84,6 +85,7 @@ class ProblemTemplate:
     b0: list = field(default_factory=list)   # (bucket, mode tuple, position, value) of F(0)
     params: dict = field(default_factory=dict)
     source: dict = field(default_factory=dict)
+    linear_params: list = field(default_factory=list)   # parameters L depends on linearly
 
     # ---------------------------------------------------------------- persistence
     def save(self, path: str) -> None:
@@ -99,7 +101,7 @@ class ProblemTemplate:
                              for b in self.buckets],
                     b0=[[int(bi), [int(j) for j in mode], int(pos), _cplx_json(v)]
                         for bi, mode, pos, v in self.b0],
-                    params=self.params, source=self.source)
+                    params=self.params, source=self.source, linear_params=self.linear_params)
         arrays = {"meta": np.array(json.dumps(meta))}
         for lam, C in self.conv.items():
             arrays[f"conv_{lam}"] = C
@@ -112,6 +114,8 @@ class ProblemTemplate:
             arrays[p + "Lc"] = b.Lc
             arrays[p + "col"] = b.col.astype(np.int32)
             arrays[p + "row"] = b.row.astype(np.int32)
+            for name, D in b.dL.items():
+                arrays[p + "dL_" + name] = D
         np.savez_compressed(path, **arrays)
 
     @classmethod
@@ -121,10 +125,13 @@ class ProblemTemplate:
         buckets = []
         for i, bm in enumerate(meta["buckets"]):
             p = f"b{i}_"
-            buckets.append(Bucket(bm["kind"], int(bm["n"]), int(bm["r"]), tuple(bm["active"]),
-                                  int(bm["sign"]), z[p + "indptr"], z[p + "indices"], z[p + "monos"],
-                                  z[p + "Mc"], z[p + "Lc"], z[p + "col"], z[p + "row"],
-                                  float(bm.get("fit_error", 0.0))))
+            bk = Bucket(bm["kind"], int(bm["n"]), int(bm["r"]), tuple(bm["active"]),
+                        int(bm["sign"]), z[p + "indptr"], z[p + "indices"], z[p + "monos"],
+                        z[p + "Mc"], z[p + "Lc"], z[p + "col"], z[p + "row"],
+                        float(bm.get("fit_error", 0.0)))
+            for name in meta.get("linear_params", []):
+                bk.dL[name] = z[p + "dL_" + name]
+            buckets.append(bk)
         return cls(name=meta["name"], axes=meta["axes"], cheb_axis=int(meta["cheb_axis"]),
                    fourier_axes=list(meta["fourier_axes"]), variables=meta["variables"],
                    equations=meta["equations"],
@@ -134,18 +141,38 @@ class ProblemTemplate:
                    conv={int(l): z[f"conv_{l}"] for l in meta["lams"]},
                    buckets=buckets,
                    b0=[(bi, tuple(mode), pos, _cplx_from(v)) for bi, mode, pos, v in meta["b0"]],
-                   params=meta.get("params", {}), source=meta.get("source", {}))
+                   params=meta.get("params", {}), source=meta.get("source", {}),
+                   linear_params=list(meta.get("linear_params", [])))
 
     # ---------------------------------------------------------------- derived
     @property
     def ncheb(self) -> int:
         return self.axes[self.cheb_axis]["N"] if self.cheb_axis >= 0 else 1
 
-    def instantiate(self, fourier_sizes=None, lengths=None) -> "Problem":
+    def instantiate(self, fourier_sizes=None, lengths=None, params=None) -> "Problem":
         """The systems of this template at the given RealFourier sizes (default: the template's) and,
         optionally, other periods of the Fourier directions (the operators are polynomials in the
-        wavenumbers 2 pi j / L, so the period is a free parameter)."""
-        return Problem(self, fourier_sizes, lengths)
+        wavenumbers 2 pi j / L, so the period is a free parameter) and other values of the
+        parameters L depends on linearly (``linear_params``)."""
+        return Problem(self, fourier_sizes, lengths, params)
+
+    def with_params(self, **values) -> "ProblemTemplate":
+        """A copy whose L is evaluated at the given values of its linear parameters."""
+        import copy
+        t = copy.copy(self)
+        t.buckets = []
+        for b in self.buckets:
+            nb = copy.copy(b)
+            nb.Lc = b.Lc.copy()
+            for name, v in values.items():
+                if name not in b.dL:
+                    raise KeyError(f"{self.name}: no linear parameter {name!r}")
+                nb.Lc = nb.Lc + float(v) * b.dL[name]
+            nb.dL = {}
+            t.buckets.append(nb)
+        t.linear_params = []
+        t.params = dict(self.params, **{k: float(v) for k, v in values.items()})
+        return t
 
 
 def _cplx_json(v):
@@ -162,7 +189,11 @@ def _cplx_from(v):
 class Problem:
     """A template at a Fourier resolution: the systems (modes, wavenumbers) of every bucket."""
 
-    def __init__(self, tpl: ProblemTemplate, fourier_sizes=None, lengths=None):
+    def __init__(self, tpl: ProblemTemplate, fourier_sizes=None, lengths=None, params=None):
+        if params:
+            tpl = tpl.with_params(**params)
+        elif tpl.linear_params:
+            tpl = tpl.with_params(**{k: tpl.params[k] for k in tpl.linear_params})
         self.tpl = tpl
         d = len(tpl.fourier_axes)
         if fourier_sizes is None:

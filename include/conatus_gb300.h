@@ -177,7 +177,7 @@ int cng_cheb_transform(int forward, const void* in, void* out, int64_t ncols, in
 int cng_fft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int ncompact,
                  int length, void* stream);
 /* Real FFT along the middle axis: backward maps nmodes Hermitian half-spectrum modes (complex128)
- * to length real points; forward maps length real points to nmodes modes (1/length). inner even.
+ * to length real points; forward maps length real points to nmodes modes (1/length).
  * Replaces cuda.rfft / irfft and realfourier_forward / backward (module.cpp:456-477). */
 int cng_rfft_axis(int forward, const void* in, void* out, int64_t outer, int inner, int nmodes,
                   int length, void* stream);

@@ -37,8 +37,8 @@ def import_reference(ref: str):
 # ------------------------------------------------------------------------------------------------
 # problems of the benchmark configurations (BASELINE configs, small resolutions for fixtures)
 
-def burgers(cn, N=128):
-    m = cn.Model(cn.Box(x=cn.walls(-1, 1)), name="Burgers", nu=0.01 / np.pi)
+def burgers(cn, N=128, nu=0.01 / np.pi):
+    m = cn.Model(cn.Box(x=cn.walls(-1, 1)), name="Burgers", nu=nu)
     m.scalar("u")
     m.equations("dt(u) - nu*lap(u) = -u*dx(u)")
     m.at("walls", u=0)
