@@ -269,6 +269,68 @@ def cpu_baseline(args, P, C0, steps=1):
             "sample": desc}
 
 
+def run_serving(args):
+    """The serving configuration: a seeded Poisson stream (rate 200/s) of Burgers / KS / RB requests
+    served by conatus_gb300.serving.ServingEngine with a 150 GB admission budget."""
+    import torch
+    from conatus_gb300 import serving
+    torch.cuda.set_device(0)
+    lo, hi = args.serve_steps
+    warm = serving.poisson_stream(6, rate=1e4, seed=1000, steps=(40, 40))
+    serving.ServingEngine(precision=args.precision).run(warm, realtime=False)     # templates, twiddles, modules
+    reqs = serving.poisson_stream(args.requests, rate=args.rate, seed=0, steps=(lo, hi))
+    eng = serving.ServingEngine(budget_bytes=150e9, precision=args.precision, chunk=args.chunk,
+                                unroll=args.unroll)
+    with ClockSampler(0) as clk:
+        st = eng.run(reqs, realtime=True)
+    out = {"metric": "served IMEX steps/s (Poisson mix Burgers/KS/RB, rate %g/s)" % args.rate,
+           "value": st["steps_per_s"], "unit": "steps/s", "n_gpus": 1, "steps": st["steps"],
+           "warmup": 6, "ms_per_step": 1e3 / st["steps_per_s"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+           "data": "synthetic (seeded request stream and initial states)",
+           "config": {"workload": f"serving {args.requests} requests, steps U[{lo},{hi}], SBDF2, "
+                                  "Burgers N 64..512 / KS N 64..256 / RB Nz 32..96 Nx 4Nz",
+                      "budget_gb": 150, "chunk": args.chunk, "unroll": args.unroll},
+           "latency_s": {"p50": st["p50_s"], "p99": st["p99_s"]}, "serving": st, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def run_ks_ensemble(args):
+    """The KS ensemble: 4096 members (L ~ U[22, 100], N = next power of two >= 2L), SBDF2, dt = 0.01,
+    one fused launch per step replayed as CUDA graphs."""
+    import torch
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ensemble import FourierEnsemble, ks_members
+    torch.cuda.set_device(0)
+    N, L = ks_members(args.members, seed=0)
+    ens = FourierEnsemble(W.load_template("ks"), N, L, scheme="SBDF2", dt=0.01, precision=args.precision)
+    ens.set_state(ens.random_state(seed=0))
+    ens.run_graph(max(args.warmup, 3), args.unroll)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(ens.stream)
+        ens.run_graph(args.steps, args.unroll)
+        e1.record(ens.stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    value = args.steps / (ms / 1e3)
+    x = np.concatenate(ens.state())
+    out = {"metric": f"ensemble steps/s ({args.members} KS members, SBDF2)", "value": value, "unit": "steps/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+           "data": "synthetic (seeded periods and initial Fourier amplitudes)",
+           "config": {"workload": f"KS ensemble {args.members} members N in 64..256, dt=0.01",
+                      "modes": int(ens.n_total), "unroll": args.unroll,
+                      "l2": "fits in L2 (the ensemble state is a few MB)",
+                      "state_finite": bool(np.all(np.isfinite(x)))},
+           "member_steps_per_s": value * args.members, "mode_updates_per_s": value * ens.mode_updates(),
+           "gpu_launches": args.steps, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -301,17 +363,32 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="channel", choices=list(METRIC))
+    ap.add_argument("--config", default="channel", choices=list(METRIC) + ["serving", "ks_ensemble"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--cpu-sample-systems", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--error-steps", type=int, default=50)
     ap.add_argument("--fourier", type=int, nargs="*", default=None,
                     help="Fourier sizes overriding the configuration's (small cases for profiling)")
+    ap.add_argument("--requests", type=int, default=200, help="serving: requests in the stream")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--serve-steps", type=int, nargs=2, default=[1000, 20000], help="serving: step range")
+    ap.add_argument("--chunk", type=int, default=500, help="serving: steps per scheduling chunk")
+    ap.add_argument("--unroll", type=int, default=50, help="steps per CUDA graph (serving, ensemble)")
+    ap.add_argument("--members", type=int, default=4096, help="ks_ensemble: members")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     from conatus_gb300 import workloads as W
+    if args.config in ("serving", "ks_ensemble"):
+        if args.impl == "reference":
+            ws, rank, _ = _dist()
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": f"{args.config}: the reference has no "
+                                  "GPU serving or ensemble path; its CPU step is timed on the channel"}))
+            return
+        (run_serving if args.config == "serving" else run_ks_ensemble)(args)
+        return
     args.cfg = W.CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args)

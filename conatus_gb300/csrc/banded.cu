@@ -1055,6 +1055,8 @@ static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaSt
     }
 }
 
+static void demote_compact(Banded& h, cudaStream_t st);
+
 static void make_fp32(Banded& h, cudaStream_t st) {
     if (h.dtype != 1) throw InvalidArgument("FP32 factors need complex128 factors (complex bucket)");
     const size_t B = h.batch, n = h.n, r = h.r;
@@ -1072,6 +1074,7 @@ static void make_fp32(Banded& h, cudaStream_t st) {
     dem(h.vt, h.vt32, (long long)(B * r * n));
     dem(h.w, h.w32, (long long)(B * r * n));
     dem(h.slu, h.slu32, (long long)(B * r * r));
+    if (h.compact_ready) demote_compact(h, st);
     CNG_CUDA(cudaStreamSynchronize(st));
     h.fp32_ready = true;
 }
@@ -1669,6 +1672,23 @@ __global__ void k_demote_n(const zd* __restrict__ a, zf* __restrict__ b, long lo
         b[i] = to_zf(a[i]);
 }
 
+// FP32 copies of the compact factor streams (the FP32 form's solves read these).
+static void demote_compact(Banded& h, cudaStream_t st) {
+    const size_t G = kGroup, W = h.cWg;
+    if (!h.c_L32) {
+        dalloc(&h.c_L32, W * std::max(h.cL, 1) * G, sizeof(zf));
+        dalloc(&h.c_U32, W * std::max(h.cU, 1) * G, sizeof(zf));
+        dalloc(&h.c_V32, W * std::max(h.cV, 1) * G, sizeof(zf));
+    }
+    auto dem = [&](const void* a, zf* b, long long c) {
+        k_demote_n<<<(int)std::min<long long>((c + 255) / 256, 152LL * 32), 256, 0, st>>>(static_cast<const zd*>(a), b, c);
+        CNG_LAUNCH("k_demote_n");
+    };
+    dem(h.c_L, h.c_L32, (long long)(W * std::max(h.cL, 1) * G));
+    dem(h.c_U, h.c_U32, (long long)(W * std::max(h.cU, 1) * G));
+    dem(h.c_V, h.c_V32, (long long)(W * std::max(h.cV, 1) * G));
+}
+
 static CompactIdx compact_idx(const Banded& h) {
     CompactIdx ix;
     ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
@@ -1763,21 +1783,7 @@ static void compact(Banded& h, cudaStream_t st) {
     k_pack_compact<zd><<<ceil_div(total, 4), 128, 0, st>>>(h.view<zd>(), compact_idx(h), static_cast<zd*>(h.c_L),
                                                            static_cast<zd*>(h.c_U), static_cast<zd*>(h.c_V), h.c_piv, total);
     CNG_LAUNCH("k_pack_compact");
-    if (h.fp32_ready || true) {
-        const size_t G = kGroup, W = h.cWg;
-        if (!h.c_L32) {
-            dalloc(&h.c_L32, W * std::max(h.cL, 1) * G, sizeof(zf));
-            dalloc(&h.c_U32, W * std::max(h.cU, 1) * G, sizeof(zf));
-            dalloc(&h.c_V32, W * std::max(h.cV, 1) * G, sizeof(zf));
-        }
-        auto dem = [&](const void* a, zf* b, long long c) {
-            k_demote_n<<<(int)std::min<long long>((c + 255) / 256, 152LL * 32), 256, 0, st>>>(static_cast<const zd*>(a), b, c);
-            CNG_LAUNCH("k_demote_n");
-        };
-        dem(h.c_L, h.c_L32, (long long)(W * std::max(h.cL, 1) * G));
-        dem(h.c_U, h.c_U32, (long long)(W * std::max(h.cU, 1) * G));
-        dem(h.c_V, h.c_V32, (long long)(W * std::max(h.cV, 1) * G));
-    }
+    if (h.fp32_ready) demote_compact(h, st);
     CNG_CUDA(cudaStreamSynchronize(st));
     h.compact_ready = true;
 }

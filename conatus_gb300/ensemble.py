@@ -173,10 +173,12 @@ class FourierEnsemble:
         for _ in range(int(steps)):
             self.step()
 
-    def run_graph(self, steps: int) -> None:
-        """``steps`` steps; after the start-up, one graph launch per step (one graph per ring phase)."""
+    def run_graph(self, steps: int, unroll: int = 1) -> None:
+        """``steps`` steps; after the start-up, graph launches of ``unroll`` steps each (one graph
+        per ring phase and length; a remainder shorter than ``unroll`` runs as one-step graphs)."""
         torch = _torch()
         steps = int(steps)
+        unroll = max(1, int(unroll))
         while steps > 0 and self.filled < self.order:
             self.step()
             steps -= 1
@@ -184,23 +186,28 @@ class FourierEnsemble:
             return
         s = _stream_handle(self.stream)
         self.stream.wait_stream(torch.cuda.current_stream())
-        for _ in range(steps):
-            nxt = (self.head + 1) % self.order
-            g = self._graphs.get(nxt)
+        while steps > 0:
+            u = unroll if steps >= unroll else 1
+            key = ((self.head + 1) % self.order, u)
+            g = self._graphs.get(key)
             if g is None:
                 self.stream.synchronize()
                 call("cng_graph_begin", s)
                 h = ctypes.c_void_p()
+                head0 = self.head
                 try:
-                    self._launch(s)
+                    for _ in range(u):
+                        self.head = self._launch(s)
                 finally:
+                    self.head = head0
                     call("cng_graph_end", s, ctypes.byref(h))
                 from .ivp import _Graph
-                g = self._graphs[nxt] = _Graph(h)
+                g = self._graphs[key] = _Graph(h)
             g.launch(s)
-            self.head = nxt
-            self.t += self.dt
-            self.iteration += 1
+            self.head = (self.head + u) % self.order
+            self.t += u * self.dt
+            self.iteration += u
+            steps -= u
         torch.cuda.current_stream().wait_stream(self.stream)
 
     def mode_updates(self) -> int:

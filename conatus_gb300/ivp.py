@@ -76,9 +76,11 @@ def _stream_handle(stream) -> int:
 class DeviceProblem:
     """A problem instance resident on the device (see module docstring)."""
 
-    def __init__(self, problem, precision: str = "fp64", device: str = "cuda", compact: bool = True):
+    def __init__(self, problem, precision: str = "fp64", device: str = "cuda", compact: bool = True,
+                 factor_sets: int | None = None):
         torch = _torch()
         _lib.lib()
+        self.factor_sets = factor_sets      # None: keep every (a, b) factorization, else at most this many
         if precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
         self.P = problem
@@ -159,10 +161,12 @@ class DeviceProblem:
         desc.nfactors = facs.shape[0]
         desc.factors = arr(facs, np.int32)
         # outputs: lambda from the rows of their equation
+        # without a Chebyshev axis every field has a single coefficient, marked n = -1: index 0
+        cheb_n = (lambda n: int(n)) if ca >= 0 else (lambda n: 0 if int(n) == -1 else int(n))
         lam_of = {}
         for b in tpl.buckets:
             for e, c, n, lam in b.row:
-                if n >= 0:
+                if cheb_n(n) >= 0:
                     lam_of[(int(e), int(c))] = max(int(lam), 0)
         outs = tpl.outputs
         desc.noutputs = len(outs)
@@ -196,14 +200,14 @@ class DeviceProblem:
             cp = -np.ones((facs.shape[0], ny), np.int32)
             for f, (v, c, *_o) in enumerate(facs):
                 for i, (cv, cc, cn) in enumerate(b.col):
-                    if cv == v and cc == c and cn >= 0:
-                        cp[f, cn] = i
+                    if cv == v and cc == c and cheb_n(cn) >= 0:
+                        cp[f, cheb_n(cn)] = i
             col_p.append(arr(cp, np.int32))
             rm = -np.ones((b.n, 2), np.int32)
             for i, (e, c, n, lam) in enumerate(b.row):
                 o = out_index.get((int(e), int(c)))
-                if o is not None and n >= 0:
-                    rm[i] = (o, n)
+                if o is not None and cheb_n(n) >= 0:
+                    rm[i] = (o, cheb_n(n))
                 else:
                     rm[i] = (-1, 0)
             row_p.append(arr(rm, np.int32))
@@ -272,7 +276,10 @@ class DeviceProblem:
         f = self._factors.get(key)
         if f is None:
             torch = _torch()
-            torch.cuda.synchronize(self.device)    # values below come from torch's stream
+            if self.factor_sets is not None:
+                while len(self._factors) >= max(1, self.factor_sets):
+                    self._factors.pop(next(iter(self._factors)))     # oldest set (its handles free on drop)
+            torch.cuda.current_stream(self.device).synchronize()    # values below come from torch's stream
             f = []
             for bi, b in enumerate(self.tpl.buckets):
                 Mv, per = self._M[bi]
@@ -434,12 +441,12 @@ class IVPSolver:
     """SBDF-q time stepper on the device (see module docstring)."""
 
     def __init__(self, problem, scheme: str = "SBDF2", dt: float = 1e-3, precision: str = "fp64",
-                 device_problem: DeviceProblem | None = None):
+                 device_problem: DeviceProblem | None = None, factor_sets: int | None = None):
         if scheme not in ("SBDF1", "SBDF2", "SBDF3", "SBDF4"):
             raise ValueError(f"scheme {scheme!r}: SBDF1..SBDF4")
         self.scheme, self.dt = scheme, float(dt)
         self.order = int(scheme[-1])
-        self.dev = device_problem or DeviceProblem(problem, precision)
+        self.dev = device_problem or DeviceProblem(problem, precision, factor_sets=factor_sets)
         z = self.dev.zeros
         self.X, self.R = z(), z()
         self.MXh = [z() for _ in range(self.order)]
@@ -512,11 +519,13 @@ class IVPSolver:
             self._step()
         self._leave()
 
-    def run_graph(self, steps: int) -> None:
-        """``steps`` steps; once the history is full, each step is one CUDA graph launch (one graph
-        per position of the history ring, captured on first use)."""
+    def run_graph(self, steps: int, unroll: int = 1) -> None:
+        """``steps`` steps; once the history is full, the steps run as CUDA graph launches, each
+        graph holding ``unroll`` steps (one graph per position of the history ring and length,
+        captured on first use; a remainder shorter than ``unroll`` runs as one-step graphs)."""
         s = _stream_handle(self.stream)
         steps = int(steps)
+        unroll = max(1, int(unroll))
         self._enter()
         while steps > 0 and self.filled < self.order:
             self._step()
@@ -526,25 +535,28 @@ class IVPSolver:
             return
         a, _ = SBDF[self.order]
         self.dev.factor(a[0] / self.dt, 1.0, s)
-        for _ in range(steps):
-            nxt = (self.head + 1) % self.order
-            g = self._graphs.get(nxt)
+        while steps > 0:
+            u = unroll if steps >= unroll else 1
+            key = ((self.head + 1) % self.order, u)
+            g = self._graphs.get(key)
             if g is None:
                 self.stream.synchronize()
                 call("cng_graph_begin", s)
                 head0, filled0 = self.head, self.filled
                 try:
-                    self._push(s)
-                    self._combine_solve(s)
+                    for _ in range(u):
+                        self._push(s)
+                        self._combine_solve(s)
                 finally:
                     h = ctypes.c_void_p()
                     call("cng_graph_end", s, ctypes.byref(h))
-                g = self._graphs[nxt] = _Graph(h)
+                g = self._graphs[key] = _Graph(h)
                 self.head, self.filled = head0, filled0     # captured, not run
             g.launch(s)
-            self.head = nxt
-            self.t += self.dt
-            self.iteration += 1
+            self.head = (self.head + u) % self.order
+            self.t += u * self.dt
+            self.iteration += u
+            steps -= u
         self._leave()
 
     def step_host(self, host_in, host_out) -> None:

@@ -1,0 +1,125 @@
+"""Device-memory planner: the bytes a run will hold on the device, predicted before anything is
+allocated (the serving loop's admission oracle).
+
+The reference predicts device bytes per solver from a liveness model of its buffers
+(python/conatus/runtime/memory.py); the prediction here follows this library's own allocations
+one by one:
+
+* state and work vectors: X and R (plus the FP32 form's refinement residual), the history ring of
+  M X and F (q slots each), complex128 over the mode layout;
+* per bucket: M values (one shared copy when M is constant, else per system), L values per system,
+  the pattern, and the factor set of ``cng_banded_create_shared`` (band LU ldab x n, pivots, the
+  border blocks V^T and W (r x n each), the capacitance LU (r x r)), its FP32 copies in the FP32
+  form, and the compact factor streams (bounded above by the band: at most kl entries of L and
+  kl + ku + 1 of U per column, r x n of V); one transient copy of a M + b L while factoring;
+* the F pipeline's work buffers (``cng_rhs_create``: the spectra S and two grid buffers).
+
+Factor sets kept: one in the steady state when the solver keeps a single set (``IVPSolver(...,
+factor_sets=1)``), else one per start-up order.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+__all__ = ["bucket_band", "plan_ivp", "plan_fourier_ensemble"]
+
+_Z = 16          # complex128
+_C = 8           # complex64
+
+
+def bucket_band(b) -> tuple:
+    """(kl, ku) of the non-border rows of a bucket in solver order (border rows 0..r-1), as the
+    factorization computes them."""
+    kl = ku = 0
+    for i in range(b.r, b.n):
+        cols = b.indices[b.indptr[i]:b.indptr[i + 1]]
+        if cols.size:
+            kl = max(kl, int(i - cols.min()))
+            ku = max(ku, int(cols.max() - i))
+    return kl, ku
+
+
+def _factor_bytes(b, nsys, precision, compact):
+    n, r = b.n, b.r
+    kl, ku = bucket_band(b)
+    ldab = 2 * kl + ku + 1
+    nnz = int(b.indices.size)
+    out = nsys * (n * ldab * _Z + n * 4 + 2 * r * n * _Z + r * r * _Z + r * 4 + 4 + 8) + n * 4 + nnz * 8
+    if precision == "fp32":
+        out += nsys * (n * ldab * _C + 2 * r * n * _C + r * r * _C)
+    if compact:
+        slots = int(math.ceil(nsys / 4)) * 4
+        per = n * kl + n * (kl + ku + 1) + r * n
+        out += slots * (per * _Z + n * 4) + 6 * (n + 1) * 4 + per * 5
+        if precision == "fp32":
+            out += slots * per * _C
+    return out
+
+
+def _rhs_bytes(problem, precision):
+    """Work buffers of the F pipeline (the sizes ``cng_rhs_create`` allocates)."""
+    from .ivp import smooth_size
+    tpl = problem.tpl
+    cs = _C if precision == "fp32" else _Z
+    rs = cs // 2
+    d = len(tpl.fourier_axes)
+    ax = tpl.axes
+    if tpl.cheb_axis >= 0:
+        ny = ax[tpl.cheb_axis]["N"]
+        my = smooth_size(ax[tpl.cheb_axis]["M"], even=True)
+    else:
+        ny = my = 1
+    Kx = problem.fourier_sizes[0] // 2 if d >= 1 else 1
+    mx = smooth_size(int(math.floor(problem.fourier_sizes[0] * ax[tpl.fourier_axes[0]].get("dealias", 1.5)))) if d >= 1 else 1
+    if d >= 2:
+        Nzc = problem.fourier_sizes[1]
+        mz = smooth_size(int(math.floor(problem.fourier_sizes[1] * ax[tpl.fourier_axes[1]].get("dealias", 1.5))))
+    else:
+        Nzc = mz = 1
+    nf, no = len(tpl.factors), len(tpl.outputs)
+    nfo = max(nf, no)
+    P = mx * mz * my
+    S = max(cs * nfo * Kx * Nzc * ny, rs * nf * P)
+    W = max(cs * nfo * Kx * Nzc * my, cs * nfo * Kx * mz * my, rs * nfo * mx * mz * my, cs * nfo * P)
+    nlam = max(tpl.conv) if tpl.conv else 0
+    return S + 2 * W + nlam * ny * ny * 8
+
+
+def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: bool = True,
+             factor_sets: int | None = None) -> dict:
+    """Predicted device bytes of ``IVPSolver(problem, scheme, precision=precision)``, by part,
+    with the total under ``"total"``."""
+    tpl = problem.tpl
+    q = int(scheme[-1])
+    n_total = sum(ns * b.n for ns, b in zip(problem.nsys, tpl.buckets))
+    vec = n_total * _Z
+    parts = {"state": vec * (2 + (1 if precision == "fp32" else 0)), "history": 2 * q * vec,
+             "rhs_work": _rhs_bytes(problem, precision)}
+    ops = fac = trans = 0
+    for b, ns in zip(tpl.buckets, problem.nsys):
+        nnz = int(b.indices.size)
+        const_m = b.m_is_constant() and b.exact is None
+        ops += (nnz * (_Z + 8) if const_m else ns * nnz * _Z) + ns * nnz * _Z + (b.n + 1 + nnz) * 4
+        fac += _factor_bytes(b, ns, precision, compact)
+        trans = max(trans, ns * nnz * _Z)
+        if precision == "fp32":
+            ops += 2 * b.n * 16 + ns * 16 * 8        # split-operator residual lists (bounded)
+    sets = q if factor_sets is None else max(1, min(q, int(factor_sets)))
+    parts["operators"] = ops
+    parts["factors"] = fac * sets
+    parts["factor_transient"] = trans
+    parts["total"] = int(sum(parts.values()))
+    return parts
+
+
+def plan_fourier_ensemble(sizes, scheme: str = "SBDF2") -> dict:
+    """Predicted device bytes of ``FourierEnsemble(tpl, sizes, ...)``: X and the history ring of
+    N/2 complex amplitudes per member, plus the per-member descriptors."""
+    q = int(scheme[-1])
+    K = int(np.sum(np.asarray(sizes) // 2))
+    m = len(sizes)
+    parts = {"state": K * _Z, "history": 2 * q * K * _Z, "descriptors": m * (4 + 4 + 8 + 8 + 4)}
+    parts["total"] = int(sum(parts.values()))
+    return parts
