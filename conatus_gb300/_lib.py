@@ -39,6 +39,7 @@ _SIGS = {
     "cng_banded_prepare_transpose": [P, P],
     "cng_banded_solve_transpose": [P, P, P],
     "cng_banded_solve_host": [P, P, P, c_int],
+    "cng_banded_solve_host_static": [P, P, P, c_int],
     "cng_banded_make_fp32": [P, P],
     "cng_banded_compact": [P, P],
     "cng_banded_solve_batch": [c_int, P, P, P, c_int, c_int, P],

@@ -1122,6 +1122,32 @@ static const Banded* as_banded(const cng_banded* h) {
     return reinterpret_cast<const Banded*>(h);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Static staging for cng_banded_solve_host_static: a fixed 8 MiB device array (1 Mi complex64 or
+// 512 Ki complex128 entries), no allocation at run time. Nothing in it needs to start at zero (a
+// solve overwrites the bytes it uses). Every call on a device uses the same array.
+namespace cng {
+constexpr size_t kStaticSolveBytes = size_t(8) << 20;
+static __device__ __align__(256) unsigned char g_static_solve[kStaticSolveBytes];
+
+// The array's device address, looked up once per device (the device current at the call).
+static void* static_solve_scratch() {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static void* ptr[kMaxDevices] = {};
+    int dev = 0;
+    CNG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw InvalidArgument("device index above 63");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptr[dev]) {
+        void* p = nullptr;
+        CNG_CUDA(cudaGetSymbolAddress(&p, g_static_solve));
+        ptr[dev] = p;
+    }
+    return ptr[dev];
+}
+}  // namespace cng
+
 extern "C" {
 
 int cng_banded_create_csr(int dtype, int batch, int n, const int32_t* indptr, const int32_t* indices,
@@ -1303,6 +1329,34 @@ int cng_banded_solve_host(cng_banded* hh, const void* b_host, void* x_host, int 
             throw;
         }
         CNG_CUDA(cudaFree(d));
+    })
+}
+
+// Host-buffer solve without any device allocation. The staging buffer is one file-scope device
+// array shared by every call on a device, looked up once per device (cudaGetSymbolAddress).
+int cng_banded_solve_host_static(cng_banded* hh, const void* b_host, void* x_host, int transpose) {
+    CNG_TRY({
+        Banded* h = as_banded(hh);
+        if (!b_host || !x_host) throw InvalidArgument("solve_host_static: null host pointer");
+        const size_t bytes = h->esz * (size_t)h->batch * h->n;
+        if (bytes > kStaticSolveBytes)
+            throw InvalidArgument("solve_host_static: the right-hand sides take " + std::to_string(bytes) +
+                                  " bytes, above the static staging buffer of " +
+                                  std::to_string(kStaticSolveBytes) + " bytes (use cng_banded_solve_host)");
+        if (transpose && !h->transposed_ready)
+            throw InvalidArgument("solve_host_static: call cng_banded_prepare_transpose first (it allocates)");
+        void* d = static_solve_scratch();
+        cudaStream_t st = nullptr;
+        CNG_CUDA(cudaMemcpyAsync(d, b_host, bytes, cudaMemcpyHostToDevice, st));
+        if (transpose) {
+            if (h->dtype == 0) launch_solve_T_t<double>(*h, d, st);
+            else launch_solve_T_t<zd>(*h, d, st);
+        } else {
+            SolveIo io{d, d, nullptr, nullptr, nullptr, nullptr};
+            launch_solve(*h, IO_PLAIN, io, st);
+        }
+        CNG_CUDA(cudaMemcpyAsync(x_host, d, bytes, cudaMemcpyDeviceToHost, st));
+        CNG_CUDA(cudaStreamSynchronize(st));
     })
 }
 

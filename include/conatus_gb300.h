@@ -115,6 +115,18 @@ int cng_banded_solve_fp32(const cng_banded* h, const void* b, void* x, int accum
  * Replaces _core.BorderedBandedBatch{D,Z}.solve (core/bindings/module.cpp:184-206). */
 int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int transpose);
 
+/* As cng_banded_solve_host, but allocates no device memory: the right-hand sides are staged in a
+ * fixed 8 MiB device array built into the library (batch * n * element size must be at most
+ * 8388608 bytes, else status 1, invalid argument; transpose needs cng_banded_prepare_transpose
+ * first).
+ * No counterpart in the reference. For callers that must not allocate: cng_banded_solve_host
+ * allocates and frees a staging buffer on every call, and freeing device memory waits for the
+ * whole device, which stalls every other stream (other runs in flight in a serving loop); a
+ * caller under a planned device-memory budget must not grow its footprint either. The first call
+ * on a device looks up the array's address. Every call on a device shares the one array:
+ * overlapping calls (from several host threads) race on it and must be serialized by the caller. */
+int cng_banded_solve_host_static(cng_banded* h, const void* b_host, void* x_host, int transpose);
+
 /* ---- pseudospectral explicit right-hand side F(X) ------------------------------------------ */
 
 typedef struct cng_rhs cng_rhs;
