@@ -74,6 +74,7 @@ class FourierEnsemble:
         self.t, self.iteration = 0.0, 0
         self.stream = torch.cuda.Stream()
         self._graphs = {}
+        self.join = True          # as IVPSolver.join: order the stream after torch's current stream
 
     def _describe(self):
         tpl = self.tpl
@@ -162,12 +163,14 @@ class FourierEnsemble:
 
     def step(self) -> None:
         torch = _torch()
-        self.stream.wait_stream(torch.cuda.current_stream())
+        if self.join:
+            self.stream.wait_stream(torch.cuda.current_stream())
         self.head = self._launch(_stream_handle(self.stream))
         self.filled = min(self.filled + 1, self.order)
         self.t += self.dt
         self.iteration += 1
-        torch.cuda.current_stream().wait_stream(self.stream)
+        if self.join:
+            torch.cuda.current_stream().wait_stream(self.stream)
 
     def run(self, steps: int) -> None:
         for _ in range(int(steps)):
@@ -185,7 +188,8 @@ class FourierEnsemble:
         if steps <= 0:
             return
         s = _stream_handle(self.stream)
-        self.stream.wait_stream(torch.cuda.current_stream())
+        if self.join:
+            self.stream.wait_stream(torch.cuda.current_stream())
         while steps > 0:
             u = unroll if steps >= unroll else 1
             key = ((self.head + 1) % self.order, u)
@@ -208,7 +212,8 @@ class FourierEnsemble:
             self.t += u * self.dt
             self.iteration += u
             steps -= u
-        torch.cuda.current_stream().wait_stream(self.stream)
+        if self.join:
+            torch.cuda.current_stream().wait_stream(self.stream)
 
     def mode_updates(self) -> int:
         """Real unknowns per step (2 per complex amplitude, 1 for the mean modes)."""

@@ -279,13 +279,15 @@ class DeviceProblem:
             if self.factor_sets is not None:
                 while len(self._factors) >= max(1, self.factor_sets):
                     self._factors.pop(next(iter(self._factors)))     # oldest set (its handles free on drop)
-            torch.cuda.current_stream(self.device).synchronize()    # values below come from torch's stream
-            f = []
+            vals_all = []
             for bi, b in enumerate(self.tpl.buckets):
                 Mv, per = self._M[bi]
                 per = per if isinstance(per, int) else 0
-                Lv = self._Lvals(bi)
-                vals = (a * (Mv if per else Mv.unsqueeze(0)) + b_ * Lv).contiguous()
+                vals_all.append((a * (Mv if per else Mv.unsqueeze(0)) + b_ * self._Lvals(bi)).contiguous())
+            torch.cuda.current_stream(self.device).synchronize()    # the values come from torch's stream
+            f = []
+            for bi, b in enumerate(self.tpl.buckets):
+                vals = vals_all[bi]
                 h = _Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
                                    list(range(b.r)), pivot=True, stream=_stream_handle(stream))
                 if self.precision == "fp32":
@@ -456,6 +458,10 @@ class IVPSolver:
         self._graphs = {}
         torch = _torch()
         self.stream = torch.cuda.Stream()
+        # join: every call orders the solver's stream after torch's current stream and back (safe
+        # default). A caller that keeps many solvers in flight on their own streams (the serving
+        # loop) turns it off after one explicit wait, so that independent runs do not serialize.
+        self.join = True
 
     def set_state(self, X, t: float = 0.0) -> None:
         """Initial state (mode layout tensor or list of per-bucket arrays); resets the history."""
@@ -491,12 +497,12 @@ class IVPSolver:
         self.dev.solve(a[0] / self.dt, 1.0, self.R, self.X, s)
 
     def _enter(self):
-        torch = _torch()
-        self.stream.wait_stream(torch.cuda.current_stream())
+        if self.join:
+            self.stream.wait_stream(_torch().cuda.current_stream())
 
     def _leave(self):
-        torch = _torch()
-        torch.cuda.current_stream().wait_stream(self.stream)
+        if self.join:
+            _torch().cuda.current_stream().wait_stream(self.stream)
 
     def step(self) -> None:
         self._enter()

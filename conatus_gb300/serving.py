@@ -40,6 +40,14 @@ SCHEME = "SBDF2"
 DT = {"burgers": 1e-4, "ks": 1e-2, "rb": 1e-4}
 
 
+def time_step(req) -> float:
+    """dt of a request: 1e-4 for Burgers, 1e-2 for KS; for RB 1e-4 up to Ra = 1e6 and 1e-4
+    (1e6/Ra)^(1/2) above (the free-fall velocity grows as Ra^(1/2))."""
+    if req.kind == "rb":
+        return DT["rb"] * min(1.0, (1e6 / req.params["Ra"]) ** 0.5)
+    return DT[req.kind]
+
+
 @dataclass
 class Request:
     rid: int
@@ -126,13 +134,17 @@ class Session:
         if req.kind == "ks":
             from .ensemble import FourierEnsemble
             p = req.params
-            self.solver = FourierEnsemble(_template("ks"), [p["N"]], [p["L"]], scheme=SCHEME, dt=DT["ks"],
+            self.solver = FourierEnsemble(_template("ks"), [p["N"]], [p["L"]], scheme=SCHEME, dt=time_step(req),
                                           precision=precision)
             self.solver.set_state(self.solver.random_state(seed=req.rid))
         else:
-            self.solver = IVPSolver(prep.problem, scheme=SCHEME, dt=DT[req.kind], precision=precision,
+            self.solver = IVPSolver(prep.problem, scheme=SCHEME, dt=time_step(req), precision=precision,
                                     factor_sets=1)
             self.solver.set_state(prep.state)
+        # one wait for the initial state (copied on torch's stream), then the run's stream is on
+        # its own: runs in flight do not wait on one another
+        self.solver.stream.wait_stream(torch.cuda.current_stream())
+        self.solver.join = False
         self.footprint = prep.bytes
         self.remaining = req.steps
         self.event = torch.cuda.Event()
@@ -151,6 +163,12 @@ class Session:
             self.in_flight = False
         return not self.in_flight
 
+    def finite(self) -> bool:
+        """The state holds no NaN or infinity (read on the run's own stream)."""
+        torch = _torch()
+        with torch.cuda.stream(self.solver.stream):
+            return bool(torch.isfinite(torch.view_as_real(self.solver.X)).all().item())
+
     def result(self):
         s = self.solver
         if hasattr(s, "dev"):
@@ -163,7 +181,8 @@ class ServingEngine:
     """Continuous-batching request loop with admission by planned device bytes."""
 
     def __init__(self, budget_bytes: float = 150e9, precision: str = "fp64", chunk: int = 500,
-                 unroll: int = 50, max_active: int = 512, keep_results: bool = False):
+                 unroll: int = 50, max_active: int = 512, keep_results: bool = False, free_batch: int = 32):
+        self.free_batch = int(free_batch)
         self.budget = float(budget_bytes)
         self.precision = precision
         self.chunk = int(chunk)
@@ -178,6 +197,8 @@ class ServingEngine:
         queue = sorted(requests, key=lambda r: r.arrival)
         prepared: Prepared | None = None
         active: list[Session] = []
+        retired: list[Session] = []     # finished runs whose device memory is not yet released
+        nonfinite = 0
         used = 0
         peak_used = 0
         done = []
@@ -199,6 +220,8 @@ class ServingEngine:
                 if prepared.bytes > self.budget:
                     raise MemoryError(f"request {prepared.req.rid} needs {prepared.bytes} bytes, above the "
                                       f"budget of {self.budget:.0f}")
+                if used + prepared.bytes > self.budget and retired:
+                    used -= self._release(retired)
                 if used + prepared.bytes > self.budget:
                     break
                 s = Session(prepared, self.precision)
@@ -220,12 +243,15 @@ class ServingEngine:
                     s.req.finished = time.perf_counter() - t0
                     if self.keep_results:
                         s.req.result = s.result()
+                    nonfinite += 0 if s.finite() else 1
                     steps_done += s.req.steps
-                    used -= s.footprint
                     active.remove(s)
+                    retired.append(s)
                     done.append(s.req)
                     continue
                 s.launch(self.chunk, self.unroll)
+            if len(retired) >= self.free_batch:
+                used -= self._release(retired)
             if not progressed:
                 wait = 2e-4
                 if not active and queue and prepared is None:
@@ -233,8 +259,19 @@ class ServingEngine:
                 time.sleep(wait)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        self._release(retired)
         lat = np.array([r.finished - r.arrival for r in done]) if done else np.zeros(1)
         return dict(requests=len(done), wall_s=wall, steps=steps_done, steps_per_s=steps_done / wall,
+                    nonfinite=nonfinite,
                     p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)),
                     peak_active=peak_active, peak_planned_bytes=int(peak_used), budget_bytes=self.budget,
                     by_kind={k: sum(1 for r in done if r.kind == k) for k in ("burgers", "ks", "rb")})
+
+    @staticmethod
+    def _release(retired: list) -> int:
+        """Free the device memory of finished runs, all at once: releasing device memory waits for
+        the whole device, so it is batched rather than done run by run. Returns the planned bytes
+        released."""
+        n = sum(s.footprint for s in retired)
+        retired.clear()
+        return n

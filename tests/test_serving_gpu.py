@@ -14,7 +14,7 @@ def _small_stream(count, seed, steps=(20, 90)):
     reqs = serving.poisson_stream(count, rate=2000.0, seed=seed, steps=steps)
     for r in reqs:           # keep the problems small enough for a quick test
         if r.kind == "rb":
-            r.params.update(Nz=32, Nx=64)
+            r.params.update(Nz=32, Nx=64, Ra=min(r.params["Ra"], 1e6))
         if r.kind == "burgers":
             r.params["N"] = min(r.params["N"], 192)
     return reqs
@@ -35,7 +35,7 @@ def test_alone_equals_mix(precision, cuda_lib):
     assert {r.kind for r in reqs} == {"burgers", "ks", "rb"}
     eng = serving.ServingEngine(budget_bytes=150e9, precision=precision, chunk=25, unroll=5, keep_results=True)
     stats = eng.run(reqs, realtime=False)
-    assert stats["requests"] == len(reqs) and stats["peak_active"] > 1
+    assert stats["requests"] == len(reqs) and stats["peak_active"] > 1 and stats["nonfinite"] == 0
     for r in reqs:
         got = r.result
         ref = _alone(serving.Request(r.rid, r.kind, dict(r.params), r.steps, 0.0), precision, 25, 5)
