@@ -208,7 +208,8 @@ def run_gpu(args):
                    "real_unknowns": P.real_unknowns(), "systems": int(sum(P.nsys)),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (state, history and factors are GBs)",
-                   "grid": dev.grid, "state_finite": finite},
+                   "grid": dev.grid, "state_finite": finite,
+                   "solve_schedule": _schedule_summary(dev)},
         "mode_updates_per_s": value * P.real_unknowns(),
         "roofline": roof,
         "e2e": {"value": ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
@@ -225,6 +226,16 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def _schedule_summary(dev):
+    """The solve schedule the autotuner kept (-1: band kernel; k >= 0: compact schedule k) and the
+    time per solve it measured for each candidate."""
+    from conatus_gb300 import autotune
+    for (prec, _), (best, times) in autotune.cache().items():
+        if prec == dev.precision:
+            return {"chosen": best, "ms_per_solve": {str(k): round(v, 4) for k, v in times.items()}}
+    return None
 
 
 def mixed_error(P, C0, cfg, steps):

@@ -1,0 +1,81 @@
+"""Autotuner of the batched banded solve: the schedule of the step's solve is picked by timing.
+
+Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_set_schedule(h,
+-1)``) and the compact-stream schedules of ``cng_banded_schedules`` (four systems per warp over the
+union pattern of the factors, with different staging chunks and ring depths). Each candidate solves
+the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
+few times on the factors at hand; the fastest is kept for every handle of the factor set. Results
+are cached per process by the shapes of the buckets (batch, n, border, band) and the precision, so
+runs of the same resolution (a serving stream, an ensemble) are timed once.
+
+The reference chooses its solve kernel by constructor flags (python/conatus/runtime/cuda.py:140-152).
+"""
+from __future__ import annotations
+
+import ctypes
+
+from ._lib import call
+
+__all__ = ["schedules", "tune_solve", "cache"]
+
+_CACHE: dict = {}
+
+
+def schedules() -> list:
+    """Candidate schedules: -1 (band kernel) and 0 .. count-1 (compact)."""
+    n = ctypes.c_int32()
+    call("cng_banded_schedules", ctypes.byref(n), None, None)
+    return [-1] + list(range(int(n.value)))
+
+
+def cache() -> dict:
+    return dict(_CACHE)
+
+
+def _signature(dev, fs):
+    return (dev.precision, tuple((h.batch, h.n, h.rank, h.kl, h.ku) for h in fs))
+
+
+def apply(fs, sched: int) -> None:
+    for h in fs:
+        call("cng_banded_set_schedule", h.h, int(sched))
+
+
+def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dict:
+    """Time every candidate schedule on the factor set ``fs`` of ``dev`` (key = (a, b)) and keep
+    the fastest. Returns {schedule: ms per solve}. Runs on ``stream`` (a torch stream or None for
+    the current one); never inside a graph capture."""
+    from .ivp import _torch
+    torch = _torch()
+    sig = _signature(dev, fs)
+    if sig in _CACHE:
+        apply(fs, _CACHE[sig][0])
+        return _CACHE[sig][1]
+    if stream is None:
+        st = torch.cuda.current_stream()
+    elif isinstance(stream, int):
+        st = torch.cuda.ExternalStream(stream)
+    else:
+        st = stream
+    rhs = dev.zeros()
+    out = dev.zeros()
+    with torch.cuda.stream(st):
+        rhs.fill_(1.0)
+    times = {}
+    for sched in (candidates if candidates is not None else schedules()):
+        try:
+            apply(fs, sched)
+            dev._solve_with(fs, key[0], key[1], rhs, out, st)          # warm-up (and first-use set-up)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                dev._solve_with(fs, key[0], key[1], rhs, out, st)
+            e1.record(st)
+            e1.synchronize()
+            times[sched] = e0.elapsed_time(e1) / reps
+        except ValueError:
+            continue                      # schedule does not fit (shared memory): not a candidate
+    best = min(times, key=times.get)
+    apply(fs, best)
+    _CACHE[sig] = (best, times)
+    return times

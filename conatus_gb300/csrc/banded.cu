@@ -405,6 +405,8 @@ __device__ __forceinline__ void cp_async_el(T* s, const T* g) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 constexpr int kChunk = 16;
 
@@ -718,6 +720,8 @@ struct Banded {
     // compact bucket-union form (built by compact())
     bool compact_ready = false;
     int cL = 0, cU = 0, cV = 0, cMaxL = 0, cMaxU = 0, cWg = 0;
+    int cMaxLk[4] = {0, 0, 0, 0}, cMaxUk[4] = {0, 0, 0, 0};   // largest stream chunk per chunk size 2, 4, 8, 16
+    int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
     int* c_offL = nullptr;
     unsigned char* c_Lrow = nullptr;
     unsigned* c_Lmask = nullptr;
@@ -1043,7 +1047,7 @@ static void launch_solve_t(const Banded& h, const SolveIo& io, cudaStream_t st) 
 static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st);
 
 static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaStream_t st) {
-    if (h.compact_ready && launch_solve_compact(h, io_kind, io, st)) return;
+    if (h.compact_ready && h.sched >= 0 && launch_solve_compact(h, io_kind, io, st)) return;
     if (h.dtype == 0) {
         if (io_kind == IO_PLAIN) launch_solve_t<double, IO_PLAIN>(h, io, st);
         else if (io_kind == IO_MAPPED) launch_solve_t<double, IO_MAPPED>(h, io, st);
@@ -1056,6 +1060,19 @@ static void launch_solve(const Banded& h, int io_kind, const SolveIo& io, cudaSt
 }
 
 static void demote_compact(Banded& h, cudaStream_t st);
+
+// FP32 band-kernel solve (one warp per system) of the mixed form: x (+)= A^{-1} b, complex128 data
+static void launch_mixed_dense(const Banded& h, const void* b, void* x, int accumulate, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
+    });
+    MixedView v{h.batch, h.n, h.r, h.kl, h.ku, h.ldab, h.ab32, h.ipiv, h.vt32, h.w32, h.slu32, h.spiv, h.perm};
+    const size_t smem = h.solve_smem(sizeof(zf));
+    k_solve_mixed<<<ceil_div(h.batch, kWarpsPerBlock), 32 * kWarpsPerBlock, smem, st>>>(
+        v, static_cast<const zd*>(b), static_cast<zd*>(x), accumulate);
+    CNG_LAUNCH("k_solve_mixed");
+}
 
 static void make_fp32(Banded& h, cudaStream_t st) {
     if (h.dtype != 1) throw InvalidArgument("FP32 factors need complex128 factors (complex bucket)");
@@ -1370,22 +1387,12 @@ int cng_banded_solve_fp32(const cng_banded* hh, const void* b, void* x, int accu
         if (!h->fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first (it allocates)");
         if (!b || !x) throw InvalidArgument("null device pointer");
         if (b == x) throw InvalidArgument("b and x must not alias");
-        static std::once_flag once;
-        std::call_once(once, [] {
-            cudaFuncSetAttribute(k_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
-        });
-        if (h->compact_ready) {
+        if (h->compact_ready && h->sched >= 0) {
             SolveIo io{b, x, nullptr, nullptr, nullptr, nullptr, accumulate};
             launch_solve_compact(*h, IO_MIXED, io, static_cast<cudaStream_t>(stream));
             return CNG_OK;
         }
-        MixedView v{h->batch, h->n, h->r, h->kl, h->ku, h->ldab, h->ab32, h->ipiv, h->vt32, h->w32,
-                    h->slu32, h->spiv, h->perm};
-        const size_t smem = h->solve_smem(sizeof(zf));
-        k_solve_mixed<<<ceil_div(h->batch, kWarpsPerBlock), 32 * kWarpsPerBlock, smem,
-                        static_cast<cudaStream_t>(stream)>>>(v, static_cast<const zd*>(b), static_cast<zd*>(x),
-                                                             accumulate);
-        CNG_LAUNCH("k_solve_mixed");
+        launch_mixed_dense(*h, b, x, accumulate, static_cast<cudaStream_t>(stream));
     })
 }
 
@@ -1435,7 +1442,18 @@ namespace cng {
 
 constexpr int kGroup = 4;
 constexpr int kLanesPer = 32 / kGroup;
-constexpr int kCChunk = 8;              // columns per staged chunk
+constexpr int kCChunk = 8;              // columns per staged chunk (the default schedule)
+
+// Schedules of the compact solve: columns per staged chunk of the factor streams and the depth of
+// the cp.async ring (chunks in flight + 1). Deeper rings keep more of the stream in flight per warp
+// (the sweep waits on memory otherwise) at the cost of shared memory, hence of resident warps; the
+// autotuner (conatus_gb300.autotune) times them on the factors at hand. Schedule 0 is the default.
+struct CompactSchedule { int chunk, stages; };
+constexpr int kNumSchedules = 8;
+constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2}, {8, 3}, {4, 3}, {16, 2},
+                                                       {16, 3}, {4, 4}, {2, 4}, {16, 4}};
+constexpr int kChunkSizes[4] = {2, 4, 8, 16};
+__host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
 struct CompactIdx {
     int n, r, kl, kv, nL, nU, nV, wgroups, batch;
@@ -1477,7 +1495,7 @@ __device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
 }
 
 // The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
-template <class TF, class TD, int IO>
+template <class TF, class TD, int IO, int CH = kCChunk, int ST = 2>
 __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const CompactData<TF>& cd,
                                                    const SolveIo& io, int block) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -1497,14 +1515,14 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     unsigned char* s_Udist = s_Lrow + ix.nL;
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)kGroup * (n + 64) + 2 * (size_t)(ix.maxLc + ix.maxUc) * kGroup +
-                            (2 * (size_t)kCChunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    const size_t per_warp = (size_t)kGroup * (n + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * kGroup +
+                            (ST * (size_t)CH * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
     TF* y = y0 + (size_t)g * (n + 64);
     TF* zb = y + n;
     TF* Lb = y0 + (size_t)kGroup * (n + 64);
-    TF* Ub = Lb + 2 * (size_t)ix.maxLc * kGroup;
-    int* Pb = reinterpret_cast<int*>(Ub + 2 * (size_t)ix.maxUc * kGroup);
+    TF* Ub = Lb + ST * (size_t)ix.maxLc * kGroup;
+    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * kGroup);
     for (int i = threadIdx.x; i <= n; i += blockDim.x) {
         s_offL[i] = ix.offL[i];
         s_offU[i] = ix.offU[i];
@@ -1532,27 +1550,28 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     const TF* Ug = cd.U + (size_t)wg * (ix.nU) * kGroup;
     const int* Pg = cd.piv + (size_t)wg * n * kGroup;
     // ---------------- forward: L with the row interchanges
+    // ST-deep ring: chunk c sits in buffer c % ST; chunks c + 1 .. c + ST - 1 are in flight while
+    // chunk c is swept (an empty commit group keeps the count of pending groups uniform)
     if (ix.kl > 0 && n > 1) {
-        const int nch = (n - 1 + kCChunk - 1) / kCChunk;
-        auto issue = [&](int c, int buf) {
-            const int j0 = c * kCChunk, j1 = min(j0 + kCChunk, n - 1);
-            warp_stage(Lb + (size_t)buf * ix.maxLc * kGroup, Lg + (size_t)s_offL[j0] * kGroup,
-                       (s_offL[j1] - s_offL[j0]) * kGroup);
-            warp_stage(Pb + (size_t)buf * kCChunk * kGroup, Pg + (size_t)j0 * kGroup, (j1 - j0) * kGroup);
+        const int nch = (n - 1 + CH - 1) / CH;
+        auto issue = [&](int c) {
+            if (c < nch) {
+                const int buf = c % ST;
+                const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
+                warp_stage(Lb + (size_t)buf * ix.maxLc * kGroup, Lg + (size_t)s_offL[j0] * kGroup,
+                           (s_offL[j1] - s_offL[j0]) * kGroup);
+                warp_stage(Pb + (size_t)buf * CH * kGroup, Pg + (size_t)j0 * kGroup, (j1 - j0) * kGroup);
+            }
             cp_async_commit();
         };
-        issue(0, 0);
+        for (int c = 0; c < ST - 1; ++c) issue(c);
         for (int c = 0; c < nch; ++c) {
-            if (c + 1 < nch) {
-                issue(c + 1, (c + 1) & 1);
-                cp_async_wait1();
-            } else {
-                cp_async_wait0();
-            }
+            issue(c + ST - 1);
+            cp_async_wait<ST - 1>();
             __syncwarp();
-            const TF* Lc = Lb + (size_t)(c & 1) * ix.maxLc * kGroup;
-            const int* Pc = Pb + (size_t)(c & 1) * kCChunk * kGroup;
-            const int j0 = c * kCChunk, j1 = min(j0 + kCChunk, n - 1);
+            const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * kGroup;
+            const int* Pc = Pb + (size_t)(c % ST) * CH * kGroup;
+            const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
             const int base = s_offL[j0];
             for (int j = j0; j < j1; ++j) {
                 const int l = Pc[(j - j0) * kGroup + g];
@@ -1575,24 +1594,22 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     }
     // ---------------- backward: U (diagonal holds 1/u_jj)
     {
-        const int nch = (n + kCChunk - 1) / kCChunk;
-        auto issue = [&](int c, int buf) {
-            const int s0 = c * kCChunk, s1 = min(s0 + kCChunk, n);
-            warp_stage(Ub + (size_t)buf * ix.maxUc * kGroup, Ug + (size_t)s_offU[s0] * kGroup,
-                       (s_offU[s1] - s_offU[s0]) * kGroup);
+        const int nch = (n + CH - 1) / CH;
+        auto issue = [&](int c) {
+            if (c < nch) {
+                const int s0 = c * CH, s1 = min(s0 + CH, n);
+                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * kGroup, Ug + (size_t)s_offU[s0] * kGroup,
+                           (s_offU[s1] - s_offU[s0]) * kGroup);
+            }
             cp_async_commit();
         };
-        issue(0, 0);
+        for (int c = 0; c < ST - 1; ++c) issue(c);
         for (int c = 0; c < nch; ++c) {
-            if (c + 1 < nch) {
-                issue(c + 1, (c + 1) & 1);
-                cp_async_wait1();
-            } else {
-                cp_async_wait0();
-            }
+            issue(c + ST - 1);
+            cp_async_wait<ST - 1>();
             __syncwarp();
-            const TF* Uc = Ub + (size_t)(c & 1) * ix.maxUc * kGroup;
-            const int s0 = c * kCChunk, s1 = min(s0 + kCChunk, n);
+            const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * kGroup;
+            const int s0 = c * CH, s1 = min(s0 + CH, n);
             const int base = s_offU[s0];
             for (int s = s0; s < s1; ++s) {
                 const int j = n - 1 - s;
@@ -1661,12 +1678,12 @@ struct MultiSolve {
     SolveIo io[kMaxMulti];
 };
 
-template <class TF, class TD, int IO>
+template <class TF, class TD, int IO, int CH, int ST>
 __global__ void __launch_bounds__(256)
 k_solve_compact_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
-    solve_compact_body<TF, TD, IO>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
+    solve_compact_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
 }
 
 }  // namespace cng
@@ -1743,10 +1760,12 @@ static void demote_compact(Banded& h, cudaStream_t st) {
     dem(h.c_V, h.c_V32, (long long)(W * std::max(h.cV, 1) * G));
 }
 
-static CompactIdx compact_idx(const Banded& h) {
+static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     CompactIdx ix;
     ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
-    ix.wgroups = h.cWg; ix.batch = h.batch; ix.maxLc = h.cMaxL; ix.maxUc = h.cMaxU;
+    ix.wgroups = h.cWg; ix.batch = h.batch;
+    ix.maxLc = h.cMaxLk[chunk_index(chunk)];
+    ix.maxUc = h.cMaxUk[chunk_index(chunk)];
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
     ix.offV = h.c_offV; ix.Vcol = h.c_Vcol;
     return ix;
@@ -1808,6 +1827,14 @@ static void compact(Banded& h, cudaStream_t st) {
     int maxL = 1, maxU = 1;
     for (int j0 = 0; j0 < n - 1; j0 += kCChunk) maxL = std::max(maxL, offL[std::min(j0 + kCChunk, n - 1)] - offL[j0]);
     for (int s0 = 0; s0 < n; s0 += kCChunk) maxU = std::max(maxU, offU[std::min(s0 + kCChunk, n)] - offU[s0]);
+    for (int k = 0; k < 4; ++k) {
+        const int ch = kChunkSizes[k];
+        int ml = 1, mu = 1;
+        for (int j0 = 0; j0 < n - 1; j0 += ch) ml = std::max(ml, offL[std::min(j0 + ch, n - 1)] - offL[j0]);
+        for (int s0 = 0; s0 < n; s0 += ch) mu = std::max(mu, offU[std::min(s0 + ch, n)] - offU[s0]);
+        h.cMaxLk[k] = ml;
+        h.cMaxUk[k] = mu;
+    }
     h.cL = (int)Lrow.size();
     h.cU = (int)Udist.size();
     h.cV = (int)Vcol.size();
@@ -1843,11 +1870,14 @@ static void compact(Banded& h, cudaStream_t st) {
 }
 
 template <class TF>
-static size_t compact_smem(const Banded& h, int nwarps) {
+static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
+    const CompactSchedule sc = kSchedules[sched];
+    const int k = chunk_index(sc.chunk);
     size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
     off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)kGroup * (h.n + 64) + 2 * (size_t)(h.cMaxL + h.cMaxU) * kGroup +
-                            (2 * (size_t)kCChunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    const size_t per_warp = (size_t)kGroup * (h.n + 64) +
+                            (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * kGroup +
+                            ((size_t)sc.stages * sc.chunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     return off + sizeof(TF) * per_warp * nwarps;
 }
 
@@ -1887,20 +1917,20 @@ static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io
 
 namespace cng {
 
-template <class TF, class TD, int IO>
-static void launch_multi(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                         const std::vector<SolveIo>& ios, cudaStream_t st) {
+template <class TF, class TD, int IO, int CH, int ST>
+static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
+                           const std::vector<SolveIo>& ios, int sched, cudaStream_t st) {
     static std::once_flag once;
     std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              220 * 1024);
     });
     // one warp count for all blocks: the largest that fits every bucket
     int nw = 8;
     for (const Banded* h : hs)
-        while (nw > 1 && compact_smem<TF>(*h, nw) > 220 * 1024) --nw;
+        while (nw > 1 && compact_smem<TF>(*h, nw, sched) > 220 * 1024) --nw;
     size_t smem = 0;
-    for (const Banded* h : hs) smem = std::max(smem, compact_smem<TF>(*h, nw));
+    for (const Banded* h : hs) smem = std::max(smem, compact_smem<TF>(*h, nw, sched));
     if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
     MultiSolve<TF> ms{};
     ms.nb = (int)hs.size();
@@ -1912,14 +1942,35 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
     for (int k = 0; k < ms.nb; ++k) {
         const int i = order[k];
         ms.block_start[k] = blocks;
-        ms.ix[k] = compact_idx(*hs[i]);
+        ms.ix[k] = compact_idx(*hs[i], CH);
         ms.cd[k] = cds[i];
         ms.io[k] = ios[i];
         blocks += ceil_div(hs[i]->cWg, nw);
     }
     ms.block_start[ms.nb] = blocks;
-    k_solve_compact_multi<TF, TD, IO><<<blocks, 32 * nw, smem, st>>>(ms);
+    k_solve_compact_multi<TF, TD, IO, CH, ST><<<blocks, 32 * nw, smem, st>>>(ms);
     CNG_LAUNCH("k_solve_compact_multi");
+}
+
+// the schedule of the handles (the autotuner sets one for all the buckets of a step; the default
+// when they differ)
+template <class TF, class TD, int IO>
+static void launch_multi(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
+                         const std::vector<SolveIo>& ios, cudaStream_t st) {
+    int sched = hs[0]->sched;
+    for (const Banded* h : hs)
+        if (h->sched != sched) sched = 0;
+    if (sched < 0 || sched >= kNumSchedules) sched = 0;
+    switch (sched) {
+        case 1: launch_multi_t<TF, TD, IO, 8, 3>(hs, cds, ios, sched, st); break;
+        case 2: launch_multi_t<TF, TD, IO, 4, 3>(hs, cds, ios, sched, st); break;
+        case 3: launch_multi_t<TF, TD, IO, 16, 2>(hs, cds, ios, sched, st); break;
+        case 4: launch_multi_t<TF, TD, IO, 16, 3>(hs, cds, ios, sched, st); break;
+        case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, sched, st); break;
+        case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, sched, st); break;
+        case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, sched, st); break;
+        default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, sched, st); break;
+    }
 }
 
 }  // namespace cng
@@ -1943,6 +1994,15 @@ int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, 
             ios.push_back(SolveIo{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate});
         }
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        bool dense = true;
+        for (const Banded* h : hs) dense = dense && h->sched < 0;
+        if (dense) {              // the band kernel, one launch per bucket
+            for (size_t k = 0; k < hs.size(); ++k) {
+                if (fp32) launch_mixed_dense(*hs[k], b[k], x[k], accumulate, st);
+                else launch_solve(*hs[k], IO_MAPPED, ios[k], st);
+            }
+            return CNG_OK;
+        }
         if (fp32) {
             std::vector<CompactData<zf>> cds;
             for (const Banded* h : hs)
@@ -1961,6 +2021,27 @@ int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, 
 
 int cng_banded_compact(cng_banded* hh, void* stream) {
     CNG_TRY({ cng::compact(*reinterpret_cast<cng::Banded*>(hh), static_cast<cudaStream_t>(stream)); })
+}
+
+int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages) {
+    CNG_TRY({
+        if (!count) throw InvalidArgument("null argument");
+        *count = kNumSchedules;
+        for (int k = 0; k < kNumSchedules; ++k) {
+            if (chunk) chunk[k] = kSchedules[k].chunk;
+            if (stages) stages[k] = kSchedules[k].stages;
+        }
+    })
+}
+
+int cng_banded_set_schedule(cng_banded* hh, int sched) {
+    CNG_TRY({
+        cng::Banded* h = reinterpret_cast<cng::Banded*>(hh);
+        if (!h) throw InvalidArgument("null handle");
+        if (sched < -1 || sched >= kNumSchedules) throw InvalidArgument("schedule out of range");
+        if (sched >= 0 && !h->compact_ready) throw InvalidArgument("compact schedules need cng_banded_compact first");
+        h->sched = sched;
+    })
 }
 
 }  // extern "C"

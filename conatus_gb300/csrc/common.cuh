@@ -114,6 +114,8 @@ __device__ inline zd shfl(zd v, int src) {
     return zd(__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src));
 }
 __device__ inline double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ inline double shfl_down_r(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ inline float shfl_down_r(float v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
 __device__ inline zd shfl_xor(zd v, int m) {
     return zd(__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m));
 }

@@ -354,6 +354,46 @@ __device__ __forceinline__ int zslot(int jz, int sign, int Nzc) {
 }
 
 // one warp per system: state -> factor spectra (with derivatives), complex<R> output
+// der[n] = sum_{k > n, k - n odd} 2 k c[k] for n < N (der[N-1] = 0): with v_k = 2 k c[k], der[n] is
+// the suffix sum from k = n + 1 over entries of parity (n + 1) % 2. Each lane sums a contiguous
+// chunk of k from the top down (one running sum per parity), the chunk totals are combined by a
+// suffix scan over the lanes, and each lane then writes der[k - 1] for the k of its chunk.
+template <class R>
+__device__ __forceinline__ void cheb_der_warp(const double2* __restrict__ c, double2* __restrict__ der, int N,
+                                              int lane) {
+    const int C = (N + 31) >> 5;
+    const int k0 = lane * C, k1 = min(k0 + C, N);
+    // chunk totals per parity (of k)
+    R tx[2] = {R(0), R(0)}, ty[2] = {R(0), R(0)};
+    for (int k = k1 - 1; k >= k0; --k) {
+        if (k == 0) continue;
+        const R w = R(2 * k);
+        tx[k & 1] = tx[k & 1] + w * R(c[k].x);
+        ty[k & 1] = ty[k & 1] + w * R(c[k].y);
+    }
+    // exclusive suffix scan over lanes: sums of the chunks above this lane
+    R sx[2] = {tx[0], tx[1]}, sy[2] = {ty[0], ty[1]};
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const R ux = shfl_down_r(sx[p], off), uy = shfl_down_r(sy[p], off);
+            if (lane + off < 32) { sx[p] = sx[p] + ux; sy[p] = sy[p] + uy; }
+        }
+    }
+    R ax[2], ay[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) { ax[p] = sx[p] - tx[p]; ay[p] = sy[p] - ty[p]; }
+    if (lane == 0 && N >= 1) der[N - 1] = make_double2(0.0, 0.0);
+    for (int k = k1 - 1; k >= k0; --k) {
+        if (k == 0) continue;
+        const R w = R(2 * k);
+        ax[k & 1] = ax[k & 1] + w * R(c[k].x);
+        ay[k & 1] = ay[k & 1] + w * R(c[k].y);
+        der[k - 1] = make_double2((double)ax[k & 1], (double)ay[k & 1]);
+    }
+}
+
 template <class R>
 __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ state, c2<R>* __restrict__ S) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -382,22 +422,11 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
             col[nn] = pos >= 0 ? x[pos] : make_double2(0.0, 0.0);
         }
         __syncwarp();
-        // Chebyshev derivative oy times: out[n] = out[n+2] + 2 (n+1) c[n+1], out[0] /= 2, x 2/L
-        // (in the transform precision R: the recurrence is part of F)
+        // Chebyshev derivative oy times: out[n] = sum_{k > n, k - n odd} 2 k c[k], out[0] /= 2,
+        // x 2/L (in the transform precision R: the derivative is part of F), as a suffix sum per
+        // parity across the warp
         for (int rep = 0; rep < oy; ++rep) {
-            if (lane < 2) {
-                const int par = lane;                 // chain of entries n with n % 2 == par
-                int start = Ny - 2;
-                if ((start & 1) != par) start -= 1;
-                R accx = R(0), accy = R(0);
-                if (((Ny - 1) & 1) == par) der[Ny - 1] = make_double2(0.0, 0.0);
-                for (int nn = start; nn >= 0; nn -= 2) {
-                    const R t = R(2 * (nn + 1));
-                    accx = accx + t * R(col[nn + 1].x);
-                    accy = accy + t * R(col[nn + 1].y);
-                    der[nn] = make_double2((double)accx, (double)accy);
-                }
-            }
+            cheb_der_warp<R>(col, der, Ny, lane);
             __syncwarp();
             const double sc = 2.0 / d.ly;
             for (int nn = lane; nn < Ny; nn += 32) {

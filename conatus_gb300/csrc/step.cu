@@ -29,35 +29,29 @@ __global__ void k_csr_matvec(int nsys, int n, const int* __restrict__ ip, const 
 }
 
 // y = M x with real M values (M of the tau systems is real: conversions between Chebyshev and
-// ultraspherical bases); two rows per thread and two partial sums per row for independent FP64
-// chains (FP64 latency is long on this part).
+// ultraspherical bases). A warp takes one row i for 32 systems (lane = system): uniform trip
+// counts across the warp, the row's entries as broadcast loads, x gathered per lane.
 __global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
                                   const double* __restrict__ val, const double2* __restrict__ x,
                                   double2* __restrict__ y) {
-    const long long total = (long long)nsys * n;
-    const long long half = (total + 1) / 2;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < half;
-         t += (long long)gridDim.x * blockDim.x) {
-        long long rows[2] = {t, t + half};
-        double ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const long long r = rows[u];
-            if (r >= total) continue;
-            const long long m = r / n;
-            const int i = (int)(r - m * n);
-            const double2* xm = x + m * n;
-            int q = 0;
-            for (int p = ip[i]; p < ip[i + 1]; ++p, q ^= 1) {
-                const double a = val[p];
-                const double2 b = xm[ix[p]];
-                ar[u][q] += a * b.x;
-                ai[u][q] += a * b.y;
-            }
+    const unsigned sysw = ((unsigned)nsys + 31u) >> 5;
+    const unsigned nwarps = sysw * (unsigned)n;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned wstride = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
+        const int i = (int)(w / sysw);
+        const unsigned m = (w - (unsigned)i * sysw) * 32u + lane;
+        if (m >= (unsigned)nsys) continue;
+        const double2* xm = x + (long long)m * n;
+        double ar[2] = {0.0, 0.0}, ai[2] = {0.0, 0.0};
+        int q = 0;
+        for (int p = ip[i]; p < ip[i + 1]; ++p, q ^= 1) {
+            const double a = val[p];
+            const double2 b = xm[ix[p]];
+            ar[q] = fma(a, b.x, ar[q]);
+            ai[q] = fma(a, b.y, ai[q]);
         }
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-            if (rows[u] < total) y[rows[u]] = make_double2(ar[u][0] + ar[u][1], ai[u][0] + ai[u][1]);
+        y[(long long)m * n + i] = make_double2(ar[0] + ar[1], ai[0] + ai[1]);
     }
 }
 
@@ -116,37 +110,55 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
 // entry list per row: entry e of row i has column col[e], real value val[e] and a code
 // code[e] = 2 t + imag (t = monomial index, -1 for M: code -2 / -1; imag: the entry is i val).
 // Every coefficient of M and of each L_t is purely real or purely imaginary (derivatives
-// contribute (i k)^p), so an entry costs two real multiply-adds.
+// contribute (i k)^p). Within a row the entries of one term (M, or one L_t) are summed first with
+// their real values (two FP64 multiply-adds per entry), and each term's sum is then scaled by a or
+// c mono[m][t] (two more per term): FP64 is the bound of this kernel, and the per-entry scaling
+// would cost a third and fourth multiply per entry. Entries of a term need not be contiguous (a
+// term split in several runs is scaled once per run).
+// Thread mapping: a warp takes one row i for 32 systems (lane = system), so every lane of a warp
+// runs the same entry list (uniform trip counts: the border rows have up to n entries, the others
+// a dozen) and the entry data is one broadcast load per warp; x is gathered per lane.
 __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                  const double* __restrict__ val, const signed char* __restrict__ code,
                                  const double* __restrict__ mono, int nmono, double a, double c,
                                  const double2* __restrict__ x, const double2* __restrict__ b,
                                  double2* __restrict__ r) {
-    const long long total = (long long)nsys * n;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long m = t / n;
-        const int i = (int)(t - m * n);
-        const double2* xm = x + m * n;
-        const double* mv = mono + m * nmono;
-        double ar[2] = {0.0, 0.0}, ai[2] = {0.0, 0.0};
-        int q = 0;
-        for (int e = ptr[i]; e < ptr[i + 1]; ++e, q ^= 1) {
-            const int cd = code[e];
-            const int tt = cd >> 1;                         // -1: M
-            const double s = val[e] * (tt < 0 ? a : c * mv[tt]);
-            const double2 xv = xm[col[e]];
-            if (cd & 1) {                                   // i s x
-                ar[q] -= s * xv.y;
-                ai[q] += s * xv.x;
-            } else {
-                ar[q] += s * xv.x;
-                ai[q] += s * xv.y;
+    const unsigned sysw = ((unsigned)nsys + 31u) >> 5;             // warps of 32 systems per row
+    const unsigned nwarps = sysw * (unsigned)n;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned wstride = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
+        const int i = (int)(w / sysw);
+        const unsigned m = (w - (unsigned)i * sysw) * 32u + lane;
+        if (m >= (unsigned)nsys) continue;
+        const long long t = (long long)m * n + i;
+        const double2* xm = x + (long long)m * n;
+        const double* mv = mono + (long long)m * nmono;
+        double ar = 0.0, ai = 0.0;
+        int e = ptr[i];
+        const int e1 = ptr[i + 1];
+        while (e < e1) {
+            const int tt = code[e] >> 1;                    // -1: M
+            double gr = 0.0, gi = 0.0;
+            for (; e < e1; ++e) {
+                const int cd = code[e];
+                if ((cd >> 1) != tt) break;
+                const double v = val[e];
+                const double2 xv = xm[col[e]];
+                if (cd & 1) {                               // i v x
+                    gr = fma(-v, xv.y, gr);
+                    gi = fma(v, xv.x, gi);
+                } else {
+                    gr = fma(v, xv.x, gr);
+                    gi = fma(v, xv.y, gi);
+                }
             }
+            const double sc = tt < 0 ? a : c * mv[tt];
+            ar = fma(sc, gr, ar);
+            ai = fma(sc, gi, ai);
         }
-        const double arr = ar[0] + ar[1], aii = ai[0] + ai[1];
         const double2 bv = b[t];
-        r[t] = make_double2(bv.x - arr, bv.y - aii);
+        r[t] = make_double2(bv.x - ar, bv.y - ai);
     }
 }
 
@@ -177,8 +189,9 @@ int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* i
         if (!indptr || !indices || !values || !x || !y) throw InvalidArgument("null device pointer");
         if (x == y) throw InvalidArgument("x and y must not alias");
         if (nsys <= 0 || n <= 0) return CNG_OK;
-        const long long half = ((long long)nsys * n + 1) / 2;
-        const int blocks = (int)std::min<long long>((half + 255) / 256, 152LL * 32);
+        if ((long long)((nsys + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("csr_matvec_real: batch too large");
+        const long long threads = (long long)((nsys + 31) / 32) * n * 32;
+        const int blocks = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
         k_csr_matvec_real<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
             nsys, n, indptr, indices, values, static_cast<const double2*>(x), static_cast<double2*>(y));
         CNG_LAUNCH("k_csr_matvec_real");
@@ -211,11 +224,13 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
             throw InvalidArgument("null device pointer");
         if (r == x || r == b) throw InvalidArgument("r must not alias x or b");
         if (nsys <= 0 || n <= 0) return CNG_OK;
-        const long long total = (long long)nsys * n;
-        const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
-        k_split_residual<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            nsys, n, ptr, col, val, reinterpret_cast<const signed char*>(code), mono, nmono, a, c,
-            static_cast<const double2*>(x), static_cast<const double2*>(b), static_cast<double2*>(r));
+        auto* sc = reinterpret_cast<const signed char*>(code);
+        if ((long long)((nsys + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("split_residual: batch too large");
+        const long long threads = (long long)((nsys + 31) / 32) * n * 32;
+        const int blk = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
+        k_split_residual<<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
+            static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
     })
 }

@@ -81,6 +81,8 @@ class DeviceProblem:
         torch = _torch()
         _lib.lib()
         self.factor_sets = factor_sets      # None: keep every (a, b) factorization, else at most this many
+        self.autotune = True                # time the solve schedules on each new factor set
+        self.tuning = None
         if precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
         self.P = problem
@@ -296,6 +298,9 @@ class DeviceProblem:
                     call("cng_banded_compact", h.h, _stream_handle(stream))
                 f.append(h)
             self._factors[key] = f
+            if self.compact and self.autotune:
+                from .autotune import tune_solve
+                self.tuning = tune_solve(self, key, f, stream)
         return f
 
     def _residual_data(self, bi):
@@ -366,6 +371,7 @@ class DeviceProblem:
                 per = per if isinstance(per, int) else 0
                 data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
                              b_ * self._Lvals(bi)).contiguous()
+                _torch().cuda.current_stream(self.device).synchronize()   # made on torch's stream
             ip, ix = self._pat[bi]
             A = data[key]
             for m in range(self.nsys[bi]):
@@ -377,8 +383,11 @@ class DeviceProblem:
         """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias), every bucket in one
         launch. FP32 form: FP32 solve, FP64 residual, FP32 correction added in FP64 (one
         refinement step)."""
-        s = _stream_handle(stream)
         fs = self.factor(a, b_, stream)
+        self._solve_with(fs, a, b_, rhs, out, stream)
+
+    def _solve_with(self, fs, a, b_, rhs, out, stream=None) -> None:
+        s = _stream_handle(stream)
         if not self.compact:
             for bi, h in enumerate(fs):
                 if self.precision == "fp64":

@@ -104,6 +104,17 @@ int cng_banded_compact(cng_banded* h, void* stream);
 int cng_banded_solve_batch(int nh, cng_banded* const* h, const void* const* b, void* const* x, int fp32,
                            int accumulate, void* stream);
 
+/* Schedules of the compact solve (the batched-solve kernel of the step): count, and per schedule
+ * the columns per staged chunk of the factor streams and the depth of the staging ring. No
+ * reference counterpart: the reference picks its solve kernel (level-scheduled streams or the band
+ * kernel) by constructor flags (python/conatus/runtime/cuda.py:140-152); here the choice is timed
+ * (conatus_gb300.autotune). */
+int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages);
+/* Schedule of a handle: 0 .. count-1 a compact schedule (needs cng_banded_compact), -1 the band
+ * kernel (one warp per system, no compact streams). cng_banded_solve_batch uses the handles'
+ * common schedule (schedule 0 when they differ; the band kernel per bucket when all are -1). */
+int cng_banded_set_schedule(cng_banded* h, int sched);
+
 /* Mixed precision: keep FP32 (complex64) copies of the FP64 factors (allocates; refreshed by
  * refactor_shared). No reference counterpart: the FP32 + FP64-refinement form of the solve. */
 int cng_banded_make_fp32(cng_banded* h, void* stream);

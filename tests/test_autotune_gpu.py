@@ -1,0 +1,49 @@
+"""GPU: the solve schedules picked by the autotuner (conatus_gb300.autotune) all solve the same
+systems: every schedule (band kernel and compact-stream schedules) against schedule 0 on the step's
+factor sets, FP64 and the FP32 form with refinement; the tuner keeps the fastest one it timed."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from _step_cases import template
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("tname,sizes", [("rb_nz16", [32]), ("channel_ny17", [8, 8])])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
+    import torch
+    from conatus_gb300 import autotune
+    from conatus_gb300.ivp import DeviceProblem
+    P = template(tname).instantiate(sizes)
+    dev = DeviceProblem(P, precision)
+    dev.autotune = False
+    a, b = 1.5e3, 1.0
+    fs = dev.factor(a, b)
+    rhs = dev.zeros()
+    rhs.copy_(torch.as_tensor(rng.standard_normal(dev.n_total) + 1j * rng.standard_normal(dev.n_total),
+                              device=rhs.device))
+    ref = dev.zeros()
+    autotune.apply(fs, 0)
+    dev.solve(a, b, rhs, ref)
+    torch.cuda.synchronize()
+    ref_h = ref.cpu().numpy()
+    # schedules differ in the order of their sums: they agree to the conditioning of the systems,
+    # and each one's FP64 residual b - A x is at rounding level
+    tol = 1e-10 if precision == "fp64" else 1e-9
+    r = dev.zeros()
+    for sched in autotune.schedules():
+        out = dev.zeros()
+        autotune.apply(fs, sched)
+        dev.solve(a, b, rhs, out)
+        dev.residual(a, b, out, rhs, r)
+        torch.cuda.synchronize()
+        err = np.linalg.norm(out.cpu().numpy() - ref_h) / np.linalg.norm(ref_h)
+        res = float(torch.linalg.vector_norm(r).item() / torch.linalg.vector_norm(rhs).item())
+        assert err < tol, (sched, err)
+        assert res < (1e-12 if precision == "fp64" else 1e-10), (sched, res)
+    times = autotune.tune_solve(dev, (a, b), fs, reps=2)
+    assert set(times) == set(autotune.schedules())
+    assert autotune.cache()[autotune._signature(dev, fs)][0] == min(times, key=times.get)
