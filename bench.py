@@ -100,22 +100,52 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def solve_bytes(dev):
-    """Algorithmic bytes of one solve over every bucket: band LU (ldab n), pivots, V^T and W
-    (2 r n), right-hand side in and solution out (2 n), complex128, per system."""
+def solve_bytes(dev, fs):
+    """Algorithmic bytes of one batched solve launch, band-equivalent (as the reference's band
+    kernel reads them): per system the band LU (ldab n), V^T and W (2 r n) and the capacitance LU
+    (r r) in the factor precision, pivots (4 n), right-hand side in and solution out (2 n
+    complex128)."""
+    ef = 8 if dev.precision == "fp32" else 16
     tot = 0
-    a, _ = dev_factor_key(dev)
-    for bi, h in enumerate(dev.factor(*dev_factor_key(dev))):
+    for h in fs:
         ns, n, r, ldab = h.batch, h.n, h.rank, h.ldab
-        tot += ns * (16 * (ldab * n + 2 * r * n + 2 * n + r * r) + 4 * n)
+        tot += ns * (ef * (ldab * n + 2 * r * n + r * r) + 4 * n + 32 * n)
     return tot
 
 
-def dev_factor_key(dev):
-    return next(iter(dev._factors))
+def step_bytes(dev, solver):
+    """Algorithmic bytes of one steady step (the model of the hot path's traffic): the solve
+    (one launch; the FP32 form: two launches, plus the FP64 residual reading x and the right-hand
+    side and writing r), the right-hand side combination ((2q + 1) vectors of the mode layout for
+    SBDF-q) and M X (X read, M X written), and F (the state read and the rows written, plus each of
+    the n_f factor and n_o output grids written once and read once in the transform precision)."""
+    fs = dev.factor(*solver._step_keys()[0])
+    vec = 16 * dev.n_total
+    b_solve = solve_bytes(dev, fs)
+    if dev.precision == "fp32":
+        b_solve = 2 * b_solve + 3 * vec
+    q = solver.ring
+    b_rhs = (2 * q + 1) * vec + 2 * vec
+    g = dev.grid
+    M_g = max(g["mx"], 1) * max(g["mz"], 1) * max(g["my"], 1)
+    s_r = 4 if dev.precision == "fp32" else 8
+    nf, no = len(dev.tpl.factors), len(dev.tpl.outputs)
+    b_F = 2 * vec + (nf + no) * 2 * M_g * s_r
+    return {"solve": b_solve, "rhs_and_MX": b_rhs, "F": b_F, "total": b_solve + b_rhs + b_F}
 
 
-def run_gpu(args):
+# DRAM bytes per system of one batched solve launch, from the ncu captures of the channel solve
+# (64x129x64, 1985 systems; dram__bytes_read.sum + dram__bytes_write.sum): the compact solve reads
+# the union pattern of the factors, not the band, so its traffic is below the band-equivalent bytes
+TRAFFIC_PER_SYSTEM = {
+    ("channel", "fp64"): ((325.945344 + 3.196416) * 1e6 / 1985,
+                          "profiles/k_solve_compact_multi_channel64x129x64_fp64.md"),
+    ("channel", "fp32"): ((172.951808 + 3.297024) * 1e6 / 1985,
+                          "profiles/k_solve_compact_multi_channel64x129x64_fp32.md"),
+}
+
+
+def run_gpu(args):def run_gpu(args):
     import torch
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
@@ -130,7 +160,7 @@ def run_gpu(args):
     solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=args.precision)
     dev = solver.dev
     solver.set_state(C0)
-    solver.run_graph(max(args.warmup, solver.order))            # start-up, capture, warm-up
+    solver.run_graph(max(args.warmup, solver.ring))            # start-up, capture, warm-up
     torch.cuda.synchronize()
 
     def barrier():
@@ -158,18 +188,18 @@ def run_gpu(args):
     value = ws * args.steps / (ms / 1e3)
     finite = bool(torch.isfinite(torch.view_as_real(solver.X)).all().item())
 
-    # ---- per-kernel timing of the dominant pieces (same stream, CUDA events)
+    # ---- per-kernel timing (same stream, CUDA events): one batched solve launch, and F
     s = solver.stream
     reps = 5
-    a0 = dev_factor_key(dev)
+    fs = dev.factor(*solver._step_keys()[0])
     R = dev.zeros()
     R.copy_(solver.X)
     X2 = dev.zeros()
     torch.cuda.synchronize()
-    ts = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ts = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ts[0].record(s)
     for _ in range(reps):
-        dev.solve(a0[0], a0[1], R, X2, s)
+        dev.solve_launch(fs, R, X2, s)
     ts[1].record(s)
     for _ in range(reps):
         dev.F(solver.X, R, s)
@@ -178,12 +208,19 @@ def run_gpu(args):
     solve_ms = ts[0].elapsed_time(ts[1]) / reps
     f_ms = ts[1].elapsed_time(ts[2]) / reps
     hbm_peak, peak_kind = measured_peaks()
-    sb = solve_bytes(dev)
-    roof = {"kernel": "k_solve (bordered-banded solves of all buckets, one launch per bucket)",
+    sb = solve_bytes(dev, fs)
+    nsys = sum(h.batch for h in fs)
+    tr = TRAFFIC_PER_SYSTEM.get((args.config, args.precision)) if args.fourier is None else None
+    roof = {"kernel": "k_solve_compact_multi (batched bordered-banded solve, all buckets in one launch)",
             "bound": "hbm", "achieved": sb / (solve_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-            "frac": sb / (solve_ms / 1e3) / 1e9 / hbm_peak, "traffic": None,
-            "algorithmic_bytes": sb, "launch_ms": solve_ms, "peak_kind": peak_kind,
+            "frac": sb / (solve_ms / 1e3) / 1e9 / hbm_peak,
+            "traffic": tr[0] * nsys if tr else None,
+            "traffic_source": (tr[1] + " (bytes per system x systems)") if tr else None,
+            "algorithmic_bytes": sb, "launch_ms": solve_ms, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "F_ms": f_ms}
+    sbytes = step_bytes(dev, solver)
+    step_roof = {"bytes_per_step": sbytes, "achieved": sbytes["total"] / (ms_step / 1e3) / 1e9,
+                 "unit": "GB/s", "frac": sbytes["total"] / (ms_step / 1e3) / 1e9 / hbm_peak}
 
     # ---- end to end through the public API: host state in and out every step
     import torch as _t
@@ -212,6 +249,7 @@ def run_gpu(args):
                    "solve_schedule": _schedule_summary(dev)},
         "mode_updates_per_s": value * P.real_unknowns(),
         "roofline": roof,
+        "step_roofline": step_roof,
         "e2e": {"value": ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": solver.launches_per_step() * args.steps,

@@ -6,13 +6,15 @@ union pattern of the factors, with different staging chunks and ring depths). Ea
 the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
 few times on the factors at hand; the fastest is kept for every handle of the factor set. Results
 are cached per process by the shapes of the buckets (batch, n, border, band) and the precision, so
-runs of the same resolution (a serving stream, an ensemble) are timed once.
+runs of the same resolution (a serving stream, an ensemble) are timed once. The environment variable
+CONATUS_GB300_SOLVE_SCHEDULE fixes the schedule instead (-1, 0, 1, ...), e.g. for profiling.
 
 The reference chooses its solve kernel by constructor flags (python/conatus/runtime/cuda.py:140-152).
 """
 from __future__ import annotations
 
 import ctypes
+import os
 
 from ._lib import call
 
@@ -39,6 +41,7 @@ def _signature(dev, fs):
 def apply(fs, sched: int) -> None:
     for h in fs:
         call("cng_banded_set_schedule", h.h, int(sched))
+        h.schedule = int(sched)
 
 
 def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dict:
@@ -47,6 +50,10 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
     the current one); never inside a graph capture."""
     from .ivp import _torch
     torch = _torch()
+    fixed = os.environ.get("CONATUS_GB300_SOLVE_SCHEDULE")
+    if fixed is not None:                 # a fixed schedule instead of timing (reproducible runs)
+        apply(fs, int(fixed))
+        return {int(fixed): None}
     sig = _signature(dev, fs)
     if sig in _CACHE:
         apply(fs, _CACHE[sig][0])

@@ -245,8 +245,8 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     }
 }
 
-// Real FFT along the outer axis of [outer][len][inner] (inner even): two adjacent inner columns
-// per complex FFT. Backward (c2r): half spectrum [outer][K][inner] complex (modes 0..K-1,
+// Real FFT along the outer axis of [outer][len][inner]: two adjacent inner columns per complex FFT
+// (an odd last column is paired with zero). Backward (c2r): half spectrum [outer][K][inner] complex (modes 0..K-1,
 // Hermitian continuation, zero padding) -> [outer][L][inner] real, unnormalized. Forward (r2c):
 // real -> modes 0..K-1, scaled 1/L.
 template <class R>
@@ -428,11 +428,11 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         for (int rep = 0; rep < oy; ++rep) {
             cheb_der_warp<R>(col, der, Ny, lane);
             __syncwarp();
-            const double sc = 2.0 / d.ly;
+            const R sc = R(2.0 / d.ly);
             for (int nn = lane; nn < Ny; nn += 32) {
                 double2 v = der[nn];
                 if (nn == 0) { v.x = v.x / 2; v.y = v.y / 2; }
-                col[nn] = make_double2(v.x * sc, v.y * sc);
+                col[nn] = make_double2((double)(R(v.x) * sc), (double)(R(v.y) * sc));
             }
             __syncwarp();
         }
@@ -450,12 +450,15 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         } else {
             dst = S + (long long)f * Ny;
         }
+        // in the transform precision R (the FP32 form's factors are FP32 from here on)
+        const R frR = R(fr), fiR = R(fi);
         for (int nn = lane; nn < Ny; nn += 32) {
             const double2 c = col[nn];
-            double vr = fr * c.x - fi * c.y, vi = fr * c.y + fi * c.x;
-            if (b.real) vi = 0.0;
-            dst[nn] = mk<R>(R(vr), R(vi));
-            if (dstc) dstc[nn] = mk<R>(R(vr), R(-vi));
+            const R cr = R(c.x), ci = R(c.y);
+            const R vr = frR * cr - fiR * ci;
+            const R vi = b.real ? R(0) : frR * ci + fiR * cr;
+            dst[nn] = mk<R>(vr, vi);
+            if (dstc) dstc[nn] = mk<R>(vr, -vi);
         }
         __syncwarp();
     }

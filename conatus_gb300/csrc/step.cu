@@ -74,6 +74,30 @@ __global__ void k_sbdf_rhs(SbdfArgs a, double* __restrict__ rhs, long long count
     }
 }
 
+constexpr int kMaxTerms = 12;
+struct LincombArgs {
+    int nterms;
+    double coef[kMaxTerms];
+    int neg[kMaxTerms];
+    const double* v[kMaxTerms];
+};
+
+// out = base + sum_k (+/-) coef_k v_k on real and imaginary parts, applied in order with explicit
+// roundings (acc = acc +/- coef_k * v_k), base = 0 when absent: the right-hand side of an IMEX
+// Runge-Kutta stage (lincomb.py:73-95) and of a CN-family step (integrator.py:581-594).
+__global__ void k_lincomb(LincombArgs a, const double* __restrict__ base, double* __restrict__ out,
+                          long long count) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x) {
+        double acc = base ? base[t] : 0.0;
+        for (int k = 0; k < a.nterms; ++k) {
+            const double p = __dmul_rn(a.coef[k], a.v[k][t]);
+            acc = a.neg[k] ? __dsub_rn(acc, p) : __dadd_rn(acc, p);
+        }
+        out[t] = acc;
+    }
+}
+
 // r = b - (a M + c sum_t mono[m][t] L_t) x per system, FP64 (the refinement residual). M values
 // shared by the bucket (nnz), L_t coefficient rows (nmono x nnz), mono (nsys x nmono).
 __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
@@ -232,6 +256,28 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
             nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
             static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
+    })
+}
+
+int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef, const int32_t* negate,
+                const void* const* vecs, void* out, void* stream) {
+    CNG_TRY({
+        if (nterms < 0 || nterms > kMaxTerms) throw InvalidArgument("lincomb: 0 to 12 terms");
+        if (!out || (nterms > 0 && (!coef || !negate || !vecs))) throw InvalidArgument("null argument");
+        if (count <= 0) return CNG_OK;
+        LincombArgs a{};
+        a.nterms = nterms;
+        for (int k = 0; k < nterms; ++k) {
+            a.coef[k] = coef[k];
+            a.neg[k] = negate[k] ? 1 : 0;
+            a.v[k] = static_cast<const double*>(vecs[k]);
+            if (!a.v[k]) throw InvalidArgument("lincomb: null vector");
+        }
+        const long long n = 2 * count;      // complex entries -> doubles
+        const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 32);
+        k_lincomb<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<const double*>(base),
+                                                                          static_cast<double*>(out), n);
+        CNG_LAUNCH("k_lincomb");
     })
 }
 

@@ -353,6 +353,21 @@ class DeviceProblem:
             ptr[i + 1] = len(col)
         return ptr, np.array(col), np.array(val), np.array(code), act
 
+    def ensure_residual(self, a, b_) -> None:
+        """Build the device data of residual(a, b, ...) now (the first call would, outside a graph
+        capture; a capture cannot allocate)."""
+        for bi, b in enumerate(self.tpl.buckets):
+            kind, data = self._residual_data(bi)
+            key = (float(a), float(b_))
+            if kind == "values" and key not in data:
+                Mv, per = self._M[bi]
+                per = per if isinstance(per, int) else 0
+                data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
+                             b_ * self._Lvals(bi)).contiguous()
+        _torch().cuda.current_stream(self.device).synchronize()
+        if self.precision == "fp32" and self._R2 is None:
+            self._R2 = self.zeros()
+
     def residual(self, a, b_, x, rhs, out, stream=None) -> None:
         """out = rhs - (a M + b L) x per bucket, FP64."""
         s = _stream_handle(stream)
@@ -410,6 +425,16 @@ class DeviceProblem:
         rp = (ctypes.c_void_p * nb)(*[self.bucket(self._R2, bi).data_ptr() for bi in range(nb)])
         call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
 
+    def solve_launch(self, fs, rhs, out, stream=None) -> None:
+        """One batched solve launch with the factor set ``fs`` (FP32 factors in the FP32 form), no
+        refinement: the unit the solve's roofline is measured on."""
+        nb = len(fs)
+        hs = (ctypes.c_void_p * nb)(*[h.h.value for h in fs])
+        bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in range(nb)])
+        xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in range(nb)])
+        call("cng_banded_solve_batch", nb, hs, bp, xp, 1 if self.precision == "fp32" else 0, 0,
+             _stream_handle(stream))
+
     def zeros(self):
         torch = _torch()
         return torch.zeros(self.n_total, dtype=torch.complex128, device=self.device)
@@ -448,21 +473,92 @@ class _Graph:
                 pass
 
 
+SBDF_SCHEMES = ("SBDF1", "SBDF2", "SBDF3", "SBDF4")
+CN_SCHEMES = ("CNAB1", "CNAB2", "MCNAB2", "CNLF2")
+RK_SCHEMES = ("RK111", "RK222", "RK443", "RKSMR", "RKGFY")
+
+
+def cn_coefficients(name: str):
+    """(a, b, c) of a constant-step CN-family multistep scheme (Wang & Ruuth 2008), a in units of
+    1/dt: sum_j (a_j/dt) M X^{n+1-j} + b_j L X^{n+1-j} = sum_{j>=1} c_j F^{n+1-j}
+    (python/conatus/timestep/schemes.py:91-103; the published coefficients)."""
+    return {"CNAB1": ([1.0, -1.0], [0.5, 0.5], [0.0, 1.0]),
+            "CNAB2": ([1.0, -1.0, 0.0], [0.5, 0.5, 0.0], [0.0, 1.5, -0.5]),
+            "MCNAB2": ([1.0, -1.0, 0.0], [9 / 16, 6 / 16, 1 / 16], [0.0, 1.5, -0.5]),
+            "CNLF2": ([0.5, 0.0, -0.5], [0.5, 0.0, 0.5], [0.0, 1.0, 0.0])}[name]
+
+
+def rk_tableau(name: str):
+    """(A, H, c) of an IMEX Runge-Kutta scheme in cumulative form M X_i = M X_0 + dt sum_j A_ij F_j
+    - dt sum_j H_ij L X_j (python/conatus/timestep/schemes.py:106-143; the published tableaux:
+    RK222 and RK443 of Ascher, Ruuth & Spiteri 1997, RKSMR of Spalart, Moser & Rogers 1991,
+    RKGFY Heun / Crank-Nicolson)."""
+    if name == "RK111":
+        return [[0, 0], [1, 0]], [[0, 0], [0, 1]], [0, 1]
+    if name == "RK222":
+        g = (2 - math.sqrt(2)) / 2
+        d = 1 - 1 / g / 2
+        return ([[0, 0, 0], [g, 0, 0], [d, 1 - d, 0]], [[0, 0, 0], [0, g, 0], [0, 1 - g, g]], [0, g, 1])
+    if name == "RK443":
+        return ([[0, 0, 0, 0, 0], [1 / 2, 0, 0, 0, 0], [11 / 18, 1 / 18, 0, 0, 0],
+                 [5 / 6, -5 / 6, 1 / 2, 0, 0], [1 / 4, 7 / 4, 3 / 4, -7 / 4, 0]],
+                [[0, 0, 0, 0, 0], [0, 1 / 2, 0, 0, 0], [0, 1 / 6, 1 / 2, 0, 0],
+                 [0, -1 / 2, 1 / 2, 1 / 2, 0], [0, 3 / 2, -3 / 2, 1 / 2, 1 / 2]],
+                [0, 1 / 2, 2 / 3, 1 / 2, 1])
+    if name == "RKSMR":
+        al, be = (29 / 96, -3 / 40, 1 / 6), (37 / 160, 5 / 24, 1 / 6)
+        ga, ze = (8 / 15, 5 / 12, 3 / 4), (-17 / 60, -5 / 12)
+        A = [[0, 0, 0, 0], [ga[0], 0, 0, 0], [ga[0] + ze[0], ga[1], 0, 0],
+             [ga[0] + ze[0], ga[1] + ze[1], ga[2], 0]]
+        H = [[0, 0, 0, 0], [al[0], be[0], 0, 0], [al[0], be[0] + al[1], be[1], 0],
+             [al[0], be[0] + al[1], be[1] + al[2], be[2]]]
+        return A, H, [0, 8 / 15, 2 / 3, 1]
+    if name == "RKGFY":
+        return ([[0, 0, 0], [1, 0, 0], [1 / 2, 1 / 2, 0]], [[0, 0, 0], [1 / 2, 1 / 2, 0], [1 / 2, 0, 1 / 2]],
+                [0, 1, 1])
+    raise ValueError(f"unknown Runge-Kutta scheme {name!r}")
+
+
 class IVPSolver:
-    """SBDF-q time stepper on the device (see module docstring)."""
+    """IMEX time stepper on the device (see module docstring): SBDF1-4, the CN family (CNAB1,
+    CNAB2, MCNAB2, CNLF2) and IMEX Runge-Kutta (RK111, RK222, RK443, RKSMR, RKGFY), start-up
+    ``lower_order`` as the reference's default."""
 
     def __init__(self, problem, scheme: str = "SBDF2", dt: float = 1e-3, precision: str = "fp64",
                  device_problem: DeviceProblem | None = None, factor_sets: int | None = None):
-        if scheme not in ("SBDF1", "SBDF2", "SBDF3", "SBDF4"):
-            raise ValueError(f"scheme {scheme!r}: SBDF1..SBDF4")
+        if scheme in SBDF_SCHEMES:
+            self.family, self.order = "sbdf", int(scheme[-1])
+            self.ring = self.order
+        elif scheme in CN_SCHEMES:
+            self.family, self.order = "cn", 0
+            self._cn = cn_coefficients(scheme)
+            self.ring = len(self._cn[0]) - 1
+        elif scheme in RK_SCHEMES:
+            self.family, self.order = "rk", 0
+            self._rk = rk_tableau(scheme)
+            self.ring = 1
+        else:
+            raise ValueError(f"scheme {scheme!r}: one of {SBDF_SCHEMES + CN_SCHEMES + RK_SCHEMES}")
         self.scheme, self.dt = scheme, float(dt)
-        self.order = int(scheme[-1])
         self.dev = device_problem or DeviceProblem(problem, precision, factor_sets=factor_sets)
         z = self.dev.zeros
         self.X, self.R = z(), z()
-        self.MXh = [z() for _ in range(self.order)]
-        self.Fh = [z() for _ in range(self.order)]
-        self.filled, self.head = 0, self.order - 1
+        nh = self.ring if self.family != "rk" else 0
+        self.MXh = [z() for _ in range(nh)]
+        self.Fh = [z() for _ in range(nh)]
+        self.LXh = [z() for _ in range(nh)] if self.family == "cn" else []     # -L X (negated)
+        if self.family == "rk":
+            S = len(self._rk[2]) - 1
+            self._MX0 = z()
+            self._Xs = [self.X] + [z() for _ in range(S - 1)]     # the last stage is written to X
+            self._Fs = [z() if any(self._rk[0][m][j] != 0 for m in range(j + 1, S + 1)) else None
+                        for j in range(S)]
+            self._LXs = [z() if any(self._rk[1][m][j] != 0 for m in range(j + 1, S + 1)) else None
+                         for j in range(S)]
+            self._Xnew = z()
+        self._zero = None
+        self._warm = False
+        self.filled, self.head = 0, self.ring - 1
         self.t, self.iteration = 0.0, 0
         self._graphs = {}
         torch = _torch()
@@ -478,32 +574,137 @@ class IVPSolver:
             X = self.dev.to_device(X)
         self.X.copy_(X)
         self.t, self.iteration = float(t), 0
-        self.filled, self.head = 0, self.order - 1
+        self.filled, self.head = 0, self.ring - 1
 
-    def set_history(self, MX_list, F_list) -> None:
-        """History of M X and F (newest first), e.g. to continue from another solver's state."""
+    def set_history(self, MX_list, F_list, LX_list=None) -> None:
+        """History (newest first) of M X and F, and of L X for the CN family, e.g. to continue from
+        another solver's state."""
+        if self.family == "rk":
+            raise ValueError("a Runge-Kutta scheme keeps no history")
         self.filled = len(MX_list)
         for j, (mx, f) in enumerate(zip(MX_list, F_list)):
-            slot = (self.head - j) % self.order
+            slot = (self.head - j) % self.ring
             self.MXh[slot].copy_(mx)
             self.Fh[slot].copy_(f)
+            if self.family == "cn":
+                self.LXh[slot].copy_(-LX_list[j])
+
+    # ------------------------------------------------------------------ pieces of a step
+    def _neg_LX(self, x, out, s):
+        """out = -L x (the FP64 operator apply of the residual kernel with a = 0, b = 1)."""
+        if self._zero is None:
+            self._zero = self.dev.zeros()
+        self.dev.residual(0.0, 1.0, x, self._zero, out, s)
 
     def _push(self, s):
-        self.head = (self.head + 1) % self.order
+        self.head = (self.head + 1) % self.ring
         self.dev.MX(self.X, self.MXh[self.head], s)
+        if self.family == "cn":
+            self._neg_LX(self.X, self.LXh[self.head], s)
         self.dev.F(self.X, self.Fh[self.head], s)
-        self.filled = min(self.filled + 1, self.order)
+        self.filled = min(self.filled + 1, self.ring)
+
+    def _lincomb(self, base, terms, out, s):
+        """out = base + sum of (negate, coef, vector) terms in order (cng_lincomb)."""
+        k = len(terms)
+        cs = (ctypes.c_double * max(k, 1))(*[t[1] for t in terms])
+        ng = (ctypes.c_int32 * max(k, 1))(*[1 if t[0] else 0 for t in terms])
+        vp = (ctypes.c_void_p * max(k, 1))(*[t[2].data_ptr() for t in terms])
+        call("cng_lincomb", self.dev.n_total, None if base is None else base.data_ptr(), k, cs, ng, vp,
+             out.data_ptr(), s)
+
+    def _cn_now(self):
+        """The scheme's coefficients once the history is full, CNAB1 before (lower-order start-up,
+        integrator.py:577-579)."""
+        return self._cn if self.filled >= self.ring else cn_coefficients("CNAB1")
+
+    def _step_keys(self):
+        """(a, b) of the solves of the next step."""
+        if self.family == "sbdf":
+            a, _ = SBDF[min(self.order, self.filled + 1)]
+            return [(a[0] / self.dt, 1.0)]
+        if self.family == "cn":
+            filled = self.filled
+            self.filled = min(self.filled + 1, self.ring)
+            a, b, _ = self._cn_now()
+            self.filled = filled
+            return [(a[0] / self.dt, b[0])]
+        A, H, c = self._rk
+        return sorted({(1.0, self.dt * H[i][i]) for i in range(1, len(c))})
+
+    def _step_factors(self, s):
+        """Factor sets (and the other device data made on first use) of the next step, made
+        outside any capture."""
+        for a, b in self._step_keys():
+            self.dev.factor(a, b, s)
+            if self.dev.precision == "fp32":
+                self.dev.ensure_residual(a, b)
+        if self.family != "sbdf":
+            self.dev.ensure_residual(0.0, 1.0)
+            if self._zero is None:
+                self._zero = self.dev.zeros()
 
     def _combine_solve(self, s):
-        q = min(self.order, self.filled)
-        a, c = SBDF[q]
-        slots = [(self.head - j) % self.order for j in range(q)]
-        cs = (ctypes.c_double * q)(*[c[j + 1] for j in range(q)])
-        ds = (ctypes.c_double * q)(*[a[j + 1] / self.dt for j in range(q)])
-        Fp = (ctypes.c_void_p * q)(*[self.Fh[k].data_ptr() for k in slots])
-        Mp = (ctypes.c_void_p * q)(*[self.MXh[k].data_ptr() for k in slots])
-        call("cng_sbdf_rhs", q, cs, ds, Fp, Mp, self.R.data_ptr(), self.dev.n_total, s)
-        self.dev.solve(a[0] / self.dt, 1.0, self.R, self.X, s)
+        if self.family == "sbdf":
+            q = min(self.order, self.filled)
+            a, c = SBDF[q]
+            slots = [(self.head - j) % self.order for j in range(q)]
+            cs = (ctypes.c_double * q)(*[c[j + 1] for j in range(q)])
+            ds = (ctypes.c_double * q)(*[a[j + 1] / self.dt for j in range(q)])
+            Fp = (ctypes.c_void_p * q)(*[self.Fh[k].data_ptr() for k in slots])
+            Mp = (ctypes.c_void_p * q)(*[self.MXh[k].data_ptr() for k in slots])
+            call("cng_sbdf_rhs", q, cs, ds, Fp, Mp, self.R.data_ptr(), self.dev.n_total, s)
+            self.dev.solve(a[0] / self.dt, 1.0, self.R, self.X, s)
+            return
+        # CN family (integrator.py:581-603): rhs = sum_{j>=1} c_j F_j - (a_j/dt) M X_j - b_j L X_j
+        a, b, c = self._cn_now()
+        terms = []
+        for j in range(1, len(a)):
+            if j > self.filled:
+                break
+            slot = (self.head - (j - 1)) % self.ring
+            if c[j] != 0:
+                terms.append((False, c[j], self.Fh[slot]))
+            if a[j] != 0:
+                terms.append((True, a[j] / self.dt, self.MXh[slot]))
+            if b[j] != 0:
+                terms.append((False, b[j], self.LXh[slot]))       # - b_j L X_j = + b_j (-L X_j)
+        self._lincomb(None, terms, self.R, s)
+        self.dev.solve(a[0] / self.dt, b[0], self.R, self.X, s)
+
+    def _rk_stages(self, s):
+        """One IMEX Runge-Kutta step (integrator.py:605-646): M X_i = M X_0 + dt sum_k A_ik F_k -
+        dt sum_k H_ik L X_k, (M + dt H_ii L) X_i = rhs; X_s is the new state."""
+        A, H, c = self._rk
+        S = len(c) - 1
+        dt = self.dt
+        self.dev.MX(self.X, self._MX0, s)
+        for i in range(1, S + 1):
+            j = i - 1
+            xj = self._Xs[j]
+            if self._Fs[j] is not None:
+                self.dev.F(xj, self._Fs[j], s)
+            if self._LXs[j] is not None:
+                self._neg_LX(xj, self._LXs[j], s)
+            terms = []
+            for k in range(i):
+                if A[i][k] != 0:
+                    terms.append((False, dt * A[i][k], self._Fs[k]))
+                if H[i][k] != 0:
+                    terms.append((False, dt * H[i][k], self._LXs[k]))   # - dt H L X = + dt H (-L X)
+            self._lincomb(self._MX0, terms, self.R, s)
+            out = self._Xs[i] if i < S else self._Xnew
+            self.dev.solve(1.0, dt * H[i][i], self.R, out, s)
+        # X_s -> X (the stage buffers keep X_0 = X)
+        call("cng_lincomb", self.dev.n_total, self._Xnew.data_ptr(), 0, None, None, None, self.X.data_ptr(), s)
+
+    def _advance(self, s):
+        """The device work of one step (no factorization: see _step_factors)."""
+        if self.family == "rk":
+            self._rk_stages(s)
+        else:
+            self._push(s)
+            self._combine_solve(s)
 
     def _enter(self):
         if self.join:
@@ -520,11 +721,9 @@ class IVPSolver:
 
     def _step(self) -> None:
         s = _stream_handle(self.stream)
-        q = min(self.order, self.filled + 1)
-        a, _ = SBDF[q]
-        self.dev.factor(a[0] / self.dt, 1.0, s)         # outside the timed/captured work
-        self._push(s)
-        self._combine_solve(s)
+        self._step_factors(s)                       # outside the timed/captured work
+        self._advance(s)
+        self._warm = True
         self.t += self.dt
         self.iteration += 1
 
@@ -535,24 +734,26 @@ class IVPSolver:
         self._leave()
 
     def run_graph(self, steps: int, unroll: int = 1) -> None:
-        """``steps`` steps; once the history is full, the steps run as CUDA graph launches, each
-        graph holding ``unroll`` steps (one graph per position of the history ring and length,
-        captured on first use; a remainder shorter than ``unroll`` runs as one-step graphs)."""
+        """``steps`` steps; once the history is full (at once for Runge-Kutta), the steps run as CUDA
+        graph launches, each graph holding ``unroll`` steps (one graph per position of the history
+        ring and length, captured on first use; a remainder shorter than ``unroll`` runs as
+        one-step graphs)."""
         s = _stream_handle(self.stream)
         steps = int(steps)
         unroll = max(1, int(unroll))
         self._enter()
-        while steps > 0 and self.filled < self.order:
+        # plain steps until the history is full, and at least one (its first launches make the
+        # lazily built device data -- tables, kernel attributes -- which a capture cannot make)
+        while steps > 0 and (not self._warm or (self.family != "rk" and self.filled < self.ring)):
             self._step()
             steps -= 1
         if steps <= 0:
             self._leave()
             return
-        a, _ = SBDF[self.order]
-        self.dev.factor(a[0] / self.dt, 1.0, s)
+        self._step_factors(s)
         while steps > 0:
             u = unroll if steps >= unroll else 1
-            key = ((self.head + 1) % self.order, u)
+            key = ((self.head + 1) % self.ring, u)
             g = self._graphs.get(key)
             if g is None:
                 self.stream.synchronize()
@@ -560,15 +761,14 @@ class IVPSolver:
                 head0, filled0 = self.head, self.filled
                 try:
                     for _ in range(u):
-                        self._push(s)
-                        self._combine_solve(s)
+                        self._advance(s)
                 finally:
                     h = ctypes.c_void_p()
                     call("cng_graph_end", s, ctypes.byref(h))
                 g = self._graphs[key] = _Graph(h)
                 self.head, self.filled = head0, filled0     # captured, not run
             g.launch(s)
-            self.head = (self.head + u) % self.order
+            self.head = (self.head + u) % self.ring
             self.t += u * self.dt
             self.iteration += u
             steps -= u
@@ -580,7 +780,7 @@ class IVPSolver:
         self._enter()
         with _torch().cuda.stream(self.stream):
             self.X.copy_(host_in, non_blocking=True)
-        if self.filled >= self.order:
+        if self.family == "rk" or self.filled >= self.ring:
             self.run_graph(1)
         else:
             self._step()
@@ -594,17 +794,26 @@ class IVPSolver:
         return self.dev.to_host(self.X)
 
     def launches_per_step(self) -> int:
-        """Kernels of this library launched by one step: M X (one per bucket), F (unpack and pack
-        per bucket, 2 Chebyshev transforms, 2 or 4 Fourier transforms, products, constant part),
-        the right-hand side combination, one solve per bucket."""
-        nb = len(self.dev.tpl.buckets)
-        d = self.dev.d
-        f = 2 * nb + 2 + (2 if d >= 1 else 2) + (2 if d >= 2 else 0) + 1 + (1 if self.dev.has_b0 else 0)
-        if self.dev.compact:
-            solve = 1 if self.dev.precision == "fp64" else 2 + nb
-        else:
-            solve = nb
-        return nb + f + 1 + solve
+        """Kernels of this library launched by one steady step: M X (one per bucket), F (unpack and
+        pack per bucket, 2 Chebyshev transforms, 2 or 4 Fourier transforms, products, constant
+        part), -L X (one per bucket, CN and Runge-Kutta), the right-hand side combination and the
+        solves (one batched launch, or one per bucket with the band kernel; the FP32 form adds the
+        residual per bucket and a second solve)."""
+        dev = self.dev
+        nb = len(dev.tpl.buckets)
+        d = dev.d
+        f = 2 * nb + 2 + 2 + (2 if d >= 2 else 0) + 1 + (1 if dev.has_b0 else 0)
+        dense = bool(dev._factors) and all(getattr(h, "schedule", 0) < 0 for fs in dev._factors.values() for h in fs)
+        one = (nb if dense else 1) if dev.compact else nb
+        solve = one if dev.precision == "fp64" else 2 * one + nb
+        if self.family == "sbdf":
+            return nb + f + 1 + solve
+        if self.family == "cn":
+            return nb + nb + f + 1 + solve
+        A, H, c = self._rk
+        S = len(c) - 1
+        return nb + sum(f for x in self._Fs if x is not None) + sum(nb for x in self._LXs if x is not None) \
+            + S * (1 + solve) + 1
 
     def synchronize(self) -> None:
         self.stream.synchronize()

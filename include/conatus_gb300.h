@@ -269,6 +269,13 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
 int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* indices, const double* values,
                         const void* x, void* y, void* stream);
 
+/* out = base + sum_k (negate[k] ? -1 : +1) coef[k] vecs[k] over count complex128 entries, the terms
+ * applied in order with explicit roundings (base NULL: start from 0); out may alias base. The
+ * right-hand side of an IMEX Runge-Kutta stage, rk_rhs (python/conatus/timestep/lincomb.py:73-95),
+ * and of a CN-family step, _cn_rhs (python/conatus/timestep/integrator.py:581-594). At most 12 terms. */
+int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef, const int32_t* negate,
+                const void* const* vecs, void* out, void* stream);
+
 /* rhs = sum_j (c_j F_j - d_j MX_j), j < q, on count complex128 entries (explicit roundings, no
  * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */
 int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,

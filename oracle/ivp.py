@@ -17,6 +17,9 @@ follows, in NumPy/SciPy:
 * ``sbdf_step``: ``IVPSolver._sbdf_step`` (python/conatus/timestep/integrator.py:361-373) with
   ``sbdf_coefficients`` (schemes.py:106-116) and ``sbdf_rhs`` (lincomb.py:146-162), solves by
   the oracle bordered-banded restatement (oracle/banded.py), factorizations cached per (a, b).
+* ``CNStepper`` / ``RKStepper``: ``IVPSolver._cn_step`` (integrator.py:567-603) and
+  ``rk_stages`` (integrator.py:605-646) with ``cn_coefficients`` / ``rk_tableau``
+  (schemes.py:91-143), lower-order start-up.
 """
 from __future__ import annotations
 
@@ -33,6 +36,38 @@ SBDF = {1: ([1, -1], [0, 1]),
         2: ([1.5, -2, 0.5], [0, 2, -1]),
         3: ([11 / 6, -3, 1.5, -1 / 3], [0, 3, -3, 1]),
         4: ([25 / 12, -4, 3, -4 / 3, 0.25], [0, 4, -6, 4, -1])}
+
+# CN family (a in units of 1/dt, b, c), schemes.py:91-103 (Wang & Ruuth 2008)
+CN = {"CNAB1": ([1.0, -1.0], [0.5, 0.5], [0.0, 1.0]),
+      "CNAB2": ([1.0, -1.0, 0.0], [0.5, 0.5, 0.0], [0.0, 1.5, -0.5]),
+      "MCNAB2": ([1.0, -1.0, 0.0], [9 / 16, 6 / 16, 1 / 16], [0.0, 1.5, -0.5]),
+      "CNLF2": ([0.5, 0.0, -0.5], [0.5, 0.0, 0.5], [0.0, 1.0, 0.0])}
+
+
+def _rk_tables():
+    """IMEX Runge-Kutta tableaux (A, H, c) in cumulative form, schemes.py:106-143."""
+    g = (2 - np.sqrt(2)) / 2
+    d = 1 - 1 / g / 2
+    al, be = (29 / 96, -3 / 40, 1 / 6), (37 / 160, 5 / 24, 1 / 6)
+    ga, ze = (8 / 15, 5 / 12, 3 / 4), (-17 / 60, -5 / 12)
+    return {
+        "RK111": ([[0, 0], [1, 0]], [[0, 0], [0, 1]], [0, 1]),
+        "RK222": ([[0, 0, 0], [g, 0, 0], [d, 1 - d, 0]], [[0, 0, 0], [0, g, 0], [0, 1 - g, g]], [0, g, 1]),
+        "RK443": ([[0, 0, 0, 0, 0], [1 / 2, 0, 0, 0, 0], [11 / 18, 1 / 18, 0, 0, 0],
+                   [5 / 6, -5 / 6, 1 / 2, 0, 0], [1 / 4, 7 / 4, 3 / 4, -7 / 4, 0]],
+                  [[0, 0, 0, 0, 0], [0, 1 / 2, 0, 0, 0], [0, 1 / 6, 1 / 2, 0, 0],
+                   [0, -1 / 2, 1 / 2, 1 / 2, 0], [0, 3 / 2, -3 / 2, 1 / 2, 1 / 2]],
+                  [0, 1 / 2, 2 / 3, 1 / 2, 1]),
+        "RKSMR": ([[0, 0, 0, 0], [ga[0], 0, 0, 0], [ga[0] + ze[0], ga[1], 0, 0],
+                   [ga[0] + ze[0], ga[1] + ze[1], ga[2], 0]],
+                  [[0, 0, 0, 0], [al[0], be[0], 0, 0], [al[0], be[0] + al[1], be[1], 0],
+                   [al[0], be[0] + al[1], be[1] + al[2], be[2]]], [0, 8 / 15, 2 / 3, 1]),
+        "RKGFY": ([[0, 0, 0], [1, 0, 0], [1 / 2, 1 / 2, 0]], [[0, 0, 0], [1 / 2, 1 / 2, 0], [1 / 2, 0, 1 / 2]],
+                  [0, 1, 1]),
+    }
+
+
+RK = _rk_tables()
 
 
 # ------------------------------------------------------------------------------------------------
@@ -342,16 +377,22 @@ class OracleProblem:
             self._factors[key] = self.P.values(bi, which)
         return self._factors[key]
 
-    def MX(self, C):
+    def _apply(self, C, which):
         out = []
         for bi, b in enumerate(self.tpl.buckets):
-            V = self._vals(bi, "M")
+            V = self._vals(bi, which)
             rows = b.coo_rows()
             Y = np.zeros_like(C[bi])
             for m in range(C[bi].shape[0]):
                 np.add.at(Y[m], rows, V[m] * C[bi][m, b.indices])
             out.append(Y)
         return out
+
+    def MX(self, C):
+        return self._apply(C, "M")
+
+    def LX(self, C):
+        return self._apply(C, "L")
 
     def factor(self, a, b_):
         key = ("lu", float(a), float(b_))
@@ -404,6 +445,75 @@ class SBDFStepper:
                 r += c[j] * self.Fh[j - 1][bi] - (a[j] / dt) * self.MXh[j - 1][bi]
             rhs.append(r)
         return op.solve(a[0] / dt, 1.0, rhs)
+
+
+class CNStepper:
+    """``IVPSolver`` CN-family multistep stepping (integrator.py:567-603): history of M X, L X and
+    F; rhs = sum_{j>=1} c_j F_j - (a_j/dt) M X_j - b_j L X_j accumulated from zero in that order
+    (zero coefficients skipped); (a_0/dt M + b_0 L) X = rhs; CNAB1 until the history is full."""
+
+    def __init__(self, oproblem, scheme, dt):
+        self.op, self.dt = oproblem, float(dt)
+        self.coefs = CN[scheme]
+        self.nhist = len(self.coefs[0]) - 1
+        self.MXh, self.LXh, self.Fh = deque(), deque(), deque()
+
+    def step(self, C):
+        op, dt = self.op, self.dt
+        self.MXh.appendleft(op.MX(C))
+        self.LXh.appendleft(op.LX(C))
+        self.Fh.appendleft(op.F(C))
+        while len(self.MXh) > self.nhist:
+            self.MXh.pop()
+            self.LXh.pop()
+            self.Fh.pop()
+        a, b, c = self.coefs if len(self.MXh) >= self.nhist else CN["CNAB1"]
+        rhs = []
+        for bi in range(len(C)):
+            r = np.zeros_like(C[bi])
+            for j in range(1, len(a)):
+                if c[j] != 0:
+                    r = r + c[j] * self.Fh[j - 1][bi]
+                if a[j] != 0:
+                    r = r - (a[j] / dt) * self.MXh[j - 1][bi]
+                if b[j] != 0:
+                    r = r - b[j] * self.LXh[j - 1][bi]
+            rhs.append(r)
+        return op.solve(a[0] / dt, b[0], rhs)
+
+
+class RKStepper:
+    """``IVPSolver`` IMEX Runge-Kutta step (integrator.py:605-646): M X_i = M X_0 + dt sum_k A_ik
+    F_k - dt sum_k H_ik L X_k, the terms added in order k = 0.., F before L X;
+    (M + dt H_ii L) X_i = rhs."""
+
+    def __init__(self, oproblem, scheme, dt):
+        self.op, self.dt = oproblem, float(dt)
+        self.A, self.H, self.c = RK[scheme]
+
+    def step(self, C):
+        op, dt, A, H = self.op, self.dt, self.A, self.H
+        S = len(self.c) - 1
+        X = [C]
+        Fs, LX = [None] * (S + 1), [None] * (S + 1)
+        MX0 = op.MX(C)
+        for i in range(1, S + 1):
+            j = i - 1
+            if any(A[m][j] != 0 for m in range(j + 1, S + 1)):
+                Fs[j] = op.F(X[j])
+            if any(H[m][j] != 0 for m in range(j + 1, S + 1)):
+                LX[j] = op.LX(X[j])
+            rhs = []
+            for bi in range(len(C)):
+                r = MX0[bi].copy()
+                for k in range(i):
+                    if A[i][k] != 0:
+                        r = r + (dt * A[i][k]) * Fs[k][bi]
+                    if H[i][k] != 0:
+                        r = r - (dt * H[i][k]) * LX[k][bi]
+                rhs.append(r)
+            X.append(op.solve(1.0, dt * H[i][i], rhs))
+        return X[-1]
 
 
 class SampledStepper:

@@ -207,6 +207,62 @@ def step_fixtures(cn, out_dir, rng):
         print(name, "N_u", s.system.n, "history", len(MXh))
 
 
+SCHEME_CASES = {
+    # case -> (model, build kwargs (without the scheme), parameters, schemes)
+    "rb32x16": ("rayleigh_benard", dict(N=(32, 16), dt=1e-4), dict(Ra=1e6, Pr=1.0),
+                ("RK443", "RK222", "CNAB2", "MCNAB2", "CNLF2")),
+    "burgers128": ("burgers", dict(N=128, dt=1e-4), {}, ("RK111", "RKSMR", "RKGFY", "CNAB1")),
+    "channel8x17x8": ("channel", dict(N=(8, 17, 8), dt=5e-3), dict(Re=4000.0), ("RK443", "CNAB2")),
+}
+
+
+def scheme_fixtures(cn, out_dir, rng, steps=3):
+    """Scheme fixtures (``scheme_<case>_<scheme>.npz``): the reference's IVPSolver with an IMEX
+    Runge-Kutta or CN-family scheme (start-up ``lower_order``) from a seeded smooth state: X_0 and
+    the states after each of ``steps`` steps (reference real layout), the maps to the mode layout and
+    the reference's M, L values; ``Xs_perturbed``: the same steps from X_0 perturbed by about one
+    ulp (three seeds), the reference's own rounding floor."""
+    from conatus_gb300.reference_adapter import reference_maps, scatter_state, template_from_solver
+    for name, (fn, kw, params, schemes) in SCHEME_CASES.items():
+        for scheme in schemes:
+            sim = globals()[fn](cn, **params).simulate(complexify=True, f_backend="fused", scheme=scheme, **kw)
+            s = sim.solver
+            tpl = template_from_solver(s, name, params=params, exact_values=True)
+            maps = reference_maps(s)
+            P = tpl.instantiate()
+            C = []
+            for bi, b in enumerate(tpl.buckets):
+                n_idx = np.maximum(b.col[:, 2], 0)
+                amp = 0.05 * np.exp(-0.35 * n_idx)
+                z = rng.standard_normal((P.nsys[bi], b.n)) + (0 if b.kind == "real" else 1j) * rng.standard_normal((P.nsys[bi], b.n))
+                C.append(z * amp)
+            X0 = scatter_state(C, maps, s.system.n).astype(s.system.dtype)
+
+            def run(x0):
+                s.X = x0.copy()
+                s.t, s.iteration = 0.0, 0
+                s._reset_history()
+                out = []
+                for _ in range(steps):
+                    s.step()
+                    out.append(np.array(s.X))
+                return np.stack(out)
+
+            Xs = run(X0)
+            pert = np.stack([run(X0 * (1 + 2.0 ** -52 * rng.standard_normal(X0.shape))) for _ in range(3)])
+            arrays = dict(X0=X0, Xs=Xs, Xs_perturbed=pert, dt=kw["dt"], scheme=scheme, nb=len(maps))
+            for bi, m in enumerate(maps):
+                p = f"m{bi}_"
+                arrays[p + "cols"] = m["cols"].astype(np.int32)
+                arrays[p + "rows"] = m["rows"].astype(np.int32)
+                arrays[p + "wc"] = m["wc"]
+                arrays[p + "wr"] = m["wr"]
+                arrays[p + "dact"] = m["dact"]
+                arrays[p + "Mv"], arrays[p + "Lv"] = tpl.buckets[bi].exact
+            np.savez_compressed(os.path.join(out_dir, f"scheme_{name}_{scheme}.npz"), **arrays)
+            print(name, scheme, "N_u", s.system.n)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -218,6 +274,8 @@ def main():
         banded_fixtures(cn, HERE, rng)
     if args.only in ("", "step"):
         step_fixtures(cn, HERE, np.random.default_rng(7))
+    if args.only in ("", "scheme"):
+        scheme_fixtures(cn, HERE, np.random.default_rng(11))
 
 
 if __name__ == "__main__":

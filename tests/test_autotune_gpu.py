@@ -30,9 +30,10 @@ def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
     dev.solve(a, b, rhs, ref)
     torch.cuda.synchronize()
     ref_h = ref.cpu().numpy()
-    # schedules differ in the order of their sums: they agree to the conditioning of the systems,
-    # and each one's FP64 residual b - A x is at rounding level
-    tol = 1e-10 if precision == "fp64" else 1e-9
+    # the compact schedules share their arithmetic (only the staging differs); the band kernel sums
+    # in another order: FP64 solutions agree to the conditioning of the systems, and the FP32 form
+    # (one refinement step) to its own error, about (cond eps32)^2
+    tol = 1e-10 if precision == "fp64" else 1e-5
     r = dev.zeros()
     for sched in autotune.schedules():
         out = dev.zeros()
@@ -43,7 +44,9 @@ def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
         err = np.linalg.norm(out.cpu().numpy() - ref_h) / np.linalg.norm(ref_h)
         res = float(torch.linalg.vector_norm(r).item() / torch.linalg.vector_norm(rhs).item())
         assert err < tol, (sched, err)
-        assert res < (1e-12 if precision == "fp64" else 1e-10), (sched, res)
+        assert res < (1e-10 if precision == "fp64" else 1e-5), (sched, res)
+        if sched >= 0:                                   # same arithmetic as schedule 0
+            assert np.array_equal(out.cpu().numpy(), ref_h), sched
     times = autotune.tune_solve(dev, (a, b), fs, reps=2)
     assert set(times) == set(autotune.schedules())
     assert autotune.cache()[autotune._signature(dev, fs)][0] == min(times, key=times.get)
