@@ -145,7 +145,7 @@ TRAFFIC_PER_SYSTEM = {
 }
 
 
-def run_gpu(args):def run_gpu(args):
+def run_gpu(args):
     import torch
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
@@ -380,6 +380,72 @@ def run_ks_ensemble(args):
     print(json.dumps(out), flush=True)
 
 
+def run_rb_ensemble(args):
+    """The RB ensemble: ``--members`` 2D Rayleigh-Benard cases (default 1024), Nz uniform in {32, 48,
+    64}, Nx = 4 Nz, Ra log-uniform in [1e4, 1e7], Pr = 1, seeded noise 1e-3. The cases of one Nz are
+    stacked into one problem (one F pass and one solve launch for all of them per step); the three
+    groups run on their own streams, each step replayed as CUDA graphs. SBDF2 with one dt per group:
+    the advective limit of its largest Ra (a quarter of Lx/Nx over sqrt(Ra), at most 1e-4)."""
+    import math
+    import torch
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ivp import IVPSolver
+    from conatus_gb300.template import StackedProblem
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(0)
+    nzs = (32, 48, 64)
+    nz = rng.choice(nzs, args.members)
+    ra = 10 ** rng.uniform(4, 7, args.members)
+    lx = 2 * math.pi / 3.117
+    groups, info = [], []
+    for n in nzs:
+        idx = np.nonzero(nz == n)[0]
+        if idx.size == 0:
+            continue
+        tpl = W.load_template(f"rb_nz{n}_ra")
+        S = StackedProblem(tpl, [4 * n], [{"Ra": float(ra[i])} for i in idx])
+        states = [W.rayleigh_benard_state(tpl.instantiate([4 * n], None, {"Ra": float(ra[i])}), seed=int(i))
+                  for i in idx]
+        dt = min(1e-4, 0.25 * (lx / (4 * n)) / math.sqrt(float(ra[idx].max())))
+        sv = IVPSolver(S, scheme="SBDF2", dt=dt, precision=args.precision, factor_sets=1)
+        sv.set_state(S.stack_states(states))
+        groups.append(sv)
+        info.append({"Nz": n, "Nx": 4 * n, "cases": int(idx.size), "dt": dt, "systems": int(sum(S.nsys)),
+                     "real_unknowns": S.real_unknowns()})
+    for sv in groups:
+        sv.run_graph(max(args.warmup, 3), args.unroll)
+    torch.cuda.synchronize()
+    cur = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for sv in groups:
+        sv.join = False
+    with ClockSampler(0) as clk:
+        e0.record(cur)
+        for sv in groups:
+            sv.stream.wait_event(e0)
+            sv.run_graph(args.steps, args.unroll)
+        for sv in groups:
+            cur.wait_stream(sv.stream)
+        e1.record(cur)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    value = args.steps / (ms / 1e3)
+    finite = all(bool(torch.isfinite(torch.view_as_real(sv.X)).all().item()) for sv in groups)
+    nu = sum(g["real_unknowns"] for g in info)
+    out = {"metric": f"ensemble steps/s ({args.members} RB 2D cases, SBDF2)", "value": value, "unit": "steps/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+           "data": "synthetic (seeded Nz, Ra and initial noise)",
+           "config": {"workload": f"RB 2D ensemble, {args.members} cases, Nz in {{32, 48, 64}}, Nx = 4 Nz, "
+                                  "Ra log-uniform [1e4, 1e7]", "groups": info, "unroll": args.unroll,
+                      "state_finite": finite,
+                      "l2": "inputs larger than L2 (factors of every case)"},
+           "member_steps_per_s": value * args.members, "mode_updates_per_s": value * nu,
+           "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -412,7 +478,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="channel", choices=list(METRIC) + ["serving", "ks_ensemble"])
+    ap.add_argument("--config", default="channel", choices=list(METRIC) + ["serving", "ks_ensemble", "rb_ensemble"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--cpu-sample-systems", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -424,19 +490,21 @@ def main():
     ap.add_argument("--serve-steps", type=int, nargs=2, default=[1000, 20000], help="serving: step range")
     ap.add_argument("--chunk", type=int, default=500, help="serving: steps per scheduling chunk")
     ap.add_argument("--unroll", type=int, default=50, help="steps per CUDA graph (serving, ensemble)")
-    ap.add_argument("--members", type=int, default=4096, help="ks_ensemble: members")
+    ap.add_argument("--members", type=int, default=None, help="ensembles: members (KS 4096, RB 1024)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.members is None:
+        args.members = 1024 if args.config == "rb_ensemble" else 4096
     from conatus_gb300 import workloads as W
-    if args.config in ("serving", "ks_ensemble"):
+    if args.config in ("serving", "ks_ensemble", "rb_ensemble"):
         if args.impl == "reference":
             ws, rank, _ = _dist()
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": f"{args.config}: the reference has no "
                                   "GPU serving or ensemble path; its CPU step is timed on the channel"}))
             return
-        (run_serving if args.config == "serving" else run_ks_ensemble)(args)
+        {"serving": run_serving, "ks_ensemble": run_ks_ensemble, "rb_ensemble": run_rb_ensemble}[args.config](args)
         return
     args.cfg = W.CONFIGS[args.config]
     if args.impl == "reference":

@@ -330,6 +330,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
 
 struct RhsDev {
     int ndir, Kx, Nzc, Ny, nfactors, noutputs, nbuckets;
+    int ncase;                 // cases stacked in the work arrays (field index case nf + f)
     double lx, lz, ly;
     const int* factors;        // nfactors x 5: var, comp, ox, oy, oz
     const int* out_lam;        // noutputs: lambda (0: no conversion)
@@ -346,6 +347,7 @@ struct BucketDev {
     const int* modes;          // nsys x 2
     const int* colpos;         // nfactors x Ny
     const int* rowmap;         // n x 2: output index (-1: none), Chebyshev index
+    const int* case_of;        // nsys: case of each system (nullptr: case 0)
 };
 
 // Spectral slot of mode (jx, jz, sign) along the compact z axis.
@@ -413,6 +415,7 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     const double kz = b.sign * 6.283185307179586476925286766559 * jz / d.lz;
     const double w = b.dact == 0 ? 1.0 : (b.dact == 1 ? 0.5 : 0.25);
     const int slot = zslot(jz, b.sign, d.Nzc);
+    const int cbase = (b.case_of ? b.case_of[m] : 0) * d.nfactors;
     for (int f = 0; f < d.nfactors; ++f) {
         const int* fd = d.factors + 5 * f;
         const int ox = fd[2], oy = fd[3], oz = fd[4];
@@ -442,13 +445,14 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         for (int q = 0; q < oz; ++q) { double t = fr; fr = -fi * kz; fi = t * kz; }
         c2<R>* dst;
         c2<R>* dstc = nullptr;
+        const long long fc = cbase + f;
         if (d.ndir == 2) {
-            dst = S + (((long long)f * d.Kx + jx) * d.Nzc + slot) * Ny;
-            if (jx == 0 && jz > 0) dstc = S + (((long long)f * d.Kx) * d.Nzc + (d.Nzc - jz)) * Ny;
+            dst = S + ((fc * d.Kx + jx) * d.Nzc + slot) * Ny;
+            if (jx == 0 && jz > 0) dstc = S + ((fc * d.Kx) * d.Nzc + (d.Nzc - jz)) * Ny;
         } else if (d.ndir == 1) {
-            dst = S + ((long long)f * d.Kx + jx) * Ny;
+            dst = S + (fc * d.Kx + jx) * Ny;
         } else {
-            dst = S + (long long)f * Ny;
+            dst = S + fc * Ny;
         }
         // in the transform precision R (the FP32 form's factors are FP32 from here on)
         const R frR = R(fr), fiR = R(fi);
@@ -468,19 +472,23 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
 // each grid point's factors are shared by several monomials)
 template <class R>
 __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P;
-         p += (long long)gridDim.x * blockDim.x) {
+    const long long total = P * d.ncase;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long c = t / P, p = t - c * P;
+        const R* Gc = G + c * d.nfactors * P;
+        R* Oc = O + c * d.noutputs * P;
         for (int o = 0; o < d.noutputs; ++o) {
             R acc = R(0);
             for (int mi = d.out_mono_ptr[o]; mi < d.out_mono_ptr[o + 1]; ++mi) {
-                R t = R(d.mono_coef[mi]);
+                R t2 = R(d.mono_coef[mi]);
                 const int* fs = d.mono_fac + 4 * mi;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (fs[q] >= 0) t = t * __ldg(G + (long long)fs[q] * P + p);
-                acc = acc + t;
+                    if (fs[q] >= 0) t2 = t2 * __ldg(Gc + (long long)fs[q] * P + p);
+                acc = acc + t2;
             }
-            O[(long long)o * P + p] = acc;
+            Oc[(long long)o * P + p] = acc;
         }
     }
 }
@@ -497,14 +505,16 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
     const int slot = zslot(jz, b.sign, d.Nzc);
     const double sc = (double)(1 << b.dact);
     double2* dst = rows + b.offset + (long long)m * b.n;
+    const long long obase = (long long)(b.case_of ? b.case_of[m] : 0) * d.noutputs;
     for (int i = lane; i < b.n; i += 32) {
         const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
         double2 v = make_double2(0.0, 0.0);
         if (o >= 0) {
             const c2<R>* h;
-            if (d.ndir == 2) h = H + (((long long)o * d.Kx + jx) * d.Nzc + slot) * Ny;
-            else if (d.ndir == 1) h = H + ((long long)o * d.Kx + jx) * Ny;
-            else h = H + (long long)o * Ny;
+            const long long oc = obase + o;
+            if (d.ndir == 2) h = H + ((oc * d.Kx + jx) * d.Nzc + slot) * Ny;
+            else if (d.ndir == 1) h = H + (oc * d.Kx + jx) * Ny;
+            else h = H + oc * Ny;
             const int lam = d.out_lam[o];
             if (lam <= 0) {
                 v = make_double2((double)h[nn].x, (double)h[nn].y);
@@ -639,6 +649,7 @@ struct Rhs {
     int Kx = 1, Nzc = 1;
     double lx = 1, lz = 1, ly = 2;
     int nfactors = 0, noutputs = 0;
+    int ncase = 1;             // cases stacked along the field index
     RhsDev dev{};
     std::vector<BucketDev> buckets;
     std::vector<void*> owned;
@@ -668,7 +679,7 @@ struct Rhs {
 template <class R>
 void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     using C = c2<R>;
-    const int nf = nfactors, no = noutputs;
+    const int nf = nfactors * ncase, no = noutputs * ncase;     // fields of every case
     C* Sp = static_cast<C*>(S);
     // 1. unpack (one warp per system)
     for (const auto& b : buckets) {
@@ -713,7 +724,7 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     }
     {
         const int threads = 256;
-        const long long blocks = std::min<long long>((P + threads - 1) / threads, 152LL * 16);
+        const long long blocks = std::min<long long>((P * ncase + threads - 1) / threads, 152LL * 16);
         k_products<R><<<(unsigned)blocks, threads, 0, st>>>(dev, G, O, P);
         CNG_LAUNCH("k_products");
     }
@@ -782,6 +793,8 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     RhsDev& dv = h->dev;
     dv.ndir = h->ndir; dv.Kx = h->Kx; dv.Nzc = h->Nzc; dv.Ny = h->ny;
     dv.nfactors = h->nfactors; dv.noutputs = h->noutputs; dv.nbuckets = D->nbuckets;
+    h->ncase = D->ncase > 0 ? D->ncase : 1;
+    dv.ncase = h->ncase;
     dv.lx = h->lx; dv.lz = h->lz; dv.ly = h->ly;
     dv.factors = h->keep(upload(D->factors, (size_t)5 * h->nfactors));
     dv.out_lam = h->keep(upload(D->out_lam, (size_t)h->noutputs));
@@ -824,6 +837,13 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
         b.modes = h->keep(upload(D->modes[bi], (size_t)2 * b.nsys));
         b.colpos = h->keep(upload(D->colpos[bi], (size_t)h->nfactors * h->ny));
         b.rowmap = h->keep(upload(D->rowmap[bi], (size_t)2 * b.n));
+        b.case_of = nullptr;
+        if (h->ncase > 1) {
+            if (!D->case_of || !D->case_of[bi]) throw InvalidArgument("stacked cases: a case index per system");
+            for (int m = 0; m < b.nsys; ++m)
+                if (D->case_of[bi][m] < 0 || D->case_of[bi][m] >= h->ncase) throw InvalidArgument("case index out of range");
+            b.case_of = h->keep(upload(D->case_of[bi], (size_t)b.nsys));
+        }
         h->buckets.push_back(b);
     }
     h->nb0 = D->nb0;
@@ -834,11 +854,11 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     // work buffers
     const size_t cs = h->precision ? sizeof(float2) : sizeof(double2);
     const size_t rs = cs / 2;
-    const int nfo = std::max(h->nfactors, h->noutputs);
+    const int nfo = std::max(h->nfactors, h->noutputs) * h->ncase;
     const long long Kx = h->ndir >= 1 ? h->Kx : 1, Nzc = h->ndir == 2 ? h->Nzc : 1;
     const long long mx = h->ndir >= 1 ? h->mx : 1, mz = h->ndir == 2 ? h->mz : 1;
     const long long P = h->grid_points();
-    h->S_bytes = std::max<size_t>(cs * nfo * Kx * Nzc * h->ny, rs * h->nfactors * P);
+    h->S_bytes = std::max<size_t>(cs * nfo * Kx * Nzc * h->ny, rs * (size_t)h->nfactors * h->ncase * P);
     size_t w = 0;
     w = std::max<size_t>(w, cs * nfo * Kx * Nzc * h->my);
     w = std::max<size_t>(w, cs * nfo * Kx * mz * h->my);

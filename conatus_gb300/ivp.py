@@ -57,7 +57,8 @@ class RhsDesc(ctypes.Structure):
                 ("buckets", ctypes.c_void_p), ("bucket_offset", ctypes.c_void_p),
                 ("modes", ctypes.c_void_p), ("colpos", ctypes.c_void_p), ("rowmap", ctypes.c_void_p),
                 ("nlam", ctypes.c_int32), ("conv", ctypes.c_void_p), ("nb0", ctypes.c_int64),
-                ("b0_index", ctypes.c_void_p), ("b0_value", ctypes.c_void_p)]
+                ("b0_index", ctypes.c_void_p), ("b0_value", ctypes.c_void_p),
+                ("ncase", ctypes.c_int32), ("case_of", ctypes.c_void_p)]
 
 
 def _torch():
@@ -218,6 +219,12 @@ class DeviceProblem:
         ptrs = [(ctypes.c_void_p * nb)(*modes_p), (ctypes.c_void_p * nb)(*col_p), (ctypes.c_void_p * nb)(*row_p)]
         keep.extend(ptrs)
         desc.modes, desc.colpos, desc.rowmap = (ctypes.cast(p, ctypes.c_void_p).value for p in ptrs)
+        ncase = int(getattr(P, "ncase", 1))
+        desc.ncase = ncase
+        if ncase > 1:                      # stacked cases: the case of every system
+            cp_ = (ctypes.c_void_p * nb)(*[arr(P.case_of[bi], np.int32) for bi in range(nb)])
+            keep.append(cp_)
+            desc.case_of = ctypes.cast(cp_, ctypes.c_void_p).value
         # conversions T -> C^(lambda) for lambda = 1..max (levels no row uses: identity, unused)
         nlam = max(tpl.conv) if tpl.conv else 0
         desc.nlam = nlam
@@ -313,26 +320,30 @@ class DeviceProblem:
             b = self.tpl.buckets[bi]
             split = None
             if b.exact is None and b.m_is_constant():
-                split = self._split_operator(b)
+                terms = self.P.split_terms(bi) if hasattr(self.P, "split_terms") else \
+                    [(b.Lc[t], self.P.mono_values(bi)[:, t]) for t in range(b.monos.shape[0])
+                     if np.any(b.Lc[t] != 0)]
+                split = self._split_operator(b, [c for c, _ in terms])
             if split is None:
                 self._resid[bi] = ("values", {})
             else:
                 ptr, col, val, code, act = split
-                mv = self.P.mono_values(bi)[:, act] if act else np.zeros((self.nsys[bi], 1))
+                mv = np.stack([terms[k][1] for k in act], axis=1) if act else np.zeros((self.nsys[bi], 1))
                 dv = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt), device=self.device)
                 self._resid[bi] = ("split", (dv(ptr, np.int32), dv(col, np.int32), dv(val, np.float64),
                                              dv(code, np.int8), dv(mv, np.float64), len(act)))
         return self._resid[bi]
 
     @staticmethod
-    def _split_operator(b):
-        """Row lists (ptr, col, val, code, active monomials) of M and the L_t, or None when some
-        coefficient is neither purely real nor purely imaginary."""
+    def _split_operator(b, lrows):
+        """Row lists (ptr, col, val, code, active terms) of M and the terms of L (coefficient rows
+        ``lrows``, each scaled per system), or None when some coefficient is neither purely real nor
+        purely imaginary."""
         t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
-        act = [t for t in range(b.monos.shape[0]) if np.any(b.Lc[t] != 0)]
+        act = [t for t in range(len(lrows)) if np.any(lrows[t] != 0)]
         rows = b.coo_rows()
         ent = [[] for _ in range(b.n)]
-        terms = [(-1, b.Mc[t0])] + [(k, b.Lc[t]) for k, t in enumerate(act)]
+        terms = [(-1, b.Mc[t0])] + [(k, lrows[t]) for k, t in enumerate(act)]
         for k, C in terms:
             nz = np.nonzero(C)[0]
             for p in nz:

@@ -78,7 +78,8 @@ def _rhs_bytes(problem, precision):
         mz = smooth_size(int(math.floor(problem.fourier_sizes[1] * ax[tpl.fourier_axes[1]].get("dealias", 1.5))))
     else:
         Nzc = mz = 1
-    nf, no = len(tpl.factors), len(tpl.outputs)
+    nc = int(getattr(problem, "ncase", 1))          # stacked cases: fields of every case
+    nf, no = len(tpl.factors) * nc, len(tpl.outputs) * nc
     nfo = max(nf, no)
     P = mx * mz * my
     S = max(cs * nfo * Kx * Nzc * ny, rs * nf * P)

@@ -287,3 +287,102 @@ class Problem:
             if hit.size:
                 out[bi][hit[0], pos] += v
         return out
+
+
+class StackedProblem:
+    """Cases of one template at one Fourier resolution, advanced as one problem (an ensemble):
+    every bucket holds the systems of all cases (case-major), the F pipeline runs over every case in
+    one pass (a case index per system), the solves over every system in one launch. The cases
+    differ in the values of the template's linear parameters (L = L0 + sum_p theta_p dL_p, e.g. Ra
+    for Rayleigh-Benard): their M, sparsity patterns, F and wavenumbers are the same.
+
+    The reference runs ensemble members as separate batched solves of one discretization
+    (python/conatus/ensembles/batched.py:442-613)."""
+
+    def __init__(self, tpl: ProblemTemplate, fourier_sizes, params_list, lengths=None):
+        if not params_list:
+            raise ValueError("at least one case")
+        names = set(params_list[0])
+        for pr in params_list:
+            if set(pr) != names or not names <= set(tpl.linear_params):
+                raise ValueError(f"every case sets the same linear parameters of {tpl.name} "
+                                 f"({tpl.linear_params})")
+        self.base_tpl = tpl
+        self.params = [dict(pr) for pr in params_list]
+        self.ncase = len(params_list)
+        first = Problem(tpl, fourier_sizes, lengths, params_list[0])
+        self.tpl = first.tpl
+        self.fourier_sizes, self.K, self.lengths = first.fourier_sizes, first.K, first.lengths
+        nb = len(tpl.buckets)
+        self._nsys_case = first.nsys
+        self.modes = [np.concatenate([first.modes[bi]] * self.ncase) for bi in range(nb)]
+        self.wavenumbers = [np.concatenate([first.wavenumbers[bi]] * self.ncase) for bi in range(nb)]
+        self.case_of = [np.repeat(np.arange(self.ncase, dtype=np.int32), first.nsys[bi]) for bi in range(nb)]
+        self._first = first
+        self.offsets, off = [], 0
+        for bi, b in enumerate(tpl.buckets):
+            self.offsets.append(off)
+            off += self.modes[bi].shape[0] * b.n
+        self.n_total = off
+
+    def axis_length(self, ax: int) -> float:
+        return self._first.axis_length(ax)
+
+    @property
+    def nsys(self):
+        return [m.shape[0] for m in self.modes]
+
+    def mono_values(self, bi: int) -> np.ndarray:
+        return np.concatenate([self._first.mono_values(bi)] * self.ncase)
+
+    def _theta(self, name):
+        return np.array([pr[name] for pr in self.params], dtype=np.float64)
+
+    def values(self, bi: int, which: str) -> np.ndarray:
+        b0 = self.base_tpl.buckets[bi]
+        mv = self._first.mono_values(bi).astype(np.complex128)
+        if which == "M":
+            return np.concatenate([mv @ b0.Mc] * self.ncase)
+        base = mv @ b0.Lc
+        out = np.empty((self.ncase * base.shape[0], base.shape[1]), np.complex128)
+        ns = base.shape[0]
+        for c, pr in enumerate(self.params):
+            v = base.copy()
+            for name, th in pr.items():
+                v = v + float(th) * (mv @ b0.dL[name])
+            out[c * ns:(c + 1) * ns] = v
+        return out
+
+    def split_terms(self, bi: int):
+        """Terms of L for the refinement residual: (coefficient row, per-system scale) -- the base
+        rows L0_t with the monomial values, and the parameter rows dL_{p,t} with the monomial values
+        times each system's theta_p."""
+        b0 = self.base_tpl.buckets[bi]
+        mv = self.mono_values(bi)
+        out = []
+        for t in range(b0.monos.shape[0]):
+            if np.any(b0.Lc[t] != 0):
+                out.append((b0.Lc[t], mv[:, t]))
+        for name in self.params[0]:
+            th = np.repeat(self._theta(name), self._nsys_case[bi])
+            for t in range(b0.monos.shape[0]):
+                if np.any(b0.dL[name][t] != 0):
+                    out.append((b0.dL[name][t], mv[:, t] * th))
+        return out
+
+    def d_active(self, bi: int) -> int:
+        return self._first.d_active(bi)
+
+    def real_unknowns(self) -> int:
+        return self._first.real_unknowns() * self.ncase
+
+    def b0_dense(self):
+        return [np.concatenate([x] * self.ncase) for x in self._first.b0_dense()]
+
+    def case_state(self, C, c: int):
+        """The mode-layout arrays of case ``c`` out of the stacked per-bucket arrays."""
+        return [np.asarray(C[bi])[c * ns:(c + 1) * ns] for bi, ns in enumerate(self._nsys_case)]
+
+    def stack_states(self, states):
+        """Per-bucket stacked arrays from the cases' mode-layout states."""
+        return [np.concatenate([st[bi] for st in states]) for bi in range(len(self._nsys_case))]

@@ -175,6 +175,12 @@ typedef struct {
     int64_t nb0;
     const int64_t* b0_index;
     const double* b0_value;
+    /* stacked cases (an ensemble of one template at one resolution): ncase (0 or 1: a single
+     * problem) and per bucket the case of each system (nsys int32); the work arrays hold the
+     * factors and outputs of every case (field index case * nfactors + f). No counterpart in the
+     * reference, which runs ensemble members as separate solves (ensembles/batched.py:442-613). */
+    int32_t ncase;
+    const int32_t* const* case_of;
 } cng_rhs_desc;
 
 /* Build the F evaluator (allocates its work buffers). Replaces the reference's compiled F
