@@ -800,6 +800,78 @@ class IVPSolver:
         self.stream.synchronize()
         self._leave()
 
+    # ------------------------------------------------------------------ checkpoints
+    def checkpoint_payload(self):
+        """(meta, host arrays) of a restart: the state, the multistep history (newest first: M X,
+        F and, CN family, L X) and the clock, as the reference's ``_checkpoint_payload``
+        (python/conatus/timestep/integrator.py:974-1007), on the mode layout."""
+        self.stream.synchronize()
+        meta = dict(scheme=self.scheme, dt=self.dt, startup="lower_order", n=int(self.dev.n_total),
+                    iteration=int(self.iteration), t=float(self.t), nhist=int(self.filled),
+                    nhist_LX=int(self.filled) if self.family == "cn" else 0,
+                    problem=self.dev.tpl.name, precision=self.dev.precision,
+                    layout="mode", fourier_sizes=list(self.dev.P.fourier_sizes))
+        h = lambda a: a.detach().cpu().numpy()
+        arrays = {"X": h(self.X)}
+        for j in range(self.filled if self.family != "rk" else 0):
+            slot = (self.head - j) % self.ring
+            arrays[f"MX{j}"] = h(self.MXh[slot])
+            arrays[f"F{j}"] = h(self.Fh[slot])
+            if self.family == "cn":
+                arrays[f"LX{j}"] = -h(self.LXh[slot])          # stored negated on the device
+        return meta, arrays
+
+    def save_checkpoint(self, path) -> str:
+        """State + multistep history + clock as ``.npz`` (written to a temporary file, then
+        renamed): a restart continues bit for bit. The reference's npz layout (integrator.py:
+        1009-1036: ``meta`` JSON, ``X``, ``MX<i>``, ``F<i>``, ``LX<i>``), on the mode layout."""
+        import json
+        import os
+        path = str(path)
+        if not path.endswith(".npz"):
+            path += ".npz"
+        meta, arrays = self.checkpoint_payload()
+        for k, a in arrays.items():
+            if not np.all(np.isfinite(a)):
+                raise ValueError(f"save_checkpoint: {k} holds NaN or infinity")
+        part = path[:-4] + ".part.npz"
+        np.savez(part, meta=json.dumps(meta), **arrays)
+        os.replace(part, path)
+        return path
+
+    def load_checkpoint(self, path) -> None:
+        """Restart from :meth:`save_checkpoint`: the numerical options must match the solver's
+        (integrator.py:1038-1097: a restart never changes the numerics silently)."""
+        import json
+        path = str(path)
+        with np.load(path, allow_pickle=False) as z:
+            arrays = {k: z[k] for k in z.files}
+        meta = json.loads(str(arrays.pop("meta")))
+        mine = dict(scheme=self.scheme, dt=self.dt, n=int(self.dev.n_total), problem=self.dev.tpl.name,
+                    layout="mode", fourier_sizes=list(self.dev.P.fourier_sizes))
+        for k, v in mine.items():
+            if meta.get(k) != v:
+                raise ValueError(f"checkpoint mismatch on {k}: {meta.get(k)!r} vs {v!r} (a restart "
+                                 "never changes the numerics silently)")
+        nh = int(meta["nhist"])
+        if self.family == "rk":
+            nh = 0
+        if nh > self.ring or arrays["X"].shape != (self.dev.n_total,):
+            raise ValueError("checkpoint: state or history does not match the solver")
+        torch = _torch()
+        dev = self.X.device
+        self.stream.synchronize()
+        self.X.copy_(torch.as_tensor(arrays["X"], device=dev))
+        self.head, self.filled = self.ring - 1, nh
+        for j in range(nh):
+            slot = (self.head - j) % self.ring
+            self.MXh[slot].copy_(torch.as_tensor(arrays[f"MX{j}"], device=dev))
+            self.Fh[slot].copy_(torch.as_tensor(arrays[f"F{j}"], device=dev))
+            if self.family == "cn":
+                self.LXh[slot].copy_(-torch.as_tensor(arrays[f"LX{j}"], device=dev))
+        self.t, self.iteration = float(meta["t"]), int(meta["iteration"])
+        torch.cuda.current_stream().synchronize()
+
     def state_to_host(self):
         self.stream.synchronize()
         return self.dev.to_host(self.X)
