@@ -173,38 +173,47 @@ __device__ c2<R>* smem_fft(c2<R>* buf0, c2<R>* buf1, const FftPlan& p, int B, co
     return a;
 }
 
-// ---- compile-time plans: the same Stockham stages with L, Ns and the radix known at compile time
+// ---- compile-time plans: the same Stockham stages with L, Ns and the radix known at compile time.
+// A thread takes one butterfly position j and a group g of the B sequences: the twiddles and the
+// index arithmetic of j are computed once and reused for the sequences g, g + G, ... (G = number
+// of groups), which keeps the integer work per butterfly low (the FP32 transforms were bound by it).
 template <class R, int L, int Ns, int RAD>
 __device__ __forceinline__ void stage_ct(const c2<R>* __restrict__ a, c2<R>* __restrict__ b, int B,
                                          const c2<R>* tw, int sign, int LS) {
     constexpr int Lr = L / RAD;
     constexpr int tstep = L / (Ns * RAD);
-    const int total = B * Lr;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        const int bt = idx / Lr;
-        const int j = idx - bt * Lr;
+    const int nt = blockDim.x;
+    const int G = nt >= Lr ? nt / Lr : 1;
+    for (int q = threadIdx.x; q < Lr * G; q += nt) {
+        const int j = q % Lr, g = q / Lr;
         const int k = j % Ns;
-        const c2<R>* ab = a + bt * LS;
-        c2<R>* bb = b + bt * LS;
-        c2<R> v[RAD];
-#pragma unroll
-        for (int t = 0; t < RAD; ++t) v[t] = ab[j + t * Lr];
+        const int d = (j / Ns) * Ns * RAD + k;
+        c2<R> w[RAD];
         if (Ns > 1) {
 #pragma unroll
             for (int t = 1; t < RAD; ++t) {
-                c2<R> w = tw[t * k * tstep];
-                if (sign > 0) w.y = -w.y;
-                v[t] = mul<R>(v[t], w);
+                w[t] = tw[t * k * tstep];
+                if (sign > 0) w[t].y = -w[t].y;
             }
         }
-        if constexpr (RAD == 2) dft2<R>(v);
-        else if constexpr (RAD == 3) dft3<R>(v, sign);
-        else if constexpr (RAD == 4) dft4<R>(v, sign);
-        else if constexpr (RAD == 5) dft5<R>(v, sign);
-        else dft8<R>(v, sign);
-        const int d = (j / Ns) * Ns * RAD + k;
+        for (int bt = g; bt < B; bt += G) {
+            const c2<R>* ab = a + bt * LS + j;
+            c2<R>* bb = b + bt * LS + d;
+            c2<R> v[RAD];
 #pragma unroll
-        for (int t = 0; t < RAD; ++t) bb[d + t * Ns] = v[t];
+            for (int t = 0; t < RAD; ++t) v[t] = ab[t * Lr];
+            if (Ns > 1) {
+#pragma unroll
+                for (int t = 1; t < RAD; ++t) v[t] = mul<R>(v[t], w[t]);
+            }
+            if constexpr (RAD == 2) dft2<R>(v);
+            else if constexpr (RAD == 3) dft3<R>(v, sign);
+            else if constexpr (RAD == 4) dft4<R>(v, sign);
+            else if constexpr (RAD == 5) dft5<R>(v, sign);
+            else dft8<R>(v, sign);
+#pragma unroll
+            for (int t = 0; t < RAD; ++t) bb[t * Ns] = v[t];
+        }
     }
 }
 

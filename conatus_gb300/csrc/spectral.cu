@@ -36,6 +36,15 @@ namespace cng {
 static constexpr int kFftThreads = 256;
 static constexpr size_t kFftSmemMax = 200 * 1024;
 
+// Division by a divisor uniform over the kernel (sizes of the staging loops): q = e / d through
+// a multiply-high with m = ceil(2^32 / d), exact for e d < 2^32 (e, d below 2^16 here); the runtime
+// integer division it replaces was the largest item of the FP32 transforms' integer work.
+struct FastDiv {
+    unsigned d, m;
+    __device__ __forceinline__ explicit FastDiv(int d_) : d((unsigned)d_), m(d_ <= 1 ? 0u : 0xFFFFFFFFu / (unsigned)d_ + 1u) {}
+    __device__ __forceinline__ int div(int e) const { return d <= 1 ? e : (int)__umulhi((unsigned)e, m); }
+};
+
 FftPlan make_plan(int L) {
     FftPlan p;
     p.L = L;
@@ -103,13 +112,14 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* b1 = b0 + (size_t)B * M;
     c2<R>* a = b1 + (size_t)B * M;     // staging of the coefficients (B x (M + 1))
     const int tid = threadIdx.x, nt = blockDim.x;
+    const FastDiv dM(M), dM1(M + 1);
     for (int q = tid; q < M; q += nt) {
         tw[q] = tw_g[q];
         tq[q] = tq_g[q];
     }
     const long long col0 = (long long)blockIdx.x * B;
     for (int e = tid; e < B * (M + 1); e += nt) {
-        const int t = e / (M + 1), k = e - t * (M + 1);
+        const int t = dM1.div(e), k = e - t * (M + 1);
         const long long col = col0 + t;
         c2<R> v = mk<R>(0, 0);
         if (col < ncols && k < N) {
@@ -121,7 +131,7 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     __syncthreads();
     // Z_k = 1/2 e^{i pi k / (2M)} (a_k - i a_{M-k}), Z_0 = a_0
     for (int e = tid; e < B * M; e += nt) {
-        const int t = e / M, k = e - t * M;
+        const int t = dM.div(e), k = e - t * M;
         const c2<R>* at = a + (size_t)t * (M + 1);
         c2<R> z;
         if (k == 0) {
@@ -137,7 +147,7 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, +1, M);
     // f_{2j} = z_j, f_{2j+1} = z_{M-1-j}
     for (int e = tid; e < B * M; e += nt) {
-        const int t = e / M, j = e - t * M;
+        const int t = dM.div(e), j = e - t * M;
         const long long col = col0 + t;
         if (col >= ncols) continue;
         const int src = (j & 1) ? (M - 1 - (j >> 1)) : (j >> 1);
@@ -157,6 +167,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* b0 = tq + M;
     c2<R>* b1 = b0 + (size_t)B * M;
     const int tid = threadIdx.x, nt = blockDim.x;
+    const FastDiv dM(M), dN(N);
     for (int q = tid; q < M; q += nt) {
         tw[q] = tw_g[q];
         tq[q] = tq_g[q];
@@ -164,7 +175,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     const long long col0 = (long long)blockIdx.x * B;
     // v_j = f_{2j}, v_{M-1-j} = f_{2j+1}
     for (int e = tid; e < B * M; e += nt) {
-        const int t = e / M, i = e - t * M;
+        const int t = dM.div(e), i = e - t * M;
         const long long col = col0 + t;
         c2<R> v = mk<R>(0, 0);
         if (col < ncols) v = in[col * M + i];
@@ -175,7 +186,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, M);
     const R invM = R(1) / R(M);
     for (int e = tid; e < B * N; e += nt) {
-        const int t = e / N, k = e - t * N;
+        const int t = dN.div(e), k = e - t * N;
         const long long col = col0 + t;
         if (col >= ncols) continue;
         const c2<R>* Zt = Z + (size_t)t * M;
@@ -202,6 +213,7 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* b0 = tw + L;
     c2<R>* b1 = b0 + (size_t)B * LS;
     const int tid = threadIdx.x, nt = blockDim.x;
+    const FastDiv dB(B);
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int chunks = (inner + B - 1) / B;
     const long long o = blockIdx.x / chunks;
@@ -215,14 +227,14 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
         __syncthreads();
         for (int e = tid; e < B * Nc; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             if (i0 + t >= inner || k == K) continue;
             const int slot = k < K ? k : L - (Nc - k);
             b0[(size_t)t * LS + slot] = src[(long long)k * inner + i0 + t];
         }
     } else {
         for (int e = tid; e < B * L; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             b0[(size_t)t * LS + k] = (i0 + t < inner) ? src[(long long)k * inner + i0 + t] : mk<R>(0, 0);
         }
     }
@@ -230,13 +242,13 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, forward ? -1 : +1, LS);
     if (!forward) {
         for (int e = tid; e < B * L; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             if (i0 + t < inner) dst[(long long)k * inner + i0 + t] = r[(size_t)t * LS + k];
         }
     } else {
         const R invL = R(1) / R(L);
         for (int e = tid; e < B * Nc; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             if (i0 + t >= inner) continue;
             c2<R> v = mk<R>(0, 0);
             if (k != K) v = scl<R>(invL, r[(size_t)t * LS + (k < K ? k : L - (Nc - k))]);
@@ -258,6 +270,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     c2<R>* b0 = tw + L;
     c2<R>* b1 = b0 + (size_t)B * LS;
     const int tid = threadIdx.x, nt = blockDim.x;
+    const FastDiv dB(B);
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int pairs = (inner + 1) / 2;             // an odd last column is paired with zero
     const int chunks = (pairs + B - 1) / B;
@@ -270,7 +283,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
         __syncthreads();
         // Z_k = A_k + i B_k, Z_{L-k} = conj(A_k) + i conj(B_k)
         for (int e = tid; e < B * K; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             const int p = p0 + t;
             if (p >= pairs) continue;
             c2<R> A = src[(long long)k * inner + 2 * p];
@@ -285,7 +298,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
         __syncthreads();
         c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, +1, LS);
         for (int e = tid; e < B * L; e += nt) {
-            const int j = e / B, t = e - j * B;
+            const int j = dB.div(e), t = e - j * B;
             const int p = p0 + t;
             if (p >= pairs) continue;
             c2<R> z = r[(size_t)t * LS + j];
@@ -297,7 +310,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
         const R* src = static_cast<const R*>(in_) + o * (long long)L * inner;
         c2<R>* dst = static_cast<c2<R>*>(out_) + o * (long long)K * inner;
         for (int e = tid; e < B * L; e += nt) {
-            const int j = e / B, t = e - j * B;
+            const int j = dB.div(e), t = e - j * B;
             const int p = p0 + t;
             c2<R> z = mk<R>(0, 0);
             if (p < pairs) {
@@ -310,7 +323,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
         c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, LS);
         const R h = R(0.5) / R(L);
         for (int e = tid; e < B * K; e += nt) {
-            const int k = e / B, t = e - k * B;
+            const int k = dB.div(e), t = e - k * B;
             const int p = p0 + t;
             if (p >= pairs) continue;
             c2<R> zk = Z[(size_t)t * LS + k];
@@ -519,14 +532,16 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
             if (lam <= 0) {
                 v = make_double2((double)h[nn].x, (double)h[nn].y);
             } else {
+                // the C^(lambda) conversion in the transform precision R
                 const double* cv = d.conv + (size_t)(lam - 1) * Ny * Ny + (size_t)nn * Ny;
                 const int hi = min(Ny - 1, nn + d.conv_bw[lam - 1]);
-                double ar = 0.0, ai = 0.0;
+                R ar = R(0), ai = R(0);
                 for (int k = nn; k <= hi; ++k) {
-                    ar += cv[k] * (double)h[k].x;
-                    ai += cv[k] * (double)h[k].y;
+                    const R c = R(cv[k]);
+                    ar += c * h[k].x;
+                    ai += c * h[k].y;
                 }
-                v = make_double2(ar, ai);
+                v = make_double2((double)ar, (double)ai);
             }
             v.x *= sc;
             v.y *= sc;
