@@ -1573,12 +1573,17 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             const int* Pc = Pb + (size_t)(c % ST) * CH * kGroup;
             const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
             const int base = s_offL[j0];
-            for (int j = j0; j < j1; ++j) {
-                const int l = Pc[(j - j0) * kGroup + g];
+            int e1 = base;
+#pragma unroll
+            for (int jj = 0; jj < CH; ++jj) {
+                const int j = j0 + jj;
+                if (j >= j1) break;
+                const int l = Pc[jj * kGroup + g];
                 const TF bj = y[l];
                 const TF yj0 = y[j];
+                const int e0 = e1;
+                e1 = s_offL[j + 1];
                 __syncwarp();
-                const int e0 = s_offL[j], e1 = s_offL[j + 1];
                 for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j + 1 + s_Lrow[e];
                     const TF v = (i == l) ? yj0 : y[i];
@@ -1611,9 +1616,14 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * kGroup;
             const int s0 = c * CH, s1 = min(s0 + CH, n);
             const int base = s_offU[s0];
-            for (int s = s0; s < s1; ++s) {
+            int e1 = base;
+#pragma unroll
+            for (int ss = 0; ss < CH; ++ss) {
+                const int s = s0 + ss;
+                if (s >= s1) break;
                 const int j = n - 1 - s;
-                const int e0 = s_offU[s], e1 = s_offU[s + 1];
+                const int e0 = e1;
+                e1 = s_offU[s + 1];
                 const TF yj = y[j];                       // entries hold u_ij / u_jj
                 __syncwarp();
                 for (int e = e0 + 1 + lg; e < e1; e += kLanesPer) {
