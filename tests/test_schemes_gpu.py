@@ -39,7 +39,6 @@ def test_gpu_scheme_matches_reference(fixture, cuda_lib):
 def test_gpu_scheme_fp32_form(scheme, cuda_lib):
     """The FP32 form (FP32 F and solves with FP64 refinement) of the RK and CN steps stays within
     the mixed-form budget of the FP64 form on a smooth RB state."""
-    import numpy as np
     from conatus_gb300 import workloads as W
     from conatus_gb300.ivp import IVPSolver
     P = W.load_template("rb_nz64").instantiate([64])

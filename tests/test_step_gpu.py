@@ -6,8 +6,6 @@ Tolerances: F to 1e-12 relative L2; X_{n+1} to 1e-12 relative L2 per field, rais
 10x the reference's own rounding floor (``field_tolerances``)."""
 from __future__ import annotations
 
-from collections import deque
-
 import numpy as np
 import pytest
 
