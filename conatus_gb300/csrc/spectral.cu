@@ -600,7 +600,8 @@ static int pick_B(int L, int extra_per_col, int maxB) {
 }
 
 template <class R>
-void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st) {
+void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st,
+                 int maxseq = 0) {
     if (ncols <= 0) return;
     if (N == 1 && M == 1) {        // no Chebyshev direction: the single coefficient is the value
         CNG_CUDA(cudaMemcpyAsync(out, in, sizeof(c2<R>) * (size_t)ncols, cudaMemcpyDeviceToDevice, st));
@@ -613,7 +614,7 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
     FftPlan plan = make_plan(M);
     const c2<R>* tw = twiddles<R>().get(M, 0);
     const c2<R>* tq = twiddles<R>().get(M, 1);
-    const int B = pick_B<R>(M, forward ? 0 : M + 1, sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64);
+    const int B = pick_B<R>(M, forward ? 0 : M + 1, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
     const long long blocks = (ncols + B - 1) / B;
     if (forward) k_cheb_fwd<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
@@ -623,13 +624,13 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
 
 template <class R>
 void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, int Nc, int L, bool forward,
-                     cudaStream_t st) {
+                     cudaStream_t st, int maxseq = 0) {
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_fft_axis<R>); });
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L + 1, 0, sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64);
+    const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * ((inner + B - 1) / B);
     k_fft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
@@ -638,13 +639,13 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
 
 template <class R>
 void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int K, int L, bool forward,
-                      cudaStream_t st) {
+                      cudaStream_t st, int maxseq = 0) {
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L + 1, 0, sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64);
+    const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * (((inner + 1) / 2 + B - 1) / B);
     k_rfft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
@@ -669,6 +670,7 @@ struct Rhs {
     double lx = 1, lz = 1, ly = 2;
     int nfactors = 0, noutputs = 0;
     int ncase = 1;             // cases stacked along the field index
+    int maxseq = 0;            // sequences per block of the transforms (0: the per-precision default)
     RhsDev dev{};
     std::vector<BucketDev> buckets;
     std::vector<void*> owned;
@@ -711,19 +713,19 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     // 2. Chebyshev backward along y: S [cols][ny] -> W1 [cols][my]
     C* A = static_cast<C*>(W1);
     C* Bf = static_cast<C*>(W2);
-    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st);
+    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st, maxseq);
     C* cur = A;
     C* other = Bf;
     // 3. z backward: [nf Kx][Nzc][my] -> [nf Kx][mz][my]
     if (ndir == 2) {
-        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st);
+        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st, maxseq);
         std::swap(cur, other);
     }
     // 4. x backward (c2r): [nf][Kx][inner] -> [nf][mx][inner] real
     const long long inner = (long long)(ndir == 2 ? mz : 1) * my;
     R* G = reinterpret_cast<R*>(cur);
     if (ndir >= 1) {
-        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st);
+        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq);
         G = reinterpret_cast<R*>(other);
         std::swap(cur, other);
     } else {
@@ -750,7 +752,7 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     std::swap(cur, other);           // cur = O
     // 6. x forward (r2c): [no][mx][inner] -> [no][Kx][inner]
     if (ndir >= 1) {
-        launch_rfft_axis<R>(cur, other, no, (int)inner, Kx, mx, true, st);
+        launch_rfft_axis<R>(cur, other, no, (int)inner, Kx, mx, true, st, maxseq);
         std::swap(cur, other);
     } else {
         complexify_kernel_launch<R>(reinterpret_cast<const R*>(cur), other, (long long)no * P, st);
@@ -758,11 +760,11 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     }
     // 7. z forward: [no Kx][mz][my] -> [no Kx][Nzc][my]
     if (ndir == 2) {
-        launch_fft_axis<R>(cur, other, (long long)no * Kx, my, Nzc, mz, true, st);
+        launch_fft_axis<R>(cur, other, (long long)no * Kx, my, Nzc, mz, true, st, maxseq);
         std::swap(cur, other);
     }
     // 8. Chebyshev forward: [cols][my] -> S [cols][ny]
-    launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st);
+    launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st, maxseq);
     // 9. pack rows and add the constant part
     for (const auto& b : buckets) {
         if (b.nsys == 0) continue;
@@ -934,6 +936,15 @@ int cng_rhs_evaluate(cng_rhs* hh, const void* state, void* rows, void* stream) {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         if (h->precision == 0) h->run<double>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
         else h->run<float>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
+    })
+}
+
+int cng_rhs_set_sequences(cng_rhs* hh, int maxseq) {
+    CNG_TRY({
+        Rhs* h = reinterpret_cast<Rhs*>(hh);
+        if (!h) throw InvalidArgument("null handle");
+        if (maxseq < 0 || maxseq > 32) throw InvalidArgument("sequences per block: 0 (default) to 32");
+        h->maxseq = maxseq;
     })
 }
 

@@ -120,6 +120,10 @@ class DeviceProblem:
         self._factors = {}
         self._resid = [None] * len(tpl.buckets)
         self._R2 = None
+        self.rhs_tuning = None
+        if self.autotune:
+            from .autotune import tune_rhs
+            self.rhs_tuning = tune_rhs(self)
 
     # ------------------------------------------------------------------ F
     def _build_rhs(self):
