@@ -247,10 +247,10 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (state, history and factors are GBs)",
                    "grid": dev.grid, "state_finite": finite,
                    "solve_schedule": _schedule_summary(dev),
-                   "rhs_sequences": ({"chosen": min(dev.rhs_tuning, key=lambda k: dev.rhs_tuning[k] or 0),
-                                      "ms_per_F": {str(k): (round(v, 4) if v else None)
-                                                   for k, v in dev.rhs_tuning.items()}}
-                                     if dev.rhs_tuning else None)},
+                   "rhs_transforms": ({"chosen": min(dev.rhs_tuning, key=lambda k: dev.rhs_tuning[k] or 0),
+                                       "ms_per_F": {k: (round(v, 4) if v else None)
+                                                    for k, v in dev.rhs_tuning.items()}}
+                                      if dev.rhs_tuning else None)},
         "mode_updates_per_s": value * P.real_unknowns(),
         "roofline": roof,
         "step_roofline": step_roof,

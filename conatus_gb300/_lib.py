@@ -53,7 +53,7 @@ _SIGS = {
     "cng_rhs_destroy": [P],
     "cng_rhs_evaluate": [P, P, P, P],
     "cng_rhs_workspace_bytes": [P, P],
-    "cng_rhs_set_sequences": [P, c_int],
+    "cng_rhs_set_tuning": [P, c_int, c_int],
     "cng_cheb_transform": [c_int, P, P, ctypes.c_int64, c_int, c_int, P],
     "cng_fft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],
     "cng_rfft_axis": [c_int, P, P, ctypes.c_int64, c_int, c_int, c_int, P],

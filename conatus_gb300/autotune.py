@@ -9,9 +9,9 @@ are cached per process by the shapes of the buckets (batch, n, border, band) and
 runs of the same resolution (a serving stream, an ensemble) are timed once. The environment variable
 CONATUS_GB300_SOLVE_SCHEDULE fixes the schedule instead (-1, 0, 1, ...), e.g. for profiling.
 
-The F evaluation's transforms are tuned the same way (``tune_rhs``: sequences per block of the
-shared-memory FFTs, 2 to 16), once per problem shape and precision; CONATUS_GB300_RHS_SEQUENCES
-fixes that value instead.
+The F evaluation's transforms are tuned the same way (``tune_rhs``: sequences and threads per
+block of the shared-memory FFTs), once per problem shape and precision; CONATUS_GB300_RHS_TUNING
+("sequences,threads") fixes them instead.
 
 The reference chooses its solve kernel by constructor flags (python/conatus/runtime/cuda.py:140-152).
 """
@@ -95,27 +95,30 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
 _RHS_CACHE: dict = {}
 
 
-def tune_rhs(dev, reps: int = 2, candidates=(2, 4, 8, 16)) -> dict:
-    """Time the F evaluation of ``dev`` (a DeviceProblem) with each number of sequences per block of
-    its shared-memory transforms and keep the fastest (``cng_rhs_set_sequences``). Cached per
-    precision, template, Fourier sizes and case count. Returns {sequences: ms per evaluation}."""
-    from .ivp import _stream_handle, _torch
+def tune_rhs(dev, reps: int = 2, candidates=((2, 128), (4, 128), (8, 128), (2, 256), (4, 256), (8, 256),
+                                               (16, 256))) -> dict:
+    """Time the F evaluation of ``dev`` (a DeviceProblem) with each launch shape of its shared-memory
+    transforms (sequences per block, threads per block) and keep the fastest
+    (``cng_rhs_set_tuning``). Cached per precision, template, Fourier sizes and case count. Returns
+    {"sequences x threads": ms per evaluation}."""
+    from .ivp import _torch
     torch = _torch()
     P = dev.P
-    fixed = os.environ.get("CONATUS_GB300_RHS_SEQUENCES")
-    if fixed is not None:                 # a fixed value instead of timing (reproducible runs)
-        call("cng_rhs_set_sequences", dev._rhs, int(fixed))
-        return {int(fixed): None}
+    fixed = os.environ.get("CONATUS_GB300_RHS_TUNING")
+    if fixed is not None:                 # "sequences,threads" instead of timing (reproducible runs)
+        q, t = (int(v) for v in fixed.split(","))
+        call("cng_rhs_set_tuning", dev._rhs, q, t)
+        return {f"{q}x{t}": None}
     key = (dev.precision, dev.tpl.name, tuple(P.fourier_sizes), int(getattr(P, "ncase", 1)),
            tuple(dev.nsys))
     if key in _RHS_CACHE:
-        call("cng_rhs_set_sequences", dev._rhs, _RHS_CACHE[key][0])
+        call("cng_rhs_set_tuning", dev._rhs, *_RHS_CACHE[key][0])
         return _RHS_CACHE[key][1]
     st = torch.cuda.Stream()
     x, out = dev.zeros(), dev.zeros()
     times = {}
-    for c in candidates:
-        call("cng_rhs_set_sequences", dev._rhs, int(c))
+    for q, t in candidates:
+        call("cng_rhs_set_tuning", dev._rhs, int(q), int(t))
         dev.F(x, out, st)                                 # warm-up (first-use set-up)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
@@ -123,8 +126,9 @@ def tune_rhs(dev, reps: int = 2, candidates=(2, 4, 8, 16)) -> dict:
             dev.F(x, out, st)
         e1.record(st)
         e1.synchronize()
-        times[c] = e0.elapsed_time(e1) / reps
+        times[(q, t)] = e0.elapsed_time(e1) / reps
     best = min(times, key=times.get)
-    call("cng_rhs_set_sequences", dev._rhs, int(best))
-    _RHS_CACHE[key] = (best, times)
-    return times
+    call("cng_rhs_set_tuning", dev._rhs, *best)
+    report = {f"{q}x{t}": v for (q, t), v in times.items()}
+    _RHS_CACHE[key] = (best, report)
+    return report

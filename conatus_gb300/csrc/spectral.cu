@@ -601,7 +601,8 @@ static int pick_B(int L, int extra_per_col, int maxB) {
 
 template <class R>
 void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st,
-                 int maxseq = 0) {
+                 int maxseq = 0, int threads = 0) {
+    if (threads <= 0) threads = kFftThreads;
     if (ncols <= 0) return;
     if (N == 1 && M == 1) {        // no Chebyshev direction: the single coefficient is the value
         CNG_CUDA(cudaMemcpyAsync(out, in, sizeof(c2<R>) * (size_t)ncols, cudaMemcpyDeviceToDevice, st));
@@ -617,14 +618,15 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
     const int B = pick_B<R>(M, forward ? 0 : M + 1, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
     const long long blocks = (ncols + B - 1) / B;
-    if (forward) k_cheb_fwd<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
-    else k_cheb_bwd<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
+    if (forward) k_cheb_fwd<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
+    else k_cheb_bwd<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
     CNG_LAUNCH("k_cheb");
 }
 
 template <class R>
 void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, int Nc, int L, bool forward,
-                     cudaStream_t st, int maxseq = 0) {
+                     cudaStream_t st, int maxseq = 0, int threads = 0) {
+    if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_fft_axis<R>); });
@@ -633,13 +635,14 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * ((inner + B - 1) / B);
-    k_fft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
+    k_fft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
     CNG_LAUNCH("k_fft_axis");
 }
 
 template <class R>
 void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int K, int L, bool forward,
-                      cudaStream_t st, int maxseq = 0) {
+                      cudaStream_t st, int maxseq = 0, int threads = 0) {
+    if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
     std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
@@ -648,7 +651,7 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * (((inner + 1) / 2 + B - 1) / B);
-    k_rfft_axis<R><<<(unsigned)blocks, kFftThreads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
+    k_rfft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
     CNG_LAUNCH("k_rfft_axis");
 }
 
@@ -671,6 +674,7 @@ struct Rhs {
     int nfactors = 0, noutputs = 0;
     int ncase = 1;             // cases stacked along the field index
     int maxseq = 0;            // sequences per block of the transforms (0: the per-precision default)
+    int threads = 0;           // threads per block of the transforms (0: 256)
     RhsDev dev{};
     std::vector<BucketDev> buckets;
     std::vector<void*> owned;
@@ -713,19 +717,19 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     // 2. Chebyshev backward along y: S [cols][ny] -> W1 [cols][my]
     C* A = static_cast<C*>(W1);
     C* Bf = static_cast<C*>(W2);
-    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st, maxseq);
+    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st, maxseq, threads);
     C* cur = A;
     C* other = Bf;
     // 3. z backward: [nf Kx][Nzc][my] -> [nf Kx][mz][my]
     if (ndir == 2) {
-        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st, maxseq);
+        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st, maxseq, threads);
         std::swap(cur, other);
     }
     // 4. x backward (c2r): [nf][Kx][inner] -> [nf][mx][inner] real
     const long long inner = (long long)(ndir == 2 ? mz : 1) * my;
     R* G = reinterpret_cast<R*>(cur);
     if (ndir >= 1) {
-        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq);
+        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq, threads);
         G = reinterpret_cast<R*>(other);
         std::swap(cur, other);
     } else {
@@ -752,7 +756,7 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     std::swap(cur, other);           // cur = O
     // 6. x forward (r2c): [no][mx][inner] -> [no][Kx][inner]
     if (ndir >= 1) {
-        launch_rfft_axis<R>(cur, other, no, (int)inner, Kx, mx, true, st, maxseq);
+        launch_rfft_axis<R>(cur, other, no, (int)inner, Kx, mx, true, st, maxseq, threads);
         std::swap(cur, other);
     } else {
         complexify_kernel_launch<R>(reinterpret_cast<const R*>(cur), other, (long long)no * P, st);
@@ -760,11 +764,11 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     }
     // 7. z forward: [no Kx][mz][my] -> [no Kx][Nzc][my]
     if (ndir == 2) {
-        launch_fft_axis<R>(cur, other, (long long)no * Kx, my, Nzc, mz, true, st, maxseq);
+        launch_fft_axis<R>(cur, other, (long long)no * Kx, my, Nzc, mz, true, st, maxseq, threads);
         std::swap(cur, other);
     }
     // 8. Chebyshev forward: [cols][my] -> S [cols][ny]
-    launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st, maxseq);
+    launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st, maxseq, threads);
     // 9. pack rows and add the constant part
     for (const auto& b : buckets) {
         if (b.nsys == 0) continue;
@@ -939,12 +943,15 @@ int cng_rhs_evaluate(cng_rhs* hh, const void* state, void* rows, void* stream) {
     })
 }
 
-int cng_rhs_set_sequences(cng_rhs* hh, int maxseq) {
+int cng_rhs_set_tuning(cng_rhs* hh, int maxseq, int threads) {
     CNG_TRY({
         Rhs* h = reinterpret_cast<Rhs*>(hh);
         if (!h) throw InvalidArgument("null handle");
         if (maxseq < 0 || maxseq > 32) throw InvalidArgument("sequences per block: 0 (default) to 32");
+        if (threads != 0 && (threads < 64 || threads > 512 || threads % 32))
+            throw InvalidArgument("threads per block: 0 (default) or a multiple of 32 in 64..512");
         h->maxseq = maxseq;
+        h->threads = threads;
     })
 }
 

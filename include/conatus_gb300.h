@@ -191,10 +191,10 @@ int cng_rhs_destroy(cng_rhs* h);
 /* rows = F(state) on the mode layout (complex128 device arrays; must not alias). Capturable.
  * Replaces IVPSolver.F (python/conatus/timestep/integrator.py:308-348). */
 int cng_rhs_evaluate(cng_rhs* h, const void* state, void* rows, void* stream);
-/* Sequences per block of the evaluator's shared-memory transforms (0: the default, 8 in FP32 and 4
- * in FP64; at most 32): a tuning knob of the autotuner (conatus_gb300.autotune). No reference
- * counterpart. */
-int cng_rhs_set_sequences(cng_rhs* h, int maxseq);
+/* Launch shape of the evaluator's shared-memory transforms: sequences per block (0: the default, 8
+ * in FP32 and 4 in FP64; at most 32) and threads per block (0: 256; else a multiple of 32 in
+ * 64..512). Knobs of the autotuner (conatus_gb300.autotune); no reference counterpart. */
+int cng_rhs_set_tuning(cng_rhs* h, int maxseq, int threads);
 /* Device bytes of the evaluator's work buffers (admission by footprint). */
 int cng_rhs_workspace_bytes(const cng_rhs* h, uint64_t* bytes);
 
