@@ -1,7 +1,7 @@
 """Autotuner of the batched banded solve: the schedule of the step's solve is picked by timing.
 
 Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_set_schedule(h,
--1)``) and the compact-stream schedules of ``cng_banded_schedules`` (four systems per warp over the
+-1)``) and the compact-stream schedules of ``cng_banded_schedules`` (two systems per warp over the
 union pattern of the factors, with different staging chunks and ring depths). Each candidate solves
 the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
 few times on the factors at hand; the fastest is kept for every handle of the factor set. Results

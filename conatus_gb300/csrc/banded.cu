@@ -1440,7 +1440,8 @@ int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream)
 // The band index lists live in shared memory; the streams are staged chunk by chunk with cp.async.
 namespace cng {
 
-constexpr int kGroup = 4;
+constexpr int kGroup = 2;               // systems per warp, 16 lanes each (measured against 1, 4 and 8:
+                                        // fastest on the channel and RB, FP64 and FP32)
 constexpr int kLanesPer = 32 / kGroup;
 constexpr int kCChunk = 8;              // columns per staged chunk (the default schedule)
 

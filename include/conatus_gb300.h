@@ -92,7 +92,7 @@ int cng_banded_prepare_transpose(cng_banded* h, void* stream);
 int cng_banded_solve_transpose(const cng_banded* h, void* b, void* stream);
 
 /* Build the compact bucket-union form of the factors (complex128 handles): the union over the
- * batch of the nonzero slots of the LU factors and of V^T, packed for lockstep solves of 4 systems
+ * batch of the nonzero slots of the LU factors and of V^T, packed for lockstep solves of 2 systems
  * per warp; later solves (all variants, FP64 and FP32) use it. Allocates and synchronizes. The
  * reference's GPU path drops the zeros of the factors per system instead (level-scheduled streams,
  * core/src/cuda/banded.cu:824-1121). */
