@@ -50,7 +50,7 @@ def _factor_bytes(b, nsys, precision, compact):
     if precision == "fp32":
         out += nsys * (n * ldab * _C + 2 * r * n * _C + r * r * _C)
     if compact:
-        slots = int(math.ceil(nsys / 4)) * 4
+        slots = int(math.ceil(nsys / 2)) * 2           # two systems per warp group
         per = n * kl + n * (kl + ku + 1) + r * n
         out += slots * (per * _Z + n * 4) + 6 * (n + 1) * 4 + per * 5
         if precision == "fp32":
