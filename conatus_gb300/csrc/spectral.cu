@@ -444,11 +444,11 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         for (int rep = 0; rep < oy; ++rep) {
             cheb_der_warp<R>(col, der, Ny, lane);
             __syncwarp();
-            const R sc = R(2.0 / d.ly);
+            const double sc = 2.0 / d.ly;
             for (int nn = lane; nn < Ny; nn += 32) {
                 double2 v = der[nn];
                 if (nn == 0) { v.x = v.x / 2; v.y = v.y / 2; }
-                col[nn] = make_double2((double)(R(v.x) * sc), (double)(R(v.y) * sc));
+                col[nn] = make_double2(v.x * sc, v.y * sc);
             }
             __syncwarp();
         }
@@ -467,7 +467,7 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         } else {
             dst = S + fc * Ny;
         }
-        // in the transform precision R (the FP32 form's factors are FP32 from here on)
+        // the scale w (i kx)^ox (i kz)^oz in the transform precision R (a product: no cancellation)
         const R frR = R(fr), fiR = R(fi);
         for (int nn = lane; nn < Ny; nn += 32) {
             const double2 c = col[nn];
@@ -532,16 +532,15 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
             if (lam <= 0) {
                 v = make_double2((double)h[nn].x, (double)h[nn].y);
             } else {
-                // the C^(lambda) conversion in the transform precision R
+                // the C^(lambda) conversion, accumulated in FP64 (its alternating sums cancel)
                 const double* cv = d.conv + (size_t)(lam - 1) * Ny * Ny + (size_t)nn * Ny;
                 const int hi = min(Ny - 1, nn + d.conv_bw[lam - 1]);
-                R ar = R(0), ai = R(0);
+                double ar = 0.0, ai = 0.0;
                 for (int k = nn; k <= hi; ++k) {
-                    const R c = R(cv[k]);
-                    ar += c * h[k].x;
-                    ai += c * h[k].y;
+                    ar += cv[k] * (double)h[k].x;
+                    ai += cv[k] * (double)h[k].y;
                 }
-                v = make_double2((double)ar, (double)ai);
+                v = make_double2(ar, ai);
             }
             v.x *= sc;
             v.y *= sc;
