@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -344,6 +345,17 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
 struct RhsDev {
     int ndir, Kx, Nzc, Ny, nfactors, noutputs, nbuckets;
     int ncase;                 // cases stacked in the work arrays (field index case nf + f)
+    // Fields that differ only by x / z derivatives share their transforms along y (and, for x,
+    // along z): the (i k)^o factors are diagonal in the Fourier indices, so they commute with the
+    // transforms of the other directions and are applied between the stages.
+    // The FP64 form shares (its transforms are FP64-pipe bound); the FP32 form does not (the extra
+    // passes cost it more than the transforms they save, and its error grows).
+    int share;                 // 1: shared transforms with expansions; 0: one transform per factor
+    int ngy, ngz;              // distinct (var, comp, oy) and (var, comp, oy, oz); nfactors if 0
+    const int* yg_rep;         // ngy: a factor of each y-group (its column positions and oy)
+    const int* zg_y;           // ngz: the y-group of each z-group
+    const int* zg_oz;          // ngz: oz of each z-group
+    const int* f_z;            // nfactors: the z-group of each factor
     double lx, lz, ly;
     const int* factors;        // nfactors x 5: var, comp, ox, oy, oz
     const int* out_lam;        // noutputs: lambda (0: no conversion)
@@ -428,10 +440,12 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     const double kz = b.sign * 6.283185307179586476925286766559 * jz / d.lz;
     const double w = b.dact == 0 ? 1.0 : (b.dact == 1 ? 0.5 : 0.25);
     const int slot = zslot(jz, b.sign, d.Nzc);
-    const int cbase = (b.case_of ? b.case_of[m] : 0) * d.nfactors;
-    for (int f = 0; f < d.nfactors; ++f) {
+    const int cbase = (b.case_of ? b.case_of[m] : 0) * d.ngy;
+    for (int gy = 0; gy < d.ngy; ++gy) {
+        const int f = d.yg_rep[gy];
         const int* fd = d.factors + 5 * f;
-        const int ox = fd[2], oy = fd[3], oz = fd[4];
+        const int oy = fd[3];
+        const int ox = d.share ? 0 : fd[2], oz = d.share ? 0 : fd[4];   // shared: applied later
         const int* cp = b.colpos + (size_t)f * Ny;
         for (int nn = lane; nn < Ny; nn += 32) {
             const int pos = cp[nn];
@@ -458,7 +472,7 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         for (int q = 0; q < oz; ++q) { double t = fr; fr = -fi * kz; fi = t * kz; }
         c2<R>* dst;
         c2<R>* dstc = nullptr;
-        const long long fc = cbase + f;
+        const long long fc = cbase + gy;
         if (d.ndir == 2) {
             dst = S + ((fc * d.Kx + jx) * d.Nzc + slot) * Ny;
             if (jx == 0 && jz > 0) dstc = S + ((fc * d.Kx) * d.Nzc + (d.Nzc - jz)) * Ny;
@@ -478,6 +492,54 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
             if (dstc) dstc[nn] = mk<R>(vr, -vi);
         }
         __syncwarp();
+    }
+}
+
+// (i k)^o v: o quarter turns and the magnitude k^o
+template <class R>
+__device__ __forceinline__ c2<R> ik_pow(c2<R> v, double k, int o) {
+    double fr = 1.0, fi = 0.0;
+    for (int q = 0; q < o; ++q) { const double t = fr; fr = -fi * k; fi = t * k; }
+    const R a = R(fr), b = R(fi);
+    return mk<R>(a * v.x - b * v.y, a * v.y + b * v.x);
+}
+
+// z-groups from y-groups on the z spectrum: Z[c ngz + gz][kx][slot][:] = (i kz(slot))^oz Y[c ngy +
+// zg_y[gz]][kx][slot][:], kz(slot) = 2 pi fftfreq(slot, Nzc) / lz. One block per row of my values.
+template <class R>
+__global__ void k_expand_z(RhsDev d, const c2<R>* __restrict__ Y, c2<R>* __restrict__ Z, int my) {
+    const long long rows = (long long)d.ncase * d.ngz * d.Kx * d.Nzc;
+    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+        long long t = row;
+        const int slot = (int)(t % d.Nzc); t /= d.Nzc;
+        const int jx = (int)(t % d.Kx); t /= d.Kx;
+        const int gz = (int)(t % d.ngz);
+        const long long c = t / d.ngz;
+        const int oz = d.zg_oz[gz];
+        const long long src = (((c * d.ngy + d.zg_y[gz]) * d.Kx + jx) * d.Nzc + slot) * my;
+        const int jz = slot < d.Nzc / 2 ? slot : slot - d.Nzc;
+        const double kz = 6.283185307179586476925286766559 * jz / d.lz;
+        for (int i = threadIdx.x; i < my; i += blockDim.x)
+            Z[row * my + i] = oz ? ik_pow<R>(Y[src + i], kz, oz) : Y[src + i];
+    }
+}
+
+// factors from z-groups (or y-groups without a z direction) on the x spectrum:
+// X[c nf + f][kx][:] = (i kx)^ox Z[c ngz + f_z[f]][kx][:], kx = 2 pi jx / lx.
+template <class R>
+__global__ void k_expand_x(RhsDev d, const c2<R>* __restrict__ Z, c2<R>* __restrict__ X, long long inner) {
+    const long long rows = (long long)d.ncase * d.nfactors * d.Kx;
+    for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int jx = (int)(row % d.Kx);
+        const long long t = row / d.Kx;
+        const int f = (int)(t % d.nfactors);
+        const long long c = t / d.nfactors;
+        const int ox = d.factors[5 * f + 2];
+        const long long src = ((c * d.ngz + d.f_z[f]) * d.Kx + jx) * inner;
+        const double kx = 6.283185307179586476925286766559 * jx / d.lx;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < inner;
+             i += (long long)gridDim.x * blockDim.x)
+            X[row * inner + i] = ox ? ik_pow<R>(Z[src + i], kx, ox) : Z[src + i];
     }
 }
 
@@ -713,21 +775,38 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
         k_unpack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, state, Sp);
         CNG_LAUNCH("k_unpack");
     }
-    // 2. Chebyshev backward along y: S [cols][ny] -> W1 [cols][my]
+    // 2. Chebyshev backward along y of the y-groups: S [cols][ny] -> W1 [cols][my]
     C* A = static_cast<C*>(W1);
     C* Bf = static_cast<C*>(W2);
-    launch_cheb<R>(Sp, A, spec_cols(nf), ny, my, false, st, maxseq, threads);
+    const int ngy = dev.ngy * ncase, ngz = dev.ngz * ncase;
+    launch_cheb<R>(Sp, A, spec_cols(ngy), ny, my, false, st, maxseq, threads);
     C* cur = A;
     C* other = Bf;
-    // 3. z backward: [nf Kx][Nzc][my] -> [nf Kx][mz][my]
+    // 3. z: the z-groups ((i kz)^oz of their y-group), then the z backward transform
+    //    [ngz Kx][Nzc][my] -> [ngz Kx][mz][my]
     if (ndir == 2) {
-        launch_fft_axis<R>(cur, other, (long long)nf * Kx, my, Nzc, mz, false, st, maxseq, threads);
+        if (dev.share) {
+            const long long rows = (long long)ngz * Kx * Nzc;
+            k_expand_z<R><<<(unsigned)std::min<long long>(rows, 152LL * 64), 128, 0, st>>>(dev, cur, other, my);
+            CNG_LAUNCH("k_expand_z");
+            std::swap(cur, other);
+        }
+        launch_fft_axis<R>(cur, other, (long long)ngz * Kx, my, Nzc, mz, false, st, maxseq, threads);
         std::swap(cur, other);
     }
-    // 4. x backward (c2r): [nf][Kx][inner] -> [nf][mx][inner] real
+    // 4. x: the factors ((i kx)^ox of their z-group), then the x backward (c2r) transform
+    //    [nf][Kx][inner] -> [nf][mx][inner] real
     const long long inner = (long long)(ndir == 2 ? mz : 1) * my;
     R* G = reinterpret_cast<R*>(cur);
     if (ndir >= 1) {
+        if (dev.share) {
+            const long long rows = (long long)nf * Kx;
+            const unsigned gx = (unsigned)std::min<long long>((inner + 255) / 256, 64);
+            const unsigned gy = (unsigned)std::min<long long>(rows, 65535);
+            k_expand_x<R><<<dim3(gx, gy), 256, 0, st>>>(dev, cur, other, inner);
+            CNG_LAUNCH("k_expand_x");
+            std::swap(cur, other);
+        }
         launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq, threads);
         G = reinterpret_cast<R*>(other);
         std::swap(cur, other);
@@ -821,6 +900,39 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     dv.ncase = h->ncase;
     dv.lx = h->lx; dv.lz = h->lz; dv.ly = h->ly;
     dv.factors = h->keep(upload(D->factors, (size_t)5 * h->nfactors));
+    {   // transform groups: distinct (var, comp, oy) and (var, comp, oy, oz), first occurrence order
+        std::vector<int> yrep, zy, zoz, fz(h->nfactors);
+        std::vector<std::array<int, 3>> ykeys;
+        std::vector<std::array<int, 4>> zkeys;
+        for (int f = 0; f < h->nfactors; ++f) {
+            const int* fd = D->factors + 5 * f;
+            if (h->ndir < 2 && fd[4] != 0) throw InvalidArgument("z derivative without a z direction");
+            if (h->ndir < 1 && fd[2] != 0) throw InvalidArgument("x derivative without an x direction");
+            const std::array<int, 3> yk{fd[0], fd[1], fd[3]};
+            int gy = (int)(std::find(ykeys.begin(), ykeys.end(), yk) - ykeys.begin());
+            if (gy == (int)ykeys.size()) { ykeys.push_back(yk); yrep.push_back(f); }
+            const std::array<int, 4> zk{fd[0], fd[1], fd[3], fd[4]};
+            int gz = (int)(std::find(zkeys.begin(), zkeys.end(), zk) - zkeys.begin());
+            if (gz == (int)zkeys.size()) { zkeys.push_back(zk); zy.push_back(gy); zoz.push_back(fd[4]); }
+            fz[f] = gz;
+        }
+        if (h->ndir == 0 && (int)ykeys.size() != h->nfactors) throw InvalidArgument("repeated factor");
+        dv.share = (h->precision == 0 && h->ndir >= 1) ? 1 : 0;
+        if (!dv.share) {                    // one transform per factor
+            ykeys.assign(h->nfactors, {0, 0, 0});
+            zkeys.assign(h->nfactors, {0, 0, 0, 0});
+            yrep.resize(h->nfactors);
+            zy.resize(h->nfactors);
+            zoz.assign(h->nfactors, 0);
+            for (int f = 0; f < h->nfactors; ++f) yrep[f] = zy[f] = fz[f] = f;
+        }
+        dv.ngy = (int)ykeys.size();
+        dv.ngz = (int)zkeys.size();
+        dv.yg_rep = h->keep(upload(yrep.data(), yrep.size()));
+        dv.zg_y = h->keep(upload(zy.data(), zy.size()));
+        dv.zg_oz = h->keep(upload(zoz.data(), zoz.size()));
+        dv.f_z = h->keep(upload(fz.data(), fz.size()));
+    }
     dv.out_lam = h->keep(upload(D->out_lam, (size_t)h->noutputs));
     dv.out_mono_ptr = h->keep(upload(D->out_mono_ptr, (size_t)h->noutputs + 1));
     const int nmono = D->out_mono_ptr[h->noutputs];
