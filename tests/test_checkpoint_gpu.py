@@ -1,7 +1,7 @@
 """GPU: checkpoints of the device solver (IVPSolver.save_checkpoint / load_checkpoint, the
 reference's npz payload on the mode layout): a run restarted from a checkpoint continues bit for bit
-(SBDF3, CNAB2 and RK443; the restart mid-way through the multistep start-up too), and a checkpoint of
-other numerics is refused."""
+(SBDF3, CNAB2 and RK443; the restart mid-way through the multistep start-up too; the FP32 form), and
+a checkpoint of other numerics is refused."""
 from __future__ import annotations
 
 import numpy as np
@@ -23,17 +23,19 @@ def _state(P, rng):
     return C
 
 
-@pytest.mark.parametrize("scheme,first", [("SBDF3", 5), ("SBDF3", 1), ("CNAB2", 4), ("RK443", 3)])
-def test_restart_is_bit_for_bit(scheme, first, tmp_path, rng, cuda_lib):
+@pytest.mark.parametrize("scheme,first,precision", [("SBDF3", 5, "fp64"), ("SBDF3", 1, "fp64"),
+                                                    ("CNAB2", 4, "fp64"), ("RK443", 3, "fp64"),
+                                                    ("SBDF3", 5, "fp32")])
+def test_restart_is_bit_for_bit(scheme, first, precision, tmp_path, rng, cuda_lib):
     import torch
     from conatus_gb300.ivp import IVPSolver
     P = template("channel_ny17").instantiate([8, 8])
-    a = IVPSolver(P, scheme=scheme, dt=5e-3)
+    a = IVPSolver(P, scheme=scheme, dt=5e-3, precision=precision)
     a.set_state(_state(P, rng))
     a.run(first)
     path = a.save_checkpoint(tmp_path / "chk")
     a.run_graph(4)
-    b = IVPSolver(P, scheme=scheme, dt=5e-3, device_problem=a.dev)
+    b = IVPSolver(P, scheme=scheme, dt=5e-3, precision=precision, device_problem=a.dev)
     b.load_checkpoint(path)
     assert b.iteration == first
     b.run_graph(4)
