@@ -571,6 +571,8 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
 // one warp per system: output spectra -> rows (C^(lambda) conversion, 2^d_act, real buckets real)
 template <class R>
 __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, double2* __restrict__ rows) {
+    // the system's output spectra are staged in shared memory (coalesced), then gathered by row
+    extern __shared__ __align__(16) unsigned char sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
     const int m = blockIdx.x * nw + wib;
@@ -581,15 +583,21 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
     const double sc = (double)(1 << b.dact);
     double2* dst = rows + b.offset + (long long)m * b.n;
     const long long obase = (long long)(b.case_of ? b.case_of[m] : 0) * d.noutputs;
+    c2<R>* hs = reinterpret_cast<c2<R>*>(sm) + (size_t)wib * d.noutputs * Ny;
+    for (int o = 0; o < d.noutputs; ++o) {
+        const long long oc = obase + o;
+        const c2<R>* h;
+        if (d.ndir == 2) h = H + ((oc * d.Kx + jx) * d.Nzc + slot) * Ny;
+        else if (d.ndir == 1) h = H + (oc * d.Kx + jx) * Ny;
+        else h = H + oc * Ny;
+        for (int nn = lane; nn < Ny; nn += 32) hs[o * Ny + nn] = h[nn];
+    }
+    __syncwarp();
     for (int i = lane; i < b.n; i += 32) {
         const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
         double2 v = make_double2(0.0, 0.0);
         if (o >= 0) {
-            const c2<R>* h;
-            const long long oc = obase + o;
-            if (d.ndir == 2) h = H + ((oc * d.Kx + jx) * d.Nzc + slot) * Ny;
-            else if (d.ndir == 1) h = H + (oc * d.Kx + jx) * Ny;
-            else h = H + oc * Ny;
+            const c2<R>* h = hs + o * Ny;
             const int lam = d.out_lam[o];
             if (lam <= 0) {
                 v = make_double2((double)h[nn].x, (double)h[nn].y);
@@ -851,7 +859,8 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     for (const auto& b : buckets) {
         if (b.nsys == 0) continue;
         const int nw = 4;
-        k_pack<R><<<ceil_div(b.nsys, nw), 32 * nw, 0, st>>>(dev, b, Sp, rows);
+        const size_t smem = (size_t)nw * noutputs * ny * sizeof(C);
+        k_pack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, Sp, rows);
         CNG_LAUNCH("k_pack");
     }
     if (nb0) {

@@ -98,6 +98,20 @@ __global__ void k_lincomb(LincombArgs a, const double* __restrict__ base, double
     }
 }
 
+// The same combination with fused multiply-adds (two FP64 operations per history level instead of
+// four): the FP32 form's right-hand side, which is not held to the reference's order of roundings.
+__global__ void k_sbdf_rhs_fused(SbdfArgs a, double* __restrict__ rhs, long long count) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int j = 0; j < a.q; ++j) {
+            acc = fma(a.c[j], a.F[j][t], acc);
+            acc = fma(-a.d[j], a.MX[j][t], acc);
+        }
+        rhs[t] = acc;
+    }
+}
+
 // r = b - (a M + c sum_t mono[m][t] L_t) x per system, FP64 (the refinement residual). M values
 // shared by the bucket (nnz), L_t coefficient rows (nmono x nnz), mono (nsys x nmono).
 __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
@@ -283,6 +297,11 @@ int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef,
 
 int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
                  void* rhs, int64_t count, void* stream) {
+    return cng_sbdf_rhs_fused(q, c, d, F, MX, rhs, count, 0, stream);
+}
+
+int cng_sbdf_rhs_fused(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
+                       void* rhs, int64_t count, int fused, void* stream) {
     CNG_TRY({
         if (q < 1 || q > 4) throw InvalidArgument("SBDF order must be 1..4");
         if (!c || !d || !F || !MX || !rhs) throw InvalidArgument("null argument");
@@ -297,7 +316,10 @@ int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, 
         }
         const long long n = 2 * count;      // complex entries -> doubles
         const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 32);
-        k_sbdf_rhs<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<double*>(rhs), n);
+        if (fused)
+            k_sbdf_rhs_fused<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<double*>(rhs), n);
+        else
+            k_sbdf_rhs<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<double*>(rhs), n);
         CNG_LAUNCH("k_sbdf_rhs");
     })
 }

@@ -668,7 +668,8 @@ class IVPSolver:
             ds = (ctypes.c_double * q)(*[a[j + 1] / self.dt for j in range(q)])
             Fp = (ctypes.c_void_p * q)(*[self.Fh[k].data_ptr() for k in slots])
             Mp = (ctypes.c_void_p * q)(*[self.MXh[k].data_ptr() for k in slots])
-            call("cng_sbdf_rhs", q, cs, ds, Fp, Mp, self.R.data_ptr(), self.dev.n_total, s)
+            call("cng_sbdf_rhs_fused", q, cs, ds, Fp, Mp, self.R.data_ptr(), self.dev.n_total,
+                 1 if self.dev.precision == "fp32" else 0, s)
             self.dev.solve(a[0] / self.dt, 1.0, self.R, self.X, s)
             return
         # CN family (integrator.py:581-603): rhs = sum_{j>=1} c_j F_j - (a_j/dt) M X_j - b_j L X_j

@@ -290,6 +290,10 @@ int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef,
  * FMA contraction, in the order of the reference's sbdf_rhs, python/conatus/timestep/lincomb.py:146-162). */
 int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
                  void* rhs, int64_t count, void* stream);
+/* The same with fused = 1: fused multiply-adds, two FP64 operations per history level instead of
+ * four (the FP32 form's combination; fused = 0 is cng_sbdf_rhs). No reference counterpart. */
+int cng_sbdf_rhs_fused(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
+                       void* rhs, int64_t count, int fused, void* stream);
 
 /* ---- CUDA graphs of whole steps ------------------------------------------------------------- */
 
