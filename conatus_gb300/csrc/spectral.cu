@@ -543,27 +543,78 @@ __global__ void k_expand_x(RhsDev d, const c2<R>* __restrict__ Z, c2<R>* __restr
     }
 }
 
-// products on the grid: out_o = sum_m c_m prod_j G_j (factor values read through the L1 cache:
-// each grid point's factors are shared by several monomials)
-template <class R>
+// products on the grid: out_o = sum_m c_m prod_j G_j. The monomial tables are staged in shared
+// memory; a thread takes V consecutive points (one 16-byte load per factor field: V = 4 in FP32,
+// 2 in FP64), which needs P % V == 0 (else V = 1).
+constexpr int kMaxMono = 64;
+template <class R> struct Vec;
+template <> struct Vec<float> { using t4 = float4; };
+template <> struct Vec<double> { using t4 = double2; };
+
+template <class R, int V>
+__device__ __forceinline__ void load_v(const R* p, R* v) {
+    if constexpr (V == 1) {
+        v[0] = __ldg(p);
+    } else if constexpr (sizeof(R) == 4) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+        const double2 q = __ldg(reinterpret_cast<const double2*>(p));
+        v[0] = q.x; v[1] = q.y;
+    }
+}
+
+template <class R, int V>
+__device__ __forceinline__ void store_v(R* p, const R* v) {
+    if constexpr (V == 1) {
+        p[0] = v[0];
+    } else if constexpr (sizeof(R) == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+        *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    }
+}
+
+template <class R, int V>
 __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
+    __shared__ int s_ptr[17];
+    __shared__ R s_coef[kMaxMono];
+    __shared__ int s_fac[4 * kMaxMono];
+    const int no = d.noutputs;
+    for (int q = threadIdx.x; q <= no; q += blockDim.x) s_ptr[q] = d.out_mono_ptr[q];
+    __syncthreads();
+    const int nm = s_ptr[no];
+    for (int q = threadIdx.x; q < nm; q += blockDim.x) s_coef[q] = R(d.mono_coef[q]);
+    for (int q = threadIdx.x; q < 4 * nm; q += blockDim.x) s_fac[q] = d.mono_fac[q];
+    __syncthreads();
     const long long total = P * d.ncase;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long c = t / P, p = t - c * P;
-        const R* Gc = G + c * d.nfactors * P;
-        R* Oc = O + c * d.noutputs * P;
-        for (int o = 0; o < d.noutputs; ++o) {
-            R acc = R(0);
-            for (int mi = d.out_mono_ptr[o]; mi < d.out_mono_ptr[o + 1]; ++mi) {
-                R t2 = R(d.mono_coef[mi]);
-                const int* fs = d.mono_fac + 4 * mi;
+    for (long long t0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * V; t0 < total;
+         t0 += (long long)gridDim.x * blockDim.x * V) {
+        const long long c = t0 / P, p = t0 - c * P;
+        const R* Gc = G + c * d.nfactors * P + p;
+        R* Oc = O + c * no * P + p;
+        for (int o = 0; o < no; ++o) {
+            R acc[V];
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (fs[q] >= 0) t2 = t2 * __ldg(Gc + (long long)fs[q] * P + p);
-                acc = acc + t2;
+            for (int v = 0; v < V; ++v) acc[v] = R(0);
+            for (int mi = s_ptr[o]; mi < s_ptr[o + 1]; ++mi) {
+                R t[V];
+#pragma unroll
+                for (int v = 0; v < V; ++v) t[v] = s_coef[mi];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int f = s_fac[4 * mi + q];
+                    if (f >= 0) {
+                        R g[V];
+                        load_v<R, V>(Gc + (long long)f * P, g);
+#pragma unroll
+                        for (int v = 0; v < V; ++v) t[v] = t[v] * g[v];
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v] = acc[v] + t[v];
             }
-            Oc[(long long)o * P + p] = acc;
+            store_v<R, V>(Oc + (long long)o * P, acc);
         }
     }
 }
@@ -835,8 +886,14 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     }
     {
         const int threads = 256;
-        const long long blocks = std::min<long long>((P * ncase + threads - 1) / threads, 152LL * 16);
-        k_products<R><<<(unsigned)blocks, threads, 0, st>>>(dev, G, O, P);
+        constexpr int V = sizeof(R) == 4 ? 4 : 2;
+        if (P % V == 0) {
+            const long long blocks = std::min<long long>((P * ncase / V + threads - 1) / threads, 152LL * 16);
+            k_products<R, V><<<(unsigned)blocks, threads, 0, st>>>(dev, G, O, P);
+        } else {
+            const long long blocks = std::min<long long>((P * ncase + threads - 1) / threads, 152LL * 16);
+            k_products<R, 1><<<(unsigned)blocks, threads, 0, st>>>(dev, G, O, P);
+        }
         CNG_LAUNCH("k_products");
     }
     std::swap(cur, other);           // cur = O
@@ -945,6 +1002,7 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     dv.out_lam = h->keep(upload(D->out_lam, (size_t)h->noutputs));
     dv.out_mono_ptr = h->keep(upload(D->out_mono_ptr, (size_t)h->noutputs + 1));
     const int nmono = D->out_mono_ptr[h->noutputs];
+    if (nmono > kMaxMono || h->noutputs > 16) throw InvalidArgument("at most 64 monomials and 16 outputs");
     for (int mi = 0; mi < 4 * nmono; ++mi)
         if (D->mono_factors[mi] >= h->nfactors) throw InvalidArgument("monomial factor id out of range");
     dv.mono_coef = h->keep(upload(D->mono_coef, (size_t)nmono));
