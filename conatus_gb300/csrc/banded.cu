@@ -1588,7 +1588,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j + 1 + s_Lrow[e];
                     const TF v = (i == l) ? yj0 : y[i];
-                    y[i] = v - Lc[(e - base) * kGroup + g] * bj;
+                    y[i] = cfms(v, Lc[(e - base) * kGroup + g], bj);
                 }
                 if (lg == 0) {
                     y[j] = bj;
@@ -1598,7 +1598,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             }
         }
     }
-    // ---------------- backward: U (diagonal holds 1/u_jj)
+    // ---------------- backward: U (diagonal holds -1/u_jj)
     {
         const int nch = (n + CH - 1) / CH;
         auto issue = [&](int c) {
@@ -1627,11 +1627,12 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 e1 = s_offU[s + 1];
                 const TF yj = y[j];                       // entries hold u_ij / u_jj
                 __syncwarp();
-                for (int e = e0 + 1 + lg; e < e1; e += kLanesPer) {
+                // the column's first entry is the diagonal, held as -1/u_jj: it takes a lane of the
+                // same pass (y_j = 0 - (-1/u_jj) y_j) instead of a pass of its own
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j - s_Udist[e];
-                    y[i] = y[i] - Uc[(e - base) * kGroup + g] * yj;
+                    y[i] = cfms(e == e0 ? TF(0.0) : y[i], Uc[(e - base) * kGroup + g], yj);
                 }
-                if (lg == 0) y[j] = yj * Uc[(e0 - base) * kGroup + g];
                 __syncwarp();
             }
         }
@@ -1642,7 +1643,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
         for (int a = 0; a < r; ++a) {
             TF acc = TF(0.0);
             for (int e = ix.offV[a] + lg; e < ix.offV[a + 1]; e += kLanesPer)
-                acc = acc + Vg[(size_t)e * kGroup + g] * y[ix.Vcol[e]];
+                acc = cfma(acc, Vg[(size_t)e * kGroup + g], y[ix.Vcol[e]]);
             for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
             if (lg == 0) zb[a] = acc;
         }
@@ -1653,7 +1654,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             const TF* Ws = cd.W + (size_t)sys * r * n;
             for (int i = lg; i < n; i += kLanesPer) {
                 TF acc = y[i];
-                for (int k = 0; k < r; ++k) acc = acc - Ws[(size_t)k * n + i] * zb[k];
+                for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
                 y[i] = acc;
             }
         }
@@ -1734,8 +1735,9 @@ __global__ void k_pack_compact(BandView<T> v, CompactIdx ix, T* __restrict__ L, 
         const T dinv = live ? ab[(size_t)j * v.ldab + kv] : T(0.0);     // 1 / u_jj
         for (int e = ix.offU[s]; e < ix.offU[s + 1]; ++e) {
             const int d = ix.Udist[e];
-            // the diagonal entry keeps 1 / u_jj; the others are pre-scaled: u_ij / u_jj
-            Uw[(size_t)e * kGroup + g] = !live ? T(0.0) : (d == 0 ? dinv : ab[(size_t)j * v.ldab + kv - d] * dinv);
+            // the diagonal entry holds -1 / u_jj (the sweep applies it as y_j = 0 - (-1/u_jj) y_j);
+            // the others are pre-scaled: u_ij / u_jj
+            Uw[(size_t)e * kGroup + g] = !live ? T(0.0) : (d == 0 ? -dinv : ab[(size_t)j * v.ldab + kv - d] * dinv);
         }
     }
     int* Pw = piv + (size_t)wg * n * kGroup;
@@ -1900,7 +1902,7 @@ static void launch_compact(const Banded& h, const CompactData<TF>& cd, const Sol
     });
     int nw = 8;
     while (nw > 1 && compact_smem<TF>(h, nw) > 220 * 1024) --nw;
-    nw = std::min(nw, h.cWg);
+    nw = std::min(nw, std::max(1, ceil_div(h.cWg, sm_count())));
     const size_t smem = compact_smem<TF>(h, nw);
     if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
     k_solve_compact<TF, TD, IO><<<ceil_div(h.cWg, nw), 32 * nw, smem, st>>>(compact_idx(h), cd, io);
@@ -1936,10 +1938,15 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              220 * 1024);
     });
-    // one warp count for all blocks: the largest that fits every bucket
-    int nw = 8;
-    for (const Banded* h : hs)
+    // one warp count for all blocks: the largest that fits every bucket, and no more than it takes
+    // to give every SM a block (a small batch spreads over the SMs: each SM's FP64 pipe and shared
+    // memory serve fewer sweeps)
+    int nw = 8, total = 0;
+    for (const Banded* h : hs) {
         while (nw > 1 && compact_smem<TF>(*h, nw, sched) > 220 * 1024) --nw;
+        total += h->cWg;
+    }
+    nw = std::min(nw, std::max(1, ceil_div(total, sm_count())));
     size_t smem = 0;
     for (const Banded* h : hs) smem = std::max(smem, compact_smem<TF>(*h, nw, sched));
     if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");

@@ -54,6 +54,14 @@ __host__ __device__ inline zd operator*(zd a, zd b) {
     return zd(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
 }
 __host__ __device__ inline zd operator*(double s, zd a) { return zd(s * a.re, s * a.im); }
+// v - a b and v + a b with two fused multiply-adds per component (four FP64 instructions, where
+// v - (a * b) takes six: two multiplies, two fused multiply-adds and two subtractions)
+__host__ __device__ inline zd cfms(zd v, zd a, zd b) {
+    return zd(fma(a.im, b.im, fma(-a.re, b.re, v.re)), fma(-a.im, b.re, fma(-a.re, b.im, v.im)));
+}
+__host__ __device__ inline zd cfma(zd v, zd a, zd b) {
+    return zd(fma(-a.im, b.im, fma(a.re, b.re, v.re)), fma(a.im, b.re, fma(a.re, b.im, v.im)));
+}
 // a / b by Smith's method (overflow-safe scaling of the denominator).
 __host__ __device__ inline zd operator/(zd a, zd b) {
     if (fabs(b.re) >= fabs(b.im)) {
@@ -78,6 +86,12 @@ __host__ __device__ inline zf operator+(zf a, zf b) { return zf(a.re + b.re, a.i
 __host__ __device__ inline zf operator-(zf a, zf b) { return zf(a.re - b.re, a.im - b.im); }
 __host__ __device__ inline zf operator*(zf a, zf b) {
     return zf(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__host__ __device__ inline zf cfms(zf v, zf a, zf b) {
+    return zf(fmaf(a.im, b.im, fmaf(-a.re, b.re, v.re)), fmaf(-a.im, b.re, fmaf(-a.re, b.im, v.im)));
+}
+__host__ __device__ inline zf cfma(zf v, zf a, zf b) {
+    return zf(fmaf(-a.im, b.im, fmaf(a.re, b.re, v.re)), fmaf(a.im, b.re, fmaf(a.re, b.im, v.im)));
 }
 __host__ __device__ inline zf operator/(zf a, zf b) {
     if (fabsf(b.re) >= fabsf(b.im)) {
@@ -148,5 +162,18 @@ __device__ inline T warp_sum(T v) {
     }
 
 inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+// Streaming multiprocessors of the current device (read once per device).
+inline int sm_count() {
+    static int cached[32] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 32) return 152;
+    if (cached[dev] <= 0) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = v > 0 ? v : 152;
+    }
+    return cached[dev];
+}
 
 }  // namespace cng

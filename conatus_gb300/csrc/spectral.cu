@@ -364,6 +364,7 @@ struct RhsDev {
     const int* mono_fac;       // per monomial: 4 factor ids (-1 pad)
     const double* conv;        // per lambda 1..: (Ny x Ny) dense, conv + (lam - 1) Ny Ny
     const int* conv_bw;        // per lambda: upper bandwidth of the conversion
+    const int* conv_step;      // per lambda: 2 when it couples one parity only (odd offsets zero), else 1
 };
 
 struct BucketDev {
@@ -386,7 +387,7 @@ __device__ __forceinline__ int zslot(int jz, int sign, int Nzc) {
 // chunk of k from the top down (one running sum per parity), the chunk totals are combined by a
 // suffix scan over the lanes, and each lane then writes der[k - 1] for the k of its chunk.
 template <class R>
-__device__ __forceinline__ void cheb_der_warp(const double2* __restrict__ c, double2* __restrict__ der, int N,
+__device__ __forceinline__ void cheb_der_warp(const c2<R>* __restrict__ c, c2<R>* __restrict__ der, int N,
                                               int lane) {
     const int C = (N + 31) >> 5;
     const int k0 = lane * C, k1 = min(k0 + C, N);
@@ -395,8 +396,8 @@ __device__ __forceinline__ void cheb_der_warp(const double2* __restrict__ c, dou
     for (int k = k1 - 1; k >= k0; --k) {
         if (k == 0) continue;
         const R w = R(2 * k);
-        tx[k & 1] = tx[k & 1] + w * R(c[k].x);
-        ty[k & 1] = ty[k & 1] + w * R(c[k].y);
+        tx[k & 1] = tx[k & 1] + w * c[k].x;
+        ty[k & 1] = ty[k & 1] + w * c[k].y;
     }
     // exclusive suffix scan over lanes: sums of the chunks above this lane
     R sx[2] = {tx[0], tx[1]}, sy[2] = {ty[0], ty[1]};
@@ -411,13 +412,13 @@ __device__ __forceinline__ void cheb_der_warp(const double2* __restrict__ c, dou
     R ax[2], ay[2];
 #pragma unroll
     for (int p = 0; p < 2; ++p) { ax[p] = sx[p] - tx[p]; ay[p] = sy[p] - ty[p]; }
-    if (lane == 0 && N >= 1) der[N - 1] = make_double2(0.0, 0.0);
+    if (lane == 0 && N >= 1) der[N - 1] = mk<R>(R(0), R(0));
     for (int k = k1 - 1; k >= k0; --k) {
         if (k == 0) continue;
         const R w = R(2 * k);
-        ax[k & 1] = ax[k & 1] + w * R(c[k].x);
-        ay[k & 1] = ay[k & 1] + w * R(c[k].y);
-        der[k - 1] = make_double2((double)ax[k & 1], (double)ay[k & 1]);
+        ax[k & 1] = ax[k & 1] + w * c[k].x;
+        ay[k & 1] = ay[k & 1] + w * c[k].y;
+        der[k - 1] = mk<R>(ax[k & 1], ay[k & 1]);
     }
 }
 
@@ -429,11 +430,15 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     const int m = blockIdx.x * nw + wib;
     if (m >= b.nsys) return;
     const int Ny = d.Ny;
-    double2* x = reinterpret_cast<double2*>(sm) + (size_t)wib * (b.n + 2 * Ny);
-    double2* col = x + b.n;
-    double2* der = col + Ny;
+    // the system's state, rounded once to the transform precision R
+    c2<R>* x = reinterpret_cast<c2<R>*>(sm) + (size_t)wib * (b.n + 2 * Ny);
+    c2<R>* col = x + b.n;
+    c2<R>* der = col + Ny;
     const double2* src = state + b.offset + (long long)m * b.n;
-    for (int i = lane; i < b.n; i += 32) x[i] = src[i];
+    for (int i = lane; i < b.n; i += 32) {
+        const double2 v = src[i];
+        x[i] = mk<R>(R(v.x), R(v.y));
+    }
     __syncwarp();
     const int jx = b.modes[2 * m], jz = b.modes[2 * m + 1];
     const double kx = 6.283185307179586476925286766559 * jx / d.lx;
@@ -449,7 +454,7 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         const int* cp = b.colpos + (size_t)f * Ny;
         for (int nn = lane; nn < Ny; nn += 32) {
             const int pos = cp[nn];
-            col[nn] = pos >= 0 ? x[pos] : make_double2(0.0, 0.0);
+            col[nn] = pos >= 0 ? x[pos] : mk<R>(R(0), R(0));
         }
         __syncwarp();
         // Chebyshev derivative oy times: out[n] = sum_{k > n, k - n odd} 2 k c[k], out[0] /= 2,
@@ -458,11 +463,11 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         for (int rep = 0; rep < oy; ++rep) {
             cheb_der_warp<R>(col, der, Ny, lane);
             __syncwarp();
-            const double sc = 2.0 / d.ly;
+            const R sc = R(2.0 / d.ly);
             for (int nn = lane; nn < Ny; nn += 32) {
-                double2 v = der[nn];
+                c2<R> v = der[nn];
                 if (nn == 0) { v.x = v.x / 2; v.y = v.y / 2; }
-                col[nn] = make_double2(v.x * sc, v.y * sc);
+                col[nn] = mk<R>(v.x * sc, v.y * sc);
             }
             __syncwarp();
         }
@@ -484,8 +489,8 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         // the scale w (i kx)^ox (i kz)^oz in the transform precision R (a product: no cancellation)
         const R frR = R(fr), fiR = R(fi);
         for (int nn = lane; nn < Ny; nn += 32) {
-            const double2 c = col[nn];
-            const R cr = R(c.x), ci = R(c.y);
+            const c2<R> c = col[nn];
+            const R cr = c.x, ci = c.y;
             const R vr = frR * cr - fiR * ci;
             const R vi = b.real ? R(0) : frR * ci + fiR * cr;
             dst[nn] = mk<R>(vr, vi);
@@ -634,32 +639,37 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
     const double sc = (double)(1 << b.dact);
     double2* dst = rows + b.offset + (long long)m * b.n;
     const long long obase = (long long)(b.case_of ? b.case_of[m] : 0) * d.noutputs;
-    c2<R>* hs = reinterpret_cast<c2<R>*>(sm) + (size_t)wib * d.noutputs * Ny;
+    double2* hs = reinterpret_cast<double2*>(sm) + (size_t)wib * d.noutputs * Ny;   // widened once
     for (int o = 0; o < d.noutputs; ++o) {
         const long long oc = obase + o;
         const c2<R>* h;
         if (d.ndir == 2) h = H + ((oc * d.Kx + jx) * d.Nzc + slot) * Ny;
         else if (d.ndir == 1) h = H + (oc * d.Kx + jx) * Ny;
         else h = H + oc * Ny;
-        for (int nn = lane; nn < Ny; nn += 32) hs[o * Ny + nn] = h[nn];
+        for (int nn = lane; nn < Ny; nn += 32) {
+            const c2<R> v = h[nn];
+            hs[o * Ny + nn] = make_double2((double)v.x, (double)v.y);
+        }
     }
     __syncwarp();
     for (int i = lane; i < b.n; i += 32) {
         const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
         double2 v = make_double2(0.0, 0.0);
         if (o >= 0) {
-            const c2<R>* h = hs + o * Ny;
+            const double2* h = hs + o * Ny;
             const int lam = d.out_lam[o];
             if (lam <= 0) {
-                v = make_double2((double)h[nn].x, (double)h[nn].y);
+                v = h[nn];
             } else {
-                // the C^(lambda) conversion, accumulated in FP64 (its alternating sums cancel)
+                // the C^(lambda) conversion, accumulated in FP64 (its alternating sums cancel);
+                // conversions that couple one parity only step over the other (its zeros)
                 const double* cv = d.conv + (size_t)(lam - 1) * Ny * Ny + (size_t)nn * Ny;
                 const int hi = min(Ny - 1, nn + d.conv_bw[lam - 1]);
+                const int step = d.conv_step[lam - 1];
                 double ar = 0.0, ai = 0.0;
-                for (int k = nn; k <= hi; ++k) {
-                    ar += cv[k] * (double)h[k].x;
-                    ai += cv[k] * (double)h[k].y;
+                for (int k = nn; k <= hi; k += step) {
+                    ar += cv[k] * h[k].x;
+                    ai += cv[k] * h[k].y;
                 }
                 v = make_double2(ar, ai);
             }
@@ -830,7 +840,7 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     for (const auto& b : buckets) {
         if (b.nsys == 0) continue;
         const int nw = 4;
-        const size_t smem = (size_t)nw * (b.n + 2 * ny) * sizeof(double2);
+        const size_t smem = (size_t)nw * (b.n + 2 * ny) * sizeof(C);
         k_unpack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, state, Sp);
         CNG_LAUNCH("k_unpack");
     }
@@ -916,7 +926,7 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     for (const auto& b : buckets) {
         if (b.nsys == 0) continue;
         const int nw = 4;
-        const size_t smem = (size_t)nw * noutputs * ny * sizeof(C);
+        const size_t smem = (size_t)nw * noutputs * ny * sizeof(double2);
         k_pack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, Sp, rows);
         CNG_LAUNCH("k_pack");
     }
@@ -1010,7 +1020,7 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     int maxlam = 0;
     for (int o = 0; o < h->noutputs; ++o) maxlam = std::max(maxlam, D->out_lam[o]);
     if (maxlam > D->nlam) throw InvalidArgument("output lambda without a conversion matrix");
-    std::vector<int> bw(std::max(1, D->nlam), 0);
+    std::vector<int> bw(std::max(1, D->nlam), 0), cstep(std::max(1, D->nlam), 2);
     for (int l = 0; l < D->nlam; ++l) {
         const double* cv = D->conv + (size_t)l * h->ny * h->ny;
         for (int i = 0; i < h->ny; ++i)
@@ -1018,15 +1028,22 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
                 if (cv[(size_t)i * h->ny + k] != 0.0) {
                     if (k < i) throw InvalidArgument("conversion matrices must be upper triangular");
                     bw[l] = std::max(bw[l], k - i);
+                    if ((k - i) & 1) cstep[l] = 1;
                 }
     }
     dv.conv = h->keep(upload(D->conv, (size_t)std::max(1, D->nlam) * h->ny * h->ny * (D->nlam ? 1 : 0)));
     dv.conv_bw = h->keep(upload(bw.data(), bw.size()));
+    dv.conv_step = h->keep(upload(cstep.data(), cstep.size()));
     for (int bi = 0; bi < D->nbuckets; ++bi) {
         const int* bd = D->buckets + 5 * bi;
         BucketDev b{};
         b.nsys = bd[0]; b.n = bd[1]; b.dact = bd[2]; b.sign = bd[3]; b.real = bd[4];
         b.offset = D->bucket_offset[bi];
+        // shared memory of unpack and pack (four warps per block): the system's vector and two
+        // columns, and the FP64 output spectra
+        if ((size_t)4 * (b.n + 2 * h->ny) * sizeof(double2) > 200 * 1024 ||
+            (size_t)4 * h->noutputs * h->ny * sizeof(double2) > 200 * 1024)
+            throw InvalidArgument("system too long for the shared-memory unpack/pack");
         for (int m = 0; m < b.nsys; ++m) {
             const int jx = D->modes[bi][2 * m], jz = D->modes[bi][2 * m + 1];
             if (jx < 0 || (h->ndir >= 1 && jx >= h->Kx) || jz < 0 || (h->ndir == 2 && jz >= h->Nzc / 2))
@@ -1082,6 +1099,8 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     std::call_once(f, [] {
         cudaFuncSetAttribute(k_unpack<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_unpack<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_pack<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_pack<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     });
     return h.release();
 }

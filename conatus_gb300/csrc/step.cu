@@ -34,15 +34,15 @@ __global__ void k_csr_matvec(int nsys, int n, const int* __restrict__ ip, const 
 __global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
                                   const double* __restrict__ val, const double2* __restrict__ x,
                                   double2* __restrict__ y) {
-    const unsigned sysw = ((unsigned)nsys + 31u) >> 5;
-    const unsigned nwarps = sysw * (unsigned)n;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned wstride = (gridDim.x * blockDim.x) >> 5;
-    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
-        const int i = (int)(w / sysw);
-        const unsigned m = (w - (unsigned)i * sysw) * 32u + lane;
-        if (m >= (unsigned)nsys) continue;
-        const double2* xm = x + (long long)m * n;
+    // one thread per (system, row), rows fastest: a warp reads a contiguous stretch of one
+    // system's vector (the band around its rows) and writes 32 consecutive rows; the row pattern
+    // and values, shared by every system, stay in L1
+    const unsigned total = (unsigned)nsys * (unsigned)n;
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const unsigned m = t / (unsigned)n;
+        const int i = (int)(t - m * (unsigned)n);
+        const double2* xm = x + (size_t)m * n;
         double ar[2] = {0.0, 0.0}, ai[2] = {0.0, 0.0};
         int q = 0;
         for (int p = ip[i]; p < ip[i + 1]; ++p, q ^= 1) {
@@ -51,7 +51,7 @@ __global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, c
             ar[q] = fma(a, b.x, ar[q]);
             ai[q] = fma(a, b.y, ai[q]);
         }
-        y[(long long)m * n + i] = make_double2(ar[0] + ar[1], ai[0] + ai[1]);
+        y[t] = make_double2(ar[0] + ar[1], ai[0] + ai[1]);
     }
 }
 
@@ -227,8 +227,8 @@ int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* i
         if (!indptr || !indices || !values || !x || !y) throw InvalidArgument("null device pointer");
         if (x == y) throw InvalidArgument("x and y must not alias");
         if (nsys <= 0 || n <= 0) return CNG_OK;
-        if ((long long)((nsys + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("csr_matvec_real: batch too large");
-        const long long threads = (long long)((nsys + 31) / 32) * n * 32;
+        const long long threads = (long long)nsys * n;
+        if (threads >= (1LL << 32) - (1LL << 24)) throw InvalidArgument("csr_matvec_real: batch too large");
         const int blocks = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
         k_csr_matvec_real<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
             nsys, n, indptr, indices, values, static_cast<const double2*>(x), static_cast<double2*>(y));

@@ -83,6 +83,7 @@ class DeviceProblem:
         _lib.lib()
         self.factor_sets = factor_sets      # None: keep every (a, b) factorization, else at most this many
         self.autotune = True                # time the solve schedules on each new factor set
+        self.refine = 1                     # FP32 form: refinement passes (FP64 residual + FP32 solve)
         self.tuning = None
         if precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
@@ -411,8 +412,8 @@ class DeviceProblem:
 
     def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
         """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias), every bucket in one
-        launch. FP32 form: FP32 solve, FP64 residual, FP32 correction added in FP64 (one
-        refinement step)."""
+        launch. FP32 form: FP32 solve, then ``refine`` passes (default one) of FP64 residual and
+        FP32 correction added in FP64."""
         fs = self.factor(a, b_, stream)
         self._solve_with(fs, a, b_, rhs, out, stream)
 
@@ -436,9 +437,10 @@ class DeviceProblem:
         if self._R2 is None:
             self._R2 = self.zeros()
         call("cng_banded_solve_batch", nb, hs, bp, xp, 1, 0, s)
-        self.residual(a, b_, out, rhs, self._R2, s)
         rp = (ctypes.c_void_p * nb)(*[self.bucket(self._R2, bi).data_ptr() for bi in range(nb)])
-        call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
+        for _ in range(self.refine):
+            self.residual(a, b_, out, rhs, self._R2, s)
+            call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
 
     def solve_launch(self, fs, rhs, out, stream=None) -> None:
         """One batched solve launch with the factor set ``fs`` (FP32 factors in the FP32 form), no
@@ -540,7 +542,8 @@ class IVPSolver:
     ``lower_order`` as the reference's default."""
 
     def __init__(self, problem, scheme: str = "SBDF2", dt: float = 1e-3, precision: str = "fp64",
-                 device_problem: DeviceProblem | None = None, factor_sets: int | None = None):
+                 device_problem: DeviceProblem | None = None, factor_sets: int | None = None,
+                 refine: int | None = None):
         if scheme in SBDF_SCHEMES:
             self.family, self.order = "sbdf", int(scheme[-1])
             self.ring = self.order
@@ -556,6 +559,15 @@ class IVPSolver:
             raise ValueError(f"scheme {scheme!r}: one of {SBDF_SCHEMES + CN_SCHEMES + RK_SCHEMES}")
         self.scheme, self.dt = scheme, float(dt)
         self.dev = device_problem or DeviceProblem(problem, precision, factor_sets=factor_sets)
+        # FP32 form: refinement passes per solve. The CN family carries -b_1 L X_n of the previous
+        # step with a weight comparable to the implicit one, and with it the previous pressure (the
+        # odd-even pressure mode of CNAB2 starts from any state that is not in balance); one pass
+        # leaves its solve error in the pressure (3e-6 relative after 20 CNAB2 steps of RB 64x64),
+        # two passes bring it to the FP32 F's own level (3e-8)
+        if refine is not None:
+            self.dev.refine = max(1, int(refine))
+        elif self.family == "cn":
+            self.dev.refine = 2
         z = self.dev.zeros
         self.X, self.R = z(), z()
         nh = self.ring if self.family != "rk" else 0
@@ -893,7 +905,7 @@ class IVPSolver:
         f = 2 * nb + 2 + 2 + (2 if d >= 2 else 0) + 1 + (1 if dev.has_b0 else 0)
         dense = bool(dev._factors) and all(getattr(h, "schedule", 0) < 0 for fs in dev._factors.values() for h in fs)
         one = (nb if dense else 1) if dev.compact else nb
-        solve = one if dev.precision == "fp64" else 2 * one + nb
+        solve = one if dev.precision == "fp64" else one + dev.refine * (one + nb)
         if self.family == "sbdf":
             return nb + f + 1 + solve
         if self.family == "cn":
