@@ -259,7 +259,7 @@ def run_gpu(args):
         "gpu_launches": solver.launches_per_step() * args.steps,
         "clocks": clk.summary(),
     }
-    if args.precision == "fp32" and rank == 0:
+    if args.precision == "fp32" and rank == 0 and args.error_steps > 0:
         out["error_vs_fp64"] = mixed_error(P, C0, cfg, args.error_steps)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, P, C0)

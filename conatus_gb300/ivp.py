@@ -111,8 +111,15 @@ class DeviceProblem:
                 t0 = int(np.nonzero(np.all(b.monos == 0, axis=1))[0][0])
                 mc = b.Mc[t0].astype(np.complex128)
                 if np.all(mc.imag == 0):       # real mass matrix: the real-valued kernel
+                    # M X runs over M's own nonzeros (the bucket pattern is that of a M + b L: on
+                    # the channel two thirds of it are zeros of M)
+                    keep = mc.real != 0
+                    rows = np.repeat(np.arange(b.n), np.diff(b.indptr))
+                    ipM = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=b.n))])
                     self._M.append((torch.as_tensor(mc, device=self.device),
-                                    torch.as_tensor(np.ascontiguousarray(mc.real), device=self.device)))
+                                    torch.as_tensor(np.ascontiguousarray(mc.real[keep]), device=self.device),
+                                    torch.as_tensor(ipM.astype(np.int32), device=self.device),
+                                    torch.as_tensor(b.indices[keep].astype(np.int32), device=self.device)))
                 else:
                     self._M.append((torch.as_tensor(mc, device=self.device), 0))
             else:
@@ -269,11 +276,12 @@ class DeviceProblem:
         s = _stream_handle(stream)
         for bi, b in enumerate(self.tpl.buckets):
             ip, ix = self._pat[bi]
-            vals, per = self._M[bi]
-            if not isinstance(per, int):                 # shared real values
-                call("cng_csr_matvec_real", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), per.data_ptr(),
+            if len(self._M[bi]) == 4:                    # shared real values on M's own pattern
+                _, mv, ipM, ixM = self._M[bi]
+                call("cng_csr_matvec_real", self.nsys[bi], b.n, ipM.data_ptr(), ixM.data_ptr(), mv.data_ptr(),
                      self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
                 continue
+            vals, per = self._M[bi]
             call("cng_csr_matvec", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), vals.data_ptr(), per,
                  self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
 
@@ -295,7 +303,7 @@ class DeviceProblem:
                     self._factors.pop(next(iter(self._factors)))     # oldest set (its handles free on drop)
             vals_all = []
             for bi, b in enumerate(self.tpl.buckets):
-                Mv, per = self._M[bi]
+                Mv, per = self._M[bi][:2]
                 per = per if isinstance(per, int) else 0
                 vals_all.append((a * (Mv if per else Mv.unsqueeze(0)) + b_ * self._Lvals(bi)).contiguous())
             torch.cuda.current_stream(self.device).synchronize()    # the values come from torch's stream
@@ -376,7 +384,7 @@ class DeviceProblem:
             kind, data = self._residual_data(bi)
             key = (float(a), float(b_))
             if kind == "values" and key not in data:
-                Mv, per = self._M[bi]
+                Mv, per = self._M[bi][:2]
                 per = per if isinstance(per, int) else 0
                 data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
                              b_ * self._Lvals(bi)).contiguous()
@@ -398,7 +406,7 @@ class DeviceProblem:
                 continue
             key = (float(a), float(b_))
             if key not in data:
-                Mv, per = self._M[bi]
+                Mv, per = self._M[bi][:2]
                 per = per if isinstance(per, int) else 0
                 data[key] = (a * (Mv if per else Mv.unsqueeze(0).expand(self.nsys[bi], -1)) +
                              b_ * self._Lvals(bi)).contiguous()
