@@ -202,12 +202,47 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
 }
 
 // ------------------------------------------------------------------------------------------------
+// Derivative expansion fused into the load of a backward transform (fields that differ only by a
+// derivative along the transform's axis share the transforms before it): output group og of the
+// batch reads input group src[og] and multiplies each value by (i k_j)^ord[og], k_j the wavenumber
+// of its index j along the axis, from a table [order - 1][nidx] rounded to R on the host. Outer row
+// o = (c nout + og) per + r reads row (c nin + src[og]) per + r.
+template <class R>
+struct Expand {
+    int nout = 0;                 // 0: no expansion (row o reads row o)
+    int nin = 0, per = 1, nidx = 0;
+    const int* src = nullptr;
+    const int* ord = nullptr;
+    const c2<R>* tab = nullptr;
+};
+
+// the source row of outer row o and its factor table (nullptr: no derivative)
+template <class R>
+__device__ __forceinline__ long long expand_row(const Expand<R>& ex, long long o, const c2<R>** wt) {
+    *wt = nullptr;
+    if (ex.nout == 0) return o;
+    const long long g = o / ex.per;
+    const long long r = o - g * ex.per;
+    const long long c = g / ex.nout;
+    const int og = (int)(g - c * ex.nout);
+    const int od = ex.ord[og];
+    if (od > 0) *wt = ex.tab + (size_t)(od - 1) * ex.nidx;
+    return (c * ex.nin + ex.src[og]) * ex.per + r;
+}
+
+// w v with w = (i k)^o (the product of the separate expansion pass)
+template <class R>
+__device__ __forceinline__ c2<R> ikmul(c2<R> w, c2<R> v) {
+    return mk<R>(w.x * v.x - w.y * v.y, w.x * v.y + w.y * v.x);
+}
+
+// ------------------------------------------------------------------------------------------------
 // complex FFT along a strided axis: data [outer][len][inner]. Backward: compact spectrum of Nc
 // entries (fftfreq order, Nyquist entry Nc/2 ignored) -> L grid points, unnormalized inverse.
 // Forward: L points -> compact Nc (|k| < Nc/2, Nyquist set to 0), scaled 1/L.
 template <class R>
 __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long outer, int inner,
-                           int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
+                           int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g, Expand<R> ex) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int L = plan.L, LS = L + 1;        // padded rows: the column-wise staging is conflict-free
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -222,7 +257,8 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     const int K = Nc / 2;
     const int lin = forward ? L : Nc;
     const int lout = forward ? Nc : L;
-    const c2<R>* src = in + o * (long long)lin * inner;
+    const c2<R>* wt;
+    const c2<R>* src = in + (forward ? o : expand_row<R>(ex, o, &wt)) * (long long)lin * inner;
     c2<R>* dst = out + o * (long long)lout * inner;
     if (!forward) {
         for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
@@ -231,7 +267,8 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
             const int k = dB.div(e), t = e - k * B;
             if (i0 + t >= inner || k == K) continue;
             const int slot = k < K ? k : L - (Nc - k);
-            b0[(size_t)t * LS + slot] = src[(long long)k * inner + i0 + t];
+            const c2<R> v = src[(long long)k * inner + i0 + t];
+            b0[(size_t)t * LS + slot] = wt ? ikmul<R>(wt[k], v) : v;
         }
     } else {
         for (int e = tid; e < B * L; e += nt) {
@@ -264,7 +301,8 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
 // real -> modes 0..K-1, scaled 1/L.
 template <class R>
 __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out_, long long outer, int inner,
-                            int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g) {
+                            int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g,
+                            Expand<R> ex) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int L = plan.L, LS = L + 1;
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -278,7 +316,8 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     const long long o = blockIdx.x / chunks;
     const int p0 = (blockIdx.x - o * chunks) * B;     // first pair
     if (!forward) {
-        const c2<R>* src = static_cast<const c2<R>*>(in_) + o * (long long)K * inner;
+        const c2<R>* wt;
+        const c2<R>* src = static_cast<const c2<R>*>(in_) + expand_row<R>(ex, o, &wt) * (long long)K * inner;
         R* dst = static_cast<R*>(out_) + o * (long long)L * inner;
         for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
         __syncthreads();
@@ -289,6 +328,11 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             if (p >= pairs) continue;
             c2<R> A = src[(long long)k * inner + 2 * p];
             c2<R> Bv = 2 * p + 1 < inner ? src[(long long)k * inner + 2 * p + 1] : mk<R>(0, 0);
+            if (wt) {
+                const c2<R> w = wt[k];
+                A = ikmul<R>(w, A);
+                Bv = ikmul<R>(w, Bv);
+            }
             if (k == 0) {
                 b0[(size_t)t * LS] = mk<R>(A.x - Bv.y, A.y + Bv.x);
             } else {
@@ -500,54 +544,6 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     }
 }
 
-// (i k)^o v: o quarter turns and the magnitude k^o
-template <class R>
-__device__ __forceinline__ c2<R> ik_pow(c2<R> v, double k, int o) {
-    double fr = 1.0, fi = 0.0;
-    for (int q = 0; q < o; ++q) { const double t = fr; fr = -fi * k; fi = t * k; }
-    const R a = R(fr), b = R(fi);
-    return mk<R>(a * v.x - b * v.y, a * v.y + b * v.x);
-}
-
-// z-groups from y-groups on the z spectrum: Z[c ngz + gz][kx][slot][:] = (i kz(slot))^oz Y[c ngy +
-// zg_y[gz]][kx][slot][:], kz(slot) = 2 pi fftfreq(slot, Nzc) / lz. One block per row of my values.
-template <class R>
-__global__ void k_expand_z(RhsDev d, const c2<R>* __restrict__ Y, c2<R>* __restrict__ Z, int my) {
-    const long long rows = (long long)d.ncase * d.ngz * d.Kx * d.Nzc;
-    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-        long long t = row;
-        const int slot = (int)(t % d.Nzc); t /= d.Nzc;
-        const int jx = (int)(t % d.Kx); t /= d.Kx;
-        const int gz = (int)(t % d.ngz);
-        const long long c = t / d.ngz;
-        const int oz = d.zg_oz[gz];
-        const long long src = (((c * d.ngy + d.zg_y[gz]) * d.Kx + jx) * d.Nzc + slot) * my;
-        const int jz = slot < d.Nzc / 2 ? slot : slot - d.Nzc;
-        const double kz = 6.283185307179586476925286766559 * jz / d.lz;
-        for (int i = threadIdx.x; i < my; i += blockDim.x)
-            Z[row * my + i] = oz ? ik_pow<R>(Y[src + i], kz, oz) : Y[src + i];
-    }
-}
-
-// factors from z-groups (or y-groups without a z direction) on the x spectrum:
-// X[c nf + f][kx][:] = (i kx)^ox Z[c ngz + f_z[f]][kx][:], kx = 2 pi jx / lx.
-template <class R>
-__global__ void k_expand_x(RhsDev d, const c2<R>* __restrict__ Z, c2<R>* __restrict__ X, long long inner) {
-    const long long rows = (long long)d.ncase * d.nfactors * d.Kx;
-    for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
-        const int jx = (int)(row % d.Kx);
-        const long long t = row / d.Kx;
-        const int f = (int)(t % d.nfactors);
-        const long long c = t / d.nfactors;
-        const int ox = d.factors[5 * f + 2];
-        const long long src = ((c * d.ngz + d.f_z[f]) * d.Kx + jx) * inner;
-        const double kx = 6.283185307179586476925286766559 * jx / d.lx;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < inner;
-             i += (long long)gridDim.x * blockDim.x)
-            X[row * inner + i] = ox ? ik_pow<R>(Z[src + i], kx, ox) : Z[src + i];
-    }
-}
-
 // products on the grid: out_o = sum_m c_m prod_j G_j. The monomial tables are staged in shared
 // memory; a thread takes V consecutive points (one 16-byte load per factor field: V = 4 in FP32,
 // 2 in FP64), which needs P % V == 0 (else V = 1).
@@ -755,7 +751,7 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
 
 template <class R>
 void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, int Nc, int L, bool forward,
-                     cudaStream_t st, int maxseq = 0, int threads = 0) {
+                     cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
@@ -765,13 +761,13 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * ((inner + B - 1) / B);
-    k_fft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw);
+    k_fft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw, ex);
     CNG_LAUNCH("k_fft_axis");
 }
 
 template <class R>
 void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int K, int L, bool forward,
-                      cudaStream_t st, int maxseq = 0, int threads = 0) {
+                      cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
     static std::once_flag f1;
@@ -781,7 +777,7 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
     const long long blocks = outer * (((inner + 1) / 2 + B - 1) / B);
-    k_rfft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw);
+    k_rfft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw, ex);
     CNG_LAUNCH("k_rfft_axis");
 }
 
@@ -816,6 +812,10 @@ struct Rhs {
     void* W1 = nullptr;
     void* W2 = nullptr;
     size_t S_bytes = 0, W_bytes = 0;
+    // shared transforms: (i k)^o tables along z (Nzc slots) and x (Kx modes), ox per factor
+    void* ktab_z = nullptr;
+    void* ktab_x = nullptr;
+    int* f_ox = nullptr;
 
     ~Rhs() {
         for (void* p : owned) cudaFree(p);
@@ -854,13 +854,12 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     // 3. z: the z-groups ((i kz)^oz of their y-group), then the z backward transform
     //    [ngz Kx][Nzc][my] -> [ngz Kx][mz][my]
     if (ndir == 2) {
+        Expand<R> ez{};
         if (dev.share) {
-            const long long rows = (long long)ngz * Kx * Nzc;
-            k_expand_z<R><<<(unsigned)std::min<long long>(rows, 152LL * 64), 128, 0, st>>>(dev, cur, other, my);
-            CNG_LAUNCH("k_expand_z");
-            std::swap(cur, other);
+            ez.nout = dev.ngz; ez.nin = dev.ngy; ez.per = Kx; ez.nidx = Nzc;
+            ez.src = dev.zg_y; ez.ord = dev.zg_oz; ez.tab = static_cast<const C*>(ktab_z);
         }
-        launch_fft_axis<R>(cur, other, (long long)ngz * Kx, my, Nzc, mz, false, st, maxseq, threads);
+        launch_fft_axis<R>(cur, other, (long long)ngz * Kx, my, Nzc, mz, false, st, maxseq, threads, ez);
         std::swap(cur, other);
     }
     // 4. x: the factors ((i kx)^ox of their z-group), then the x backward (c2r) transform
@@ -868,15 +867,12 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     const long long inner = (long long)(ndir == 2 ? mz : 1) * my;
     R* G = reinterpret_cast<R*>(cur);
     if (ndir >= 1) {
+        Expand<R> exx{};
         if (dev.share) {
-            const long long rows = (long long)nf * Kx;
-            const unsigned gx = (unsigned)std::min<long long>((inner + 255) / 256, 64);
-            const unsigned gy = (unsigned)std::min<long long>(rows, 65535);
-            k_expand_x<R><<<dim3(gx, gy), 256, 0, st>>>(dev, cur, other, inner);
-            CNG_LAUNCH("k_expand_x");
-            std::swap(cur, other);
+            exx.nout = nfactors; exx.nin = dev.ngz; exx.per = 1; exx.nidx = Kx;
+            exx.src = dev.f_z; exx.ord = f_ox; exx.tab = static_cast<const C*>(ktab_x);
         }
-        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq, threads);
+        launch_rfft_axis<R>(cur, other, nf, (int)inner, Kx, mx, false, st, maxseq, threads, exx);
         G = reinterpret_cast<R*>(other);
         std::swap(cur, other);
     } else {
@@ -1008,6 +1004,37 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
         dv.zg_y = h->keep(upload(zy.data(), zy.size()));
         dv.zg_oz = h->keep(upload(zoz.data(), zoz.size()));
         dv.f_z = h->keep(upload(fz.data(), fz.size()));
+        if (dv.share) {
+            // (i k)^o per index along z (compact fftfreq slots) and x (modes 0..Kx-1), o = 1..max,
+            // in the transform precision: fr + i fi by o quarter turns of k in double, then rounded
+            std::vector<int> ox(h->nfactors);
+            int maxz = 0, maxx = 0;
+            for (int f = 0; f < h->nfactors; ++f) { ox[f] = D->factors[5 * f + 2]; maxx = std::max(maxx, ox[f]); }
+            for (int o : zoz) maxz = std::max(maxz, o);
+            auto table = [&](int nidx, int maxo, bool zaxis) -> void* {
+                std::vector<double> re((size_t)std::max(1, maxo) * nidx), im(re.size());
+                for (int o = 1; o <= maxo; ++o)
+                    for (int j = 0; j < nidx; ++j) {
+                        const int jj = zaxis ? (j < nidx / 2 ? j : j - nidx) : j;
+                        const double k = 6.283185307179586476925286766559 * jj / (zaxis ? h->lz : h->lx);
+                        double fr = 1.0, fi = 0.0;
+                        for (int q = 0; q < o; ++q) { const double t = fr; fr = -fi * k; fi = t * k; }
+                        re[(size_t)(o - 1) * nidx + j] = fr;
+                        im[(size_t)(o - 1) * nidx + j] = fi;
+                    }
+                if (h->precision) {
+                    std::vector<float2> t(re.size());
+                    for (size_t i = 0; i < re.size(); ++i) t[i] = make_float2((float)re[i], (float)im[i]);
+                    return h->keep(upload(t.data(), t.size()));
+                }
+                std::vector<double2> t(re.size());
+                for (size_t i = 0; i < re.size(); ++i) t[i] = make_double2(re[i], im[i]);
+                return h->keep(upload(t.data(), t.size()));
+            };
+            if (h->ndir == 2) h->ktab_z = table(h->Nzc, maxz, true);
+            h->ktab_x = table(h->Kx, maxx, false);
+            h->f_ox = h->keep(upload(ox.data(), ox.size()));
+        }
     }
     dv.out_lam = h->keep(upload(D->out_lam, (size_t)h->noutputs));
     dv.out_mono_ptr = h->keep(upload(D->out_mono_ptr, (size_t)h->noutputs + 1));
