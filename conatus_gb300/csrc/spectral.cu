@@ -599,21 +599,39 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
 #pragma unroll
             for (int v = 0; v < V; ++v) acc[v] = R(0);
             for (int mi = s_ptr[o]; mi < s_ptr[o + 1]; ++mi) {
-                R t[V];
+                // c G_a (G_b G_c G_d): the product of the later factors, then one fused
+                // multiply-add with the first factor times c (c = +-1 costs nothing)
+                const R cf = s_coef[mi];
+                R pr[V];
+                bool have = false;
 #pragma unroll
-                for (int v = 0; v < V; ++v) t[v] = s_coef[mi];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 1; q < 4; ++q) {
                     const int f = s_fac[4 * mi + q];
                     if (f >= 0) {
                         R g[V];
                         load_v<R, V>(Gc + (long long)f * P, g);
 #pragma unroll
-                        for (int v = 0; v < V; ++v) t[v] = t[v] * g[v];
+                        for (int v = 0; v < V; ++v) pr[v] = have ? pr[v] * g[v] : g[v];
+                        have = true;
                     }
                 }
+                const int f0 = s_fac[4 * mi];
+                R a[V];
+                if (f0 >= 0) {
+                    load_v<R, V>(Gc + (long long)f0 * P, a);
+                    if (cf == R(-1)) {
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc[v] = acc[v] + t[v];
+                        for (int v = 0; v < V; ++v) a[v] = -a[v];
+                    } else if (cf != R(1)) {
+#pragma unroll
+                        for (int v = 0; v < V; ++v) a[v] = cf * a[v];
+                    }
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) a[v] = cf;
+                }
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v] = have ? fmar(a[v], pr[v], acc[v]) : acc[v] + a[v];
             }
             store_v<R, V>(Oc + (long long)o * P, acc);
         }
