@@ -1938,13 +1938,26 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              220 * 1024);
     });
-    // one warp count for all blocks: the largest that fits every bucket, and no more than it takes
-    // to give every SM a block (a small batch spreads over the SMs: each SM's FP64 pipe and shared
-    // memory serve fewer sweeps)
-    int nw = 8, total = 0;
-    for (const Banded* h : hs) {
-        while (nw > 1 && compact_smem<TF>(*h, nw, sched) > 220 * 1024) --nw;
-        total += h->cWg;
+    // one warp count for all blocks: the one that keeps the most warps resident per SM (blocks per
+    // SM are bounded by their shared memory: eight warps in one block can lose to seven in two),
+    // and no more than it takes to give every SM a block (a small batch spreads over the SMs: each
+    // SM's FP64 pipe and shared memory serve fewer sweeps)
+    auto smem_of = [&](int w) {
+        size_t m = 0;
+        for (const Banded* h : hs) m = std::max(m, compact_smem<TF>(*h, w, sched));
+        return m;
+    };
+    int total = 0;
+    for (const Banded* h : hs) total += h->cWg;
+    int nw = 1, resident = 0;
+    for (int w = 1; w <= 8; ++w) {
+        const size_t m = smem_of(w);
+        if (m > 220 * 1024) break;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_compact_multi<TF, TD, IO, CH, ST>, 32 * w,
+                                                          m) != cudaSuccess)
+            per_sm = 1;
+        if (per_sm * w >= resident) { resident = per_sm * w; nw = w; }
     }
     nw = std::min(nw, std::max(1, ceil_div(total, sm_count())));
     size_t smem = 0;
