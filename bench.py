@@ -145,6 +145,60 @@ TRAFFIC_PER_SYSTEM = {
 }
 
 
+# DRAM bytes of one x backward real transform of the factor fields (k_rfft_axis<double>), from the
+# ncu capture of the channel 64x129x64 (12 fields, 32 modes -> 96 points, 96 x 200 columns), and
+# the algorithmic bytes of that launch: the full launch's traffic is scaled by the algorithmic
+# bytes (the transform streams each field once: traffic grows with the lines)
+RFFT_TRAFFIC = (None, None, "profiles/k_rfft_axis_channel64x129x64_fp64.md")
+FP64_NOMINAL_TFLOPS = 1.25     # GB300 FP64 (2 DFMA per clock per SM): nominal, not measured
+
+
+def rfft_roofline(dev, stream, hbm_peak, peak_kind, reps=5):
+    """Roofline of the FP64 step's dominant kernel: the x backward real transform of every factor
+    field (k_rfft_axis<double>), launched alone through cng_rfft_axis with the step's shapes.
+    Algorithmic bytes: K complex modes read and L reals written per column and field. FLOPs: the
+    conventional 2.5 L log2 L per real transform of length L. The kernel is bound by the FP64 pipe
+    (GB300 issues FP64 at 1/64 of the FP32 rate), so its HBM fraction is low by construction; the
+    FP64 fraction is against the nominal FP64 peak."""
+    import math
+    import torch
+    from conatus_gb300._lib import call
+    g = dev.grid
+    nf = len(dev.tpl.factors) * int(getattr(dev.P, "ncase", 1))
+    K = dev.P.fourier_sizes[0] // 2
+    inner = max(g["mz"], 1) * max(g["my"], 1)
+    L = g["mx"]
+    x = torch.zeros(nf * K * inner, dtype=torch.complex128, device="cuda")
+    y = torch.zeros(nf * L * inner, dtype=torch.float64, device="cuda")
+    x.real.normal_()
+    x.imag.normal_()
+    sh = stream.cuda_stream
+    torch.cuda.synchronize()
+    call("cng_rfft_axis", 0, x.data_ptr(), y.data_ptr(), nf, inner, K, L, sh)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call("cng_rfft_axis", 0, x.data_ptr(), y.data_ptr(), nf, inner, K, L, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = nf * inner * (16 * K + 8 * L)
+    flops = nf * inner * 2.5 * L * math.log2(L)
+    achieved = nbytes / (ms / 1e3) / 1e9
+    small_traffic, small_bytes, src = RFFT_TRAFFIC
+    traffic = small_traffic * nbytes / small_bytes if small_traffic else None
+    del x, y
+    return {"kernel": f"k_rfft_axis<double> (x backward, {nf} factor fields, {K} modes -> {L} points, "
+                      f"{inner} columns), launched alone",
+            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+            "traffic": traffic, "traffic_source": (src + " (scaled by algorithmic bytes)") if traffic else None,
+            "algorithmic_bytes": nbytes, "launch_ms": ms, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "binding_roof": {"pipe": "fp64", "achieved_tflops": flops / (ms / 1e3) / 1e12,
+                             "peak_tflops": FP64_NOMINAL_TFLOPS, "peak_kind": "nominal",
+                             "frac": flops / (ms / 1e3) / 1e12 / FP64_NOMINAL_TFLOPS,
+                             "flops": flops, "flop_count": "2.5 L log2 L per real transform"}}
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = _dist()
@@ -211,13 +265,21 @@ def run_gpu(args):
     sb = solve_bytes(dev, fs)
     nsys = sum(h.batch for h in fs)
     tr = TRAFFIC_PER_SYSTEM.get((args.config, args.precision)) if args.fourier is None else None
-    roof = {"kernel": "k_solve_compact_multi (batched bordered-banded solve, all buckets in one launch)",
+    solve_roof = {"kernel": "k_solve_compact_multi (batched bordered-banded solve, all buckets in one launch)",
             "bound": "hbm", "achieved": sb / (solve_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
             "frac": sb / (solve_ms / 1e3) / 1e9 / hbm_peak,
             "traffic": tr[0] * nsys if tr else None,
             "traffic_source": (tr[1] + " (bytes per system x systems)") if tr else None,
             "algorithmic_bytes": sb, "launch_ms": solve_ms, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "F_ms": f_ms}
+    # the dominant kernel: the batched solve (two launches per step in the FP32 form), unless the
+    # x backward real transform takes longer (the FP64 channel: FP64-pipe bound)
+    roof = solve_roof
+    if args.precision == "fp64" and dev.d >= 1:
+        rf = rfft_roofline(dev, s, hbm_peak, peak_kind)
+        if rf["launch_ms"] > solve_ms:
+            roof = rf
+            roof["F_ms"] = f_ms
     sbytes = step_bytes(dev, solver)
     step_roof = {"bytes_per_step": sbytes, "achieved": sbytes["total"] / (ms_step / 1e3) / 1e9,
                  "unit": "GB/s", "frac": sbytes["total"] / (ms_step / 1e3) / 1e9 / hbm_peak}
@@ -253,6 +315,7 @@ def run_gpu(args):
                                       if dev.rhs_tuning else None)},
         "mode_updates_per_s": value * P.real_unknowns(),
         "roofline": roof,
+        "solve_roofline": solve_roof,
         "step_roofline": step_roof,
         "e2e": {"value": ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},

@@ -66,14 +66,16 @@ FftPlan make_plan(int L) {
 
 // ---- twiddle tables (host double precision, uploaded once per length and precision) ----------
 // kind 0: exp(-2 pi i q / L), q < L (FFT twiddles); kind 1: exp(-i pi k / (2L)), k < L (the
-// Makhoul post-twiddles of the Chebyshev transforms). Angles reduced in long double.
+// Makhoul post-twiddles of the Chebyshev transforms); kind 2: (-1)^k / 2 exp(+i pi k / (2L)) (the
+// backward pre-twiddles with the sign of a_k = (-1)^k c_k and the factor 1/2 folded in: exact
+// scalings, so the product is the one of the separate steps). Angles reduced in long double.
 template <class R>
 struct TwiddleCache {
     std::mutex mu;
     std::vector<std::pair<long long, c2<R>*>> tables;
     const c2<R>* get(int L, int kind = 0) {
         std::lock_guard<std::mutex> lock(mu);
-        const long long key = (long long)L * 2 + kind;
+        const long long key = (long long)L * 4 + kind;
         for (auto& t : tables)
             if (t.first == key) return t.second;
         std::vector<c2<R>> h(L);
@@ -82,6 +84,11 @@ struct TwiddleCache {
             const long double ang = kind == 0 ? -2.0L * pi * q / L : -pi * q / (2.0L * L);
             h[q].x = static_cast<R>(cosl(ang));
             h[q].y = static_cast<R>(sinl(ang));
+            if (kind == 2) {
+                const R sc = (q & 1) ? R(-0.5) : R(0.5);
+                h[q].x = sc * h[q].x;
+                h[q].y = -sc * h[q].y;
+            }
         }
         c2<R>* d = nullptr;
         CNG_CUDA(cudaMalloc(&d, sizeof(c2<R>) * L));
@@ -123,14 +130,12 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         const int t = dM1.div(e), k = e - t * (M + 1);
         const long long col = col0 + t;
         c2<R> v = mk<R>(0, 0);
-        if (col < ncols && k < N) {
-            v = in[col * N + k];
-            if (k & 1) v = mk<R>(-v.x, -v.y);          // a_k = c_k (-1)^k
-        }
+        if (col < ncols && k < N) v = in[col * N + k];     // c_k (the sign of a_k is in tq)
         a[e] = v;
     }
     __syncthreads();
-    // Z_k = 1/2 e^{i pi k / (2M)} (a_k - i a_{M-k}), Z_0 = a_0
+    // Z_k = 1/2 e^{i pi k / (2M)} (a_k - i a_{M-k}) = tq_k (c_k - i c_{M-k}) with a_k = (-1)^k c_k
+    // (M even) and tq_k = (-1)^k / 2 e^{i pi k / (2M)}; Z_0 = a_0 = c_0
     for (int e = tid; e < B * M; e += nt) {
         const int t = dM.div(e), k = e - t * M;
         const c2<R>* at = a + (size_t)t * (M + 1);
@@ -139,8 +144,8 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
             z = at[0];
         } else {
             c2<R> u = at[k], w = at[M - k];
-            c2<R> d = mk<R>(u.x + w.y, u.y - w.x);     // a_k - i a_{M-k}
-            z = scl<R>(R(0.5), mul<R>(conjg<R>(tq[k]), d));   // e^{+i pi k / (2M)}
+            c2<R> d = mk<R>(u.x + w.y, u.y - w.x);     // c_k - i c_{M-k}
+            z = mul<R>(tq[k], d);
         }
         b0[e] = z;
     }
@@ -185,7 +190,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     }
     __syncthreads();
     c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, M);
-    const R invM = R(1) / R(M);
+    const R invM = R(1) / R(M), invMh = invM * R(0.5);
     for (int e = tid; e < B * N; e += nt) {
         const int t = dN.div(e), k = e - t * N;
         const long long col = col0 + t;
@@ -195,8 +200,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         const c2<R> w = tq[k];                         // e^{-i pi k / (2M)}
         R re = mul<R>(w, add<R>(zk, zm)).x;
         R im = mul<R>(w, sub<R>(zk, zm)).y;
-        R sg = (k & 1) ? -invM : invM;
-        if (k == 0) sg *= R(0.5);
+        const R sg = k == 0 ? invMh : ((k & 1) ? -invM : invM);
         out[col * N + k] = mk<R>(re * sg, im * sg);
     }
 }
@@ -580,12 +584,16 @@ template <class R, int V>
 __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
     __shared__ int s_ptr[17];
     __shared__ R s_coef[kMaxMono];
+    __shared__ int s_kind[kMaxMono];         // 1: coefficient +1, -1: coefficient -1, 0: other
     __shared__ int s_fac[4 * kMaxMono];
     const int no = d.noutputs;
     for (int q = threadIdx.x; q <= no; q += blockDim.x) s_ptr[q] = d.out_mono_ptr[q];
     __syncthreads();
     const int nm = s_ptr[no];
-    for (int q = threadIdx.x; q < nm; q += blockDim.x) s_coef[q] = R(d.mono_coef[q]);
+    for (int q = threadIdx.x; q < nm; q += blockDim.x) {
+        s_coef[q] = R(d.mono_coef[q]);
+        s_kind[q] = d.mono_coef[q] == 1.0 ? 1 : (d.mono_coef[q] == -1.0 ? -1 : 0);
+    }
     for (int q = threadIdx.x; q < 4 * nm; q += blockDim.x) s_fac[q] = d.mono_fac[q];
     __syncthreads();
     const long long total = P * d.ncase;
@@ -600,8 +608,10 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
             for (int v = 0; v < V; ++v) acc[v] = R(0);
             for (int mi = s_ptr[o]; mi < s_ptr[o + 1]; ++mi) {
                 // c G_a (G_b G_c G_d): the product of the later factors, then one fused
-                // multiply-add with the first factor times c (c = +-1 costs nothing)
+                // multiply-add with the first factor times c (c = +-1: the sign goes into the
+                // fused multiply-add; the kind of c is read, not compared, per point)
                 const R cf = s_coef[mi];
+                const int kind = s_kind[mi];
                 R pr[V];
                 bool have = false;
 #pragma unroll
@@ -610,8 +620,13 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
                     if (f >= 0) {
                         R g[V];
                         load_v<R, V>(Gc + (long long)f * P, g);
+                        if (have) {
 #pragma unroll
-                        for (int v = 0; v < V; ++v) pr[v] = have ? pr[v] * g[v] : g[v];
+                            for (int v = 0; v < V; ++v) pr[v] = pr[v] * g[v];
+                        } else {
+#pragma unroll
+                            for (int v = 0; v < V; ++v) pr[v] = g[v];
+                        }
                         have = true;
                     }
                 }
@@ -619,10 +634,7 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
                 R a[V];
                 if (f0 >= 0) {
                     load_v<R, V>(Gc + (long long)f0 * P, a);
-                    if (cf == R(-1)) {
-#pragma unroll
-                        for (int v = 0; v < V; ++v) a[v] = -a[v];
-                    } else if (cf != R(1)) {
+                    if (kind == 0) {
 #pragma unroll
                         for (int v = 0; v < V; ++v) a[v] = cf * a[v];
                     }
@@ -630,8 +642,19 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
 #pragma unroll
                     for (int v = 0; v < V; ++v) a[v] = cf;
                 }
+                if (have && f0 >= 0 && kind < 0) {
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc[v] = have ? fmar(a[v], pr[v], acc[v]) : acc[v] + a[v];
+                    for (int v = 0; v < V; ++v) acc[v] = fmar(-a[v], pr[v], acc[v]);
+                } else if (have) {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v] = fmar(a[v], pr[v], acc[v]);
+                } else if (f0 >= 0 && kind < 0) {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v] = acc[v] - a[v];
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v] = acc[v] + a[v];
+                }
             }
             store_v<R, V>(Oc + (long long)o * P, acc);
         }
@@ -758,7 +781,7 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
     if (M % 2) throw InvalidArgument("Chebyshev grid size must be even");
     FftPlan plan = make_plan(M);
     const c2<R>* tw = twiddles<R>().get(M, 0);
-    const c2<R>* tq = twiddles<R>().get(M, 1);
+    const c2<R>* tq = twiddles<R>().get(M, forward ? 1 : 2);
     const int B = pick_B<R>(M, forward ? 0 : M + 1, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
     const size_t smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
     const long long blocks = (ncols + B - 1) / B;
