@@ -156,6 +156,7 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
 // Thread mapping: a warp takes one row i for 32 systems (lane = system), so every lane of a warp
 // runs the same entry list (uniform trip counts: the border rows have up to n entries, the others
 // a dozen) and the entry data is one broadcast load per warp; x is gathered per lane.
+template <bool CONE>
 __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                  const double* __restrict__ val, const signed char* __restrict__ code,
                                  const double* __restrict__ mono, int nmono, double a, double c,
@@ -191,7 +192,7 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
                     gi = fma(v, xv.y, gi);
                 }
             }
-            const double sc = tt < 0 ? a : c * mv[tt];
+            const double sc = tt < 0 ? a : (CONE ? mv[tt] : c * mv[tt]);     // c = 1: no multiply
             ar = fma(sc, gr, ar);
             ai = fma(sc, gi, ai);
         }
@@ -266,9 +267,14 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
         if ((long long)((nsys + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("split_residual: batch too large");
         const long long threads = (long long)((nsys + 31) / 32) * n * 32;
         const int blk = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
-        k_split_residual<<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
-            static_cast<const double2*>(b), static_cast<double2*>(r));
+        if (c == 1.0)
+            k_split_residual<true><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+                nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
+                static_cast<const double2*>(b), static_cast<double2*>(r));
+        else
+            k_split_residual<false><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+                nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
+                static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
     })
 }

@@ -593,6 +593,7 @@ class IVPSolver:
             self._Xnew = z()
         self._zero = None
         self._warm = False
+        self._side = None          # side stream of M X (and -L X), beside F
         self.filled, self.head = 0, self.ring - 1
         self.t, self.iteration = 0.0, 0
         self._graphs = {}
@@ -632,11 +633,23 @@ class IVPSolver:
         self.dev.residual(0.0, 1.0, x, self._zero, out, s)
 
     def _push(self, s):
+        """History of the new state: M X (and -L X) on a side stream forked from the step's stream,
+        F on the step's stream, joined before the combination (in a captured step the two become
+        parallel branches of the graph)."""
+        torch = _torch()
+        if self._side is None:
+            self._side = (torch.cuda.Stream(), torch.cuda.Event(), torch.cuda.Event())
+        side, fork, join = self._side
         self.head = (self.head + 1) % self.ring
-        self.dev.MX(self.X, self.MXh[self.head], s)
+        fork.record(self.stream)
+        side.wait_event(fork)
+        hs = side.cuda_stream
+        self.dev.MX(self.X, self.MXh[self.head], hs)
         if self.family == "cn":
-            self._neg_LX(self.X, self.LXh[self.head], s)
+            self._neg_LX(self.X, self.LXh[self.head], hs)
         self.dev.F(self.X, self.Fh[self.head], s)
+        join.record(side)
+        self.stream.wait_event(join)
         self.filled = min(self.filled + 1, self.ring)
 
     def _lincomb(self, base, terms, out, s):
