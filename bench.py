@@ -203,6 +203,19 @@ def rfft_roofline(dev, stream, hbm_peak, peak_kind, reps=5):
                              "flops": flops, "flop_count": "2.5 L log2 L per real transform"}}
 
 
+L2_BYTES = 129e6      # GB300 L2
+
+
+def _l2_note(P, cfg, precision):
+    """Whether the timed steps stream from HBM: the planned device bytes of the run against L2."""
+    from conatus_gb300 import memory
+    nbytes = memory.plan_ivp(P, cfg["scheme"], precision)["total"]
+    if nbytes > L2_BYTES:
+        return f"inputs larger than L2 (state, history and factors: {nbytes / 1e9:.2f} GB planned)"
+    return (f"fits in L2 ({nbytes / 1e6:.1f} MB planned; not flushed between steps: the steps of a "
+            f"small problem run from L2 in use too)")
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = _dist()
@@ -312,7 +325,7 @@ def run_gpu(args):
         "config": {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
                    "real_unknowns": P.real_unknowns(), "systems": int(sum(P.nsys)),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (state, history and factors are GBs)",
+                   "l2": _l2_note(P, cfg, args.precision),
                    "grid": dev.grid, "state_finite": finite,
                    "solve_schedule": _schedule_summary(dev),
                    "rhs_transforms": ({"chosen": min(dev.rhs_tuning, key=lambda k: dev.rhs_tuning[k] or 0),

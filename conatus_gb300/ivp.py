@@ -639,6 +639,11 @@ class IVPSolver:
         self._zero = None
         self._warm = False
         self._side = None          # side stream of M X (and -L X), beside F
+        # fork: M X on a side stream beside F (and, in the FP32 form, the refinement in two bucket
+        # groups on two streams). A caller that keeps many solvers in flight (the serving loop)
+        # turns it off: the device is busy with the other runs, and the extra streams and events
+        # only add dependencies
+        self.fork = True
         self.filled, self.head = 0, self.ring - 1
         self.t, self.iteration = 0.0, 0
         self._graphs = {}
@@ -681,11 +686,19 @@ class IVPSolver:
         """History of the new state: M X (and -L X) on a side stream forked from the step's stream,
         F on the step's stream, joined before the combination (in a captured step the two become
         parallel branches of the graph)."""
+        self.head = (self.head + 1) % self.ring
+        self.dev.overlap_refine = self.fork
+        if not self.fork:
+            self.dev.MX(self.X, self.MXh[self.head], s)
+            if self.family == "cn":
+                self._neg_LX(self.X, self.LXh[self.head], s)
+            self.dev.F(self.X, self.Fh[self.head], s)
+            self.filled = min(self.filled + 1, self.ring)
+            return
         torch = _torch()
         if self._side is None:
             self._side = (torch.cuda.Stream(), torch.cuda.Event(), torch.cuda.Event())
         side, fork, join = self._side
-        self.head = (self.head + 1) % self.ring
         fork.record(self.stream)
         side.wait_event(fork)
         hs = side.cuda_stream

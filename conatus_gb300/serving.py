@@ -151,6 +151,9 @@ class Session:
         # its own: runs in flight do not wait on one another
         self.solver.stream.wait_stream(torch.cuda.current_stream())
         self.solver.join = False
+        if hasattr(self.solver, "fork"):
+            self.solver.fork = False            # runs in flight already fill the device
+            self.solver.dev.overlap_refine = False
         self.footprint = prep.bytes
         self.remaining = req.steps
         self.event = torch.cuda.Event()
