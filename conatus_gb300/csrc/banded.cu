@@ -256,6 +256,30 @@ __device__ void small_getrs(const T* a, const int* piv, T* z, int r) {
     }
 }
 
+// z := S^{-1} z with the small LU staged in shared memory (lane 0; r <= kMaxRUnroll): the
+// pivots are read at once, the factor from shared memory
+constexpr int kMaxRUnroll = 8;
+template <class T>
+__device__ void small_getrs_staged(const T* a, const int* piv, T* z, int r) {
+    int pv[kMaxRUnroll];
+#pragma unroll
+    for (int k = 0; k < kMaxRUnroll; ++k) pv[k] = k < r ? piv[k] : k;
+#pragma unroll
+    for (int k = 0; k < kMaxRUnroll; ++k) {
+        if (k < r && pv[k] != k) {
+            T t = z[k];
+            z[k] = z[pv[k]];
+            z[pv[k]] = t;
+        }
+    }
+    for (int k = 0; k < r; ++k)
+        for (int i = k + 1; i < r; ++i) z[i] = z[i] - a[k * r + i] * z[k];
+    for (int k = r - 1; k >= 0; --k) {
+        z[k] = z[k] * a[k * r + k];
+        for (int i = 0; i < k; ++i) z[i] = z[i] - a[k * r + i] * z[k];
+    }
+}
+
 // 1-norm of an r x r column-major matrix (NaN propagates as in the reference's norm1).
 template <class T>
 __device__ double small_norm1(const T* a, int r) {
@@ -1533,18 +1557,28 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) s_Udist[i] = ix.Udist[i];
     __syncthreads();
     if (!wlive) return;
-    // gather the right-hand side (permuted rows first)
-    for (int i = lg; i < n; i += kLanesPer) {
-        TF v = TF(0.0);
-        if (live) {
-            if constexpr (IO == IO_MIXED) {
-                const zd b = static_cast<const zd*>(io.rhs)[(size_t)sys * n + cd.perm[i]];
-                v = to_zf(b);
-            } else {
-                v = io_load<TF, IO>(io, sys, n, cd.perm[i]);
+    // gather the right-hand side (permuted rows first); four rows per lane in flight (the loads of
+    // one row wait on the permutation, not on the previous row)
+    constexpr int kU = 4;
+    for (int i0 = lg; i0 < n; i0 += kU * kLanesPer) {
+        int pr[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) pr[u] = (live && i0 + u * kLanesPer < n) ? cd.perm[i0 + u * kLanesPer] : -1;
+        TF v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            v[u] = TF(0.0);
+            if (pr[u] >= 0) {
+                if constexpr (IO == IO_MIXED) {
+                    v[u] = to_zf(static_cast<const zd*>(io.rhs)[(size_t)sys * n + pr[u]]);
+                } else {
+                    v[u] = io_load<TF, IO>(io, sys, n, pr[u]);
+                }
             }
         }
-        y[i] = v;
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+            if (i0 + u * kLanesPer < n) y[i0 + u * kLanesPer] = v[u];
     }
     __syncwarp();
     const TF* Lg = cd.L + (size_t)wg * ix.nL * kGroup;
@@ -1639,36 +1673,83 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     }
     // ---------------- Woodbury: z = S^{-1} V^T y, y -= W z
     if (r > 0) {
+        // the small LU of S staged beside z in shared memory (one round trip for all its entries),
+        // when it fits in the 64 slots after the system's vector
+        const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
+        TF* sl = zb + r;
+        if (staged && live)
+            for (int q = lg; q < r * r; q += kLanesPer) sl[q] = cd.slu[(size_t)sys * r * r + q];
         const TF* Vg = cd.V + (size_t)wg * ix.nV * kGroup;
         for (int a = 0; a < r; ++a) {
             TF acc = TF(0.0);
-            for (int e = ix.offV[a] + lg; e < ix.offV[a + 1]; e += kLanesPer)
-                acc = cfma(acc, Vg[(size_t)e * kGroup + g], y[ix.Vcol[e]]);
+            const int ea = ix.offV[a], eb = ix.offV[a + 1];
+            for (int e0 = ea + lg; e0 < eb; e0 += kU * kLanesPer) {
+                int c[kU];
+                TF v[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int e = e0 + u * kLanesPer;
+                    c[u] = e < eb ? ix.Vcol[e] : -1;
+                    v[u] = e < eb ? Vg[(size_t)e * kGroup + g] : TF(0.0);
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                    if (c[u] >= 0) acc = cfma(acc, v[u], y[c[u]]);
+            }
             for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
             if (lg == 0) zb[a] = acc;
         }
         __syncwarp();
-        if (lg == 0 && live) small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        if (lg == 0 && live) {
+            if (staged) small_getrs_staged(sl, cd.spiv + (size_t)sys * r, zb, r);
+            else small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        }
         __syncwarp();
         if (live) {
             const TF* Ws = cd.W + (size_t)sys * r * n;
-            for (int i = lg; i < n; i += kLanesPer) {
-                TF acc = y[i];
-                for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
-                y[i] = acc;
+            if (r <= kMaxRUnroll) {
+                // the r entries of W for a row loaded together, then the r updates
+                for (int i = lg; i < n; i += kLanesPer) {
+                    TF w[kMaxRUnroll];
+#pragma unroll
+                    for (int k = 0; k < kMaxRUnroll; ++k)
+                        if (k < r) w[k] = Ws[(size_t)k * n + i];
+                    TF acc = y[i];
+#pragma unroll
+                    for (int k = 0; k < kMaxRUnroll; ++k)
+                        if (k < r) acc = cfms(acc, w[k], zb[k]);
+                    y[i] = acc;
+                }
+            } else {
+                for (int i = lg; i < n; i += kLanesPer) {
+                    TF acc = y[i];
+                    for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
+                    y[i] = acc;
+                }
             }
         }
         __syncwarp();
     }
     if (!live) return;
-    for (int i = lg; i < n; i += kLanesPer) {
-        if constexpr (IO == IO_MIXED) {
-            zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
-            const zd d(y[i].re, y[i].im);
-            xs[i] = io.accumulate ? xs[i] + d : d;
+    if constexpr (IO == IO_MIXED) {
+        zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
+        if (io.accumulate) {
+            for (int i0 = lg; i0 < n; i0 += kU * kLanesPer) {
+                zd o[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                    if (i0 + u * kLanesPer < n) o[u] = xs[i0 + u * kLanesPer];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = i0 + u * kLanesPer;
+                    if (i < n) xs[i] = o[u] + zd(y[i].re, y[i].im);
+                }
+            }
         } else {
-            io_store<TF, IO>(io, sys, n, i, y[i]);
+            for (int i = lg; i < n; i += kLanesPer) xs[i] = zd(y[i].re, y[i].im);
         }
+    } else {
+        for (int i = lg; i < n; i += kLanesPer) io_store<TF, IO>(io, sys, n, i, y[i]);
     }
 }
 
