@@ -156,12 +156,14 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
 // Thread mapping: a warp takes one row i for 32 systems (lane = system), so every lane of a warp
 // runs the same entry list (uniform trip counts: the border rows have up to n entries, the others
 // a dozen) and the entry data is one broadcast load per warp; x is gathered per lane.
+constexpr int kMergedTerm = 63;          // an entry list shared by several terms: scale per (row, system)
+
 template <bool CONE>
 __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                  const double* __restrict__ val, const signed char* __restrict__ code,
                                  const double* __restrict__ mono, int nmono, double a, double c,
-                                 const double2* __restrict__ x, const double2* __restrict__ b,
-                                 double2* __restrict__ r) {
+                                 const double* __restrict__ rowscale, const double2* __restrict__ x,
+                                 const double2* __restrict__ b, double2* __restrict__ r) {
     const unsigned sysw = ((unsigned)nsys + 31u) >> 5;             // warps of 32 systems per row
     const unsigned nwarps = sysw * (unsigned)n;
     const unsigned lane = threadIdx.x & 31u;
@@ -192,7 +194,9 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
                     gi = fma(v, xv.y, gi);
                 }
             }
-            const double sc = tt < 0 ? a : (CONE ? mv[tt] : c * mv[tt]);     // c = 1: no multiply
+            // c = 1: no multiply; a merged list: its scale per (row, system) (NaN without the table)
+            const double sc = tt == kMergedTerm ? (rowscale ? rowscale[(size_t)i * nsys + m] : __longlong_as_double(0x7ff8000000000000LL))
+                                                : (tt < 0 ? a : (CONE ? mv[tt] : c * mv[tt]));
             ar = fma(sc, gr, ar);
             ai = fma(sc, gi, ai);
         }
@@ -256,8 +260,8 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
 }
 
 int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
-                       const int8_t* code, const double* mono, int nmono, double a, double c, const void* x,
-                       const void* b, void* r, void* stream) {
+                       const int8_t* code, const double* mono, int nmono, double a, double c,
+                       const double* rowscale, const void* x, const void* b, void* r, void* stream) {
     CNG_TRY({
         if (!ptr || !col || !val || !code || (nmono > 0 && !mono) || !x || !b || !r)
             throw InvalidArgument("null device pointer");
@@ -269,11 +273,11 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
         const int blk = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
         if (c == 1.0)
             k_split_residual<true><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-                nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
+                nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
                 static_cast<const double2*>(b), static_cast<double2*>(r));
         else
             k_split_residual<false><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-                nsys, n, ptr, col, val, sc, mono, nmono, a, c, static_cast<const double2*>(x),
+                nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
                 static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
     })

@@ -74,6 +74,9 @@ def _stream_handle(stream) -> int:
     return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
 
 
+SPLIT_MERGED = 63      # code >> 1 of a merged entry list of the split residual (scale per row, system)
+
+
 class DeviceProblem:
     """A problem instance resident on the device (see module docstring)."""
 
@@ -343,12 +346,41 @@ class DeviceProblem:
             if split is None:
                 self._resid[bi] = ("values", {})
             else:
-                ptr, col, val, code, act = split
+                ptr, col, val, code, act, rowsets = split
                 mv = np.stack([terms[k][1] for k in act], axis=1) if act else np.zeros((self.nsys[bi], 1))
                 dv = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt), device=self.device)
                 self._resid[bi] = ("split", (dv(ptr, np.int32), dv(col, np.int32), dv(val, np.float64),
-                                             dv(code, np.int8), dv(mv, np.float64), len(act)))
+                                             dv(code, np.int8), dv(mv, np.float64), len(act), rowsets,
+                                             np.asarray(mv, np.float64), {}))
         return self._resid[bi]
+
+    def _rowscale(self, bi, a, c):
+        """Per-(row, system) scales of the merged entry lists of bucket bi's split residual for
+        (a, c): sum over the row's merged terms of rho_k (a for M, c mono_k(system) for L_k); None
+        when the bucket has no merged rows. Made once per (a, c), outside any capture."""
+        kind, data = self._residual_data(bi)
+        if kind != "split" or not data[6]:
+            return None
+        rowsets, mvh, cache = data[6], data[7], data[8]
+        key = (float(a), float(c))
+        if key not in cache:
+            torch = _torch()
+            tab = self._rowscale_table(rowsets, mvh, self.tpl.buckets[bi].n, a, c)
+            cache[key] = torch.as_tensor(tab, device=self.device)
+            torch.cuda.current_stream(self.device).synchronize()
+        return cache[key]
+
+    @staticmethod
+    def _rowscale_table(rowsets, mvh, n, a, c):
+        """(n, systems) scales of the merged lists: row i, system m: sum over (k, rho) of the row's
+        set of rho (a for k = -1, c mvh[m, k] otherwise); zero for rows without a merged list."""
+        tab = np.zeros((n, mvh.shape[0]))
+        for i, st in rowsets.items():
+            acc = np.zeros(mvh.shape[0])
+            for k, rho in st:
+                acc += rho * (a if k < 0 else c * mvh[:, k])
+            tab[i] = acc
+        return tab
 
     @staticmethod
     def _split_operator(b, lrows):
@@ -370,15 +402,49 @@ class DeviceProblem:
                     ent[rows[p]].append((int(b.indices[p]), v.imag, 2 * k + 1))
                 else:
                     return None
+        # terms of a row with the same columns and proportional values (on the channel: M and the
+        # kx^2 and kz^2 parts of L share the conversion operator) become one entry list with a
+        # per-(row, system) scale sum_k rho_k s_k (code 2 MERGED + imag), computed once per (a, b)
         ptr = np.zeros(b.n + 1, np.int64)
         col, val, code = [], [], []
+        rowsets = {}
         for i in range(b.n):
+            groups = {}
             for c_, v_, cd in ent[i]:
-                col.append(c_)
-                val.append(v_)
-                code.append(cd)
+                groups.setdefault(cd >> 1, []).append((c_, v_, cd & 1))
+            order = list(groups)
+            merged = None
+            for gi, k0 in enumerate(order):
+                base = groups[k0]
+                bc = [e[0] for e in base]
+                bv = np.array([e[1] for e in base])
+                st = [(k0, 1.0)]
+                for k in order[gi + 1:]:
+                    g = groups[k]
+                    if [e[0] for e in g] != bc or any(e[2] != base[0][2] for e in g + base):
+                        continue
+                    gv = np.array([e[1] for e in g])
+                    rho = gv[0] / bv[0]
+                    if np.all(np.abs(gv - rho * bv) <= 1e-15 * np.abs(gv)):
+                        st.append((k, float(rho)))
+                if len(st) > 1:
+                    merged = (k0, st)
+                    break
+            if merged is not None:
+                k0, st = merged
+                rowsets[i] = st
+                for c_, v_, im in groups[k0]:
+                    col.append(c_)
+                    val.append(v_)
+                    code.append(2 * SPLIT_MERGED + im)
+            done = {k for k, _ in merged[1]} if merged is not None else set()
+            for c_, v_, cd in ent[i]:
+                if (cd >> 1) not in done:
+                    col.append(c_)
+                    val.append(v_)
+                    code.append(cd)
             ptr[i + 1] = len(col)
-        return ptr, np.array(col), np.array(val), np.array(code), act
+        return ptr, np.array(col), np.array(val), np.array(code), act, rowsets
 
     def ensure_residual(self, a, b_) -> None:
         """Build the device data of residual(a, b, ...) now (the first call would, outside a graph
@@ -386,6 +452,7 @@ class DeviceProblem:
         for bi, b in enumerate(self.tpl.buckets):
             kind, data = self._residual_data(bi)
             key = (float(a), float(b_))
+            self._rowscale(bi, a, b_)
             if kind == "values" and key not in data:
                 Mv, per = self._M[bi][:2]
                 per = per if isinstance(per, int) else 0
@@ -404,10 +471,11 @@ class DeviceProblem:
             kind, data = self._residual_data(bi)
             xb, rb, ob = self.bucket(x, bi), self.bucket(rhs, bi), self.bucket(out, bi)
             if kind == "split":
-                ptr, col, val, code, mv, nm = data
+                ptr, col, val, code, mv, nm = data[:6]
+                rs = self._rowscale(bi, a, b_)
                 call("cng_split_residual", self.nsys[bi], b.n, ptr.data_ptr(), col.data_ptr(), val.data_ptr(),
-                     code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_), xb.data_ptr(), rb.data_ptr(),
-                     ob.data_ptr(), s)
+                     code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_),
+                     rs.data_ptr() if rs is not None else None, xb.data_ptr(), rb.data_ptr(), ob.data_ptr(), s)
                 continue
             key = (float(a), float(b_))
             if key not in data:

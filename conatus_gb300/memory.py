@@ -8,7 +8,8 @@ one by one:
 * state and work vectors: X and R (plus the FP32 form's refinement residual), the history ring of
   M X and F (q slots each), complex128 over the mode layout;
 * per bucket: M values (one shared copy when M is constant, else per system), L values per system,
-  the pattern, and the factor set of ``cng_banded_create_shared`` (band LU ldab x n, pivots, the
+  the pattern, the per-(row, system) scales of the residual's merged entry lists (one table per
+  factor set, plus one for -L X), and the factor set of ``cng_banded_create_shared`` (band LU ldab x n, pivots, the
   border blocks V^T and W (r x n each), the capacitance LU (r x r)), its FP32 copies in the FP32
   form, and the compact factor streams (bounded above by the band: at most kl entries of L and
   kl + ku + 1 of U per column, r x n of V); one transient copy of a M + b L while factoring;
@@ -98,7 +99,7 @@ def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: b
     vec = n_total * _Z
     parts = {"state": vec * (2 + (1 if precision == "fp32" else 0)), "history": 2 * q * vec,
              "rhs_work": _rhs_bytes(problem, precision)}
-    ops = fac = trans = 0
+    ops = fac = trans = rows = 0
     for b, ns in zip(tpl.buckets, problem.nsys):
         nnz = int(b.indices.size)
         const_m = b.m_is_constant() and b.exact is None
@@ -107,8 +108,10 @@ def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: b
         trans = max(trans, ns * nnz * _Z)
         if precision == "fp32":
             ops += 2 * b.n * 16 + ns * 16 * 8        # split-operator residual lists (bounded)
+        if const_m:
+            rows += ns * b.n * 8                     # per-(row, system) scales of merged residual lists
     sets = q if factor_sets is None else max(1, min(q, int(factor_sets)))
-    parts["operators"] = ops
+    parts["operators"] = ops + rows * (sets + 1)
     parts["factors"] = fac * sets
     parts["factor_transient"] = trans
     parts["total"] = int(sum(parts.values()))

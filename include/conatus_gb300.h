@@ -269,10 +269,12 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
 
 /* The same residual with the operator split per wavenumber monomial into real coefficients:
  * row i has entries ptr[i]..ptr[i+1]-1 with column col[e], real val[e] and code[e] = 2 t + imag
- * (t = monomial index, -1 for M; imag = 1 when the coefficient is i val). */
+ * (t = monomial index, -1 for M; imag = 1 when the coefficient is i val). t = 63 marks one entry
+ * list shared by several terms of the row (proportional coefficients), scaled by rowscale[i nsys +
+ * system] (row-major n x nsys, FP64; NULL when no code holds t = 63). */
 int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
-                       const int8_t* code, const double* mono, int nmono, double a, double c, const void* x,
-                       const void* b, void* r, void* stream);
+                       const int8_t* code, const double* mono, int nmono, double a, double c,
+                       const double* rowscale, const void* x, const void* b, void* r, void* stream);
 
 /* y = M x with one real value array shared by every system of the bucket (the mass matrices of the
  * tau systems are real). */
