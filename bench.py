@@ -203,6 +203,25 @@ def rfft_roofline(dev, stream, hbm_peak, peak_kind, reps=5):
                              "flops": flops, "flop_count": "2.5 L log2 L per real transform"}}
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest x over the ranks of the process group (x itself without one): the timed region
+    of the slowest replica. NCCL reduces on the GPU, gloo on the host."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, steps: int, ms: float) -> float:
+    """Whole-job steps/s of ``world`` independent replicas of ``steps`` steps each, timed by the
+    slowest (weak scaling: every replica does the full workload)."""
+    return world * steps / (ms / 1e3)
+
+
 L2_BYTES = 129e6      # GB300 L2
 
 
@@ -251,14 +270,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
     barrier()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1))
     ms_step = ms / args.steps
-    value = ws * args.steps / (ms / 1e3)
+    value = replica_throughput(ws, args.steps, ms)
     finite = bool(torch.isfinite(torch.view_as_real(solver.X)).all().item())
 
     # ---- per-kernel timing (same stream, CUDA events): one batched solve launch, and F
