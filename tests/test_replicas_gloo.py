@@ -31,7 +31,7 @@ def test_two_replicas_max_time_and_total_steps():
     import torch.multiprocessing as mp
     world = 2
     port = _free_port()
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:
         out = man.dict()
         mp.start_processes(_rank, args=(world, port, out), nprocs=world, start_method="spawn", join=True)
         res = dict(out)
