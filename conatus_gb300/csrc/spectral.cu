@@ -417,8 +417,10 @@ struct RhsDev {
     // Fields that differ only by x / z derivatives share their transforms along y (and, for x,
     // along z): the (i k)^o factors are diagonal in the Fourier indices, so they commute with the
     // transforms of the other directions and are applied between the stages.
-    // The FP64 form shares (its transforms are FP64-pipe bound); the FP32 form does not (the extra
-    // passes cost it more than the transforms they save, and its error grows).
+    // Both forms share whenever there is a Fourier direction: the derivative factor (i k)^o is
+    // constant along the transforms it is moved across, so each line's relative rounding error is
+    // the same as with the derivative applied first (the FP32 form's error against the FP64 form:
+    // 5.2e-7 -> 5.5e-7 after 50 channel steps, its F 2.77 -> 2.43 ms).
     int share;                 // 1: shared transforms with expansions; 0: one transform per factor
     int ngy, ngz;              // distinct (var, comp, oy) and (var, comp, oy, oz); nfactors if 0
     const int* yg_rep;         // ngy: a factor of each y-group (its column positions and oy)
@@ -1051,7 +1053,7 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
             fz[f] = gz;
         }
         if (h->ndir == 0 && (int)ykeys.size() != h->nfactors) throw InvalidArgument("repeated factor");
-        dv.share = (h->precision == 0 && h->ndir >= 1) ? 1 : 0;
+        dv.share = h->ndir >= 1 ? 1 : 0;
         if (!dv.share) {                    // one transform per factor
             ykeys.assign(h->nfactors, {0, 0, 0});
             zkeys.assign(h->nfactors, {0, 0, 0, 0});
