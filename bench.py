@@ -357,6 +357,11 @@ def run_gpu(args):
     }
     if args.precision == "fp32" and rank == 0 and args.error_steps > 0:
         out["error_vs_fp64"] = mixed_error(P, C0, cfg, args.error_steps)
+    if args.precision == "fp64" and args.config == "channel" and ws == 1 and not args.no_forms:
+        # the precision form beside the drop-in, on the same workload and GPU
+        del solver, dev, R, X2
+        torch.cuda.empty_cache()
+        out["forms"] = {"fp32": form_fp32(P, C0, cfg, args)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, P, C0)
     if rank == 0:
@@ -364,6 +369,32 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def form_fp32(P, C0, cfg, args):
+    """The FP32 form (FP32 F and solves, FP64 refinement, state and history) on the workload of the
+    FP64 line: steps/s over the same number of graph-launched steps (CUDA events on its stream) and
+    its error per field against the FP64 form after ``error_steps`` steps."""
+    import torch
+    from conatus_gb300.ivp import IVPSolver
+    s = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision="fp32")
+    s.set_state(C0)
+    s.run_graph(max(args.warmup, s.ring))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s.stream)
+    s.run_graph(args.steps)
+    e1.record(s.stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    res = {"metric": METRIC[args.config] + " FP32 form", "value": args.steps / (ms / 1e3), "unit": "steps/s",
+           "ms_per_step": ms / args.steps, "steps": args.steps, "dtype": "f32+f64",
+           "gpu_launches": s.launches_per_step() * args.steps}
+    del s
+    torch.cuda.empty_cache()
+    if args.error_steps > 0:
+        res["error_vs_fp64"] = mixed_error(P, C0, cfg, args.error_steps)
+    return res
 
 
 def _schedule_summary(dev):
@@ -582,6 +613,7 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--cpu-sample-systems", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="channel FP64: skip the FP32 form's line")
     ap.add_argument("--error-steps", type=int, default=50)
     ap.add_argument("--fourier", type=int, nargs="*", default=None,
                     help="Fourier sizes overriding the configuration's (small cases for profiling)")
