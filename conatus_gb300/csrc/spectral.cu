@@ -46,23 +46,6 @@ struct FastDiv {
     __device__ __forceinline__ int div(int e) const { return d <= 1 ? e : (int)__umulhi((unsigned)e, m); }
 };
 
-// f(k, t) for k < X and t < B, t fastest across the block's threads (coalesced columns): when the
-// block's threads are a multiple of B a thread keeps one sequence t and steps k, with no division
-// per element (the staging loops of the FP32 transforms were bound by their integer work)
-template <class F>
-__device__ __forceinline__ void for_kt(int X, int B, const FastDiv& dB, F&& f) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    if (nt % B == 0) {
-        const int t = tid % B, step = nt / B;
-        for (int k = tid / B; k < X; k += step) f(k, t);
-    } else {
-        for (int e = tid; e < B * X; e += nt) {
-            const int k = dB.div(e);
-            f(k, e - k * B);
-        }
-    }
-}
-
 FftPlan make_plan(int L) {
     FftPlan p;
     p.L = L;
@@ -282,37 +265,37 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     const c2<R>* src = in + (forward ? o : expand_row<R>(ex, o, &wt)) * (long long)lin * inner;
     c2<R>* dst = out + o * (long long)lout * inner;
     if (!forward) {
-        // zero the padding slots K .. L - Nc + K (the loop below writes the others: disjoint)
-        const int zc = L - Nc + 1;
-        for (int e = tid; e < B * zc; e += nt) {
-            const int t = e / zc;
-            b0[(size_t)t * LS + K + (e - t * zc)] = mk<R>(0, 0);
-        }
-        for_kt(Nc, B, dB, [&](int k, int t) {
-            if (i0 + t >= inner || k == K) return;
+        for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
+        __syncthreads();
+        for (int e = tid; e < B * Nc; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
+            if (i0 + t >= inner || k == K) continue;
             const int slot = k < K ? k : L - (Nc - k);
             const c2<R> v = src[(long long)k * inner + i0 + t];
             b0[(size_t)t * LS + slot] = wt ? ikmul<R>(wt[k], v) : v;
-        });
+        }
     } else {
-        for_kt(L, B, dB, [&](int k, int t) {
+        for (int e = tid; e < B * L; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
             b0[(size_t)t * LS + k] = (i0 + t < inner) ? src[(long long)k * inner + i0 + t] : mk<R>(0, 0);
-        });
+        }
     }
     __syncthreads();
     c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, forward ? -1 : +1, LS);
     if (!forward) {
-        for_kt(L, B, dB, [&](int k, int t) {
+        for (int e = tid; e < B * L; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
             if (i0 + t < inner) dst[(long long)k * inner + i0 + t] = r[(size_t)t * LS + k];
-        });
+        }
     } else {
         const R invL = R(1) / R(L);
-        for_kt(Nc, B, dB, [&](int k, int t) {
-            if (i0 + t >= inner) return;
+        for (int e = tid; e < B * Nc; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
+            if (i0 + t >= inner) continue;
             c2<R> v = mk<R>(0, 0);
             if (k != K) v = scl<R>(invL, r[(size_t)t * LS + (k < K ? k : L - (Nc - k))]);
             dst[(long long)k * inner + i0 + t] = v;
-        });
+        }
     }
 }
 
@@ -340,16 +323,13 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
         const c2<R>* wt;
         const c2<R>* src = static_cast<const c2<R>*>(in_) + expand_row<R>(ex, o, &wt) * (long long)K * inner;
         R* dst = static_cast<R*>(out_) + o * (long long)L * inner;
-        // zero the padding slots K .. L - K (the loop below writes the others)
-        const int zc = L - 2 * K + 1;
-        for (int e = tid; e < B * zc; e += nt) {
-            const int t = e / zc;
-            b0[(size_t)t * LS + K + (e - t * zc)] = mk<R>(0, 0);
-        }
+        for (int e = tid; e < B * LS; e += nt) b0[e] = mk<R>(0, 0);
+        __syncthreads();
         // Z_k = A_k + i B_k, Z_{L-k} = conj(A_k) + i conj(B_k)
-        for_kt(K, B, dB, [&](int k, int t) {
+        for (int e = tid; e < B * K; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
             const int p = p0 + t;
-            if (p >= pairs) return;
+            if (p >= pairs) continue;
             c2<R> A = src[(long long)k * inner + 2 * p];
             c2<R> Bv = 2 * p + 1 < inner ? src[(long long)k * inner + 2 * p + 1] : mk<R>(0, 0);
             if (wt) {
@@ -363,39 +343,38 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
                 b0[(size_t)t * LS + k] = mk<R>(A.x - Bv.y, A.y + Bv.x);
                 b0[(size_t)t * LS + L - k] = mk<R>(A.x + Bv.y, -A.y + Bv.x);
             }
-        });
+        }
         __syncthreads();
         c2<R>* r = smem_fft_fast<R>(b0, b1, plan, B, tw, +1, LS);
-        for_kt(L, B, dB, [&](int j, int t) {
+        for (int e = tid; e < B * L; e += nt) {
+            const int j = dB.div(e), t = e - j * B;
             const int p = p0 + t;
-            if (p >= pairs) return;
+            if (p >= pairs) continue;
             c2<R> z = r[(size_t)t * LS + j];
             R* d = dst + (long long)j * inner + 2 * p;
-            if ((inner & 1) == 0) {
-                *reinterpret_cast<c2<R>*>(d) = z;        // both columns in one aligned store
-            } else {
-                d[0] = z.x;
-                if (2 * p + 1 < inner) d[1] = z.y;
-            }
-        });
+            d[0] = z.x;
+            if (2 * p + 1 < inner) d[1] = z.y;
+        }
     } else {
         const R* src = static_cast<const R*>(in_) + o * (long long)L * inner;
         c2<R>* dst = static_cast<c2<R>*>(out_) + o * (long long)K * inner;
-        for_kt(L, B, dB, [&](int j, int t) {
+        for (int e = tid; e < B * L; e += nt) {
+            const int j = dB.div(e), t = e - j * B;
             const int p = p0 + t;
             c2<R> z = mk<R>(0, 0);
             if (p < pairs) {
                 const R* s = src + (long long)j * inner + 2 * p;
-                z = (inner & 1) == 0 ? *reinterpret_cast<const c2<R>*>(s) : mk<R>(s[0], 2 * p + 1 < inner ? s[1] : R(0));
+                z = mk<R>(s[0], 2 * p + 1 < inner ? s[1] : R(0));
             }
             b0[(size_t)t * LS + j] = z;
-        });
+        }
         __syncthreads();
         c2<R>* Z = smem_fft_fast<R>(b0, b1, plan, B, tw, -1, LS);
         const R h = R(0.5) / R(L);
-        for_kt(K, B, dB, [&](int k, int t) {
+        for (int e = tid; e < B * K; e += nt) {
+            const int k = dB.div(e), t = e - k * B;
             const int p = p0 + t;
-            if (p >= pairs) return;
+            if (p >= pairs) continue;
             c2<R> zk = Z[(size_t)t * LS + k];
             c2<R> zm = conjg<R>(Z[(size_t)t * LS + (k == 0 ? 0 : L - k)]);
             c2<R> A = scl<R>(h, add<R>(zk, zm));
@@ -403,7 +382,7 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
             c2<R> Bv = mk<R>(h * d.y, -h * d.x);
             dst[(long long)k * inner + 2 * p] = A;
             if (2 * p + 1 < inner) dst[(long long)k * inner + 2 * p + 1] = Bv;
-        });
+        }
     }
 }
 
