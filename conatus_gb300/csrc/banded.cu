@@ -551,6 +551,7 @@ struct SolveIo {
     const long long* rows_s;
     const long long* cols_s;
     int accumulate = 0;
+    void* xT = nullptr;            // IO_MIXED: x also written row-major over the systems, [n][batch]
 };
 
 template <class T, int IO>
@@ -1733,6 +1734,8 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     if (!live) return;
     if constexpr (IO == IO_MIXED) {
         zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
+        zd* xt = static_cast<zd*>(io.xT);
+        const size_t nb = (size_t)ix.batch;
         if (io.accumulate) {
             for (int i0 = lg; i0 < n; i0 += kU * kLanesPer) {
                 zd o[kU];
@@ -1742,11 +1745,19 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
 #pragma unroll
                 for (int u = 0; u < kU; ++u) {
                     const int i = i0 + u * kLanesPer;
-                    if (i < n) xs[i] = o[u] + zd(y[i].re, y[i].im);
+                    if (i < n) {
+                        const zd v = o[u] + zd(y[i].re, y[i].im);
+                        xs[i] = v;
+                        if (xt) xt[(size_t)i * nb + sys] = v;
+                    }
                 }
             }
         } else {
-            for (int i = lg; i < n; i += kLanesPer) xs[i] = zd(y[i].re, y[i].im);
+            for (int i = lg; i < n; i += kLanesPer) {
+                const zd v(y[i].re, y[i].im);
+                xs[i] = v;
+                if (xt) xt[(size_t)i * nb + sys] = v;
+            }
         }
     } else {
         for (int i = lg; i < n; i += kLanesPer) io_store<TF, IO>(io, sys, n, i, y[i]);
@@ -2128,6 +2139,31 @@ int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, 
                                               static_cast<const zd*>(h->slu), h->spiv, h->perm});
             launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, st);
         }
+    })
+}
+
+int cng_banded_solve_batch_xt(int nh, cng_banded* const* hh, const void* const* b, void* const* x,
+                              void* const* xt, int accumulate, void* stream) {
+    CNG_TRY({
+        if (nh < 1 || nh > kMaxMulti) throw InvalidArgument("1 to 8 handles per batched solve");
+        if (!hh || !b || !x || !xt) throw InvalidArgument("null argument");
+        std::vector<const Banded*> hs;
+        std::vector<SolveIo> ios;
+        std::vector<CompactData<zf>> cds;
+        for (int k = 0; k < nh; ++k) {
+            const Banded* h = reinterpret_cast<const Banded*>(hh[k]);
+            if (!h || !h->compact_ready || h->dtype != 1 || !h->fp32_ready)
+                throw InvalidArgument("batched solve needs complex128 handles in compact form with FP32 factors");
+            if (h->sched < 0) throw InvalidArgument("the transposed copy of x: compact schedules only");
+            if (!b[k] || !x[k] || b[k] == x[k] || (xt[k] && (xt[k] == x[k] || xt[k] == b[k])))
+                throw InvalidArgument("b, x and xt: device pointers, not aliased");
+            hs.push_back(h);
+            SolveIo io{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate};
+            io.xT = xt[k];
+            ios.push_back(io);
+            cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm});
+        }
+        launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, static_cast<cudaStream_t>(stream));
     })
 }
 

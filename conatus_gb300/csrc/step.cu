@@ -163,7 +163,8 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
                                  const double* __restrict__ val, const signed char* __restrict__ code,
                                  const double* __restrict__ mono, int nmono, double a, double c,
                                  const double* __restrict__ rowscale, const double2* __restrict__ x,
-                                 const double2* __restrict__ b, double2* __restrict__ r) {
+                                 const double2* __restrict__ xT, const double2* __restrict__ b,
+                                 double2* __restrict__ r) {
     const unsigned sysw = ((unsigned)nsys + 31u) >> 5;             // warps of 32 systems per row
     const unsigned nwarps = sysw * (unsigned)n;
     const unsigned lane = threadIdx.x & 31u;
@@ -185,7 +186,8 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
                 const int cd = code[e];
                 if ((cd >> 1) != tt) break;
                 const double v = val[e];
-                const double2 xv = xm[col[e]];
+                // x row-major over the systems when given: the warp's 32 systems read one line
+                const double2 xv = xT ? xT[(size_t)col[e] * nsys + m] : xm[col[e]];
                 if (cd & 1) {                               // i v x
                     gr = fma(-v, xv.y, gr);
                     gi = fma(v, xv.x, gi);
@@ -261,7 +263,8 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
 
 int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
                        const int8_t* code, const double* mono, int nmono, double a, double c,
-                       const double* rowscale, const void* x, const void* b, void* r, void* stream) {
+                       const double* rowscale, const void* x, const void* xT, const void* b, void* r,
+                       void* stream) {
     CNG_TRY({
         if (!ptr || !col || !val || !code || (nmono > 0 && !mono) || !x || !b || !r)
             throw InvalidArgument("null device pointer");
@@ -274,11 +277,11 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
         if (c == 1.0)
             k_split_residual<true><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
                 nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
-                static_cast<const double2*>(b), static_cast<double2*>(r));
+                static_cast<const double2*>(xT), static_cast<const double2*>(b), static_cast<double2*>(r));
         else
             k_split_residual<false><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
                 nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
-                static_cast<const double2*>(b), static_cast<double2*>(r));
+                static_cast<const double2*>(xT), static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
     })
 }

@@ -90,6 +90,7 @@ class DeviceProblem:
         self.overlap_refine = True          # FP32 form: two bucket groups refined on two streams
         self._aux = None
         self._groups = None
+        self._XT = None                     # FP32 form: x row-major over each bucket's systems
         self.tuning = None
         if precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
@@ -462,8 +463,9 @@ class DeviceProblem:
         if self.precision == "fp32" and self._R2 is None:
             self._R2 = self.zeros()
 
-    def residual(self, a, b_, x, rhs, out, stream=None, buckets=None) -> None:
-        """out = rhs - (a M + b L) x per bucket (all, or the indices in ``buckets``), FP64."""
+    def residual(self, a, b_, x, rhs, out, stream=None, buckets=None, xT=None) -> None:
+        """out = rhs - (a M + b L) x per bucket (all, or the indices in ``buckets``), FP64; ``xT``:
+        x also row-major over the systems of each bucket (read by the split kernel instead)."""
         s = _stream_handle(stream)
         for bi, b in enumerate(self.tpl.buckets):
             if buckets is not None and bi not in buckets:
@@ -475,7 +477,8 @@ class DeviceProblem:
                 rs = self._rowscale(bi, a, b_)
                 call("cng_split_residual", self.nsys[bi], b.n, ptr.data_ptr(), col.data_ptr(), val.data_ptr(),
                      code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_),
-                     rs.data_ptr() if rs is not None else None, xb.data_ptr(), rb.data_ptr(), ob.data_ptr(), s)
+                     rs.data_ptr() if rs is not None else None, xb.data_ptr(),
+                     self.bucket(xT, bi).data_ptr() if xT is not None else None, rb.data_ptr(), ob.data_ptr(), s)
                 continue
             key = (float(a), float(b_))
             if key not in data:
@@ -558,10 +561,23 @@ class DeviceProblem:
         bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in group])
         xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in group])
         rp = (ctypes.c_void_p * nb)(*[self.bucket(self._R2, bi).data_ptr() for bi in group])
-        call("cng_banded_solve_batch", nb, hs, bp, xp, 1, 0, s)
-        for _ in range(self.refine):
-            self.residual(a, b_, out, rhs, self._R2, s, buckets=group)
-            call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
+        # x also row-major over the systems (coalesced reads of the residual kernel), with the
+        # compact schedules
+        xt = None
+        if all(getattr(fs[bi], "schedule", 0) >= 0 for bi in group):
+            if self._XT is None:
+                self._XT = self.zeros()
+            xt = (ctypes.c_void_p * nb)(*[self.bucket(self._XT, bi).data_ptr() for bi in group])
+        if xt is not None:
+            call("cng_banded_solve_batch_xt", nb, hs, bp, xp, xt, 0, s)
+        else:
+            call("cng_banded_solve_batch", nb, hs, bp, xp, 1, 0, s)
+        for p in range(self.refine):
+            self.residual(a, b_, out, rhs, self._R2, s, buckets=group, xT=self._XT if xt is not None else None)
+            if xt is not None and p + 1 < self.refine:
+                call("cng_banded_solve_batch_xt", nb, hs, rp, xp, xt, 1, s)
+            else:
+                call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
 
     def solve_launch(self, fs, rhs, out, stream=None) -> None:
         """One batched solve launch with the factor set ``fs`` (FP32 factors in the FP32 form), no

@@ -5,7 +5,8 @@ The reference predicts device bytes per solver from a liveness model of its buff
 (python/conatus/runtime/memory.py); the prediction here follows this library's own allocations
 one by one:
 
-* state and work vectors: X and R (plus the FP32 form's refinement residual), the history ring of
+* state and work vectors: X and R (plus the FP32 form's refinement residual and its copy of x
+  row-major over the systems), the history ring of
   M X and F (q slots each), complex128 over the mode layout;
 * per bucket: M values (one shared copy when M is constant, else per system), L values per system,
   the pattern, the per-(row, system) scales of the residual's merged entry lists (one table per
@@ -97,7 +98,7 @@ def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: b
     q = int(scheme[-1])
     n_total = sum(ns * b.n for ns, b in zip(problem.nsys, tpl.buckets))
     vec = n_total * _Z
-    parts = {"state": vec * (2 + (1 if precision == "fp32" else 0)), "history": 2 * q * vec,
+    parts = {"state": vec * (2 + (2 if precision == "fp32" else 0)), "history": 2 * q * vec,
              "rhs_work": _rhs_bytes(problem, precision)}
     ops = fac = trans = rows = 0
     for b, ns in zip(tpl.buckets, problem.nsys):

@@ -104,6 +104,12 @@ int cng_banded_compact(cng_banded* h, void* stream);
 int cng_banded_solve_batch(int nh, cng_banded* const* h, const void* const* b, void* const* x, int fp32,
                            int accumulate, void* stream);
 
+/* cng_banded_solve_batch with the FP32 factors that also writes x row-major over the systems,
+ * xt[k] = [n][batch] complex128 (NULL: not written), for the refinement residual's coalesced reads
+ * (cng_split_residual's xT). */
+int cng_banded_solve_batch_xt(int nh, cng_banded* const* h, const void* const* b, void* const* x,
+                              void* const* xt, int accumulate, void* stream);
+
 /* Schedules of the compact solve (the batched-solve kernel of the step): count, and per schedule
  * the columns per staged chunk of the factor streams and the depth of the staging ring. No
  * reference counterpart: the reference picks its solve kernel (level-scheduled streams or the band
@@ -271,10 +277,12 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
  * row i has entries ptr[i]..ptr[i+1]-1 with column col[e], real val[e] and code[e] = 2 t + imag
  * (t = monomial index, -1 for M; imag = 1 when the coefficient is i val). t = 63 marks one entry
  * list shared by several terms of the row (proportional coefficients), scaled by rowscale[i nsys +
- * system] (row-major n x nsys, FP64; NULL when no code holds t = 63). */
+ * system] (row-major n x nsys, FP64; NULL when no code holds t = 63). xT (may be NULL): x row-major
+ * over the systems ([n][nsys], as cng_banded_solve_batch_xt writes it), read instead of x. */
 int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
                        const int8_t* code, const double* mono, int nmono, double a, double c,
-                       const double* rowscale, const void* x, const void* b, void* r, void* stream);
+                       const double* rowscale, const void* x, const void* xT, const void* b, void* r,
+                       void* stream);
 
 /* y = M x with one real value array shared by every system of the bucket (the mass matrices of the
  * tau systems are real). */
