@@ -43,7 +43,7 @@ _SIGS = {
     "cng_banded_make_fp32": [P, P],
     "cng_banded_compact": [P, P],
     "cng_banded_solve_batch": [c_int, P, P, P, c_int, c_int, P],
-    "cng_banded_schedules": [P, P, P],
+    "cng_banded_schedules": [P, P, P, P],
     "cng_banded_set_schedule": [P, c_int],
     "cng_banded_solve_fp32": [P, P, P, c_int, P],
     "cng_poly_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P],

@@ -2,7 +2,8 @@
 
 Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_set_schedule(h,
 -1)``) and the compact-stream schedules of ``cng_banded_schedules`` (two systems per warp over the
-union pattern of the factors, with different staging chunks and ring depths). Each candidate solves
+union pattern of the factors, with different staging chunks and ring depths, and one system per
+warp with the lanes split over entries and components for small batches). Each candidate solves
 the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
 few times on the factors at hand; the fastest is kept for every handle of the factor set. Results
 are cached per process by the shapes of the buckets (batch, n, border, band) and the precision, so
@@ -22,7 +23,7 @@ import os
 
 from ._lib import call
 
-__all__ = ["schedules", "tune_solve", "tune_rhs", "cache"]
+__all__ = ["schedules", "split_schedules", "tune_solve", "tune_rhs", "cache"]
 
 _CACHE: dict = {}
 
@@ -30,8 +31,19 @@ _CACHE: dict = {}
 def schedules() -> list:
     """Candidate schedules: -1 (band kernel) and 0 .. count-1 (compact)."""
     n = ctypes.c_int32()
-    call("cng_banded_schedules", ctypes.byref(n), None, None)
+    call("cng_banded_schedules", ctypes.byref(n), None, None, None)
     return [-1] + list(range(int(n.value)))
+
+
+def split_schedules() -> set:
+    """Compact schedules that run one system per warp with the lanes split over entries and
+    components (the latency variant: the same sweeps, another order of sums in the border
+    correction)."""
+    n = ctypes.c_int32()
+    call("cng_banded_schedules", ctypes.byref(n), None, None, None)
+    flags = (ctypes.c_int32 * n.value)()
+    call("cng_banded_schedules", ctypes.byref(n), None, None, flags)
+    return {k for k in range(n.value) if flags[k]}
 
 
 def cache() -> dict:

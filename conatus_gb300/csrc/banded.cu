@@ -1474,10 +1474,13 @@ constexpr int kCChunk = 8;              // columns per staged chunk (the default
 // the cp.async ring (chunks in flight + 1). Deeper rings keep more of the stream in flight per warp
 // (the sweep waits on memory otherwise) at the cost of shared memory, hence of resident warps; the
 // autotuner (conatus_gb300.autotune) times them on the factors at hand. Schedule 0 is the default.
-struct CompactSchedule { int chunk, stages; };
-constexpr int kNumSchedules = 8;
-constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2}, {8, 3}, {4, 3}, {16, 2},
-                                                       {16, 3}, {4, 4}, {2, 4}, {16, 4}};
+// Schedules 8-10 run one system per warp with the lanes split over entries and components (the
+// latency variant for small batches, k_solve_split_multi).
+struct CompactSchedule { int chunk, stages, split; };
+constexpr int kNumSchedules = 11;
+constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
+                                                       {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
+                                                       {8, 2, 1}, {16, 2, 1}, {4, 3, 1}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1790,6 +1793,211 @@ k_solve_compact_multi(MultiSolve<TF> ms) {
     solve_compact_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
 }
 
+// ---- one system per warp, lanes split over (entry, real/imaginary part) -------------------------
+// The latency variant for small batches: a column's updates take two fused multiply-adds per lane
+// (one component each) where the two-systems-per-warp sweep takes four, so the chain from column
+// to column is half as long; throughput per system is the same. It reads the same compact streams
+// (system sys is slot sys % 2 of warp group sys / 2) and stages the pair's chunk.
+template <class TF> struct CompT;
+template <> struct CompT<zd> { using T = double; };
+template <> struct CompT<zf> { using T = float; };
+__device__ __forceinline__ double fm(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fm(float a, float b, float c) { return fmaf(a, b, c); }
+template <class TF>
+__device__ __forceinline__ typename CompT<TF>::T comp(const TF& v, int c) { return c ? v.im : v.re; }
+// component c of v - a b, in the order of cfms (the two-systems sweep's arithmetic)
+template <class TF>
+__device__ __forceinline__ typename CompT<TF>::T cfms_comp(typename CompT<TF>::T vc, const TF& a, const TF& b, int c) {
+    return c ? fm(-a.im, b.re, fm(-a.re, b.im, vc)) : fm(a.im, b.im, fm(-a.re, b.re, vc));
+}
+
+template <class TF, class TD, int IO, int CH, int ST>
+__device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const CompactData<TF>& cd,
+                                                 const SolveIo& io, int block) {
+    using T = typename CompT<TF>::T;
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int sys = block * nw + wib;
+    const int gs = sys & 1, wgs = sys >> 1;
+    const int es = lane >> 1, c = lane & 1;           // entry slot, component
+    const bool live = sys < ix.batch;
+    const int n = ix.n, r = ix.r;
+    int* s_offL = reinterpret_cast<int*>(sm);
+    int* s_offU = s_offL + (n + 1);
+    unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
+    unsigned char* s_Lrow = reinterpret_cast<unsigned char*>(s_Lmask + n);
+    unsigned char* s_Udist = s_Lrow + ix.nL;
+    size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
+    off = (off + 15) & ~(size_t)15;
+    const size_t per_warp = (size_t)(n + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * 2 +
+                            (ST * (size_t)CH * 2 * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    TF* y = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
+    TF* zb = y + n;
+    TF* Lb = y + (n + 64);
+    TF* Ub = Lb + ST * (size_t)ix.maxLc * 2;
+    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * 2);
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) {
+        s_offL[i] = ix.offL[i];
+        s_offU[i] = ix.offU[i];
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_Lmask[i] = ix.Lmask[i];
+    for (int i = threadIdx.x; i < ix.nL; i += blockDim.x) s_Lrow[i] = ix.Lrow[i];
+    for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) s_Udist[i] = ix.Udist[i];
+    __syncthreads();
+    if (!live) return;                               // one system per warp: the whole warp leaves
+    constexpr int kU = 4;
+    for (int i0 = lane; i0 < n; i0 += kU * 32) {
+        int pr[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) pr[u] = i0 + u * 32 < n ? cd.perm[i0 + u * 32] : -1;
+        TF v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            v[u] = TF(0.0);
+            if (pr[u] >= 0) {
+                if constexpr (IO == IO_MIXED) v[u] = to_zf(static_cast<const zd*>(io.rhs)[(size_t)sys * n + pr[u]]);
+                else v[u] = io_load<TF, IO>(io, sys, n, pr[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+            if (i0 + u * 32 < n) y[i0 + u * 32] = v[u];
+    }
+    __syncwarp();
+    const TF* Lg = cd.L + (size_t)wgs * ix.nL * 2;
+    const TF* Ug = cd.U + (size_t)wgs * ix.nU * 2;
+    const int* Pg = cd.piv + (size_t)wgs * n * 2;
+    if (ix.kl > 0 && n > 1) {
+        const int nch = (n - 1 + CH - 1) / CH;
+        auto issue = [&](int ch) {
+            if (ch < nch) {
+                const int buf = ch % ST;
+                const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+                warp_stage(Lb + (size_t)buf * ix.maxLc * 2, Lg + (size_t)s_offL[j0] * 2, (s_offL[j1] - s_offL[j0]) * 2);
+                warp_stage(Pb + (size_t)buf * CH * 2, Pg + (size_t)j0 * 2, (j1 - j0) * 2);
+            }
+            cp_async_commit();
+        };
+        for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
+        for (int ch = 0; ch < nch; ++ch) {
+            issue(ch + ST - 1);
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const TF* Lc = Lb + (size_t)(ch % ST) * ix.maxLc * 2;
+            const int* Pc = Pb + (size_t)(ch % ST) * CH * 2;
+            const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+            const int base = s_offL[j0];
+            int e1 = base;
+#pragma unroll
+            for (int jj = 0; jj < CH; ++jj) {
+                const int j = j0 + jj;
+                if (j >= j1) break;
+                const int l = Pc[jj * 2 + gs];
+                const TF bj = y[l];
+                const TF yj0 = y[j];
+                const int e0 = e1;
+                e1 = s_offL[j + 1];
+                __syncwarp();
+                for (int e = e0 + es; e < e1; e += 16) {
+                    const int i = j + 1 + s_Lrow[e];
+                    T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                    const T vc = (i == l) ? comp(yj0, c) : *yi;
+                    *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bj, c);
+                }
+                if (lane == 0) {
+                    y[j] = bj;
+                    if (l != j && !((s_Lmask[j] >> (l - j - 1)) & 1u)) y[l] = yj0;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    {
+        const int nch = (n + CH - 1) / CH;
+        auto issue = [&](int ch) {
+            if (ch < nch) {
+                const int s0 = ch * CH, s1 = min(s0 + CH, n);
+                warp_stage(Ub + (size_t)(ch % ST) * ix.maxUc * 2, Ug + (size_t)s_offU[s0] * 2, (s_offU[s1] - s_offU[s0]) * 2);
+            }
+            cp_async_commit();
+        };
+        for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
+        for (int ch = 0; ch < nch; ++ch) {
+            issue(ch + ST - 1);
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const TF* Uc = Ub + (size_t)(ch % ST) * ix.maxUc * 2;
+            const int s0 = ch * CH, s1 = min(s0 + CH, n);
+            const int base = s_offU[s0];
+            int e1 = base;
+#pragma unroll
+            for (int ss = 0; ss < CH; ++ss) {
+                const int s = s0 + ss;
+                if (s >= s1) break;
+                const int j = n - 1 - s;
+                const int e0 = e1;
+                e1 = s_offU[s + 1];
+                const TF yj = y[j];
+                __syncwarp();
+                for (int e = e0 + es; e < e1; e += 16) {
+                    const int i = j - s_Udist[e];
+                    T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                    const T vc = e == e0 ? T(0) : *yi;
+                    *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], yj, c);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (r > 0) {
+        const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
+        TF* sl = zb + r;
+        if (staged)
+            for (int q = lane; q < r * r; q += 32) sl[q] = cd.slu[(size_t)sys * r * r + q];
+        const TF* Vg = cd.V + (size_t)wgs * ix.nV * 2;
+        for (int a = 0; a < r; ++a) {
+            TF acc = TF(0.0);
+            for (int e = ix.offV[a] + lane; e < ix.offV[a + 1]; e += 32)
+                acc = cfma(acc, Vg[(size_t)e * 2 + gs], y[ix.Vcol[e]]);
+            for (int m = 16; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
+            if (lane == 0) zb[a] = acc;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (staged) small_getrs_staged(sl, cd.spiv + (size_t)sys * r, zb, r);
+            else small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        }
+        __syncwarp();
+        const TF* Ws = cd.W + (size_t)sys * r * n;
+        for (int i = lane; i < n; i += 32) {
+            TF acc = y[i];
+            for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
+            y[i] = acc;
+        }
+        __syncwarp();
+    }
+    if constexpr (IO == IO_MIXED) {
+        zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
+        zd* xt = static_cast<zd*>(io.xT);
+        for (int i = lane; i < n; i += 32) {
+            const zd v = io.accumulate ? xs[i] + zd(y[i].re, y[i].im) : zd(y[i].re, y[i].im);
+            xs[i] = v;
+            if (xt) xt[(size_t)i * ix.batch + sys] = v;
+        }
+    } else {
+        for (int i = lane; i < n; i += 32) io_store<TF, IO>(io, sys, n, i, y[i]);
+    }
+}
+
+template <class TF, class TD, int IO, int CH, int ST>
+__global__ void __launch_bounds__(256)
+k_solve_split_multi(MultiSolve<TF> ms) {
+    int b = 0;
+    while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
+    solve_split_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
+}
+
 }  // namespace cng
 
 namespace cng {
@@ -2075,6 +2283,66 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
     CNG_LAUNCH("k_solve_compact_multi");
 }
 
+template <class TF>
+static size_t split_smem(const Banded& h, int nwarps, int sched) {
+    const CompactSchedule sc = kSchedules[sched];
+    const int k = chunk_index(sc.chunk);
+    size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
+    off = (off + 15) & ~(size_t)15;
+    const size_t per_warp = (size_t)(h.n + 64) + (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * 2 +
+                            ((size_t)sc.stages * sc.chunk * 2 * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    return off + sizeof(TF) * per_warp * nwarps;
+}
+
+template <class TF, class TD, int IO, int CH, int ST>
+static void launch_split_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
+                           const std::vector<SolveIo>& ios, int sched, cudaStream_t st) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(k_solve_split_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024);
+    });
+    // warps per block as launch_multi_t: the most resident warps per SM, and a block for every SM
+    // when the batch is small
+    auto smem_of = [&](int w) {
+        size_t m = 0;
+        for (const Banded* h : hs) m = std::max(m, split_smem<TF>(*h, w, sched));
+        return m;
+    };
+    int total = 0;
+    for (const Banded* h : hs) total += h->batch;
+    int nw = 1, resident = 0;
+    for (int w = 1; w <= 8; ++w) {
+        const size_t m = smem_of(w);
+        if (m > 220 * 1024) break;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_split_multi<TF, TD, IO, CH, ST>, 32 * w,
+                                                          m) != cudaSuccess)
+            per_sm = 1;
+        if (per_sm * w >= resident) { resident = per_sm * w; nw = w; }
+    }
+    nw = std::min(nw, std::max(1, ceil_div(total, sm_count())));
+    const size_t smem = smem_of(nw);
+    if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
+    MultiSolve<TF> ms{};
+    ms.nb = (int)hs.size();
+    std::vector<int> order(hs.size());
+    for (size_t i = 0; i < hs.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->batch > hs[b]->batch; });
+    int blocks = 0;
+    for (int k = 0; k < ms.nb; ++k) {
+        const int i = order[k];
+        ms.block_start[k] = blocks;
+        ms.ix[k] = compact_idx(*hs[i], CH);
+        ms.cd[k] = cds[i];
+        ms.io[k] = ios[i];
+        blocks += ceil_div(hs[i]->batch, nw);
+    }
+    ms.block_start[ms.nb] = blocks;
+    k_solve_split_multi<TF, TD, IO, CH, ST><<<blocks, 32 * nw, smem, st>>>(ms);
+    CNG_LAUNCH("k_solve_split_multi");
+}
+
 // the schedule of the handles (the autotuner sets one for all the buckets of a step; the default
 // when they differ)
 template <class TF, class TD, int IO>
@@ -2092,6 +2360,9 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, sched, st); break;
         case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, sched, st); break;
         case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, sched, st); break;
+        case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, sched, st); break;
+        case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, sched, st); break;
+        case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, sched, st); break;
     }
 }
@@ -2171,13 +2442,14 @@ int cng_banded_compact(cng_banded* hh, void* stream) {
     CNG_TRY({ cng::compact(*reinterpret_cast<cng::Banded*>(hh), static_cast<cudaStream_t>(stream)); })
 }
 
-int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages) {
+int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages, int32_t* split) {
     CNG_TRY({
         if (!count) throw InvalidArgument("null argument");
         *count = kNumSchedules;
         for (int k = 0; k < kNumSchedules; ++k) {
             if (chunk) chunk[k] = kSchedules[k].chunk;
             if (stages) stages[k] = kSchedules[k].stages;
+            if (split) split[k] = kSchedules[k].split;
         }
     })
 }

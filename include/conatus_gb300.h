@@ -111,11 +111,13 @@ int cng_banded_solve_batch_xt(int nh, cng_banded* const* h, const void* const* b
                               void* const* xt, int accumulate, void* stream);
 
 /* Schedules of the compact solve (the batched-solve kernel of the step): count, and per schedule
- * the columns per staged chunk of the factor streams and the depth of the staging ring. No
+ * the columns per staged chunk of the factor streams, the depth of the staging ring and whether it
+ * runs one system per warp with the lanes split over entries and real/imaginary parts (split = 1:
+ * the latency variant for small batches; else two systems per warp). Any output may be NULL. No
  * reference counterpart: the reference picks its solve kernel (level-scheduled streams or the band
  * kernel) by constructor flags (python/conatus/runtime/cuda.py:140-152); here the choice is timed
  * (conatus_gb300.autotune). */
-int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages);
+int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages, int32_t* split);
 /* Schedule of a handle: 0 .. count-1 a compact schedule (needs cng_banded_compact), -1 the band
  * kernel (one warp per system, no compact streams). cng_banded_solve_batch uses the handles'
  * common schedule (schedule 0 when they differ; the band kernel per bucket when all are -1). */
