@@ -35,7 +35,7 @@ def import_reference(ref: str):
 
 
 # ------------------------------------------------------------------------------------------------
-# problems of the benchmark configurations (BASELINE configs, small resolutions for fixtures)
+# problems of the benchmark configurations (small resolutions for the fixtures)
 
 def burgers(cn, N=128, nu=0.01 / np.pi):
     m = cn.Model(cn.Box(x=cn.walls(-1, 1)), name="Burgers", nu=nu)
