@@ -176,33 +176,41 @@ __global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, c
         const long long t = (long long)m * n + i;
         const double2* xm = x + (long long)m * n;
         const double* mv = mono + (long long)m * nmono;
+        const double2 bv = b[t];                            // in flight during the row's entries
         double ar = 0.0, ai = 0.0;
-        int e = ptr[i];
-        const int e1 = ptr[i + 1];
-        while (e < e1) {
-            const int tt = code[e] >> 1;                    // -1: M
-            double gr = 0.0, gi = 0.0;
-            for (; e < e1; ++e) {
-                const int cd = code[e];
-                if ((cd >> 1) != tt) break;
-                const double v = val[e];
-                // x row-major over the systems when given: the warp's 32 systems read one line
-                const double2 xv = xT ? xT[(size_t)col[e] * nsys + m] : xm[col[e]];
-                if (cd & 1) {                               // i v x
-                    gr = fma(-v, xv.y, gr);
-                    gi = fma(v, xv.x, gi);
-                } else {
-                    gr = fma(v, xv.x, gr);
-                    gi = fma(v, xv.y, gi);
-                }
-            }
+        const int e0 = ptr[i], e1 = ptr[i + 1];
+        // one pass over the row's entries (no data-dependent inner loop, so the loads of the next
+        // entries issue ahead); a term's group sum joins ar, ai when the term changes, as in the
+        // group-by-group order
+        auto scale = [&](int tt) {
             // c = 1: no multiply; a merged list: its scale per (row, system) (NaN without the table)
-            const double sc = tt == kMergedTerm ? (rowscale ? rowscale[(size_t)i * nsys + m] : __longlong_as_double(0x7ff8000000000000LL))
-                                                : (tt < 0 ? a : (CONE ? mv[tt] : c * mv[tt]));
+            return tt == kMergedTerm ? (rowscale ? rowscale[(size_t)i * nsys + m] : __longlong_as_double(0x7ff8000000000000LL))
+                                     : (tt < 0 ? a : (CONE ? mv[tt] : c * mv[tt]));
+        };
+        int tt = e0 < e1 ? code[e0] >> 1 : 0;
+        double gr = 0.0, gi = 0.0;
+#pragma unroll 4
+        for (int e = e0; e < e1; ++e) {
+            const int cd = code[e];
+            if ((cd >> 1) != tt) {
+                const double sc = scale(tt);
+                ar = fma(sc, gr, ar);
+                ai = fma(sc, gi, ai);
+                gr = gi = 0.0;
+                tt = cd >> 1;
+            }
+            const double v = val[e];
+            // x row-major over the systems when given: the warp's 32 systems read one line
+            const double2 xv = xT ? xT[(size_t)col[e] * nsys + m] : xm[col[e]];
+            const bool im = cd & 1;                          // i v x
+            gr = fma(im ? -v : v, im ? xv.y : xv.x, gr);
+            gi = fma(v, im ? xv.x : xv.y, gi);
+        }
+        if (e0 < e1) {
+            const double sc = scale(tt);
             ar = fma(sc, gr, ar);
             ai = fma(sc, gi, ai);
         }
-        const double2 bv = b[t];
         r[t] = make_double2(bv.x - ar, bv.y - ai);
     }
 }
