@@ -485,7 +485,8 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     c2<R>* col = x + b.n;
     c2<R>* der = col + Ny;
     const double2* src = state + b.offset + (long long)m * b.n;
-    for (int i = lane; i < b.n; i += 32) {
+#pragma unroll 4
+    for (int i = lane; i < b.n; i += 32) {             // unrolled: the loads of 4 rows in flight
         const double2 v = src[i];
         x[i] = mk<R>(R(v.x), R(v.y));
     }
@@ -502,6 +503,7 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
         const int oy = fd[3];
         const int ox = d.share ? 0 : fd[2], oz = d.share ? 0 : fd[4];   // shared: applied later
         const int* cp = b.colpos + (size_t)f * Ny;
+#pragma unroll 4
         for (int nn = lane; nn < Ny; nn += 32) {
             const int pos = cp[nn];
             col[nn] = pos >= 0 ? x[pos] : mk<R>(R(0), R(0));
@@ -685,12 +687,14 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
         if (d.ndir == 2) h = H + ((oc * d.Kx + jx) * d.Nzc + slot) * Ny;
         else if (d.ndir == 1) h = H + (oc * d.Kx + jx) * Ny;
         else h = H + oc * Ny;
+#pragma unroll 4
         for (int nn = lane; nn < Ny; nn += 32) {
             const c2<R> v = h[nn];
             hs[o * Ny + nn] = make_double2((double)v.x, (double)v.y);
         }
     }
     __syncwarp();
+#pragma unroll 2
     for (int i = lane; i < b.n; i += 32) {
         const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
         double2 v = make_double2(0.0, 0.0);
