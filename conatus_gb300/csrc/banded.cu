@@ -744,7 +744,7 @@ struct Banded {
     std::vector<int> perm_host;
     // compact bucket-union form (built by compact())
     bool compact_ready = false;
-    int cL = 0, cU = 0, cV = 0, cMaxL = 0, cMaxU = 0, cWg = 0;
+    int cL = 0, cU = 0, cV = 0, cWg = 0;
     int cMaxLk[4] = {0, 0, 0, 0}, cMaxUk[4] = {0, 0, 0, 0};   // largest stream chunk per chunk size 2, 4, 8, 16
     int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
     int* c_offL = nullptr;
@@ -2137,9 +2137,6 @@ static void compact(Banded& h, cudaStream_t st) {
             if (mvt[(size_t)a * n + i]) Vcol.push_back(i);
         offV[a + 1] = (int)Vcol.size();
     }
-    int maxL = 1, maxU = 1;
-    for (int j0 = 0; j0 < n - 1; j0 += kCChunk) maxL = std::max(maxL, offL[std::min(j0 + kCChunk, n - 1)] - offL[j0]);
-    for (int s0 = 0; s0 < n; s0 += kCChunk) maxU = std::max(maxU, offU[std::min(s0 + kCChunk, n)] - offU[s0]);
     for (int k = 0; k < 4; ++k) {
         const int ch = kChunkSizes[k];
         int ml = 1, mu = 1;
@@ -2151,8 +2148,6 @@ static void compact(Banded& h, cudaStream_t st) {
     h.cL = (int)Lrow.size();
     h.cU = (int)Udist.size();
     h.cV = (int)Vcol.size();
-    h.cMaxL = maxL;
-    h.cMaxU = maxU;
     h.cWg = (h.batch + kGroup - 1) / kGroup;
     auto up = [&](auto** d, const auto& v) {
         using E = std::remove_reference_t<decltype(v[0])>;
