@@ -34,3 +34,19 @@ def test_library_reports_no_device_on_cpu_host():
     from conatus_gb300 import _lib
     if not torch.cuda.is_available():
         assert _lib.lib().cng_cuda_available() == 0
+
+
+def test_solve_schedule_table():
+    """The schedules the autotuner times: chunks of 2-16 columns, rings 2-4 deep, the split-lane
+    variants flagged (a host-only query)."""
+    from conatus_gb300 import autotune
+    n = ctypes.c_int32()
+    from conatus_gb300._lib import call
+    call("cng_banded_schedules", ctypes.byref(n), None, None, None)
+    chunk, stages, split = ((ctypes.c_int32 * n.value)() for _ in range(3))
+    call("cng_banded_schedules", ctypes.byref(n), chunk, stages, split)
+    assert n.value >= 8
+    assert all(chunk[k] in (2, 4, 8, 16) and 2 <= stages[k] <= 4 for k in range(n.value))
+    assert autotune.schedules() == [-1] + list(range(n.value))
+    assert autotune.split_schedules() == {k for k in range(n.value) if split[k]}
+    assert autotune.split_schedules()                     # the latency variant is offered
