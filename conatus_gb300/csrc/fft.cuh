@@ -195,6 +195,38 @@ __device__ __forceinline__ void stage_ct(const c2<R>* __restrict__ a, c2<R>* __r
     constexpr int Lr = L / RAD;
     constexpr int tstep = L / (Ns * RAD);
     const int nt = blockDim.x;
+    if constexpr (Ns == 1 || (Ns < 32 && sizeof(R) == 8)) {
+        // early stages (short runs of Ns consecutive outputs): the sequence index fastest across
+        // the threads, so the stride-RAD writes of neighbouring threads fall in rows LS apart (LS
+        // odd: other banks) instead of Ns RAD elements apart in one row (a few banks for all).
+        // Measured on the channel's F: the first stage in both precisions (FP32 2.40 -> 2.20 ms),
+        // the twiddled early stages in FP64 only (FP64 15.29 -> 14.94 ms; FP32 lost 0.07 ms: its
+        // twiddles are then loaded per butterfly instead of once per thread)
+        if ((B & (B - 1)) == 0) {
+            const int sh = __ffs(B) - 1;
+            for (int q = threadIdx.x; q < Lr * B; q += nt) {
+                const int bt = q & (B - 1), j = q >> sh;
+                const int k = j % Ns;
+                const c2<R>* ab = a + bt * LS + j;
+                c2<R>* bb = b + bt * LS + (j / Ns) * Ns * RAD + k;
+                c2<R> v[RAD];
+#pragma unroll
+                for (int t = 0; t < RAD; ++t) v[t] = ab[t * Lr];
+                if (Ns > 1) {
+#pragma unroll
+                    for (int t = 1; t < RAD; ++t) {
+                        c2<R> w = tw[t * k * tstep];
+                        if (S > 0) w.y = -w.y;
+                        v[t] = mul<R>(v[t], w);
+                    }
+                }
+                dft<R, S, RAD>(v);
+#pragma unroll
+                for (int t = 0; t < RAD; ++t) bb[t * Ns] = v[t];
+            }
+            return;
+        }
+    }
     const int G = nt >= Lr ? nt / Lr : 1;
     for (int q = threadIdx.x; q < Lr * G; q += nt) {
         const int j = q % Lr, g = q / Lr;
