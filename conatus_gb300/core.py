@@ -70,7 +70,7 @@ def _pack_csr(mats, dtype):
         d = np.ascontiguousarray(d, dtype=np.complex128 if _kind(dtype) else np.float64)
         if ip.shape[0] != n + 1:
             raise ValueError("indptr must have n+1 entries")
-        if ix.shape[0] != d.shape[0]:
+        if ix.shape[0] != d.shape[0] or ip[0] != 0 or ip[-1] != d.shape[0]:
             raise ValueError("inconsistent CSR arrays (indptr[0] = 0, indptr[n] = nnz = "
                              "len(indices) = len(data) required)")
         ips.append(ip)

@@ -917,6 +917,9 @@ static void build_csr(Banded& h, const int* indptr, const int* indices, const T*
         const int* ix = indices + off[k];
         const T* d = data + off[k];
         check_csr(n, ip, ix, ip[n]);
+        if (k + 1 < B && off[k] + ip[n] > off[k + 1])
+            throw InvalidArgument("CSR: matrix " + std::to_string(k) + " has " + std::to_string(ip[n]) +
+                                  " entries and overlaps the next matrix's");
         check_finite(n, ip, ix, d);
         for (int o = 0; o < n; ++o) {
             const int i = pos[o];
@@ -1001,7 +1004,6 @@ static void build_shared_structure(Banded& h, const int* indptr, const int* indi
     h.ku = ku;
     h.ldab = 2 * kl + ku + 1;
     h.nnz = nnz;
-    alloc_handle(h);
     const int kv = kl + ku;
     std::vector<long long> dest(std::max(nnz, 1), -1);
     std::vector<int> bptr(h.r + 1, 0), bp, bcol;
@@ -1026,6 +1028,7 @@ static void build_shared_structure(Banded& h, const int* indptr, const int* indi
         if (std::adjacent_find(d2.begin(), d2.end()) != d2.end())
             throw InvalidArgument("shared CSR pattern has duplicate entries (sum them first)");
     }
+    alloc_handle(h);     // after every host check: invalid input is refused before device work
     dalloc(&h.bulk_dest, dest.size(), sizeof(long long));
     dalloc(&h.bptr, bptr.size(), sizeof(int));
     dalloc(&h.bp, std::max<size_t>(bp.size(), 1), sizeof(int));
@@ -1207,27 +1210,19 @@ int cng_banded_create_csr(int dtype, int batch, int n, const int32_t* indptr, co
         h->dtype = dtype; h->batch = batch; h->n = n; h->r = r; h->pivot = pivot ? 1 : 0;
         h->esz = dtype ? sizeof(zd) : sizeof(double);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        cudaEvent_t e0, e1;
-        CNG_CUDA(cudaEventCreate(&e0));
-        CNG_CUDA(cudaEventCreate(&e1));
-        try {
-            if (dtype == 0)
-                build_csr<double>(*h, indptr, indices, static_cast<const double*>(data),
-                                  reinterpret_cast<const long long*>(nnz_offsets), border, st);
-            else
-                build_csr<zd>(*h, indptr, indices, static_cast<const zd*>(data),
+        // the host checks of build_csr (pattern, border rows, finite entries) run before any
+        // device call, so invalid input is refused the same way with or without a device
+        if (dtype == 0)
+            build_csr<double>(*h, indptr, indices, static_cast<const double*>(data),
                               reinterpret_cast<const long long*>(nnz_offsets), border, st);
-            check_smem(*h);
-            CNG_CUDA(cudaEventRecord(e0, st));
-            launch_factor(*h, st);
-            finish_factor(*h, st, e0, e1);
-        } catch (...) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            throw;
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        else
+            build_csr<zd>(*h, indptr, indices, static_cast<const zd*>(data),
+                          reinterpret_cast<const long long*>(nnz_offsets), border, st);
+        check_smem(*h);
+        EventPair ev;
+        CNG_CUDA(cudaEventRecord(ev.e0, st));
+        launch_factor(*h, st);
+        finish_factor(*h, st, ev.e0, ev.e1);
         *out = reinterpret_cast<cng_banded*>(h.release());
     })
 }
@@ -1249,21 +1244,11 @@ int cng_banded_create_shared(int dtype, int batch, int n, const int32_t* indptr,
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         build_shared_structure(*h, indptr, indices, nnz, border, st);
         check_smem(*h);
-        cudaEvent_t e0, e1;
-        CNG_CUDA(cudaEventCreate(&e0));
-        CNG_CUDA(cudaEventCreate(&e1));
-        try {
-            CNG_CUDA(cudaEventRecord(e0, st));
-            launch_layout_shared(*h, values, st);
-            launch_factor(*h, st);
-            finish_factor(*h, st, e0, e1);
-        } catch (...) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            throw;
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        EventPair ev;
+        CNG_CUDA(cudaEventRecord(ev.e0, st));
+        launch_layout_shared(*h, values, st);
+        launch_factor(*h, st);
+        finish_factor(*h, st, ev.e0, ev.e1);
         *out = reinterpret_cast<cng_banded*>(h.release());
     })
 }
@@ -1427,23 +1412,13 @@ int cng_banded_refactor_shared(cng_banded* hh, const void* values, void* stream)
         if (!h->bulk_dest) throw InvalidArgument("refactor_shared: handle was not created from a shared pattern");
         if (!values) throw InvalidArgument("null values");
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        cudaEvent_t e0, e1;
-        CNG_CUDA(cudaEventCreate(&e0));
-        CNG_CUDA(cudaEventCreate(&e1));
-        try {
-            CNG_CUDA(cudaEventRecord(e0, st));
-            launch_layout_shared(*h, values, st);
-            launch_factor(*h, st);
-            h->transposed_ready = false;
-            finish_factor(*h, st, e0, e1);
-            if (h->fp32_ready) make_fp32(*h, st);
-        } catch (...) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            throw;
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        EventPair ev;
+        CNG_CUDA(cudaEventRecord(ev.e0, st));
+        launch_layout_shared(*h, values, st);
+        launch_factor(*h, st);
+        h->transposed_ready = false;
+        finish_factor(*h, st, ev.e0, ev.e1);
+        if (h->fp32_ready) make_fp32(*h, st);
     })
 }
 

@@ -40,6 +40,25 @@ inline void cuda_check(cudaError_t e, const char* what) {
 #define CNG_CUDA(call) ::cng::cuda_check((call), #call)
 #define CNG_LAUNCH(what) ::cng::cuda_check(cudaGetLastError(), what)
 
+// Two timing events, destroyed on every exit path (a failed second creation frees the first).
+struct EventPair {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    EventPair() {
+        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+        const cudaError_t e = cudaEventCreate(&e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cuda_check(e, "cudaEventCreate");
+        }
+    }
+    ~EventPair() {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+};
+
 // ---- complex double with explicit operations (no library dependency in device code) ----------
 struct alignas(16) zd {
     double re, im;
