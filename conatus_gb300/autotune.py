@@ -98,6 +98,8 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
             times[sched] = e0.elapsed_time(e1) / reps
         except ValueError:
             continue                      # schedule does not fit (shared memory): not a candidate
+    if not times:
+        raise ValueError("no solve schedule fits these systems (shared memory)")
     best = min(times, key=times.get)
     apply(fs, best)
     _CACHE[sig] = (best, times)
