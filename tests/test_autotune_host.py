@@ -121,3 +121,17 @@ def test_environment_fixes_the_schedule(fake, monkeypatch):
     dev = _Dev(fake)
     assert autotune.tune_solve(dev, (1.0, 0.5), fs) == {3: None}
     assert fs[0].schedule == 3 and dev.solves == 0
+
+
+def test_refine_groups_balance_the_work():
+    """The FP32 form's two refinement groups (two streams): buckets split largest first into two
+    groups of about equal work (systems x length); every bucket in exactly one group."""
+    from conatus_gb300.ivp import DeviceProblem
+    B = types.SimpleNamespace
+    stub = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None)
+    g = DeviceProblem._refine_groups(stub)
+    assert sorted(sum(g, [])) == [0, 1, 2, 3, 4]
+    w = [sum(stub.nsys[b] * stub.tpl.buckets[b].n for b in grp) for grp in g]
+    assert len(g) == 2 and abs(w[0] - w[1]) <= 96 * 522
+    one = B(nsys=[127], tpl=B(buckets=[B(n=262)]), _groups=None)
+    assert DeviceProblem._refine_groups(one) == [[0]]
