@@ -1293,7 +1293,12 @@ int cng_banded_solve_mapped(const cng_banded* hh, const void* rhs, const int64_t
     CNG_TRY({
         const Banded* h = as_banded(hh);
         if (!rhs || !x) throw InvalidArgument("BandedBatch.solve_mapped_ptr: null device pointer");
-        if (rhs == x) throw InvalidArgument("BandedBatch.solve_mapped_ptr: rhs and x must not alias");
+        // in place with one map for both is a solve in place (every kernel reads a system's whole
+        // right-hand side before it writes any of its solution, and the systems' entries are
+        // disjoint); with two maps, systems would read entries that others already wrote
+        if (rhs == x && rows != cols)
+            throw InvalidArgument("BandedBatch.solve_mapped_ptr: rhs and x alias with different maps "
+                                  "(pass a separate x, or the same map for rows and cols)");
         SolveIo io{rhs, x, reinterpret_cast<const long long*>(rows), reinterpret_cast<const long long*>(cols),
                    nullptr, nullptr};
         launch_solve(*h, IO_MAPPED, io, static_cast<cudaStream_t>(stream));

@@ -84,6 +84,17 @@ def test_mapped_and_split(rng, cuda_lib):
         torch.cuda.synchronize()
         tol = tol_vs_reference("banded_rb32x16.npz", label)
         assert rel(xg.cpu().numpy()[cols], x) < tol, label
+        # in place with one map for rows and cols (allowed, as in the reference); two maps refused
+        gi = _t(glob)
+        B.solve_mapped_ptr(gi.data_ptr(), r_.data_ptr(), gi.data_ptr(), r_.data_ptr())
+        torch.cuda.synchronize()
+        assert rel(gi.cpu().numpy()[rows], x) < tol, label
+        gn = _t(glob[rows].reshape(-1))
+        B.solve_mapped_ptr(gn.data_ptr(), 0, gn.data_ptr(), 0)
+        torch.cuda.synchronize()
+        assert rel(gn.cpu().numpy().reshape(Bn, n), x) < tol, label
+        with pytest.raises(ValueError, match="alias"):
+            B.solve_mapped_ptr(g.data_ptr(), r_.data_ptr(), g.data_ptr(), c_.data_ptr())
         if dtype.kind == "c":
             # split: real data vector, b = re[rows_c] + i re[rows_s]
             tot2 = 2 * tot
