@@ -75,7 +75,7 @@ int cng_banded_solve(const cng_banded* h, void* b, void* stream);
 /* b_m[i] = rhs[rows[m*n + i]], x[cols[m*n + i]] = x_m[i]; rows/cols int64 device arrays, NULL =
  * contiguous. rhs == x is a solve in place and needs one map for both (rows == cols, or both
  * NULL); rhs == x with two maps is refused (status 1). Replaces cuda.BandedBatch.solve_mapped_ptr
- * (module.cpp:300-311; in place with one map as python/conatus/runtime/cuda.py:219-229 allows). */
+ * (module.cpp:300-311; in place with one map as python/conatus/runtime/cuda.py:218-230 allows). */
 int cng_banded_solve_mapped(const cng_banded* h, const void* rhs, const int64_t* rows, void* x,
                             const int64_t* cols, void* stream);
 
