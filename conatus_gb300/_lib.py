@@ -27,6 +27,8 @@ _SIGS = {
     "cng_cuda_available": [],
     "cng_device_name": [c_int, c_char_p, c_int],
     "cng_mem_info": [P, P],
+    "cng_pool_stats": [P, P, P, P],
+    "cng_pool_trim": [],
     "cng_banded_create_csr": [c_int, c_int, c_int, P, P, P, P, P, c_int, c_int, P, P],
     "cng_banded_create_shared": [c_int, c_int, c_int, P, P, c_int, P, P, c_int, c_int, P, P],
     "cng_banded_refactor_shared": [P, P, P],

@@ -244,8 +244,22 @@ class _BandedBatch:
     capacitance_cond_max = property(lambda self: self._h.cond_max)
     col_border = property(lambda self: False)
     col_border_nnz = property(lambda self: 0)
-    # the GB300 solve reads the band directly (one warp per system); no level schedule is built
+    # the GB300 solve reads the band directly (one warp per system); no level schedule is built,
+    # so the reference's level-schedule diagnostics (module.cpp:356-373) report none
     level_scheduled = property(lambda self: False)
+    level_transposed = property(lambda self: False)
+    level_merged = property(lambda self: False)
+    level_depth_forward = property(lambda self: 0)
+    level_depth_backward = property(lambda self: 0)
+    level_steps_forward = property(lambda self: 0)
+    level_steps_backward = property(lambda self: 0)
+    level_stream_bytes = property(lambda self: 0)
+    level_t_stream_bytes = property(lambda self: 0)
+    level_note = property(lambda self: "no level schedule: the GB300 solve sweeps the LU band, "
+                                       "one warp per system")
+    level_t_note = property(lambda self: "no level schedule: the transposed solve sweeps the LU band")
+    level_t_steps = property(lambda self: (0, 0))
+    band_released = property(lambda self: False)
 
     def _check_dims(self, batch, n, where):
         if batch != self._h.batch or n != self._h.n:
@@ -270,6 +284,10 @@ class _BandedBatch:
 
     def build_transpose_schedule(self):
         self.prepare_transpose()
+
+    def release_band(self):
+        """The reference frees the LU band once its level schedules hold the factors
+        (module.cpp:366-367). Every solve here reads the band, so it stays: nothing to release."""
 
     def solve_transpose_ptr(self, ptr, batch, n, stream=0):
         self._check_dims(batch, n, "solve_transpose_ptr")
@@ -311,9 +329,30 @@ def synchronize() -> None:
     torch.cuda.synchronize()
 
 
+def pool_stats() -> tuple:
+    """(live bytes, cached bytes, allocations, reuses) of the device memory the library's handles
+    hold, as the reference core's cuda.pool_stats (core/bindings/module.cpp:450-453). Nothing is
+    cached: a handle's memory goes back to the driver when the handle is destroyed."""
+    v = [ctypes.c_uint64() for _ in range(4)]
+    call("cng_pool_stats", *(ctypes.byref(x) for x in v))
+    return tuple(int(x.value) for x in v)
+
+
+def pool_trim() -> None:
+    """The reference's cuda.pool_trim (module.cpp:454): no cached blocks here, so nothing to do."""
+    call("cng_pool_trim")
+
+
+def plan_cache_size() -> int:
+    """The reference's count of cached cuFFT plans (module.cpp:455). The transforms here use
+    compile-time plans inside the kernels and keep no runtime plans: 0."""
+    return 0
+
+
 cuda = types.SimpleNamespace(
     BandedBatchD=BandedBatchD, BandedBatchZ=BandedBatchZ, available=available,
-    device_name=device_name, synchronize=synchronize)
+    device_name=device_name, synchronize=synchronize, pool_stats=pool_stats, pool_trim=pool_trim,
+    plan_cache_size=plan_cache_size)
 
 
 def cuda_compiled() -> bool:

@@ -781,7 +781,7 @@ struct Banded {
                         (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
                         (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
                         (void*)c_U32, (void*)c_V32})
-            if (p) cudaFree(p);
+            dev_free(p);
     }
 
     template <class T>
@@ -803,15 +803,7 @@ struct Banded {
 
 template <class P>
 static void dalloc(P** p, size_t count, size_t esz) {
-    void* q = nullptr;
-    size_t bytes = std::max<size_t>(count * esz, 16);
-    cudaError_t e = cudaMalloc(&q, bytes);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        throw CudaFailure(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes failed: " +
-                          cudaGetErrorString(e));
-    }
-    *p = static_cast<P*>(q);
+    *p = static_cast<P*>(dev_alloc(std::max<size_t>(count * esz, 16)));
 }
 
 static void alloc_handle(Banded& h) {

@@ -33,6 +33,13 @@ struct CudaFailure : std::runtime_error {
 
 void set_error(const std::string& msg);
 
+// Device memory held by the library's handles (banded factors, evaluator buffers): cudaMalloc and
+// cudaFree with live-byte and allocation counters (the counters of the reference core's pool).
+// dev_free also takes pointers that dev_alloc did not return (they are freed, not counted).
+void* dev_alloc(size_t bytes);
+void dev_free(void* p);
+void pool_counters(uint64_t* live_bytes, uint64_t* n_alloc);
+
 inline void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess)
         throw CudaFailure(std::string(what) + ": " + cudaGetErrorString(e));

@@ -2,7 +2,9 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "common.cuh"
 #include "conatus_gb300.h"
@@ -10,6 +12,61 @@
 namespace cng {
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+struct Pool {
+    std::mutex mu;
+    std::unordered_map<void*, size_t> bytes;
+    uint64_t live = 0, n_alloc = 0;
+};
+// never destroyed: handles may still be released while the process exits
+Pool& pool() {
+    static Pool* p = new Pool;
+    return *p;
+}
+}  // namespace
+
+void* dev_alloc(size_t bytes) {
+    void* q = nullptr;
+    const cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw CudaFailure(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes failed: " +
+                          cudaGetErrorString(e));
+    }
+    Pool& p = pool();
+    try {
+        std::lock_guard<std::mutex> lock(p.mu);
+        p.bytes[q] = bytes;
+        p.live += bytes;
+        ++p.n_alloc;
+    } catch (...) {
+        cudaFree(q);
+        throw;
+    }
+    return q;
+}
+
+void dev_free(void* q) {
+    if (!q) return;
+    {
+        Pool& p = pool();
+        std::lock_guard<std::mutex> lock(p.mu);
+        auto it = p.bytes.find(q);
+        if (it != p.bytes.end()) {
+            p.live -= it->second;
+            p.bytes.erase(it);
+        }
+    }
+    cudaFree(q);
+}
+
+void pool_counters(uint64_t* live_bytes, uint64_t* n_alloc) {
+    Pool& p = pool();
+    std::lock_guard<std::mutex> lock(p.mu);
+    if (live_bytes) *live_bytes = p.live;
+    if (n_alloc) *n_alloc = p.n_alloc;
+}
 }  // namespace cng
 
 extern "C" {
@@ -52,6 +109,16 @@ int cng_mem_info(uint64_t* free_bytes, uint64_t* total_bytes) {
     if (total_bytes) *total_bytes = t;
     return 0;
 }
+
+int cng_pool_stats(uint64_t* live_bytes, uint64_t* cached_bytes, uint64_t* n_alloc, uint64_t* n_reuse) {
+    CNG_TRY({
+        cng::pool_counters(live_bytes, n_alloc);
+        if (cached_bytes) *cached_bytes = 0;       // freed memory goes back to the driver at once
+        if (n_reuse) *n_reuse = 0;
+    })
+}
+
+int cng_pool_trim(void) { return 0; }
 
 struct cng_graph {
     cudaGraph_t graph = nullptr;

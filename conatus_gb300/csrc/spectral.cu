@@ -833,9 +833,14 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
 
 template <class P>
 static P* upload(const P* h, size_t n) {
-    P* d = nullptr;
-    CNG_CUDA(cudaMalloc(&d, std::max<size_t>(sizeof(P) * n, 16)));
-    if (n) CNG_CUDA(cudaMemcpy(d, h, sizeof(P) * n, cudaMemcpyHostToDevice));
+    P* d = static_cast<P*>(dev_alloc(std::max<size_t>(sizeof(P) * n, 16)));
+    if (n) {
+        const cudaError_t e = cudaMemcpy(d, h, sizeof(P) * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            dev_free(d);
+            cuda_check(e, "cudaMemcpy (upload)");
+        }
+    }
     return d;
 }
 
@@ -865,7 +870,7 @@ struct Rhs {
     int* f_ox = nullptr;
 
     ~Rhs() {
-        for (void* p : owned) cudaFree(p);
+        for (void* p : owned) dev_free(p);
     }
     template <class P> P* keep(P* p) { owned.push_back((void*)p); return p; }
 
@@ -1159,12 +1164,9 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     w = std::max<size_t>(w, rs * nfo * mx * mz * h->my);
     w = std::max<size_t>(w, cs * nfo * P);
     h->W_bytes = w;
-    CNG_CUDA(cudaMalloc(&h->S, h->S_bytes));
-    h->keep(h->S);
-    CNG_CUDA(cudaMalloc(&h->W1, w));
-    h->keep(h->W1);
-    CNG_CUDA(cudaMalloc(&h->W2, w));
-    h->keep(h->W2);
+    h->S = h->keep(dev_alloc(h->S_bytes));
+    h->W1 = h->keep(dev_alloc(w));
+    h->W2 = h->keep(dev_alloc(w));
     // the Nyquist and padding slots of the spectra are never written: zero them once
     CNG_CUDA(cudaMemset(h->S, 0, h->S_bytes));
     CNG_CUDA(cudaMemset(h->W1, 0, w));

@@ -31,6 +31,13 @@ int cng_device_name(int dev, char* buf, int buflen);
 /* Free and total device memory in bytes (admission by footprint; the reference's memory planner
  * python/conatus/runtime/memory.py predicts the same quantity). */
 int cng_mem_info(uint64_t* free_bytes, uint64_t* total_bytes);
+/* Device memory held by the library's handles: live bytes and allocations so far; cached bytes and
+ * reuses are 0 (freed memory goes back to the driver at once, there is no pool). Replaces
+ * cuda.pool_stats (core/bindings/module.cpp:450-453). Any argument may be NULL. */
+int cng_pool_stats(uint64_t* live_bytes, uint64_t* cached_bytes, uint64_t* n_alloc, uint64_t* n_reuse);
+/* Nothing is cached, so nothing to return to the driver: 0. Replaces cuda.pool_trim
+ * (core/bindings/module.cpp:454). */
+int cng_pool_trim(void);
 
 /* ---- batched bordered-banded factor and solves --------------------------------------------- */
 

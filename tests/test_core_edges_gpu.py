@@ -138,3 +138,24 @@ def test_factorizations_leave_no_device_memory(rng, cuda_lib):
         del B
     torch.cuda.synchronize()
     assert free() >= f0 - (2 << 20)                     # driver page granularity
+
+
+def test_pool_counts_handle_memory(rng, cuda_lib):
+    """cuda.pool_stats counts the device memory of live handles: a factored batch adds at least
+    its LU band, and destroying it gives every byte back."""
+    import gc
+    from conatus_gb300 import core
+    gc.collect()
+    live0, _, nalloc0, _ = core.cuda.pool_stats()
+    n, batch = 40, 3
+    mats = []
+    for _ in range(batch):
+        C = sp.csr_matrix(_almost_banded(rng, n, 2, 3, [0, 1], float))
+        mats.append((n, C.indptr, C.indices, C.data))
+    B = core.cuda.BandedBatchD(mats, [0, 1])
+    live1, _, nalloc1, _ = core.cuda.pool_stats()
+    ldab = 2 * B.kl + B.ku + 1
+    assert live1 - live0 >= batch * n * ldab * 8 and nalloc1 > nalloc0
+    del B
+    gc.collect()
+    assert core.cuda.pool_stats()[0] == live0

@@ -50,3 +50,23 @@ def test_solve_schedule_table():
     assert autotune.schedules() == [-1] + list(range(n.value))
     assert autotune.split_schedules() == {k for k in range(n.value) if split[k]}
     assert autotune.split_schedules()                     # the latency variant is offered
+
+
+def test_pool_queries_and_device_surface_attributes():
+    """Host-only queries of the reference core's device surface: the pool counters (nothing
+    cached), pool_trim, plan_cache_size, and every member the reference's runtime wrapper reads
+    from a device BandedBatch (python/conatus/runtime/cuda.py)."""
+    from conatus_gb300 import core
+    live, cached, n_alloc, n_reuse = core.cuda.pool_stats()
+    assert live >= 0 and n_alloc >= 0 and cached == 0 and n_reuse == 0
+    core.cuda.pool_trim()
+    assert core.cuda.plan_cache_size() == 0
+    for name in ("batch", "build_transpose_schedule", "capacitance_cond_max", "col_border",
+                 "col_border_nnz", "factor_ms", "kl", "ku", "n", "pivot", "rank", "prepare_transpose",
+                 "release_band", "solve", "solve_ptr", "solve_mapped_ptr", "solve_split_ptr",
+                 "solve_transpose", "solve_transpose_ptr", "level_scheduled", "level_transposed",
+                 "level_merged", "level_depth_forward", "level_depth_backward", "level_steps_forward",
+                 "level_steps_backward", "level_stream_bytes", "level_t_stream_bytes", "level_note",
+                 "level_t_note", "level_t_steps", "band_released"):
+        for cls in (core.BandedBatchD, core.BandedBatchZ):
+            assert hasattr(cls, name), (cls.__name__, name)
