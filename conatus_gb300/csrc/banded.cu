@@ -1162,7 +1162,7 @@ static const Banded* as_banded(const cng_banded* h) {
 // ------------------------------------------------------------------------------------------------
 // Static staging for cng_banded_solve_host_static: a fixed 8 MiB device array (1 Mi complex64 or
 // 512 Ki complex128 entries), no allocation at run time. Nothing in it needs to start at zero (a
-// solve overwrites the bytes it uses). Every call on a device uses the same array.
+// solve overwrites the bytes it uses). Every call on a device uses the same array, one at a time.
 namespace cng {
 constexpr size_t kStaticSolveBytes = size_t(8) << 20;
 static __device__ __align__(256) unsigned char g_static_solve[kStaticSolveBytes];
@@ -1182,6 +1182,17 @@ static void* static_solve_scratch() {
         ptr[dev] = p;
     }
     return ptr[dev];
+}
+
+// Calls on one device take turns on the array: each holds the device's lock from its copy in to
+// the end of its copy out, so calls from several host threads do not overwrite each other's data.
+static std::mutex& static_solve_turn() {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu[kMaxDevices];
+    int dev = 0;
+    CNG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw InvalidArgument("device index above 63");
+    return mu[dev];
 }
 }  // namespace cng
 
@@ -1369,6 +1380,7 @@ int cng_banded_solve_host_static(cng_banded* hh, const void* b_host, void* x_hos
                                   std::to_string(kStaticSolveBytes) + " bytes (use cng_banded_solve_host)");
         if (transpose && !h->transposed_ready)
             throw InvalidArgument("solve_host_static: call cng_banded_prepare_transpose first (it allocates)");
+        std::lock_guard<std::mutex> turn(static_solve_turn());
         void* d = static_solve_scratch();
         cudaStream_t st = nullptr;
         CNG_CUDA(cudaMemcpyAsync(d, b_host, bytes, cudaMemcpyHostToDevice, st));

@@ -150,8 +150,8 @@ int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int t
  * allocates and frees a staging buffer on every call, and freeing device memory waits for the
  * whole device, which stalls every other stream (other runs in flight in a serving loop); a
  * caller under a planned device-memory budget must not grow its footprint either. The first call
- * on a device looks up the array's address. Every call on a device shares the one array:
- * overlapping calls (from several host threads) race on it and must be serialized by the caller. */
+ * on a device looks up the array's address. Every call on a device shares the one array, so
+ * calls on one device take turns (a per-device lock, held from the copy in to the copy out). */
 int cng_banded_solve_host_static(cng_banded* h, const void* b_host, void* x_host, int transpose);
 
 /* ---- pseudospectral explicit right-hand side F(X) ------------------------------------------ */
