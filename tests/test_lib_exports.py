@@ -70,3 +70,28 @@ def test_pool_queries_and_device_surface_attributes():
                  "level_t_note", "level_t_steps", "band_released"):
         for cls in (core.BandedBatchD, core.BandedBatchZ):
             assert hasattr(cls, name), (cls.__name__, name)
+
+
+def test_product_path_does_not_use_the_oracle():
+    """The package never imports the oracle (it is the checker, not a fallback), and bench.py
+    touches it only in its CPU-baseline and reference-arm functions."""
+    import ast
+    pkg = os.path.join(ROOT, "conatus_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith(".py"):
+                tree = ast.parse(open(os.path.join(dirpath, f)).read())
+                for node in ast.walk(tree):
+                    if isinstance(node, ast.ImportFrom):
+                        assert not (node.module or "").startswith("oracle"), (f, node.module)
+                    elif isinstance(node, ast.Import):
+                        assert not any(a.name.startswith("oracle") for a in node.names), f
+    tree = ast.parse(open(os.path.join(ROOT, "bench.py")).read())
+    users = set()
+    for fn in [n for n in tree.body if isinstance(n, ast.FunctionDef)]:
+        for node in ast.walk(fn):
+            if isinstance(node, ast.ImportFrom) and (node.module or "").startswith("oracle"):
+                users.add(fn.name)
+    assert users <= {"cpu_baseline", "run_reference"}, users
+    top = [n for n in tree.body if isinstance(n, (ast.Import, ast.ImportFrom))]
+    assert not any(isinstance(n, ast.ImportFrom) and (n.module or "").startswith("oracle") for n in top)
