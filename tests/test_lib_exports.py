@@ -95,3 +95,21 @@ def test_product_path_does_not_use_the_oracle():
     assert users <= {"cpu_baseline", "run_reference"}, users
     top = [n for n in tree.body if isinstance(n, (ast.Import, ast.ImportFrom))]
     assert not any(isinstance(n, ast.ImportFrom) and (n.module or "").startswith("oracle") for n in top)
+
+
+def test_binding_argument_counts_match_the_header():
+    """Every ctypes signature in the Python binding has as many arguments as the header's
+    declaration of that function (a mismatch would pass wrong values across the C-ABI)."""
+    from conatus_gb300 import _lib
+    txt = open(os.path.join(ROOT, "include", "conatus_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    decls = dict(re.findall(r"\b(cng_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt))
+    checked = 0
+    for name, argtypes in _lib._SIGS.items():
+        if name not in decls:
+            continue
+        params = decls[name].strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert n == len(argtypes), (name, n, len(argtypes))
+        checked += 1
+    assert checked >= 40
