@@ -98,9 +98,15 @@ def test_product_path_does_not_use_the_oracle():
 
 
 def test_binding_argument_counts_match_the_header():
-    """Every ctypes signature in the Python binding has as many arguments as the header's
-    declaration of that function (a mismatch would pass wrong values across the C-ABI)."""
+    """Every ctypes signature in the Python binding has the header declaration's arguments, in
+    number and in type (a mismatch would pass wrong values across the C-ABI: a 32-bit int where
+    the function takes a 64-bit one leaves the register's upper half undefined)."""
     from conatus_gb300 import _lib
+    C = ctypes
+    accepted = {"ptr": (C.c_void_p, C.c_char_p), "int": (C.c_int, C.c_int32), "int32_t": (C.c_int32, C.c_int),
+                "int64_t": (C.c_int64, C.c_longlong), "long long": (C.c_longlong, C.c_int64),
+                "double": (C.c_double,), "float": (C.c_float,), "size_t": (C.c_size_t,),
+                "uint64_t": (C.c_uint64,)}
     txt = open(os.path.join(ROOT, "include", "conatus_gb300.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     decls = dict(re.findall(r"\b(cng_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt))
@@ -109,7 +115,10 @@ def test_binding_argument_counts_match_the_header():
         if name not in decls:
             continue
         params = decls[name].strip()
-        n = 0 if params in ("", "void") else params.count(",") + 1
-        assert n == len(argtypes), (name, n, len(argtypes))
+        params = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+        assert len(params) == len(argtypes), (name, len(params), len(argtypes))
+        for p, a in zip(params, argtypes):
+            kind = "ptr" if "*" in p else " ".join(p.replace("const ", "").split()[:-1])
+            assert a in accepted[kind], (name, p, a)
         checked += 1
     assert checked >= 40
