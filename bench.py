@@ -12,7 +12,8 @@ through the public API with the state copied in from pinned host memory and back
 N > 1 (torchrun): independent replicas, one per GPU (weak scaling, no collective on the path).
 
 ``--impl reference`` times the reference algorithm on the host cores instead: the CPU restatement
-of the reference's IVPSolver step (oracle/ivp.py), on a bounded sample of the same workload.
+of the reference's IVPSolver step (oracle/ivp.py), full steps of the same workload, the solves of
+every system spread over one process per core.
 """
 from __future__ import annotations
 
@@ -245,6 +246,16 @@ def _l2_note(P, cfg, precision):
             f"small problem run from L2 in use too)")
 
 
+def workload_config(args, P, ws):
+    """The ``config`` of both arms' lines: the workload, its size, the replicas and whether the
+    timed steps stream from HBM (the same dict for the GB300 arm and the reference arm)."""
+    cfg = args.cfg
+    return {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
+            "real_unknowns": P.real_unknowns(), "systems": int(sum(P.nsys)),
+            "parallelism": f"replicas x{ws}" if ws > 1 else "1 replica",
+            "l2": _l2_note(P, cfg, args.precision)}
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = _dist()
@@ -346,16 +357,13 @@ def run_gpu(args):
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded initial state of the configuration, conatus_gb300.workloads)",
-        "config": {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
-                   "real_unknowns": P.real_unknowns(), "systems": int(sum(P.nsys)),
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
-                   "l2": _l2_note(P, cfg, args.precision),
-                   "grid": dev.grid, "state_finite": finite,
-                   "solve_schedule": _schedule_summary(dev),
-                   "rhs_transforms": ({"chosen": min(dev.rhs_tuning, key=lambda k: dev.rhs_tuning[k] or 0),
-                                       "ms_per_F": {k: (round(v, 4) if v else None)
-                                                    for k, v in dev.rhs_tuning.items()}}
-                                      if dev.rhs_tuning else None)},
+        "config": workload_config(args, P, ws),
+        "details": {"grid": dev.grid, "state_finite": finite,
+                    "solve_schedule": _schedule_summary(dev),
+                    "rhs_transforms": ({"chosen": min(dev.rhs_tuning, key=lambda k: dev.rhs_tuning[k] or 0),
+                                        "ms_per_F": {k: (round(v, 4) if v else None)
+                                                     for k, v in dev.rhs_tuning.items()}}
+                                       if dev.rhs_tuning else None)},
         "mode_updates_per_s": value * P.real_unknowns(),
         "roofline": roof,
         "solve_roofline": solve_roof,
@@ -444,17 +452,23 @@ def mixed_error(P, C0, cfg, steps):
     return {"steps": steps, "relative_l2": errs, "max": max(errs.values()) if errs else 0.0}
 
 
-def cpu_baseline(args, P, C0, steps=1):
-    """The oracle (CPU restatement of the reference's step) on a bounded sample of the workload:
-    the full F, M X and right-hand side, and the banded solves of a subset of the systems of every
-    bucket (scaled to all systems); factorizations outside the timing."""
-    from oracle.ivp import SampledStepper
+def _host_cores():
     import multiprocessing
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else multiprocessing.cpu_count()
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else multiprocessing.cpu_count()
+
+
+def cpu_baseline(args, P, C0, steps=1, warmup=1):
+    """The oracle (CPU restatement of the reference's step) on the host cores: full steps (F, M X,
+    right-hand side and the solves of every system, spread over one process per core), after the
+    untimed factorization and one untimed step."""
+    from oracle.ivp import ParallelStepper
+    cores = _host_cores()
     cfg = args.cfg
-    st = SampledStepper(P, int(cfg["scheme"][-1]), cfg["dt"], sample_systems=args.cpu_sample_systems,
-                        workers=cores)
-    t_step, desc = st.time_steps(C0, steps)
+    st = ParallelStepper(P, int(cfg["scheme"][-1]), cfg["dt"], workers=cores)
+    try:
+        t_step, desc = st.time_steps(C0, steps, warmup=warmup)
+    finally:
+        st.close()
     return {"value": 1.0 / t_step, "unit": "steps/s", "cores": cores, "kind": "port",
             "sample": desc}
 
@@ -588,26 +602,29 @@ def run_rb_ensemble(args):
 
 
 def run_reference(args):
+    """The reference arm: the oracle's restatement of the reference's CPU step (the reference
+    cannot run on the GPU host: its core needs nanobind and conda LAPACK, its GPU path CuPy) on
+    every host core, ``args.warmup`` untimed and ``args.steps`` timed full steps of the workload."""
     ws, rank, local = _dist()
     if rank != 0:
         return
     from conatus_gb300 import workloads as W
+    from oracle.ivp import ParallelStepper
     P = W.problem(args.config)
     C0 = W.initial_state(args.config, P, seed=0)
-    from oracle.ivp import SampledStepper
-    import multiprocessing
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else multiprocessing.cpu_count()
+    cores = _host_cores()
     cfg = args.cfg
-    st = SampledStepper(P, int(cfg["scheme"][-1]), cfg["dt"], sample_systems=args.cpu_sample_systems,
-                        workers=cores)
-    t_step, desc = st.time_steps(C0, max(1, min(args.steps, 2)), warmup=min(args.warmup, 1))
+    st = ParallelStepper(P, int(cfg["scheme"][-1]), cfg["dt"], workers=cores)
+    try:
+        t_step, desc = st.time_steps(C0, args.steps, warmup=args.warmup)
+    finally:
+        st.close()
     value = 1.0 / t_step
     out = {"impl": "reference", "metric": METRIC[args.config] + " plain FP64", "value": value,
            "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic (seeded initial state of the configuration)",
-           "config": {"workload": f"{args.config} {P.fourier_sizes} x {P.tpl.ncheb} {cfg['scheme']} dt={cfg['dt']}",
-                      "real_unknowns": P.real_unknowns()},
+           "dtype": "f64", "data": "synthetic (seeded initial state of the configuration, conatus_gb300.workloads)",
+           "config": workload_config(args, P, ws),
            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": desc},
            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -621,10 +638,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="channel", choices=list(METRIC) + ["serving", "ks_ensemble", "rb_ensemble"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--cpu-sample-systems", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="channel FP64: skip the FP32 form's line")
-    ap.add_argument("--error-steps", type=int, default=50)
+    ap.add_argument("--error-steps", type=int, default=None,
+                    help="steps of the FP32 form's error run (default: the configuration's length)")
     ap.add_argument("--fourier", type=int, nargs="*", default=None,
                     help="Fourier sizes overriding the configuration's (small cases for profiling)")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests in the stream")
@@ -649,6 +666,8 @@ def main():
         {"serving": run_serving, "ks_ensemble": run_ks_ensemble, "rb_ensemble": run_rb_ensemble}[args.config](args)
         return
     args.cfg = W.CONFIGS[args.config]
+    if args.error_steps is None:
+        args.error_steps = args.cfg.get("finite_steps", args.cfg["steps"])
     if args.impl == "reference":
         run_reference(args)
     else:

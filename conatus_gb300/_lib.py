@@ -64,6 +64,7 @@ _SIGS = {
     "cng_sbdf_rhs": [c_int, P, P, P, P, P, ctypes.c_int64, P],
     "cng_sbdf_rhs_fused": [c_int, P, P, P, P, P, ctypes.c_int64, c_int, P],
     "cng_lincomb": [ctypes.c_int64, P, c_int, P, P, P, P, P],
+    "cng_check_finite": [P, ctypes.c_int64, ctypes.c_int64, P, P],
     "cng_split_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P, P, P],
     "cng_banded_solve_batch_xt": [c_int, P, P, P, P, c_int, P],
     "cng_graph_begin": [P],

@@ -112,6 +112,18 @@ __global__ void k_sbdf_rhs_fused(SbdfArgs a, double* __restrict__ rhs, long long
     }
 }
 
+// Finite-state check: if any of the count doubles of x is a NaN or an infinity (exponent bits all
+// ones), flag[0] = min(flag[0], iteration). One vote per warp, one atomic per warp that saw one.
+__global__ void k_check_finite(const unsigned long long* __restrict__ x, long long count, long long iteration,
+                               unsigned long long* __restrict__ flag) {
+    bool bad = false;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x)
+        bad |= (x[t] & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+    const unsigned any = __ballot_sync(0xffffffffu, bad);
+    if (any && (threadIdx.x & 31) == 0) atomicMin(flag, (unsigned long long)iteration);
+}
+
 // r = b - (a M + c sum_t mono[m][t] L_t) x per system, FP64 (the refinement residual). M values
 // shared by the bucket (nnz), L_t coefficient rows (nmono x nnz), mono (nsys x nmono).
 __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
@@ -313,6 +325,19 @@ int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef,
         k_lincomb<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, static_cast<const double*>(base),
                                                                           static_cast<double*>(out), n);
         CNG_LAUNCH("k_lincomb");
+    })
+}
+
+int cng_check_finite(const void* x, int64_t count, int64_t iteration, int64_t* flag, void* stream) {
+    CNG_TRY({
+        if (!x || !flag) throw InvalidArgument("null argument");
+        if (count < 0 || iteration < 0) throw InvalidArgument("check_finite: negative count or iteration");
+        if (count == 0) return CNG_OK;
+        const long long n = 2 * count;      // complex entries -> doubles
+        const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
+        k_check_finite<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const unsigned long long*>(x), n, iteration, reinterpret_cast<unsigned long long*>(flag));
+        CNG_LAUNCH("k_check_finite");
     })
 }
 

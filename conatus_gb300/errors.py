@@ -11,6 +11,12 @@ class CudaError(RuntimeError):
     """A CUDA failure, or the CUDA library is missing (never a silent CPU fallback)."""
 
 
+class NumericalError(RuntimeError):
+    """A run has blown up: its state holds a NaN or an infinity (the reference's
+    ``conatus.errors.NumericalError`` of the finite-state check, python/conatus/timestep/
+    run_checks.py:67-99)."""
+
+
 def check_status(status: int, message: str, where: str) -> None:
     if status == 1:
         raise ValueError(message)

@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib
 from ._lib import call
 from .core import _Handle
-from .errors import CudaError
+from .errors import CudaError, NumericalError
 
 SBDF = {1: ([1, -1], [0, 1]),
         2: ([1.5, -2, 0.5], [0, 2, -1]),
@@ -75,6 +75,24 @@ def _stream_handle(stream) -> int:
 
 
 SPLIT_MERGED = 63      # code >> 1 of a merged entry list of the split residual (scale per row, system)
+
+#: finite-state check cadence in steps (the reference's FINITE_CHECK_EVERY,
+#: python/conatus/timestep/run_checks.py:15-20)
+FINITE_CHECK_EVERY = 100
+_FLAG_CLEAR = 2 ** 63 - 1
+
+
+def finite_cadence(check_finite, where: str = "IVPSolver") -> int:
+    """Steps between two finite-state checks: True -> 100, False -> 0 (off), n > 0 -> n
+    (run_checks.finite_cadence, python/conatus/timestep/run_checks.py:36-51)."""
+    if check_finite is True:
+        return FINITE_CHECK_EVERY
+    if check_finite is False:
+        return 0
+    if isinstance(check_finite, (int, np.integer)) and not isinstance(check_finite, bool) and check_finite > 0:
+        return int(check_finite)
+    raise ValueError(f"{where}: check_finite={check_finite!r}: True (every {FINITE_CHECK_EVERY} steps), "
+                     "False (off) or a positive number of steps")
 
 
 class DeviceProblem:
@@ -680,7 +698,7 @@ class IVPSolver:
 
     def __init__(self, problem, scheme: str = "SBDF2", dt: float = 1e-3, precision: str = "fp64",
                  device_problem: DeviceProblem | None = None, factor_sets: int | None = None,
-                 refine: int | None = None):
+                 refine: int | None = None, check_finite=True):
         if scheme in SBDF_SCHEMES:
             self.family, self.order = "sbdf", int(scheme[-1])
             self.ring = self.order
@@ -695,6 +713,10 @@ class IVPSolver:
         else:
             raise ValueError(f"scheme {scheme!r}: one of {SBDF_SCHEMES + CN_SCHEMES + RK_SCHEMES}")
         self.scheme, self.dt = scheme, float(dt)
+        self._finite_every = finite_cadence(check_finite)
+        self._flag = None                    # device int64: first iteration found non-finite
+        self._finite_ok = None               # (iteration, t) of the last check found finite
+        self._probed = None                  # (iteration, t) of the last check launched
         self.dev = device_problem or DeviceProblem(problem, precision, factor_sets=factor_sets)
         # FP32 form: refinement passes per solve. The CN family carries -b_1 L X_n of the previous
         # step with a weight comparable to the implicit one, and with it the previous pressure (the
@@ -745,6 +767,13 @@ class IVPSolver:
         self.X.copy_(X)
         self.t, self.iteration = float(t), 0
         self.filled, self.head = 0, self.ring - 1
+        self._reset_finite()
+
+    def _reset_finite(self) -> None:
+        """A new state: forget the finite-state checks of the previous one."""
+        if self._flag is not None:
+            self._flag.fill_(_FLAG_CLEAR)
+        self._finite_ok = self._probed = None
 
     def set_history(self, MX_list, F_list, LX_list=None) -> None:
         """History (newest first) of M X and F, and of L X for the CN family, e.g. to continue from
@@ -919,31 +948,96 @@ class IVPSolver:
         self.iteration += 1
 
     def run(self, steps: int) -> None:
+        """``steps`` plain steps; with the finite-state check on, the state is checked every
+        ``check_finite`` steps and at the end of the call, and a blown-up run stops with
+        NumericalError (integrator.py:745-767)."""
         self._enter()
+        fe = self._finite_every
+        s = _stream_handle(self.stream)
         for _ in range(int(steps)):
             self._step()
+            if fe and self.iteration % fe == 0:
+                self._probe(s)
+                self._finite_raise("IVPSolver.run")
+        if fe and int(steps) > 0:
+            self._probe(s)
+            self._finite_raise("IVPSolver.run (end of the call)")
         self._leave()
 
-    def run_graph(self, steps: int, unroll: int = 1) -> None:
+    # ------------------------------------------------------------------ finite-state check
+    def _probe(self, s) -> None:
+        """Launch the finite-state check of the current state on stream s (asynchronous)."""
+        if self._flag is None:
+            torch = _torch()
+            self._flag = torch.full((1,), _FLAG_CLEAR, dtype=torch.int64, device=self.X.device)
+            torch.cuda.current_stream(self.X.device).synchronize()
+        call("cng_check_finite", self.X.data_ptr(), self.dev.n_total, int(self.iteration), self._flag.data_ptr(), s)
+        self._probed = (int(self.iteration), float(self.t))
+
+    def finite_status(self):
+        """None while every check launched so far found the state finite, else the first iteration
+        found non-finite. Reads a device flag: the checks must have completed (call after a
+        synchronization of the solver's stream)."""
+        if self._flag is None:
+            return None
+        v = int(self._flag.item())
+        return None if v == _FLAG_CLEAR else v
+
+    def _finite_raise(self, where: str) -> None:
+        """Wait for the checks launched so far; raise NumericalError if one found the state
+        non-finite, naming the iteration, the first non-finite variable and the last iteration
+        checked finite (run_checks.check_state_finite, python/conatus/timestep/run_checks.py:67-99)."""
+        self.stream.synchronize()
+        bad = self.finite_status()
+        if bad is None:
+            self._finite_ok = self._probed
+            return
+        name, count = "?", 0
+        C = self.dev.to_host(self.X)
+        for v, var in enumerate(self.dev.tpl.variables):
+            cnt = sum(int(np.count_nonzero(~np.isfinite(Cb[:, b.col[:, 0] == v])))
+                      for Cb, b in zip(C, self.dev.tpl.buckets))
+            if cnt:
+                name, count = var["name"], cnt
+                break
+        last = self._finite_ok
+        since = f"; last checked finite at iteration {last[0]} (t = {last[1]:.10g})" if last else ""
+        raise NumericalError(
+            f"{where}: non-finite state (NaN or inf) at iteration {bad}: unknown {name!r} ({count} "
+            f"non-finite coefficient(s) now, at iteration {self.iteration}){since}; reduce dt (now "
+            f"{self.dt:g}), raise the resolution or check the initial state; check_finite=False "
+            "turns the check off")
+
+    def run_graph(self, steps: int, unroll: int = 1, wait: bool = True) -> None:
         """``steps`` steps; once the history is full (at once for Runge-Kutta), the steps run as CUDA
         graph launches, each graph holding ``unroll`` steps (one graph per position of the history
         ring and length, captured on first use; a remainder shorter than ``unroll`` runs as
-        one-step graphs)."""
+        one-step graphs). The finite-state check runs between graphs every ``check_finite`` steps
+        and at the end of the call (graphs end on those iterations); ``wait``: wait for it at the
+        end and raise NumericalError on a blown-up state, else leave the result to
+        :meth:`finite_status` (a caller that keeps many runs in flight)."""
         s = _stream_handle(self.stream)
         steps = int(steps)
         unroll = max(1, int(unroll))
+        fe = self._finite_every
+        ran = steps > 0
         self._enter()
         # plain steps until the history is full, and at least one (its first launches make the
         # lazily built device data -- tables, kernel attributes -- which a capture cannot make)
         while steps > 0 and (not self._warm or (self.family != "rk" and self.filled < self.ring)):
             self._step()
             steps -= 1
+            if fe and self.iteration % fe == 0:
+                self._probe(s)
         if steps <= 0:
+            self._end_run_graph(s, ran, wait)
             self._leave()
             return
         self._step_factors(s)
         while steps > 0:
             u = unroll if steps >= unroll else 1
+            if fe:                             # graphs end on the check's iterations
+                u = min(u, fe - self.iteration % fe)
             key = ((self.head + 1) % self.ring, u)
             g = self._graphs.get(key)
             if g is None:
@@ -963,7 +1057,19 @@ class IVPSolver:
             self.t += u * self.dt
             self.iteration += u
             steps -= u
+            if fe and self.iteration % fe == 0:
+                self._probe(s)
+        self._end_run_graph(s, ran, wait)
         self._leave()
+
+    def _end_run_graph(self, s, ran, wait) -> None:
+        """The finite-state check at the end of a run_graph call: launched, and (``wait``) waited
+        for, raising NumericalError on a blown-up state."""
+        if self._finite_every and ran:
+            if self._probed is None or self._probed[0] != self.iteration:
+                self._probe(s)
+            if wait:
+                self._finite_raise("IVPSolver.run_graph (end of the call)")
 
     def step_host(self, host_in, host_out) -> None:
         """One step through host buffers: the state is copied in from ``host_in`` (pinned, mode
@@ -1050,6 +1156,7 @@ class IVPSolver:
             if self.family == "cn":
                 self.LXh[slot].copy_(-torch.as_tensor(arrays[f"LX{j}"], device=dev))
         self.t, self.iteration = float(meta["t"]), int(meta["iteration"])
+        self._reset_finite()
         torch.cuda.current_stream().synchronize()
 
     def state_to_host(self):

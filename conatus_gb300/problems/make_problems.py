@@ -1,6 +1,9 @@
 """Generate the problem templates of this directory from the reference (run where it is importable).
 
-    python -m conatus_gb300.problems.make_problems [--ref /root/reference] [--only NAME]
+    python -m conatus_gb300.problems.make_problems --ref REFERENCE_TREE [--only NAME]
+
+The reference tree is given by ``--ref`` or the environment variable ``CONATUS_REFERENCE``;
+there is no default.
 
 Each template is the reference's own discretization of a benchmark model (``template_from_solver``
 in conatus_gb300/reference_adapter.py), built with ``complexify=True`` and ``f_backend="fused"``.
@@ -45,9 +48,12 @@ for _nz in (32, 48, 64, 80, 96):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CONATUS_REFERENCE"),
+                    help="the reference source tree (or set CONATUS_REFERENCE)")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference source tree is needed: pass --ref or set CONATUS_REFERENCE")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     import make_golden as mg
     cn = mg.import_reference(args.ref)

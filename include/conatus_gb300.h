@@ -315,6 +315,14 @@ int cng_sbdf_rhs(int q, const double* c, const double* d, const void* const* F, 
 int cng_sbdf_rhs_fused(int q, const double* c, const double* d, const void* const* F, const void* const* MX,
                        void* rhs, int64_t count, int fused, void* stream);
 
+/* Finite-state check of count complex128 entries of x: when one of them holds a NaN or an
+ * infinity, flag[0] (device int64, set to INT64_MAX by the caller) becomes min(flag[0], iteration).
+ * Asynchronous on `stream`, capturable; the caller reads the flag. Replaces the reference's
+ * check_state_finite (python/conatus/timestep/run_checks.py:67-99), the NumericalError check of
+ * IVPSolver.run every FINITE_CHECK_EVERY = 100 steps and at the end of a run
+ * (run_checks.py:15-20, python/conatus/timestep/integrator.py:764-767,1306-1312). */
+int cng_check_finite(const void* x, int64_t count, int64_t iteration, int64_t* flag, void* stream);
+
 /* ---- CUDA graphs of whole steps ------------------------------------------------------------- */
 
 typedef struct cng_graph cng_graph;

@@ -24,6 +24,7 @@ follows, in NumPy/SciPy:
 from __future__ import annotations
 
 import itertools
+import os
 from collections import deque
 
 import numpy as np
@@ -516,79 +517,156 @@ class RKStepper:
         return X[-1]
 
 
-class SampledStepper:
-    """Timing of the oracle step on a bounded sample of a large workload (the CPU baseline): the
-    full F, M X and SBDF right-hand side, and the banded solves of ``sample_systems`` systems
-    spread over the buckets, scaled to every system. Factorizations happen before the timing (the
-    reference times steps after a warm-up that includes them)."""
+def _solve_worker(conn):
+    """A worker process of ``ParallelStepper``: holds the factorizations of its share of the systems
+    of every bucket (the oracle restatement of banded.hpp) and solves them on request."""
+    from .banded import BorderedBandedBatch
+    batches = []
+    while True:
+        msg = conn.recv()
+        if msg[0] == "factor":
+            batches = []
+            for n, r, real, indptr, indices, monos_val, Mc, Lc, a, b_ in msg[1]:
+                if monos_val.shape[0] == 0:
+                    batches.append(None)
+                    continue
+                Vm = monos_val.astype(np.complex128) @ Mc
+                Vl = monos_val.astype(np.complex128) @ Lc
+                vals = a * Vm + b_ * Vl
+                if real:
+                    vals = vals.real
+                mats = [(n, indptr, indices, v) for v in vals]
+                batches.append(BorderedBandedBatch(mats, list(range(r)),
+                                                   dtype=np.float64 if real else np.complex128))
+            conn.send("ok")
+        elif msg[0] == "solve":
+            out = []
+            for B, rhs in zip(batches, msg[1]):
+                if B is None:
+                    out.append(None)
+                elif B.sys[0].dtype == np.float64:
+                    out.append(B.solve(rhs.real).astype(np.complex128))
+                else:
+                    out.append(B.solve(rhs))
+            conn.send(out)
+        else:
+            conn.close()
+            return
 
-    def __init__(self, problem, order, dt, sample_systems=256, workers=None):
+
+class ParallelStepper:
+    """The oracle's SBDF-q step on a whole workload, timed as the CPU baseline: F (transforms on
+    ``workers`` scipy.fft threads), M X, the right-hand side of ``SBDFStepper.step`` and the solves
+    of every system of every bucket, spread over ``workers`` processes (started with ``spawn``),
+    each holding the factorizations of its share (made before the timing: the reference times
+    steps after a warm-up that factors, examples/benchmarks/cases.py:27-43)."""
+
+    def __init__(self, problem, order, dt, workers=None):
+        import multiprocessing as mp
         global WORKERS
+        workers = int(workers or os.cpu_count() or 1)
         WORKERS = workers
         self.op = OracleProblem(problem)
         self.P = problem
         self.order, self.dt = int(order), float(dt)
-        tot = sum(problem.nsys)
-        frac = min(1.0, sample_systems / max(tot, 1))
-        self.sample = [np.arange(min(ns, max(1, int(np.ceil(frac * ns))))) for ns in problem.nsys]
-        self.scale = [ns / max(len(s), 1) for ns, s in zip(problem.nsys, self.sample)]
+        self.workers = workers
         a0 = SBDF[self.order][0][0] / self.dt
-        self._lu = []
-        for bi, b in enumerate(problem.tpl.buckets):
-            Vm, Vl = self.op._vals(bi, "M"), self.op._vals(bi, "L")
-            mats = [(b.n, b.indptr, b.indices, a0 * Vm[m] + Vl[m]) for m in self.sample[bi]]
-            self._lu.append(BorderedBandedBatch(mats, list(range(b.r)), dtype=np.complex128))
-        self._Mcsr = []
-        for bi, b in enumerate(problem.tpl.buckets):
-            V = self.op._vals(bi, "M")
-            self._Mcsr.append(V)
+        ctx = mp.get_context("spawn")
+        self._procs, self._conns, self._shares = [], [], []
+        nb = len(problem.tpl.buckets)
+        bounds = [np.linspace(0, ns, workers + 1).round().astype(int) for ns in problem.nsys]
+        for w in range(workers):
+            parent, child = ctx.Pipe()
+            pr = ctx.Process(target=_solve_worker, args=(child,), daemon=True)
+            pr.start()
+            child.close()
+            jobs, share = [], []
+            for bi, b in enumerate(problem.tpl.buckets):
+                lo, hi = int(bounds[bi][w]), int(bounds[bi][w + 1])
+                mv = problem.mono_values(bi)[lo:hi]
+                jobs.append((b.n, b.r, b.kind == "real", b.indptr, b.indices, mv, b.Mc, b.Lc, a0, 1.0))
+                share.append((lo, hi))
+            parent.send(("factor", jobs))
+            self._procs.append(pr)
+            self._conns.append(parent)
+            self._shares.append(share)
+        for c in self._conns:
+            if c.recv() != "ok":
+                raise RuntimeError("oracle worker failed to factor")
+        self._Mcsr = [self.op._vals(bi, "M") if not problem.tpl.buckets[bi].m_is_constant() else None
+                      for bi in range(nb)]
+
+    def close(self):
+        for c in self._conns:
+            try:
+                c.send(("stop",))
+            except (BrokenPipeError, OSError):
+                pass
+        for p in self._procs:
+            p.join(timeout=10)
+        self._conns, self._procs = [], []
+
+    def __del__(self):
+        if getattr(self, "_conns", None):
+            self.close()
 
     def _mx(self, C):
         out = []
         for bi, b in enumerate(self.P.tpl.buckets):
-            V = self._Mcsr[bi]
-            if np.all(V == V[:1]):
-                A = sp.csr_matrix((V[0], b.indices, b.indptr), shape=(b.n, b.n))
+            if self._Mcsr[bi] is None:               # one M for every system of the bucket
+                mv = self.P.mono_values(bi)[:1].astype(np.complex128) @ b.Mc
+                A = sp.csr_matrix((mv[0], b.indices, b.indptr), shape=(b.n, b.n))
                 out.append(np.asarray(C[bi] @ A.T))
             else:
-                out.append(self.op.MX([C[bi]])[0] if len(self.P.tpl.buckets) == 1 else self.op.MX(C)[bi])
+                V = self._Mcsr[bi]
+                rows = b.coo_rows()
+                Y = np.zeros_like(C[bi])
+                for m in range(C[bi].shape[0]):
+                    np.add.at(Y[m], rows, V[m] * C[bi][m, b.indices])
+                out.append(Y)
+        return out
+
+    def _solve(self, rhs):
+        for c, share in zip(self._conns, self._shares):
+            c.send(("solve", [np.ascontiguousarray(r[lo:hi]) for r, (lo, hi) in zip(rhs, share)]))
+        out = [np.empty_like(r) for r in rhs]
+        for c, share in zip(self._conns, self._shares):
+            xs = c.recv()
+            for bi, (x, (lo, hi)) in enumerate(zip(xs, share)):
+                if x is not None:
+                    out[bi][lo:hi] = x
         return out
 
     def time_steps(self, C0, steps=1, warmup=0):
+        """Seconds per step (mean over ``steps`` steps after ``warmup`` untimed ones) from the
+        state C0, and a description. Every step is of the full order: the history starts as
+        ``order - 1`` copies of C0's M X and F (made before the timing), so that one factor set
+        serves every step (the reference's lower-order start-up would need one set per order)."""
         import time
-        C = [np.asarray(c) for c in C0]
-        hist_f, hist_mx = deque(), deque()
+        C = [np.asarray(c, np.complex128) for c in C0]
+        F0, MX0 = self.op.F(C), self._mx(C)
+        hist_f = deque([F0] * (self.order - 1))
+        hist_mx = deque([MX0] * (self.order - 1))
         a, c = SBDF[self.order]
         times = []
         for it in range(warmup + steps):
             t0 = time.perf_counter()
-            F = self.op.F(C)
-            MX = self._mx(C)
-            hist_f.appendleft(F)
-            hist_mx.appendleft(MX)
+            hist_f.appendleft(self.op.F(C))
+            hist_mx.appendleft(self._mx(C))
             while len(hist_f) > self.order:
                 hist_f.pop()
                 hist_mx.pop()
-            q = len(hist_f)
             rhs = []
             for bi in range(len(C)):
                 r = np.zeros_like(C[bi])
-                for j in range(q):
-                    r += c[j + 1] * hist_f[j][bi] - (a[j + 1] / self.dt) * hist_mx[j][bi]
+                for j in range(1, self.order + 1):
+                    r += c[j] * hist_f[j - 1][bi] - (a[j] / self.dt) * hist_mx[j - 1][bi]
                 rhs.append(r)
-            t1 = time.perf_counter()
-            t_solve = 0.0
-            newC = [x.copy() for x in C]
-            for bi, B in enumerate(self._lu):
-                ts = time.perf_counter()
-                xs = B.solve(rhs[bi][self.sample[bi]])
-                t_solve += (time.perf_counter() - ts) * self.scale[bi]
-                newC[bi][self.sample[bi]] = xs
-            C = newC
+            C = self._solve(rhs)
             if it >= warmup:
-                times.append((t1 - t0) + t_solve)
-        nsamp = int(sum(len(s) for s in self.sample))
-        desc = (f"{steps} step(s): full F, M X and right-hand side on {self.P.real_unknowns()} unknowns; "
-                f"banded solves of {nsamp} of {sum(self.P.nsys)} systems scaled to all; "
-                f"factorizations untimed; scipy.fft workers={WORKERS}")
+                times.append(time.perf_counter() - t0)
+        self.state = C
+        desc = (f"{steps} full step(s) after {warmup} untimed: F, M X, right-hand side and the "
+                f"banded solves of all {sum(self.P.nsys)} systems ({self.P.real_unknowns()} unknowns) "
+                f"on {self.workers} processes; factorizations untimed; scipy.fft workers={WORKERS}")
         return float(np.mean(times)), desc

@@ -97,3 +97,51 @@ class RefBatch:
         if h:
             lib().ref_batch_destroy(int(self.cplx), h)
             self._h = None
+
+
+def install_compiled_core(version: str = "0.5.0"):
+    """Insert a ``conatus._core`` whose batched bordered-banded solver is the reference's own
+    compiled ``BorderedBanded<T>`` (this library), so that the reference's Python package runs its
+    CPU path on its own C++ solves (threaded as the reference threads them, core/bindings/
+    module.cpp:181-206). Single systems use the oracle restatement. Test infrastructure only."""
+    import sys
+    import types
+    from .banded import BorderedBanded
+
+    class _Batch:
+        def __init__(self, mats, border, col_border=False):
+            if col_border:
+                raise NotImplementedError("oracle: the column border is not bound")
+            self._b = RefBatch(mats, border, self._dtype)
+            info = [self._b.info(k) for k in range(self._b.batch)]
+            self._kl = max((i["kl"] for i in info), default=0)
+            self._ku = max((i["ku"] for i in info), default=0)
+
+        kl = property(lambda self: self._kl)
+        ku = property(lambda self: self._ku)
+
+        def __len__(self):
+            return self._b.batch
+
+        def solve(self, b, transpose=False, threads=1):
+            return self._b.solve(b, transpose, threads)
+
+    def typed(base, dtype, suffix):
+        return type(base.__name__ + suffix, (base,), {"_dtype": dtype})
+
+    def single(dtype, suffix):
+        class Typed(BorderedBanded):
+            def __init__(self, *a, **k):
+                super().__init__(*a, dtype=dtype, **k)
+        Typed.__name__ = "BorderedBanded" + suffix
+        return Typed
+
+    m = types.ModuleType("conatus._core")
+    m.__version__ = version
+    m.BorderedBandedBatchD = typed(_Batch, np.float64, "D")
+    m.BorderedBandedBatchZ = typed(_Batch, np.complex128, "Z")
+    m.BorderedBandedD = single(np.float64, "D")
+    m.BorderedBandedZ = single(np.complex128, "Z")
+    m.cuda_compiled = lambda: False
+    sys.modules["conatus._core"] = m
+    return m

@@ -1,6 +1,9 @@
 """Generate the golden fixtures of tests/golden/ from the reference (run where it is importable).
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref REFERENCE_TREE
+
+The reference tree is given by ``--ref`` or the environment variable ``CONATUS_REFERENCE``;
+there is no default.
 
 Banded fixtures (``banded_<case>.npz``): the bucket matrices a M + b L that the reference's
 ``GlobalSystem.factor`` builds for the problems of the benchmark configurations (at small
@@ -184,6 +187,7 @@ def step_fixtures(cn, out_dir, rng):
         state = (np.array(s.X), s.t, s.iteration, list(s._MXh), list(s._Fh))
         s.step()
         Xn1 = np.array(s.X)
+        MXn = np.array(s._MXh[0])             # the step pushed M X_n on its history
         # the reference's own rounding floor: the same step from X_n perturbed by ~1 ulp
         floors = []
         for trial in range(3):
@@ -193,7 +197,7 @@ def step_fixtures(cn, out_dir, rng):
             s._Fh.clear(); s._Fh.extend(state[4])
             s.step()
             floors.append(np.array(s.X))
-        arrays = dict(Xn=Xn, Xn1=Xn1, Fn=Fn, MXh=np.stack(MXh), Fh=np.stack(Fh), dt=kw["dt"],
+        arrays = dict(Xn=Xn, Xn1=Xn1, Fn=Fn, MXn=MXn, MXh=np.stack(MXh), Fh=np.stack(Fh), dt=kw["dt"],
                       order=int(kw["scheme"][-1]), nb=len(maps), Xn1_perturbed=np.stack(floors))
         for bi, m in enumerate(maps):
             p = f"m{bi}_"
@@ -263,11 +267,72 @@ def scheme_fixtures(cn, out_dir, rng, steps=3):
             print(name, scheme, "N_u", s.system.n)
 
 
+TRAJECTORY_CASES = {
+    # case -> (model, build kwargs, parameters, committed template, template parameters, Fourier
+    #          sizes, workload, recorded steps)
+    "burgers128": ("burgers", dict(N=128, scheme="SBDF2", dt=1e-4), {}, "burgers_n128", None, None,
+                   "burgers", (1000, 2500, 5000)),
+    # the Rayleigh-Benard configuration (Ra = 1e6, dt = 1e-4) blows up in the reference itself
+    # between steps 150 and 200 (convection sets in near t = 0.015 with velocities of order
+    # sqrt(Ra) = 1e3, far beyond the advective limit of dt = 1e-4 on this grid): recorded up to step
+    # 150; the configured length is run at Ra = 1e4, stable over the 2000 steps
+    "rb256x64_ra1e6": ("rayleigh_benard", dict(N=(256, 64), scheme="SBDF2", dt=1e-4), dict(Ra=1e6, Pr=1.0),
+                       "rb_nz64", None, [256], "rayleigh_benard", (50, 100, 150)),
+    "rb256x64_ra1e4": ("rayleigh_benard", dict(N=(256, 64), scheme="SBDF2", dt=1e-4), dict(Ra=1e4, Pr=1.0),
+                       "rb_nz64_ra", {"Ra": 1e4}, [256], "rayleigh_benard", (1000, 2000)),
+    "channel16x17x16": ("channel", dict(N=(16, 17, 16), scheme="SBDF3", dt=5e-3), dict(Re=4000.0),
+                        "channel_ny17", None, [16, 16], "channel", (100, 500)),
+}
+
+
+def trajectory_fixtures(cn, out_dir):
+    """Trajectory fixtures (``traj_<case>.npz``): the reference's IVPSolver (fused F,
+    complexify=True, start-up ``lower_order``) run over the configuration's whole length from the
+    benchmark's initial state (``conatus_gb300.workloads``, mapped into the reference's layout), the
+    state recorded at a few steps as the coefficient arrays of every variable (the layout-free form
+    ``oracle.ivp.OracleProblem.to_arrays`` gives), so that a GPU run of the same length compares
+    field by field with no teacher forcing."""
+    import time
+    sys.path.insert(0, ROOT)
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.reference_adapter import gather_state, reference_maps, scatter_state
+    from oracle.ivp import OracleProblem
+    for name, (fn, kw, params, tname, tparams, sizes, wl, rec) in TRAJECTORY_CASES.items():
+        t0 = time.time()
+        sim = globals()[fn](cn, **params).simulate(complexify=True, f_backend="fused", **kw)
+        s = sim.solver
+        maps = reference_maps(s)
+        P = W.load_template(tname).instantiate(sizes, params=tparams)
+        for bi, (b, m) in enumerate(zip(P.tpl.buckets, maps)):
+            if m["cols"].shape[-2:] != (P.nsys[bi], b.n) or not np.array_equal(m["modes"], P.modes[bi]):
+                raise RuntimeError(f"{name}: bucket {bi} of the template does not match the reference build")
+        C0 = W.initial_state(wl, P, seed=0)
+        s.X = scatter_state(C0, maps, s.system.n).astype(s.system.dtype)
+        s.t, s.iteration = 0.0, 0
+        s._reset_history()
+        op = OracleProblem(P)
+        arrays = dict(steps=np.array(rec, np.int64), dt=kw["dt"], scheme=kw["scheme"],
+                      variables=np.array([v["name"] for v in P.tpl.variables]))
+        done = 0
+        for r in rec:
+            s.run(r - done)
+            done = r
+            C = [gather_state(np.asarray(s.X), m) for m in maps]
+            for v, a in enumerate(op.to_arrays(C)):
+                arrays[f"s{r}_v{v}"] = a
+        arrays["finite"] = np.array(bool(np.all(np.isfinite(np.asarray(s.X)))))
+        np.savez_compressed(os.path.join(out_dir, f"traj_{name}.npz"), **arrays)
+        print(name, "steps", rec, "N_u", s.system.n, f"{time.time() - t0:.1f} s")
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CONATUS_REFERENCE"),
+                    help="the reference source tree (or set CONATUS_REFERENCE)")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference source tree is needed: pass --ref or set CONATUS_REFERENCE")
     cn = import_reference(args.ref)
     rng = np.random.default_rng(20261203)
     if args.only in ("", "banded"):
@@ -276,6 +341,8 @@ def main():
         step_fixtures(cn, HERE, np.random.default_rng(7))
     if args.only in ("", "scheme"):
         scheme_fixtures(cn, HERE, np.random.default_rng(11))
+    if args.only in ("", "trajectory"):
+        trajectory_fixtures(cn, HERE)
 
 
 if __name__ == "__main__":

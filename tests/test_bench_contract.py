@@ -39,7 +39,10 @@ def test_reference_arm_line(config):
     assert d["n_gpus"] == 1 and d["dtype"] == "f64"
     assert d["value"] > 0 and abs(d["value"] * d["ms_per_step"] / 1e3 - 1.0) < 1e-9
     assert "workload" in d["config"] and "model" not in d["config"]
+    # the same config dict as the GPU arm's line (bench.workload_config)
+    assert set(d["config"]) == {"workload", "real_unknowns", "systems", "parallelism", "l2"}
     cb = d["cpu_baseline"]
+    assert "full step" in cb["sample"] and "all" in cb["sample"]      # measured, not extrapolated
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,

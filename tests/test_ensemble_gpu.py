@@ -53,7 +53,8 @@ def test_ensemble_fp32_and_graphs(cuda_lib):
         torch.cuda.synchronize()
         out[prec] = np.concatenate(ens.state())
     err = np.linalg.norm(out["fp32"] - out["fp64"]) / np.linalg.norm(out["fp64"])
-    assert err < 1e-5, err
+    print("KS ensemble FP32 form vs FP64 after 40 steps:", err)
+    assert err < 1e-6, err
     a = FourierEnsemble(tpl, N, L, scheme="SBDF2", dt=0.01, precision="fp64")
     a.set_state(a.random_state(seed=5))
     a.run(40)

@@ -45,9 +45,12 @@ def test_oracle_MX_matches_reference(fixture):
     P, g, maps = load_step(fixture)
     op = OracleProblem(P)
     C = [gather_state(g["Xn"], m) for m in maps]
-    # history[0] of the fixture is M X_{n-1}: check M X on X_n through the next step's history
+    # MXn: the M X_n the reference's step pushed on its history (rows in the reference's layout)
     MX = op.MX(C)
-    assert all(np.all(np.isfinite(x)) for x in MX)
+    MX_ref = [gather_rows(g["MXn"], m) for m in maps]
+    num = sum(float(np.sum(np.abs(a - b) ** 2)) for a, b in zip(MX, MX_ref))
+    den = sum(float(np.sum(np.abs(b) ** 2)) for b in MX_ref)
+    assert den > 0 and (num / den) ** 0.5 < 1e-14, (num / den) ** 0.5
 
 
 @pytest.mark.parametrize("fixture", list(STEP_CASES))

@@ -108,3 +108,46 @@ def test_graph_replay_equals_steps(rng, cuda_lib):
     b.run_graph(7)
     torch.cuda.synchronize()
     assert torch.equal(a.X, b.X)
+
+
+@pytest.mark.parametrize("fixture", list(STEP_CASES))
+def test_gpu_MX_matches_reference(fixture, cuda_lib):
+    """M X_n on the device against the M X_n the reference's own step pushed on its history."""
+    import torch
+    from conatus_gb300.ivp import DeviceProblem
+    P, g, maps = load_step(fixture)
+    dev = DeviceProblem(P)
+    X = dev.to_device([gather_state(g["Xn"], m) for m in maps])
+    out = dev.zeros()
+    dev.MX(X, out)
+    torch.cuda.synchronize()
+    assert _rel(dev.to_host(out), [gather_rows(g["MXn"], m) for m in maps]) < 1e-13
+
+
+@pytest.mark.parametrize("config", ["rayleigh_benard", "burgers"])
+def test_gpu_config_steps_match_oracle(config, cuda_lib):
+    """The configuration at its own size (RB 256 x 64, Burgers 128) from its benchmark state: F and
+    three steps (lower-order start-up included) against the oracle, 1e-12 relative L2 per field
+    (1e-10 for the tau variables)."""
+    import torch
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ivp import IVPSolver
+    from oracle.ivp import OracleProblem, SBDFStepper
+    cfg = W.CONFIGS[config]
+    P = W.problem(config)
+    C0 = W.initial_state(config, P, seed=0)
+    op = OracleProblem(P)
+    solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"])
+    out = solver.dev.zeros()
+    solver.dev.F(solver.dev.to_device(C0), out)
+    torch.cuda.synchronize()
+    assert _rel(solver.dev.to_host(out), op.F(C0)) < 1e-12
+    st = SBDFStepper(op, int(cfg["scheme"][-1]), cfg["dt"])
+    C = C0
+    for _ in range(3):
+        C = st.step(C)
+    solver.set_state(C0)
+    solver.run(3)
+    errs = field_errors(P, solver.state_to_host(), C)
+    for k, e in errs.items():
+        assert e <= (1e-10 if k.startswith("tau") else 1e-12), errs

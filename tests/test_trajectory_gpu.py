@@ -1,0 +1,110 @@
+"""GPU: whole trajectories of the configurations against the reference's own runs, with no teacher
+forcing (golden fixtures ``traj_*.npz`` from the reference's IVPSolver, tests/golden/make_golden.py).
+
+Each case starts from the benchmark's initial state (conatus_gb300.workloads), runs the plain FP64
+drop-in for the configuration's length on the GPU and compares the coefficient arrays of every
+variable with the reference's at the recorded steps (relative L2 per field). Over a trajectory the
+two FP64 implementations drift apart by their rounding differences, amplified by the dynamics; the
+tolerances below are the bound each case must keep (step-wise parity, teacher-forced to 1e-12, is
+tests/test_step_gpu.py).
+
+* Burgers N = 128, SBDF2, dt = 1e-4, 5000 steps, u0 = -sin(pi x) (field by field with the
+  reference's NumPy path): 1e-11.
+* Rayleigh-Benard 256 x 64, SBDF2, dt = 1e-4: at Ra = 1e6 (the configuration) the reference itself
+  blows up between steps 150 and 200 (convection sets in with velocities of order sqrt(Ra), far
+  beyond the advective limit of dt = 1e-4): compared at steps 50, 100 and 150, and the GPU run's
+  finite-state check stops at step 200 exactly as the reference's does; the configured 2000 steps
+  at Ra = 1e4, stable: 1e-10.
+* Channel 16 x 17 x 16 (the configuration at a reduced resolution), SBDF3, dt = 5e-3, 500 steps:
+  1e-10.
+
+The measured deviations are printed (``pytest -s``)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # fixture -> (template, template parameters, Fourier sizes, workload, tolerance, tau tolerance)
+    "traj_burgers128.npz": ("burgers_n128", None, None, "burgers", 1e-11, 1e-8),
+    "traj_rb256x64_ra1e6.npz": ("rb_nz64", None, [256], "rayleigh_benard", 1e-10, 1e-8),
+    "traj_rb256x64_ra1e4.npz": ("rb_nz64_ra", {"Ra": 1e4}, [256], "rayleigh_benard", 1e-10, 1e-8),
+    "traj_channel16x17x16.npz": ("channel_ny17", None, [16, 16], "channel", 1e-10, 1e-8),
+}
+
+
+def _field_errors(arrs, g, step, names):
+    out = {}
+    for v, name in enumerate(names):
+        ref = g[f"s{step}_v{v}"]
+        den = float(np.linalg.norm(ref))
+        out[name] = float(np.linalg.norm(arrs[v] - ref)) / den if den > 0 else float(np.linalg.norm(arrs[v]))
+    return out
+
+
+@pytest.mark.parametrize("fixture", list(CASES))
+def test_trajectory_matches_reference(fixture, cuda_lib):
+    import torch
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ivp import IVPSolver
+    from oracle.ivp import OracleProblem
+    tname, tparams, sizes, wl, tol, tol_tau = CASES[fixture]
+    g = golden(fixture)
+    P = W.load_template(tname).instantiate(sizes, params=tparams)
+    names = [str(x) for x in g["variables"]]
+    assert names == [v["name"] for v in P.tpl.variables]
+    solver = IVPSolver(P, scheme=str(g["scheme"]), dt=float(g["dt"]))
+    solver.set_state(W.initial_state(wl, P, seed=0))
+    op = OracleProblem(P)
+    done = 0
+    report = {}
+    for step in (int(k) for k in g["steps"]):
+        solver.run_graph(step - done)
+        done = step
+        torch.cuda.synchronize()
+        errs = _field_errors(op.to_arrays(solver.state_to_host()), g, step, names)
+        report[step] = errs
+        for name, e in errs.items():
+            assert e <= (tol_tau if name.startswith("tau") else tol), (fixture, step, errs)
+    print(fixture, {k: {n: f"{e:.2e}" for n, e in v.items()} for k, v in report.items()})
+
+
+def test_blow_up_stops_like_the_reference(cuda_lib):
+    """The Rayleigh-Benard configuration blows up in the reference between steps 150 and 200; its
+    finite-state check raises at iteration 200 (the first multiple of 100 after the blow-up), last
+    checked finite at 100. The GPU run stops at the same check."""
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.errors import NumericalError
+    from conatus_gb300.ivp import IVPSolver
+    P = W.problem("rayleigh_benard")
+    solver = IVPSolver(P, scheme="SBDF2", dt=1e-4)
+    solver.set_state(W.initial_state("rayleigh_benard", P, seed=0))
+    solver.run_graph(100)                   # checked finite at 100
+    with pytest.raises(NumericalError, match=r"at iteration 200.*last checked finite at iteration 100"):
+        solver.run_graph(150)
+    assert solver.finite_status() == 200
+
+
+def test_finite_check_off_and_cadence(cuda_lib):
+    """check_finite=False runs on through a blown-up state; check_finite=n checks every n steps."""
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.errors import NumericalError
+    from conatus_gb300.ivp import IVPSolver
+    P = W.problem("rayleigh_benard")
+    C0 = W.initial_state("rayleigh_benard", P, seed=0)
+    off = IVPSolver(P, scheme="SBDF2", dt=1e-4, check_finite=False)
+    off.set_state(C0)
+    off.run_graph(250)
+    assert off.finite_status() is None
+    every = IVPSolver(P, scheme="SBDF2", dt=1e-4, check_finite=25, device_problem=off.dev)
+    every.set_state(C0)
+    with pytest.raises(NumericalError) as ei:
+        every.run(250)
+    bad = every.finite_status()
+    assert bad is not None and bad % 25 == 0 and 150 < bad <= 200, str(ei.value)
+    with pytest.raises(ValueError):
+        IVPSolver(P, scheme="SBDF2", dt=1e-4, check_finite=0, device_problem=off.dev)
