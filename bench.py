@@ -115,11 +115,15 @@ def solve_bytes(dev, fs):
     """Algorithmic bytes of one batched solve launch, band-equivalent (as the reference's band
     kernel reads them): per system the band LU (ldab n), V^T and W (2 r n) and the capacitance LU
     (r r) in the factor precision, pivots (4 n), right-hand side in and solution out (2 n
-    complex128)."""
+    complex128); a shared pair's partner reads its primary's factors in the same sweep (the
+    reference's SharedFactor), so only its right-hand side and solution count."""
     ef = 8 if dev.precision == "fp32" else 16
     tot = 0
     for h in fs:
         ns, n, r, ldab = h.batch, h.n, h.rank, h.ldab
+        if getattr(h, "primary", None) is not None:     # shared pair: the primary's factors, read once
+            tot += ns * 32 * n
+            continue
         tot += ns * (ef * (ldab * n + 2 * r * n + r * r) + 4 * n + 32 * n)
     return tot
 

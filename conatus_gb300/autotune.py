@@ -51,11 +51,13 @@ def cache() -> dict:
 
 
 def _signature(dev, fs):
-    return (dev.precision, tuple((h.batch, h.n, h.rank, h.kl, h.ku) for h in fs))
+    return (dev.precision, tuple((h.batch, h.n, h.rank, h.kl, h.ku, getattr(h, "primary", -1)) for h in fs))
 
 
 def apply(fs, sched: int) -> None:
     for h in fs:
+        if h.h is None:                   # a shared pair's partner: solved with its primary's schedule
+            continue
         call("cng_banded_set_schedule", h.h, int(sched))
         h.schedule = int(sched)
 
@@ -97,7 +99,8 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
             e1.synchronize()
             times[sched] = e0.elapsed_time(e1) / reps
         except ValueError:
-            continue                      # schedule does not fit (shared memory): not a candidate
+            continue                      # schedule does not fit (shared memory), or does not solve
+                                          # shared pairs: not a candidate
     if not times:
         raise ValueError("no solve schedule fits these systems (shared memory)")
     best = min(times, key=times.get)

@@ -747,6 +747,10 @@ struct Banded {
     int cL = 0, cU = 0, cV = 0, cWg = 0;
     int cMaxLk[4] = {0, 0, 0, 0}, cMaxUk[4] = {0, 0, 0, 0};   // largest stream chunk per chunk size 2, 4, 8, 16
     int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
+    int cG = 2;                     // systems per warp group of the compact streams (1: shared pair)
+    bool shared = false;            // factors shared with a sign-similar partner bucket
+    unsigned char* flip_r = nullptr;    // partner = diag(dr) A diag(dc): 1 where dr_i = -1
+    unsigned char* flip_c = nullptr;    //                                1 where dc_j = -1
     int* c_offL = nullptr;
     unsigned char* c_Lrow = nullptr;
     unsigned* c_Lmask = nullptr;
@@ -780,7 +784,7 @@ struct Banded {
                         (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32,
                         (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
                         (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
-                        (void*)c_U32, (void*)c_V32})
+                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c})
             dev_free(p);
     }
 
@@ -1470,6 +1474,8 @@ __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch
 
 struct CompactIdx {
     int n, r, kl, kv, nL, nU, nV, wgroups, batch;
+    int gs;                             // systems per warp group in the streams: kGroup, or 1 for a
+                                        // shared pair (both halves of the warp read one system's factors)
     int maxLc, maxUc;                   // largest chunk of the L / U streams (entries)
     const int* offL;                    // n + 1
     const unsigned char* Lrow;          // nL: t (row kv + 1 + t of the column)
@@ -1490,6 +1496,10 @@ struct CompactData {
     const TF* slu;      // [sys][r][r] (1/u_kk on the diagonal)
     const int* spiv;    // [sys][r]
     const int* perm;    // n
+    // shared pair (gs = 1): the partner's matrix is diag(dr) A diag(dc); flip_r[i] = 1 where dr_i =
+    // -1 (row index of the matrix), flip_c[j] = 1 where dc_j = -1
+    const unsigned char* flip_r = nullptr;
+    const unsigned char* flip_c = nullptr;
 };
 
 template <class T>
@@ -1508,16 +1518,25 @@ __device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
 }
 
 // The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
+// Shared pair (ix.gs = 1): warp group wg is system wg of the handle; lanes 0-15 solve it for io,
+// lanes 16-31 solve the partner system wg (io2, matrix diag(dr) A diag(dc)) with the same factors:
+// y = A^{-1} (dr b), x = dc y, which is bit for bit the partner's own factorization's solve (the
+// pivot search compares magnitudes, and every operation commutes with exact sign flips).
 template <class TF, class TD, int IO, int CH = kCChunk, int ST = 2>
 __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const CompactData<TF>& cd,
-                                                   const SolveIo& io, int block) {
+                                                   const SolveIo& io0, const SolveIo& io2, int block) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int g = lane / kLanesPer, lg = lane % kLanesPer;
     const int wg = block * nw + wib;
-    const int sys = wg * kGroup + g;
-    const bool live = sys < ix.batch;
+    const int gs = ix.gs;
+    const bool pair = gs == 1;
+    const bool partner = pair && g == 1;
+    const int gsel = pair ? 0 : g;              // slot of this half in the interleaved streams
+    const int sys = pair ? wg : wg * kGroup + g;
+    const SolveIo& io = partner ? io2 : io0;
+    const bool live = sys < ix.batch && (!partner || io2.rhs != nullptr);
     const bool wlive = wg < ix.wgroups;
     const int n = ix.n, r = ix.r;
     // shared memory: index lists, then y[G][n + 64], then the staging buffers
@@ -1528,14 +1547,14 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     unsigned char* s_Udist = s_Lrow + ix.nL;
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)kGroup * (n + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * kGroup +
-                            (ST * (size_t)CH * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    const size_t per_warp = (size_t)kGroup * (n + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * gs +
+                            (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
     TF* y = y0 + (size_t)g * (n + 64);
     TF* zb = y + n;
     TF* Lb = y0 + (size_t)kGroup * (n + 64);
-    TF* Ub = Lb + ST * (size_t)ix.maxLc * kGroup;
-    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * kGroup);
+    TF* Ub = Lb + ST * (size_t)ix.maxLc * gs;
+    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * gs);
     for (int i = threadIdx.x; i <= n; i += blockDim.x) {
         s_offL[i] = ix.offL[i];
         s_offU[i] = ix.offU[i];
@@ -1562,6 +1581,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 } else {
                     v[u] = io_load<TF, IO>(io, sys, n, pr[u]);
                 }
+                if (partner && cd.flip_r[pr[u]]) v[u] = -v[u];
             }
         }
 #pragma unroll
@@ -1569,9 +1589,9 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             if (i0 + u * kLanesPer < n) y[i0 + u * kLanesPer] = v[u];
     }
     __syncwarp();
-    const TF* Lg = cd.L + (size_t)wg * ix.nL * kGroup;
-    const TF* Ug = cd.U + (size_t)wg * (ix.nU) * kGroup;
-    const int* Pg = cd.piv + (size_t)wg * n * kGroup;
+    const TF* Lg = cd.L + (size_t)wg * ix.nL * gs;
+    const TF* Ug = cd.U + (size_t)wg * (ix.nU) * gs;
+    const int* Pg = cd.piv + (size_t)wg * n * gs;
     // ---------------- forward: L with the row interchanges
     // ST-deep ring: chunk c sits in buffer c % ST; chunks c + 1 .. c + ST - 1 are in flight while
     // chunk c is swept (an empty commit group keeps the count of pending groups uniform)
@@ -1581,9 +1601,9 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             if (c < nch) {
                 const int buf = c % ST;
                 const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
-                warp_stage(Lb + (size_t)buf * ix.maxLc * kGroup, Lg + (size_t)s_offL[j0] * kGroup,
-                           (s_offL[j1] - s_offL[j0]) * kGroup);
-                warp_stage(Pb + (size_t)buf * CH * kGroup, Pg + (size_t)j0 * kGroup, (j1 - j0) * kGroup);
+                warp_stage(Lb + (size_t)buf * ix.maxLc * gs, Lg + (size_t)s_offL[j0] * gs,
+                           (s_offL[j1] - s_offL[j0]) * gs);
+                warp_stage(Pb + (size_t)buf * CH * gs, Pg + (size_t)j0 * gs, (j1 - j0) * gs);
             }
             cp_async_commit();
         };
@@ -1592,8 +1612,8 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             issue(c + ST - 1);
             cp_async_wait<ST - 1>();
             __syncwarp();
-            const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * kGroup;
-            const int* Pc = Pb + (size_t)(c % ST) * CH * kGroup;
+            const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * gs;
+            const int* Pc = Pb + (size_t)(c % ST) * CH * gs;
             const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
             const int base = s_offL[j0];
             int e1 = base;
@@ -1601,7 +1621,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             for (int jj = 0; jj < CH; ++jj) {
                 const int j = j0 + jj;
                 if (j >= j1) break;
-                const int l = Pc[jj * kGroup + g];
+                const int l = Pc[jj * gs + gsel];
                 const TF bj = y[l];
                 const TF yj0 = y[j];
                 const int e0 = e1;
@@ -1610,7 +1630,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j + 1 + s_Lrow[e];
                     const TF v = (i == l) ? yj0 : y[i];
-                    y[i] = cfms(v, Lc[(e - base) * kGroup + g], bj);
+                    y[i] = cfms(v, Lc[(e - base) * gs + gsel], bj);
                 }
                 if (lg == 0) {
                     y[j] = bj;
@@ -1626,8 +1646,8 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
         auto issue = [&](int c) {
             if (c < nch) {
                 const int s0 = c * CH, s1 = min(s0 + CH, n);
-                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * kGroup, Ug + (size_t)s_offU[s0] * kGroup,
-                           (s_offU[s1] - s_offU[s0]) * kGroup);
+                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * gs, Ug + (size_t)s_offU[s0] * gs,
+                           (s_offU[s1] - s_offU[s0]) * gs);
             }
             cp_async_commit();
         };
@@ -1636,7 +1656,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
             issue(c + ST - 1);
             cp_async_wait<ST - 1>();
             __syncwarp();
-            const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * kGroup;
+            const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * gs;
             const int s0 = c * CH, s1 = min(s0 + CH, n);
             const int base = s_offU[s0];
             int e1 = base;
@@ -1653,7 +1673,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 // same pass (y_j = 0 - (-1/u_jj) y_j) instead of a pass of its own
                 for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j - s_Udist[e];
-                    y[i] = cfms(e == e0 ? TF(0.0) : y[i], Uc[(e - base) * kGroup + g], yj);
+                    y[i] = cfms(e == e0 ? TF(0.0) : y[i], Uc[(e - base) * gs + gsel], yj);
                 }
                 __syncwarp();
             }
@@ -1667,7 +1687,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
         TF* sl = zb + r;
         if (staged && live)
             for (int q = lg; q < r * r; q += kLanesPer) sl[q] = cd.slu[(size_t)sys * r * r + q];
-        const TF* Vg = cd.V + (size_t)wg * ix.nV * kGroup;
+        const TF* Vg = cd.V + (size_t)wg * ix.nV * gs;
         for (int a = 0; a < r; ++a) {
             TF acc = TF(0.0);
             const int ea = ix.offV[a], eb = ix.offV[a + 1];
@@ -1678,7 +1698,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 for (int u = 0; u < kU; ++u) {
                     const int e = e0 + u * kLanesPer;
                     c[u] = e < eb ? ix.Vcol[e] : -1;
-                    v[u] = e < eb ? Vg[(size_t)e * kGroup + g] : TF(0.0);
+                    v[u] = e < eb ? Vg[(size_t)e * gs + gsel] : TF(0.0);
                 }
 #pragma unroll
                 for (int u = 0; u < kU; ++u)
@@ -1719,6 +1739,9 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
         __syncwarp();
     }
     if (!live) return;
+    if (partner)                                 // x = dc y (each lane flips the entries it stores)
+        for (int i = lg; i < n; i += kLanesPer)
+            if (cd.flip_c[i]) y[i] = -y[i];
     if constexpr (IO == IO_MIXED) {
         zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
         zd* xt = static_cast<zd*>(io.xT);
@@ -1754,7 +1777,8 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
 template <class TF, class TD, int IO>
 __global__ void __launch_bounds__(256)
 k_solve_compact(CompactIdx ix, CompactData<TF> cd, SolveIo io) {
-    solve_compact_body<TF, TD, IO>(ix, cd, io, blockIdx.x);
+    const SolveIo none{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    solve_compact_body<TF, TD, IO>(ix, cd, io, none, blockIdx.x);
 }
 
 // One launch for several buckets (the systems of a whole step): blocks block_start[b] ..
@@ -1767,6 +1791,7 @@ struct MultiSolve {
     CompactIdx ix[kMaxMulti];
     CompactData<TF> cd[kMaxMulti];
     SolveIo io[kMaxMulti];
+    SolveIo io2[kMaxMulti];         // the partner bucket of a shared pair (rhs NULL: none)
 };
 
 template <class TF, class TD, int IO, int CH, int ST>
@@ -1774,7 +1799,7 @@ __global__ void __launch_bounds__(256)
 k_solve_compact_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
-    solve_compact_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
+    solve_compact_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
 }
 
 // ---- one system per warp, lanes split over (entry, real/imaginary part) -------------------------
@@ -2005,6 +2030,7 @@ __global__ void k_pack_compact(BandView<T> v, CompactIdx ix, T* __restrict__ L, 
     const int sys = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (sys >= total_sys) return;
     const int lane = threadIdx.x & 31;
+    const int kGroup = ix.gs;                   // systems per warp group of the streams
     const int wg = sys / kGroup, g = sys % kGroup;
     const bool live = sys < v.batch;
     const int n = v.n, kv = v.kl + v.ku;
@@ -2042,7 +2068,7 @@ __global__ void k_demote_n(const zd* __restrict__ a, zf* __restrict__ b, long lo
 
 // FP32 copies of the compact factor streams (the FP32 form's solves read these).
 static void demote_compact(Banded& h, cudaStream_t st) {
-    const size_t G = kGroup, W = h.cWg;
+    const size_t G = h.cG, W = h.cWg;
     if (!h.c_L32) {
         dalloc(&h.c_L32, W * std::max(h.cL, 1) * G, sizeof(zf));
         dalloc(&h.c_U32, W * std::max(h.cU, 1) * G, sizeof(zf));
@@ -2060,7 +2086,7 @@ static void demote_compact(Banded& h, cudaStream_t st) {
 static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     CompactIdx ix;
     ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
-    ix.wgroups = h.cWg; ix.batch = h.batch;
+    ix.wgroups = h.cWg; ix.batch = h.batch; ix.gs = h.cG;
     ix.maxLc = h.cMaxLk[chunk_index(chunk)];
     ix.maxUc = h.cMaxUk[chunk_index(chunk)];
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
@@ -2132,7 +2158,8 @@ static void compact(Banded& h, cudaStream_t st) {
     h.cL = (int)Lrow.size();
     h.cU = (int)Udist.size();
     h.cV = (int)Vcol.size();
-    h.cWg = (h.batch + kGroup - 1) / kGroup;
+    h.cG = h.shared ? 1 : kGroup;
+    h.cWg = (h.batch + h.cG - 1) / h.cG;
     auto up = [&](auto** d, const auto& v) {
         using E = std::remove_reference_t<decltype(v[0])>;
         dalloc(d, std::max<size_t>(v.size(), 1), sizeof(E));
@@ -2141,7 +2168,7 @@ static void compact(Banded& h, cudaStream_t st) {
     if (!h.c_offL) {
         up(&h.c_offL, offL); up(&h.c_Lrow, Lrow); up(&h.c_Lmask, Lmask); up(&h.c_offU, offU);
         up(&h.c_Udist, Udist); up(&h.c_offV, offV); up(&h.c_Vcol, Vcol);
-        const size_t G = kGroup, W = h.cWg;
+        const size_t G = h.cG, W = h.cWg;
         dalloc(&h.c_L, W * std::max(h.cL, 1) * G, sizeof(zd));
         dalloc(&h.c_U, W * std::max(h.cU, 1) * G, sizeof(zd));
         dalloc(&h.c_V, W * std::max(h.cV, 1) * G, sizeof(zd));
@@ -2152,7 +2179,7 @@ static void compact(Banded& h, cudaStream_t st) {
     }
     CNG_CUDA(cudaStreamSynchronize(st));
     // 3. pack
-    const int total = h.cWg * kGroup;
+    const int total = h.cWg * h.cG;
     k_pack_compact<zd><<<ceil_div(total, 4), 128, 0, st>>>(h.view<zd>(), compact_idx(h), static_cast<zd*>(h.c_L),
                                                            static_cast<zd*>(h.c_U), static_cast<zd*>(h.c_V), h.c_piv, total);
     CNG_LAUNCH("k_pack_compact");
@@ -2168,8 +2195,8 @@ static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
     size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
     off = (off + 15) & ~(size_t)15;
     const size_t per_warp = (size_t)kGroup * (h.n + 64) +
-                            (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * kGroup +
-                            ((size_t)sc.stages * sc.chunk * kGroup * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+                            (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG +
+                            ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     return off + sizeof(TF) * per_warp * nwarps;
 }
 
@@ -2211,7 +2238,8 @@ namespace cng {
 
 template <class TF, class TD, int IO, int CH, int ST>
 static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                           const std::vector<SolveIo>& ios, int sched, cudaStream_t st) {
+                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2, int sched,
+                           cudaStream_t st) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2255,6 +2283,7 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         ms.ix[k] = compact_idx(*hs[i], CH);
         ms.cd[k] = cds[i];
         ms.io[k] = ios[i];
+        ms.io2[k] = ios2[i];
         blocks += ceil_div(hs[i]->cWg, nw);
     }
     ms.block_start[ms.nb] = blocks;
@@ -2275,7 +2304,11 @@ static size_t split_smem(const Banded& h, int nwarps, int sched) {
 
 template <class TF, class TD, int IO, int CH, int ST>
 static void launch_split_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                           const std::vector<SolveIo>& ios, int sched, cudaStream_t st) {
+                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>&, int sched,
+                           cudaStream_t st) {
+    for (const Banded* h : hs)
+        if (h->cG != kGroup)
+            throw InvalidArgument("the split-lane schedules do not solve shared pairs: a compact two-system schedule");
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_solve_split_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2326,23 +2359,23 @@ static void launch_split_t(const std::vector<const Banded*>& hs, const std::vect
 // when they differ)
 template <class TF, class TD, int IO>
 static void launch_multi(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                         const std::vector<SolveIo>& ios, cudaStream_t st) {
+                         const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2, cudaStream_t st) {
     int sched = hs[0]->sched;
     for (const Banded* h : hs)
         if (h->sched != sched) sched = 0;
     if (sched < 0 || sched >= kNumSchedules) sched = 0;
     switch (sched) {
-        case 1: launch_multi_t<TF, TD, IO, 8, 3>(hs, cds, ios, sched, st); break;
-        case 2: launch_multi_t<TF, TD, IO, 4, 3>(hs, cds, ios, sched, st); break;
-        case 3: launch_multi_t<TF, TD, IO, 16, 2>(hs, cds, ios, sched, st); break;
-        case 4: launch_multi_t<TF, TD, IO, 16, 3>(hs, cds, ios, sched, st); break;
-        case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, sched, st); break;
-        case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, sched, st); break;
-        case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, sched, st); break;
-        case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, sched, st); break;
-        case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, sched, st); break;
-        case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, sched, st); break;
-        default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, sched, st); break;
+        case 1: launch_multi_t<TF, TD, IO, 8, 3>(hs, cds, ios, ios2, sched, st); break;
+        case 2: launch_multi_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, sched, st); break;
+        case 3: launch_multi_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, sched, st); break;
+        case 4: launch_multi_t<TF, TD, IO, 16, 3>(hs, cds, ios, ios2, sched, st); break;
+        case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, ios2, sched, st); break;
+        case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, ios2, sched, st); break;
+        case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, ios2, sched, st); break;
+        case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, sched, st); break;
+        case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, sched, st); break;
+        case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, sched, st); break;
+        default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, sched, st); break;
     }
 }
 
@@ -2350,26 +2383,47 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
 
 extern "C" {
 
-int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, void* const* x, int fp32,
-                           int accumulate, void* stream) {
+int cng_banded_solve_batch2(int nh, cng_banded* const* hh, const void* const* b, void* const* x,
+                            const void* const* b2, void* const* x2, void* const* xt, void* const* xt2, int fp32,
+                            int accumulate, void* stream) {
     CNG_TRY({
         if (nh < 1 || nh > kMaxMulti) throw InvalidArgument("1 to 8 handles per batched solve");
         if (!hh || !b || !x) throw InvalidArgument("null argument");
+        if ((xt || xt2) && !fp32) throw InvalidArgument("the row-major copy of x is written by the FP32 solve only");
         std::vector<const Banded*> hs;
-        std::vector<SolveIo> ios;
+        std::vector<SolveIo> ios, ios2;
+        bool any_pair = false;
         for (int k = 0; k < nh; ++k) {
             const Banded* h = reinterpret_cast<const Banded*>(hh[k]);
             if (!h || !h->compact_ready || h->dtype != 1)
                 throw InvalidArgument("batched solve needs complex128 handles in compact form");
             if (fp32 && !h->fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first");
             if (!b[k] || !x[k] || b[k] == x[k]) throw InvalidArgument("b and x: device pointers, not aliased");
+            const void* pb = b2 ? b2[k] : nullptr;
+            void* px = x2 ? x2[k] : nullptr;
+            if ((pb == nullptr) != (px == nullptr))
+                throw InvalidArgument("a partner right-hand side needs its solution and the converse");
+            if (pb) {
+                if (!h->shared) throw InvalidArgument("a partner solve needs a handle shared with cng_banded_share");
+                if (pb == px || px == x[k] || pb == x[k] || px == b[k])
+                    throw InvalidArgument("partner b and x: device pointers, not aliased with each other or b, x");
+                any_pair = true;
+            }
+            if (xt && xt[k] && (xt[k] == x[k] || xt[k] == b[k])) throw InvalidArgument("xt aliases b or x");
             hs.push_back(h);
-            ios.push_back(SolveIo{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate});
+            SolveIo io{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate};
+            io.xT = xt ? xt[k] : nullptr;
+            ios.push_back(io);
+            SolveIo io2{pb, px, nullptr, nullptr, nullptr, nullptr, accumulate};
+            io2.xT = (pb && xt2) ? xt2[k] : nullptr;
+            ios2.push_back(io2);
         }
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         bool dense = true;
         for (const Banded* h : hs) dense = dense && h->sched < 0;
         if (dense) {              // the band kernel, one launch per bucket
+            if (any_pair) throw InvalidArgument("the band kernel does not solve shared pairs: a compact schedule");
+            if (xt) throw InvalidArgument("the transposed copy of x: compact schedules only");
             for (size_t k = 0; k < hs.size(); ++k) {
                 if (fp32) launch_mixed_dense(*hs[k], b[k], x[k], accumulate, st);
                 else launch_solve(*hs[k], IO_MAPPED, ios[k], st);
@@ -2379,41 +2433,62 @@ int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, 
         if (fp32) {
             std::vector<CompactData<zf>> cds;
             for (const Banded* h : hs)
-                cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm});
-            launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, st);
+                cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm,
+                                              h->flip_r, h->flip_c});
+            launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, ios2, st);
         } else {
             std::vector<CompactData<zd>> cds;
             for (const Banded* h : hs)
                 cds.push_back(CompactData<zd>{static_cast<const zd*>(h->c_L), static_cast<const zd*>(h->c_U), h->c_piv,
                                               static_cast<const zd*>(h->c_V), static_cast<const zd*>(h->w),
-                                              static_cast<const zd*>(h->slu), h->spiv, h->perm});
-            launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, st);
+                                              static_cast<const zd*>(h->slu), h->spiv, h->perm, h->flip_r, h->flip_c});
+            launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, ios2, st);
         }
     })
 }
 
+int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, void* const* x, int fp32,
+                           int accumulate, void* stream) {
+    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, nullptr, nullptr, fp32, accumulate, stream);
+}
+
 int cng_banded_solve_batch_xt(int nh, cng_banded* const* hh, const void* const* b, void* const* x,
                               void* const* xt, int accumulate, void* stream) {
+    if (!xt) {
+        cng::set_error("null argument");
+        return cng::CNG_EINVAL;
+    }
+    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, xt, nullptr, 1, accumulate, stream);
+}
+
+int cng_banded_share(cng_banded* hh, const int8_t* dr, const int8_t* dc, void* stream) {
     CNG_TRY({
-        if (nh < 1 || nh > kMaxMulti) throw InvalidArgument("1 to 8 handles per batched solve");
-        if (!hh || !b || !x || !xt) throw InvalidArgument("null argument");
-        std::vector<const Banded*> hs;
-        std::vector<SolveIo> ios;
-        std::vector<CompactData<zf>> cds;
-        for (int k = 0; k < nh; ++k) {
-            const Banded* h = reinterpret_cast<const Banded*>(hh[k]);
-            if (!h || !h->compact_ready || h->dtype != 1 || !h->fp32_ready)
-                throw InvalidArgument("batched solve needs complex128 handles in compact form with FP32 factors");
-            if (h->sched < 0) throw InvalidArgument("the transposed copy of x: compact schedules only");
-            if (!b[k] || !x[k] || b[k] == x[k] || (xt[k] && (xt[k] == x[k] || xt[k] == b[k])))
-                throw InvalidArgument("b, x and xt: device pointers, not aliased");
-            hs.push_back(h);
-            SolveIo io{b[k], x[k], nullptr, nullptr, nullptr, nullptr, accumulate};
-            io.xT = xt[k];
-            ios.push_back(io);
-            cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm});
+        cng::Banded* h = reinterpret_cast<cng::Banded*>(hh);
+        if (!h || !dr || !dc) throw InvalidArgument("null argument");
+        if (h->dtype != 1) throw InvalidArgument("shared factors: complex128 handles");
+        if (h->compact_ready) throw InvalidArgument("cng_banded_share must come before cng_banded_compact");
+        const int n = h->n;
+        std::vector<unsigned char> fr(n), fc(n);
+        for (int i = 0; i < n; ++i) {
+            if ((dr[i] != 1 && dr[i] != -1) || (dc[i] != 1 && dc[i] != -1))
+                throw InvalidArgument("sign vectors hold +1 or -1");
+            fr[i] = dr[i] < 0;
+            fc[i] = dc[i] < 0;
         }
-        launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, static_cast<cudaStream_t>(stream));
+        // the band part of the partner is the sign flip of this one only if every border row keeps
+        // the sign of its s e_i (dr_i dc_i = +1 at the border positions)
+        for (int k = 0; k < h->r; ++k)
+            if (dr[h->perm_host[k]] * dc[k] != 1)
+                throw InvalidArgument("shared factors: a border row changes the sign of its diagonal");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (!h->flip_r) {
+            dalloc(&h->flip_r, n, 1);
+            dalloc(&h->flip_c, n, 1);
+        }
+        CNG_CUDA(cudaMemcpyAsync(h->flip_r, fr.data(), n, cudaMemcpyHostToDevice, st));
+        CNG_CUDA(cudaMemcpyAsync(h->flip_c, fc.data(), n, cudaMemcpyHostToDevice, st));
+        CNG_CUDA(cudaStreamSynchronize(st));
+        h->shared = true;
     })
 }
 

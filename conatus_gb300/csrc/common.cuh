@@ -110,6 +110,7 @@ struct alignas(8) zf {
 };
 __host__ __device__ inline zf operator+(zf a, zf b) { return zf(a.re + b.re, a.im + b.im); }
 __host__ __device__ inline zf operator-(zf a, zf b) { return zf(a.re - b.re, a.im - b.im); }
+__host__ __device__ inline zf operator-(zf a) { return zf(-a.re, -a.im); }
 __host__ __device__ inline zf operator*(zf a, zf b) {
     return zf(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
 }

@@ -99,7 +99,7 @@ class DeviceProblem:
     """A problem instance resident on the device (see module docstring)."""
 
     def __init__(self, problem, precision: str = "fp64", device: str = "cuda", compact: bool = True,
-                 factor_sets: int | None = None):
+                 factor_sets: int | None = None, share: bool = True):
         torch = _torch()
         _lib.lib()
         self.factor_sets = factor_sets      # None: keep every (a, b) factorization, else at most this many
@@ -116,6 +116,10 @@ class DeviceProblem:
         self.tpl = tpl = problem.tpl
         self.precision = precision
         self.compact = bool(compact)
+        # buckets solved with another bucket's factors (the reference's SharedFactor): structural
+        # candidates here, the values checked at every factorization
+        self._pairs = tpl.sign_pairs() if (share and self.compact) else {}
+        self.shared = {}                    # partner -> primary of the current factor set
         self.device = torch.device(device)
         self.d = len(tpl.fourier_axes)
         self.nsys = list(problem.nsys)
@@ -331,22 +335,52 @@ class DeviceProblem:
                 Mv, per = self._M[bi][:2]
                 per = per if isinstance(per, int) else 0
                 vals_all.append((a * (Mv if per else Mv.unsqueeze(0)) + b_ * self._Lvals(bi)).contiguous())
+            shared = self._check_pairs(vals_all)
             torch.cuda.current_stream(self.device).synchronize()    # the values come from torch's stream
             f = []
             for bi, b in enumerate(self.tpl.buckets):
+                if bi in shared:                 # solved with its primary's factors
+                    f.append(_Partner(shared[bi], f[shared[bi]]))
+                    continue
                 vals = vals_all[bi]
                 h = _Handle.shared(np.complex128, self.nsys[bi], b.n, b.indptr, b.indices, vals,
                                    list(range(b.r)), pivot=True, stream=_stream_handle(stream))
                 if self.precision == "fp32":
                     call("cng_banded_make_fp32", h.h, _stream_handle(stream))
+                rel = next(((dr, dc) for j, (i, dr, dc) in self._pairs.items() if i == bi and j in shared), None)
+                if rel is not None:
+                    call("cng_banded_share", h.h, np.ascontiguousarray(rel[0], np.int8).ctypes.data,
+                         np.ascontiguousarray(rel[1], np.int8).ctypes.data, _stream_handle(stream))
                 if self.compact:
                     call("cng_banded_compact", h.h, _stream_handle(stream))
                 f.append(h)
+            del vals_all
+            self.shared = dict(shared)
+            self._groups = None
             self._factors[key] = f
             if self.compact and self.autotune:
                 from .autotune import tune_solve
                 self.tuning = tune_solve(self, key, f, stream)
         return f
+
+    def _check_pairs(self, vals_all) -> dict:
+        """{partner: primary} of the structural pairs whose values satisfy the relation exactly at
+        this (a, b): no zero entry in the primary (a zero carries no sign), and every entry of the
+        partner equal to dr_i dc_j times the primary's (the reference's rule,
+        python/conatus/timestep/shared_factors.py:104-138)."""
+        torch = _torch()
+        out = {}
+        for j, (i, dr, dc) in self._pairs.items():
+            A, B = vals_all[i], vals_all[j]
+            if A.shape != B.shape:
+                continue
+            b = self.tpl.buckets[i]
+            flip = torch.as_tensor((dr[b.coo_rows()] * dc[b.indices]) < 0, device=self.device)
+            if bool((A == 0).any()):
+                continue
+            if bool(torch.equal(B, torch.where(flip.unsqueeze(0), -A, A))):
+                out[j] = i
+        return out
 
     def _residual_data(self, bi):
         """Device data of the FP64 refinement residual of bucket bi: M and every wavenumber monomial
@@ -530,11 +564,8 @@ class DeviceProblem:
                     raise ValueError("the FP32 form needs the compact solve")
             return
         nb = len(fs)
-        hs = (ctypes.c_void_p * nb)(*[h.h.value for h in fs])
-        bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in range(nb)])
-        xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in range(nb)])
         if self.precision == "fp64":
-            call("cng_banded_solve_batch", nb, hs, bp, xp, 0, 0, s)
+            self._batch_call(fs, list(range(nb)), rhs, out, None, 0, 0, s)
             return
         if self._R2 is None:
             self._R2 = self.zeros()
@@ -560,52 +591,64 @@ class DeviceProblem:
         main.wait_event(join)
 
     def _refine_groups(self):
-        """Buckets split in two groups of about equal work (systems x length), largest first."""
+        """Buckets split in two groups of about equal work (systems x length), largest first; a
+        shared pair (one factor set, both solved in one sweep) stays in one group."""
         if self._groups is None:
-            order = sorted(range(len(self.nsys)), key=lambda bi: -self.nsys[bi] * self.tpl.buckets[bi].n)
+            units = {}
+            for bi in range(len(self.nsys)):
+                units.setdefault(self.shared.get(bi, bi), []).append(bi)
+            work = lambda u: sum(self.nsys[bi] * self.tpl.buckets[bi].n for bi in units[u])
+            order = sorted(units, key=lambda u: -work(u))
             g, w = [[], []], [0, 0]
-            for bi in order:
+            for u in order:
                 k = 0 if w[0] <= w[1] else 1
-                g[k].append(bi)
-                w[k] += self.nsys[bi] * self.tpl.buckets[bi].n
+                g[k].extend(units[u])
+                w[k] += work(u)
             self._groups = [sorted(x) for x in g if x]
         return self._groups
+
+    def _batch_call(self, fs, group, rhs, out, xt, fp32, accumulate, s) -> None:
+        """One batched solve launch over the buckets in ``group``: every handle of the group, a
+        shared pair's partner solved in the same sweep as its primary (cng_banded_solve_batch2)."""
+        prim = [bi for bi in group if not isinstance(fs[bi], _Partner)]
+        part = {fs[bj].primary: bj for bj in group if isinstance(fs[bj], _Partner)}
+        if any(fs[bj].primary not in prim for bj in part.values()):
+            raise ValueError("a shared pair must be solved in one launch")
+        nb = len(prim)
+        V = ctypes.c_void_p * nb
+        ptr = lambda X, bi: self.bucket(X, bi).data_ptr() if bi is not None else None
+        hs = V(*[fs[bi].h.value for bi in prim])
+        bp, xp = V(*[ptr(rhs, bi) for bi in prim]), V(*[ptr(out, bi) for bi in prim])
+        b2 = x2 = xt1 = xt2 = None
+        if part:
+            b2 = V(*[ptr(rhs, part.get(bi)) for bi in prim])
+            x2 = V(*[ptr(out, part.get(bi)) for bi in prim])
+        if xt is not None:
+            xt1 = V(*[ptr(xt, bi) for bi in prim])
+            if part:
+                xt2 = V(*[ptr(xt, part.get(bi)) for bi in prim])
+        call("cng_banded_solve_batch2", nb, hs, bp, xp, b2, x2, xt1, xt2, fp32, accumulate, s)
 
     def _refine_chain(self, fs, group, a, b_, rhs, out, s) -> None:
         """FP32 solve of the buckets in ``group``, then ``refine`` passes of FP64 residual and FP32
         correction added in FP64, all on stream ``s``."""
-        nb = len(group)
-        hs = (ctypes.c_void_p * nb)(*[fs[bi].h.value for bi in group])
-        bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in group])
-        xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in group])
-        rp = (ctypes.c_void_p * nb)(*[self.bucket(self._R2, bi).data_ptr() for bi in group])
         # x also row-major over the systems (coalesced reads of the residual kernel), with the
         # compact schedules
         xt = None
         if all(getattr(fs[bi], "schedule", 0) >= 0 for bi in group):
             if self._XT is None:
                 self._XT = self.zeros()
-            xt = (ctypes.c_void_p * nb)(*[self.bucket(self._XT, bi).data_ptr() for bi in group])
-        if xt is not None:
-            call("cng_banded_solve_batch_xt", nb, hs, bp, xp, xt, 0, s)
-        else:
-            call("cng_banded_solve_batch", nb, hs, bp, xp, 1, 0, s)
+            xt = self._XT
+        self._batch_call(fs, group, rhs, out, xt, 1, 0, s)
         for p in range(self.refine):
-            self.residual(a, b_, out, rhs, self._R2, s, buckets=group, xT=self._XT if xt is not None else None)
-            if xt is not None and p + 1 < self.refine:
-                call("cng_banded_solve_batch_xt", nb, hs, rp, xp, xt, 1, s)
-            else:
-                call("cng_banded_solve_batch", nb, hs, rp, xp, 1, 1, s)
+            self.residual(a, b_, out, rhs, self._R2, s, buckets=group, xT=xt)
+            self._batch_call(fs, group, self._R2, out, xt if p + 1 < self.refine else None, 1, 1, s)
 
     def solve_launch(self, fs, rhs, out, stream=None) -> None:
         """One batched solve launch with the factor set ``fs`` (FP32 factors in the FP32 form), no
         refinement: the unit the solve's roofline is measured on."""
-        nb = len(fs)
-        hs = (ctypes.c_void_p * nb)(*[h.h.value for h in fs])
-        bp = (ctypes.c_void_p * nb)(*[self.bucket(rhs, bi).data_ptr() for bi in range(nb)])
-        xp = (ctypes.c_void_p * nb)(*[self.bucket(out, bi).data_ptr() for bi in range(nb)])
-        call("cng_banded_solve_batch", nb, hs, bp, xp, 1 if self.precision == "fp32" else 0, 0,
-             _stream_handle(stream))
+        self._batch_call(fs, list(range(len(fs))), rhs, out, None, 1 if self.precision == "fp32" else 0, 0,
+                         _stream_handle(stream))
 
     def zeros(self):
         torch = _torch()
@@ -628,6 +671,22 @@ class DeviceProblem:
                 _lib.lib().cng_rhs_destroy(h)
             except Exception:
                 pass
+
+
+class _Partner:
+    """Factor-list entry of a bucket solved with the factors of bucket ``primary`` (a shared pair:
+    the partner's matrix is diag(dr) A diag(dc), python/conatus/timestep/shared_factors.py:40-60).
+    Holds no device memory; shapes and schedule are the primary's."""
+
+    def __init__(self, primary: int, handle):
+        self.primary, self._p = primary, handle
+        self.h = None
+        for k in ("batch", "n", "rank", "kl", "ku", "ldab", "pivot"):
+            setattr(self, k, getattr(handle, k))
+
+    @property
+    def schedule(self):
+        return getattr(self._p, "schedule", 0)
 
 
 class _Graph:

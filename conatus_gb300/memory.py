@@ -16,6 +16,9 @@ one by one:
   kl + ku + 1 of U per column, r x n of V); one transient copy of a M + b L while factoring;
 * the F pipeline's work buffers (``cng_rhs_create``: the spectra S and two grid buffers).
 
+A shared pair's partner (the (kx, -kz) systems solved with the (kx, +kz) factors) holds no factors;
+its primary's compact streams hold one system per warp group.
+
 Factor sets kept: one in the steady state when the solver keeps a single set (``IVPSolver(...,
 factor_sets=1)``), else one per start-up order.
 """
@@ -43,7 +46,7 @@ def bucket_band(b) -> tuple:
     return kl, ku
 
 
-def _factor_bytes(b, nsys, precision, compact):
+def _factor_bytes(b, nsys, precision, compact, shared=False):
     n, r = b.n, b.r
     kl, ku = bucket_band(b)
     ldab = 2 * kl + ku + 1
@@ -51,8 +54,11 @@ def _factor_bytes(b, nsys, precision, compact):
     out = nsys * (n * ldab * _Z + n * 4 + 2 * r * n * _Z + r * r * _Z + r * 4 + 4 + 8) + n * 4 + nnz * 8
     if precision == "fp32":
         out += nsys * (n * ldab * _C + 2 * r * n * _C + r * r * _C)
+    if shared:
+        out += 2 * n                                   # the sign flags of the partner
     if compact:
-        slots = int(math.ceil(nsys / 2)) * 2           # two systems per warp group
+        # two systems per warp group, one for a shared pair's primary
+        slots = nsys if shared else int(math.ceil(nsys / 2)) * 2
         per = n * kl + n * (kl + ku + 1) + r * n
         out += slots * (per * _Z + n * 4) + 6 * (n + 1) * 4 + per * 5
         if precision == "fp32":
@@ -91,7 +97,7 @@ def _rhs_bytes(problem, precision):
 
 
 def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: bool = True,
-             factor_sets: int | None = None) -> dict:
+             factor_sets: int | None = None, share: bool = True) -> dict:
     """Predicted device bytes of ``IVPSolver(problem, scheme, precision=precision)``, by part,
     with the total under ``"total"``."""
     tpl = problem.tpl
@@ -101,11 +107,17 @@ def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: b
     parts = {"state": vec * (2 + (2 if precision == "fp32" else 0)), "history": 2 * q * vec,
              "rhs_work": _rhs_bytes(problem, precision)}
     ops = fac = trans = rows = 0
-    for b, ns in zip(tpl.buckets, problem.nsys):
+    # shared pairs (conatus_gb300.ivp: partners solved with their primary's factors)
+    pairs = tpl.sign_pairs() if compact and share else {}
+    primaries = {i for i, _, _ in pairs.values()}
+    vals = 0
+    for bi, (b, ns) in enumerate(zip(tpl.buckets, problem.nsys)):
         nnz = int(b.indices.size)
         const_m = b.m_is_constant() and b.exact is None
         ops += (nnz * (_Z + 8) if const_m else ns * nnz * _Z) + ns * nnz * _Z + (b.n + 1 + nnz) * 4
-        fac += _factor_bytes(b, ns, precision, compact)
+        if bi not in pairs:
+            fac += _factor_bytes(b, ns, precision, compact, shared=bi in primaries)
+        vals += ns * nnz * _Z                          # a M + b L of every bucket while factoring
         trans = max(trans, ns * nnz * _Z)
         if precision == "fp32":
             ops += 2 * b.n * 16 + ns * 16 * 8        # split-operator residual lists (bounded)
@@ -114,7 +126,8 @@ def plan_ivp(problem, scheme: str = "SBDF2", precision: str = "fp64", compact: b
     sets = q if factor_sets is None else max(1, min(q, int(factor_sets)))
     parts["operators"] = ops + rows * (sets + 1)
     parts["factors"] = fac * sets
-    parts["factor_transient"] = trans
+    # while factoring: the values of every bucket (the pairs are checked on them), plus one copy
+    parts["factor_transient"] = vals + trans
     parts["total"] = int(sum(parts.values()))
     return parts
 

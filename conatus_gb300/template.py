@@ -70,6 +70,58 @@ class Bucket:
         return bool(not others or np.all(self.Mc[others] == 0))
 
 
+def sign_similarity(a: Bucket, b: Bucket):
+    """(dr, dc), int8 vectors of +1/-1, with b's matrix = diag(dr) (a's matrix) diag(dc) at every
+    mode and for every (a, b) combination of M and L, or None. Structural: a and b are the two
+    sign views (kx, +kz) and (kx, -kz) of the same groups (same pattern and the same polynomials
+    in the signed wavenumbers), so b's entry e is a's with kz -> -kz; it is + or - a's entry at
+    every mode iff every term of e (in M and in L) has the same parity in kz, and the entry signs
+    must factor as dr_i dc_j (a spanning forest of the pattern's bipartite graph gives the
+    candidate, every entry checks it). A border row k (rows 0 .. r-1) must keep the sign of its
+    diagonal: dr_k dc_k = +1. The reference's sign_similarity (python/conatus/timestep/
+    shared_factors.py:104-138) checks the same relation on the assembled values; conatus_gb300.ivp
+    checks the values too before sharing."""
+    if (a.kind != "complex" or b.kind != "complex" or a.n != b.n or a.r != b.r or a.active != b.active
+            or a.sign == b.sign or len(a.active) < 2 or not all(a.active)):
+        return None
+    if not (np.array_equal(a.indptr, b.indptr) and np.array_equal(a.indices, b.indices)
+            and np.array_equal(a.monos, b.monos) and np.array_equal(a.Mc, b.Mc) and np.array_equal(a.Lc, b.Lc)):
+        return None
+    odd = (a.monos[:, 1] % 2 == 1)[:, None]             # terms odd in kz flip with the sign view
+    used = (a.Mc != 0) | (a.Lc != 0)                    # (nmono, nnz)
+    has_odd = np.any(used & odd, axis=0)
+    has_even = np.any(used & ~odd, axis=0)
+    if np.any(has_odd & has_even) or not np.all(has_odd | has_even):
+        return None                                     # mixed parity (or an empty entry): no relation
+    sgn = np.where(has_odd, -1, 1).astype(np.int8)      # entry sign of b relative to a
+    n = a.n
+    rows = np.repeat(np.arange(n), np.diff(a.indptr))
+    cols = a.indices.astype(np.int64)
+    # spanning forest of the bipartite graph (rows 0..n-1, columns n..2n-1), breadth first
+    adj = [[] for _ in range(2 * n)]
+    for e, (i, j) in enumerate(zip(rows, cols)):
+        adj[i].append((n + j, e))
+        adj[n + j].append((i, e))
+    d = np.zeros(2 * n, np.int8)
+    for root in range(2 * n):
+        if d[root]:
+            continue
+        d[root] = 1
+        queue = [root]
+        while queue:
+            v = queue.pop()
+            for w, e in adj[v]:
+                if not d[w]:
+                    d[w] = d[v] * sgn[e]
+                    queue.append(w)
+    dr, dc = d[:n].copy(), d[n:].copy()
+    if not np.array_equal(dr[rows] * dc[cols], sgn):
+        return None                                     # entry signs do not factor as dr_i dc_j
+    if a.r and not np.all(dr[:a.r] * dc[:a.r] == 1):
+        return None                                     # a border row's s e_k would change sign
+    return dr, dc
+
+
 @dataclass
 class ProblemTemplate:
     name: str
@@ -145,6 +197,21 @@ class ProblemTemplate:
                    linear_params=list(meta.get("linear_params", [])))
 
     # ---------------------------------------------------------------- derived
+    def sign_pairs(self) -> dict:
+        """Buckets solved with another bucket's factors: {partner index: (primary index, dr, dc)}
+        (``sign_similarity``), each primary used once."""
+        out, used = {}, set()
+        for j, b in enumerate(self.buckets):
+            for i, a in enumerate(self.buckets[:j]):
+                if i in used or i in out:
+                    continue
+                rel = sign_similarity(a, b)
+                if rel is not None:
+                    out[j] = (i, rel[0], rel[1])
+                    used.add(i)
+                    break
+        return out
+
     @property
     def ncheb(self) -> int:
         return self.axes[self.cheb_axis]["N"] if self.cheb_axis >= 0 else 1

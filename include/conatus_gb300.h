@@ -118,6 +118,29 @@ int cng_banded_solve_batch(int nh, cng_banded* const* h, const void* const* b, v
 int cng_banded_solve_batch_xt(int nh, cng_banded* const* h, const void* const* b, void* const* x,
                               void* const* xt, int accumulate, void* stream);
 
+/* Shared factors of sign-similar buckets. With two RealFourier directions the (kx, +kz) and
+ * (kx, -kz) systems of a group often differ only by signs: B = diag(dr) A diag(dc), dr and dc of
+ * +1/-1 (host int8 arrays of n, in the matrix's own row and column order), the same for every
+ * system of the batch. Then B x = b is y = A^{-1} (dr b), x = dc y with A's factors, bit for bit the
+ * solve with B's own factorization (the pivot search compares magnitudes; sign flips are exact).
+ * Marks handle h (A's batch) as shared: its compact streams (cng_banded_compact, which must come
+ * after this call) hold one system per warp group, the partner's systems take the other half of
+ * each warp. A border row k must keep the sign of its diagonal s e_k: dr[border[k]] dc[k] = +1,
+ * else status 1. The caller checks the relation on the values (every entry of B equal to + or - the
+ * entry of A, signs factoring as dr_i dc_j); this call takes it as given. Replaces the reference's
+ * SharedFactor (python/conatus/timestep/shared_factors.py:1-40, found by sign_similarity,
+ * shared_factors.py:104-138, and solved in timestep/device.py:396-485). */
+int cng_banded_share(cng_banded* h, const int8_t* dr, const int8_t* dc, void* stream);
+
+/* The general batched solve: cng_banded_solve_batch, plus for a shared handle k (cng_banded_share)
+ * the partner's right-hand side b2[k] and solution x2[k] (NULL entries, or NULL arrays: no partner),
+ * solved in the same sweep over the factor streams; fp32 = 1 may also write x row-major over the
+ * systems into xt[k] and xt2[k] (the refinement residual's coalesced copy; NULL: not written). The
+ * band kernel (schedule -1) and the split-lane schedules do not solve partners (status 1). */
+int cng_banded_solve_batch2(int nh, cng_banded* const* h, const void* const* b, void* const* x,
+                            const void* const* b2, void* const* x2, void* const* xt, void* const* xt2,
+                            int fp32, int accumulate, void* stream);
+
 /* Schedules of the compact solve (the batched-solve kernel of the step): count, and per schedule
  * the columns per staged chunk of the factor streams, the depth of the staging ring and whether it
  * runs one system per warp with the lanes split over entries and real/imaginary parts (split = 1:

@@ -285,18 +285,33 @@ TRAJECTORY_CASES = {
 }
 
 
-def trajectory_fixtures(cn, out_dir):
+TRAJ_FLOOR = 1e-8      # a field's norm counts as at least this fraction of the state's norm
+
+
+def field_spread(arrs, ref, floor=TRAJ_FLOOR):
+    """Relative L2 difference per variable of coefficient arrays ``arrs`` against ``ref``, each
+    field's norm taken at least ``floor`` times the norm of the whole state (the tau variables,
+    zero up to rounding, are judged against the state)."""
+    tot = sum(float(np.sum(np.asarray(r) ** 2)) for r in ref) ** 0.5
+    return np.array([float(np.linalg.norm(np.asarray(a) - np.asarray(r))) /
+                     max(float(np.linalg.norm(r)), floor * tot, 1e-300) for a, r in zip(arrs, ref)])
+
+
+def trajectory_fixtures(cn, out_dir, seeds=2):
     """Trajectory fixtures (``traj_<case>.npz``): the reference's IVPSolver (fused F,
     complexify=True, start-up ``lower_order``) run over the configuration's whole length from the
     benchmark's initial state (``conatus_gb300.workloads``, mapped into the reference's layout), the
     state recorded at a few steps as the coefficient arrays of every variable (the layout-free form
     ``oracle.ivp.OracleProblem.to_arrays`` gives), so that a GPU run of the same length compares
-    field by field with no teacher forcing."""
+    field by field with no teacher forcing. ``spread_s<step>``: per variable, the largest
+    difference (``field_spread``) of the reference's own runs from the initial state perturbed by
+    about one ulp (``seeds`` seeds): how far two correct FP64 runs drift apart by rounding alone."""
     import time
     sys.path.insert(0, ROOT)
     from conatus_gb300 import workloads as W
     from conatus_gb300.reference_adapter import gather_state, reference_maps, scatter_state
     from oracle.ivp import OracleProblem
+    rng = np.random.default_rng(13)
     for name, (fn, kw, params, tname, tparams, sizes, wl, rec) in TRAJECTORY_CASES.items():
         t0 = time.time()
         sim = globals()[fn](cn, **params).simulate(complexify=True, f_backend="fused", **kw)
@@ -307,22 +322,35 @@ def trajectory_fixtures(cn, out_dir):
             if m["cols"].shape[-2:] != (P.nsys[bi], b.n) or not np.array_equal(m["modes"], P.modes[bi]):
                 raise RuntimeError(f"{name}: bucket {bi} of the template does not match the reference build")
         C0 = W.initial_state(wl, P, seed=0)
-        s.X = scatter_state(C0, maps, s.system.n).astype(s.system.dtype)
-        s.t, s.iteration = 0.0, 0
-        s._reset_history()
+        X0 = scatter_state(C0, maps, s.system.n).astype(s.system.dtype)
         op = OracleProblem(P)
+
+        def run(x0):
+            s.X = x0.copy()
+            s.t, s.iteration = 0.0, 0
+            s._reset_history()
+            out, done = {}, 0
+            for r in rec:
+                s.run(r - done)
+                done = r
+                out[r] = op.to_arrays([gather_state(np.asarray(s.X), m) for m in maps])
+            return out
+
+        main = run(X0)
+        spread = {r: np.zeros(len(P.tpl.variables)) for r in rec}
+        for _ in range(seeds):
+            pert = run(X0 * (1 + 2.0 ** -52 * rng.standard_normal(X0.shape)))
+            for r in rec:
+                spread[r] = np.maximum(spread[r], field_spread(pert[r], main[r]))
         arrays = dict(steps=np.array(rec, np.int64), dt=kw["dt"], scheme=kw["scheme"],
                       variables=np.array([v["name"] for v in P.tpl.variables]))
-        done = 0
         for r in rec:
-            s.run(r - done)
-            done = r
-            C = [gather_state(np.asarray(s.X), m) for m in maps]
-            for v, a in enumerate(op.to_arrays(C)):
+            for v, a in enumerate(main[r]):
                 arrays[f"s{r}_v{v}"] = a
-        arrays["finite"] = np.array(bool(np.all(np.isfinite(np.asarray(s.X)))))
+            arrays[f"spread_s{r}"] = spread[r]
         np.savez_compressed(os.path.join(out_dir, f"traj_{name}.npz"), **arrays)
-        print(name, "steps", rec, "N_u", s.system.n, f"{time.time() - t0:.1f} s")
+        print(name, "steps", rec, "N_u", s.system.n, "spread", {r: np.round(np.log10(spread[r] + 1e-300), 1)
+                                                               for r in rec}, f"{time.time() - t0:.1f} s")
 
 
 def main():

@@ -11,14 +11,15 @@ from _step_cases import template
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("tname,sizes", [("rb_nz16", [32]), ("channel_ny17", [8, 8])])
+@pytest.mark.parametrize("tname,sizes,share", [("rb_nz16", [32], True), ("channel_ny17", [8, 8], True),
+                                               ("channel_ny17", [8, 8], False)])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
+def test_every_schedule_solves_alike(tname, sizes, share, precision, rng, cuda_lib):
     import torch
     from conatus_gb300 import autotune
     from conatus_gb300.ivp import DeviceProblem
     P = template(tname).instantiate(sizes)
-    dev = DeviceProblem(P, precision)
+    dev = DeviceProblem(P, precision, share=share)
     dev.autotune = False
     a, b = 1.5e3, 1.0
     fs = dev.factor(a, b)
@@ -37,9 +38,16 @@ def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
     tol = 1e-10 if precision == "fp64" else 1e-5
     r = dev.zeros()
     split = autotune.split_schedules()
+    refused = set()
     for sched in autotune.schedules():
         out = dev.zeros()
         autotune.apply(fs, sched)
+        if dev.shared and (sched < 0 or sched in split):
+            # a shared pair needs a compact two-system schedule: refused, never run otherwise
+            with pytest.raises(ValueError):
+                dev.solve(a, b, rhs, out)
+            refused.add(sched)
+            continue
         dev.solve(a, b, rhs, out)
         dev.residual(a, b, out, rhs, r)
         torch.cuda.synchronize()
@@ -49,6 +57,7 @@ def test_every_schedule_solves_alike(tname, sizes, precision, rng, cuda_lib):
         assert res < (1e-10 if precision == "fp64" else 1e-5), (sched, res)
         if sched >= 0 and sched not in split:            # same arithmetic as schedule 0
             assert np.array_equal(out.cpu().numpy(), ref_h), sched
+    assert bool(dev.shared) == (share and tname.startswith("channel"))
     times = autotune.tune_solve(dev, (a, b), fs, reps=2)
-    assert set(times) == set(autotune.schedules())
+    assert set(times) == set(autotune.schedules()) - refused
     assert autotune.cache()[autotune._signature(dev, fs)][0] == min(times, key=times.get)

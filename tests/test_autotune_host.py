@@ -128,10 +128,17 @@ def test_refine_groups_balance_the_work():
     groups of about equal work (systems x length); every bucket in exactly one group."""
     from conatus_gb300.ivp import DeviceProblem
     B = types.SimpleNamespace
-    stub = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None)
+    stub = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None,
+             shared={})
     g = DeviceProblem._refine_groups(stub)
     assert sorted(sum(g, [])) == [0, 1, 2, 3, 4]
     w = [sum(stub.nsys[b] * stub.tpl.buckets[b].n for b in grp) for grp in g]
     assert len(g) == 2 and abs(w[0] - w[1]) <= 96 * 522
-    one = B(nsys=[127], tpl=B(buckets=[B(n=262)]), _groups=None)
+    one = B(nsys=[127], tpl=B(buckets=[B(n=262)]), _groups=None, shared={})
     assert DeviceProblem._refine_groups(one) == [[0]]
+    # a shared pair (bucket 4 solved with bucket 3's factors) stays in one group
+    pair = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None,
+             shared={4: 3})
+    g = DeviceProblem._refine_groups(pair)
+    assert sorted(sum(g, [])) == [0, 1, 2, 3, 4]
+    assert any(3 in grp and 4 in grp for grp in g)

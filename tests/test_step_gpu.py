@@ -125,10 +125,11 @@ def test_gpu_MX_matches_reference(fixture, cuda_lib):
 
 
 @pytest.mark.parametrize("config", ["rayleigh_benard", "burgers"])
-def test_gpu_config_steps_match_oracle(config, cuda_lib):
-    """The configuration at its own size (RB 256 x 64, Burgers 128) from its benchmark state: F and
-    three steps (lower-order start-up included) against the oracle, 1e-12 relative L2 per field
-    (1e-10 for the tau variables)."""
+def test_gpu_config_steps_match_oracle(config, rng, cuda_lib):
+    """The configuration at its own size (RB 256 x 64, Burgers 128) from its benchmark state: F to
+    1e-12 and three steps (lower-order start-up included) against the oracle, 1e-12 relative L2 per
+    field raised to 10x the oracle's own spread from the state perturbed by about one ulp (two
+    seeds); each field's norm taken at least 1e-8 times the state's (the tau variables)."""
     import torch
     from conatus_gb300 import workloads as W
     from conatus_gb300.ivp import IVPSolver
@@ -142,12 +143,20 @@ def test_gpu_config_steps_match_oracle(config, cuda_lib):
     solver.dev.F(solver.dev.to_device(C0), out)
     torch.cuda.synchronize()
     assert _rel(solver.dev.to_host(out), op.F(C0)) < 1e-12
-    st = SBDFStepper(op, int(cfg["scheme"][-1]), cfg["dt"])
-    C = C0
-    for _ in range(3):
-        C = st.step(C)
+
+    def oracle_run(C):
+        st = SBDFStepper(op, int(cfg["scheme"][-1]), cfg["dt"])
+        for _ in range(3):
+            C = st.step(C)
+        return C
+
+    C = oracle_run(C0)
+    tol = {k: 1e-12 for k in (v["name"] for v in P.tpl.variables)}
+    for _ in range(2):
+        Cp = oracle_run([c * (1 + 2.0 ** -52 * rng.standard_normal(c.shape)) for c in C0])
+        for k, e in field_errors(P, Cp, C, floor=1e-8).items():
+            tol[k] = max(tol[k], 10 * e)
     solver.set_state(C0)
     solver.run(3)
-    errs = field_errors(P, solver.state_to_host(), C)
-    for k, e in errs.items():
-        assert e <= (1e-10 if k.startswith("tau") else 1e-12), errs
+    errs = field_errors(P, solver.state_to_host(), C, floor=1e-8)
+    assert all(errs[k] <= tol[k] for k in errs), (errs, tol)

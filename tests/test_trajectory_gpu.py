@@ -8,15 +8,19 @@ two FP64 implementations drift apart by their rounding differences, amplified by
 tolerances below are the bound each case must keep (step-wise parity, teacher-forced to 1e-12, is
 tests/test_step_gpu.py).
 
+Tolerance per field: 1e-11 relative L2, raised to 10 times the reference's own spread (the
+difference of its runs from X_0 perturbed by about one ulp, recorded in the fixture); each field's
+norm is taken at least 1e-8 times the state's (the tau variables, zero up to rounding, are judged
+against the state).
+
 * Burgers N = 128, SBDF2, dt = 1e-4, 5000 steps, u0 = -sin(pi x) (field by field with the
-  reference's NumPy path): 1e-11.
+  reference's NumPy path).
 * Rayleigh-Benard 256 x 64, SBDF2, dt = 1e-4: at Ra = 1e6 (the configuration) the reference itself
   blows up between steps 150 and 200 (convection sets in with velocities of order sqrt(Ra), far
   beyond the advective limit of dt = 1e-4): compared at steps 50, 100 and 150, and the GPU run's
   finite-state check stops at step 200 exactly as the reference's does; the configured 2000 steps
-  at Ra = 1e4, stable: 1e-10.
-* Channel 16 x 17 x 16 (the configuration at a reduced resolution), SBDF3, dt = 5e-3, 500 steps:
-  1e-10.
+  at Ra = 1e4, stable.
+* Channel 16 x 17 x 16 (the configuration at a reduced resolution), SBDF3, dt = 5e-3, 500 steps.
 
 The measured deviations are printed (``pytest -s``)."""
 from __future__ import annotations
@@ -29,21 +33,22 @@ from conftest import golden
 pytestmark = pytest.mark.gpu
 
 CASES = {
-    # fixture -> (template, template parameters, Fourier sizes, workload, tolerance, tau tolerance)
-    "traj_burgers128.npz": ("burgers_n128", None, None, "burgers", 1e-11, 1e-8),
-    "traj_rb256x64_ra1e6.npz": ("rb_nz64", None, [256], "rayleigh_benard", 1e-10, 1e-8),
-    "traj_rb256x64_ra1e4.npz": ("rb_nz64_ra", {"Ra": 1e4}, [256], "rayleigh_benard", 1e-10, 1e-8),
-    "traj_channel16x17x16.npz": ("channel_ny17", None, [16, 16], "channel", 1e-10, 1e-8),
+    # fixture -> (template, template parameters, Fourier sizes, workload)
+    "traj_burgers128.npz": ("burgers_n128", None, None, "burgers"),
+    "traj_rb256x64_ra1e6.npz": ("rb_nz64", None, [256], "rayleigh_benard"),
+    "traj_rb256x64_ra1e4.npz": ("rb_nz64_ra", {"Ra": 1e4}, [256], "rayleigh_benard"),
+    "traj_channel16x17x16.npz": ("channel_ny17", None, [16, 16], "channel"),
 }
+BASE = 1e-11          # relative L2 per field
+FACTOR = 10.0         # times the reference's own spread from a one-ulp perturbation of X_0
+FLOOR = 1e-8          # a field's norm counts as at least this fraction of the state's norm
 
 
-def _field_errors(arrs, g, step, names):
-    out = {}
-    for v, name in enumerate(names):
-        ref = g[f"s{step}_v{v}"]
-        den = float(np.linalg.norm(ref))
-        out[name] = float(np.linalg.norm(arrs[v] - ref)) / den if den > 0 else float(np.linalg.norm(arrs[v]))
-    return out
+def _field_errors(arrs, g, step, floor=FLOOR):
+    ref = [g[f"s{step}_v{v}"] for v in range(len(arrs))]
+    tot = sum(float(np.sum(r ** 2)) for r in ref) ** 0.5
+    return np.array([float(np.linalg.norm(a - r)) / max(float(np.linalg.norm(r)), floor * tot, 1e-300)
+                     for a, r in zip(arrs, ref)])
 
 
 @pytest.mark.parametrize("fixture", list(CASES))
@@ -52,7 +57,7 @@ def test_trajectory_matches_reference(fixture, cuda_lib):
     from conatus_gb300 import workloads as W
     from conatus_gb300.ivp import IVPSolver
     from oracle.ivp import OracleProblem
-    tname, tparams, sizes, wl, tol, tol_tau = CASES[fixture]
+    tname, tparams, sizes, wl = CASES[fixture]
     g = golden(fixture)
     P = W.load_template(tname).instantiate(sizes, params=tparams)
     names = [str(x) for x in g["variables"]]
@@ -66,11 +71,11 @@ def test_trajectory_matches_reference(fixture, cuda_lib):
         solver.run_graph(step - done)
         done = step
         torch.cuda.synchronize()
-        errs = _field_errors(op.to_arrays(solver.state_to_host()), g, step, names)
-        report[step] = errs
-        for name, e in errs.items():
-            assert e <= (tol_tau if name.startswith("tau") else tol), (fixture, step, errs)
-    print(fixture, {k: {n: f"{e:.2e}" for n, e in v.items()} for k, v in report.items()})
+        errs = _field_errors(op.to_arrays(solver.state_to_host()), g, step)
+        tols = np.maximum(BASE, FACTOR * g[f"spread_s{step}"])
+        report[step] = {n: (f"{e:.2e}", f"{t:.1e}") for n, e, t in zip(names, errs, tols)}
+        assert np.all(errs <= tols), (fixture, step, report[step])
+    print(fixture, "error (tolerance) per field:", report)
 
 
 def test_blow_up_stops_like_the_reference(cuda_lib):
