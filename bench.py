@@ -429,31 +429,43 @@ def _schedule_summary(dev):
     return None
 
 
-def mixed_error(P, C0, cfg, steps):
+def mixed_error(P, C0, cfg, steps, marks=5):
     """Relative L2 error per field of the mixed form against the plain FP64 form (which matches the
-    reference's FP64 CPU path step by step) after ``steps`` steps from the same state."""
+    reference's FP64 CPU path step by step) after ``steps`` steps from the same state, and its
+    history at ``marks`` evenly spaced steps (the error at the end of the run is ``max``)."""
     import torch
     from conatus_gb300.ivp import IVPSolver
+    at = sorted({max(1, round(steps * (k + 1) / marks)) for k in range(marks)})
     res = {}
     for prec in ("fp64", "fp32"):
         s = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=prec)
         s.set_state(C0)
-        s.run_graph(steps)
-        torch.cuda.synchronize()
-        res[prec] = s.dev.to_host(s.X)
+        res[prec], done = {}, 0
+        for m in at:
+            s.run_graph(m - done)
+            done = m
+            torch.cuda.synchronize()
+            res[prec][m] = s.dev.to_host(s.X)
         del s
         torch.cuda.empty_cache()
-    errs = {}
-    for v, var in enumerate(P.tpl.variables):
-        if var["name"].startswith("tau"):
-            continue
-        num = den = 0.0
-        for bi, b in enumerate(P.tpl.buckets):
-            sel = b.col[:, 0] == v
-            num += float(np.sum(np.abs(res["fp32"][bi][:, sel] - res["fp64"][bi][:, sel]) ** 2))
-            den += float(np.sum(np.abs(res["fp64"][bi][:, sel]) ** 2))
-        errs[var["name"]] = (num / den) ** 0.5 if den else 0.0
-    return {"steps": steps, "relative_l2": errs, "max": max(errs.values()) if errs else 0.0}
+
+    def errs(a, b):
+        out = {}
+        for v, var in enumerate(P.tpl.variables):
+            if var["name"].startswith("tau"):
+                continue
+            num = den = 0.0
+            for bi, bk in enumerate(P.tpl.buckets):
+                sel = bk.col[:, 0] == v
+                num += float(np.sum(np.abs(a[bi][:, sel] - b[bi][:, sel]) ** 2))
+                den += float(np.sum(np.abs(b[bi][:, sel]) ** 2))
+            out[var["name"]] = (num / den) ** 0.5 if den else 0.0
+        return out
+
+    hist = {m: errs(res["fp32"][m], res["fp64"][m]) for m in at}
+    final = hist[at[-1]]
+    return {"steps": steps, "relative_l2": final, "max": max(final.values()) if final else 0.0,
+            "history": {str(m): {k: float(f"{v:.3e}") for k, v in e.items()} for m, e in hist.items()}}
 
 
 def _host_cores():

@@ -66,8 +66,10 @@ _SIGS = {
     "cng_lincomb": [ctypes.c_int64, P, c_int, P, P, P, P, P],
     "cng_check_finite": [P, ctypes.c_int64, ctypes.c_int64, P, P],
     "cng_split_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P, P, P],
+    "cng_split_residual_range": [c_int, c_int, c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P,
+                                 P, P, P],
     "cng_banded_solve_batch_xt": [c_int, P, P, P, P, c_int, P],
-    "cng_banded_solve_batch2": [c_int, P, P, P, P, P, P, P, c_int, c_int, P],
+    "cng_banded_solve_batch2": [c_int, P, P, P, P, P, P, P, P, c_int, c_int, P],
     "cng_banded_share": [P, P, P, P],
     "cng_graph_begin": [P],
     "cng_graph_end": [P, P],

@@ -1476,6 +1476,7 @@ struct CompactIdx {
     int n, r, kl, kv, nL, nU, nV, wgroups, batch;
     int gs;                             // systems per warp group in the streams: kGroup, or 1 for a
                                         // shared pair (both halves of the warp read one system's factors)
+    int wg0;                            // first warp group solved (wgroups: one past the last)
     int maxLc, maxUc;                   // largest chunk of the L / U streams (entries)
     const int* offL;                    // n + 1
     const unsigned char* Lrow;          // nL: t (row kv + 1 + t of the column)
@@ -1529,7 +1530,7 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int g = lane / kLanesPer, lg = lane % kLanesPer;
-    const int wg = block * nw + wib;
+    const int wg = ix.wg0 + block * nw + wib;
     const int gs = ix.gs;
     const bool pair = gs == 1;
     const bool partner = pair && g == 1;
@@ -1827,10 +1828,11 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
     extern __shared__ __align__(16) unsigned char sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int sys = block * nw + wib;
+    // systems ix.wg0 .. ix.wgroups - 1 (one per warp; launch_split_t sets the range in systems)
+    const int sys = ix.wg0 + block * nw + wib;
     const int gs = sys & 1, wgs = sys >> 1;
     const int es = lane >> 1, c = lane & 1;           // entry slot, component
-    const bool live = sys < ix.batch;
+    const bool live = sys < ix.wgroups;
     const int n = ix.n, r = ix.r;
     int* s_offL = reinterpret_cast<int*>(sm);
     int* s_offU = s_offL + (n + 1);
@@ -2086,7 +2088,7 @@ static void demote_compact(Banded& h, cudaStream_t st) {
 static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     CompactIdx ix;
     ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
-    ix.wgroups = h.cWg; ix.batch = h.batch; ix.gs = h.cG;
+    ix.wgroups = h.cWg; ix.batch = h.batch; ix.gs = h.cG; ix.wg0 = 0;
     ix.maxLc = h.cMaxLk[chunk_index(chunk)];
     ix.maxUc = h.cMaxUk[chunk_index(chunk)];
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
@@ -2236,10 +2238,17 @@ static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io
 
 namespace cng {
 
+// warp groups [first, end) of handle h that solve systems [s0, s1) (s1 < 0: all)
+static void group_range(const Banded& h, int s0, int s1, int& first, int& end) {
+    if (s1 < 0) { first = 0; end = h.cWg; return; }
+    first = s0 / h.cG;
+    end = std::min(h.cWg, (s1 + h.cG - 1) / h.cG);
+}
+
 template <class TF, class TD, int IO, int CH, int ST>
 static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2, int sched,
-                           cudaStream_t st) {
+                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2,
+                           const std::vector<int>& rng, int sched, cudaStream_t st) {
     static std::once_flag once;
     std::call_once(once, [] {
         cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2254,8 +2263,12 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         for (const Banded* h : hs) m = std::max(m, compact_smem<TF>(*h, w, sched));
         return m;
     };
+    std::vector<int> first(hs.size()), end(hs.size());
     int total = 0;
-    for (const Banded* h : hs) total += h->cWg;
+    for (size_t i = 0; i < hs.size(); ++i) {
+        group_range(*hs[i], rng[2 * i], rng[2 * i + 1], first[i], end[i]);
+        total += end[i] - first[i];
+    }
     int nw = 1, resident = 0;
     for (int w = 1; w <= 8; ++w) {
         const size_t m = smem_of(w);
@@ -2275,16 +2288,18 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
     // largest buckets first: their long tails start earliest
     std::vector<int> order(hs.size());
     for (size_t i = 0; i < hs.size(); ++i) order[i] = (int)i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->cWg > hs[b]->cWg; });
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return end[a] - first[a] > end[b] - first[b]; });
     int blocks = 0;
     for (int k = 0; k < ms.nb; ++k) {
         const int i = order[k];
         ms.block_start[k] = blocks;
         ms.ix[k] = compact_idx(*hs[i], CH);
+        ms.ix[k].wg0 = first[i];
+        ms.ix[k].wgroups = end[i];
         ms.cd[k] = cds[i];
         ms.io[k] = ios[i];
         ms.io2[k] = ios2[i];
-        blocks += ceil_div(hs[i]->cWg, nw);
+        blocks += ceil_div(end[i] - first[i], nw);
     }
     ms.block_start[ms.nb] = blocks;
     k_solve_compact_multi<TF, TD, IO, CH, ST><<<blocks, 32 * nw, smem, st>>>(ms);
@@ -2304,8 +2319,8 @@ static size_t split_smem(const Banded& h, int nwarps, int sched) {
 
 template <class TF, class TD, int IO, int CH, int ST>
 static void launch_split_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>&, int sched,
-                           cudaStream_t st) {
+                           const std::vector<SolveIo>& ios, const std::vector<SolveIo>&,
+                           const std::vector<int>& rng, int sched, cudaStream_t st) {
     for (const Banded* h : hs)
         if (h->cG != kGroup)
             throw InvalidArgument("the split-lane schedules do not solve shared pairs: a compact two-system schedule");
@@ -2321,8 +2336,13 @@ static void launch_split_t(const std::vector<const Banded*>& hs, const std::vect
         for (const Banded* h : hs) m = std::max(m, split_smem<TF>(*h, w, sched));
         return m;
     };
+    std::vector<int> first(hs.size()), end(hs.size());
     int total = 0;
-    for (const Banded* h : hs) total += h->batch;
+    for (size_t i = 0; i < hs.size(); ++i) {
+        first[i] = rng[2 * i + 1] < 0 ? 0 : rng[2 * i];
+        end[i] = rng[2 * i + 1] < 0 ? hs[i]->batch : rng[2 * i + 1];
+        total += end[i] - first[i];
+    }
     int nw = 1, resident = 0;
     for (int w = 1; w <= 8; ++w) {
         const size_t m = smem_of(w);
@@ -2340,15 +2360,17 @@ static void launch_split_t(const std::vector<const Banded*>& hs, const std::vect
     ms.nb = (int)hs.size();
     std::vector<int> order(hs.size());
     for (size_t i = 0; i < hs.size(); ++i) order[i] = (int)i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->batch > hs[b]->batch; });
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return end[a] - first[a] > end[b] - first[b]; });
     int blocks = 0;
     for (int k = 0; k < ms.nb; ++k) {
         const int i = order[k];
         ms.block_start[k] = blocks;
         ms.ix[k] = compact_idx(*hs[i], CH);
+        ms.ix[k].wg0 = first[i];              // in systems: one system per warp
+        ms.ix[k].wgroups = end[i];
         ms.cd[k] = cds[i];
         ms.io[k] = ios[i];
-        blocks += ceil_div(hs[i]->batch, nw);
+        blocks += ceil_div(end[i] - first[i], nw);
     }
     ms.block_start[ms.nb] = blocks;
     k_solve_split_multi<TF, TD, IO, CH, ST><<<blocks, 32 * nw, smem, st>>>(ms);
@@ -2359,23 +2381,24 @@ static void launch_split_t(const std::vector<const Banded*>& hs, const std::vect
 // when they differ)
 template <class TF, class TD, int IO>
 static void launch_multi(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                         const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2, cudaStream_t st) {
+                         const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2, const std::vector<int>& rng,
+                         cudaStream_t st) {
     int sched = hs[0]->sched;
     for (const Banded* h : hs)
         if (h->sched != sched) sched = 0;
     if (sched < 0 || sched >= kNumSchedules) sched = 0;
     switch (sched) {
-        case 1: launch_multi_t<TF, TD, IO, 8, 3>(hs, cds, ios, ios2, sched, st); break;
-        case 2: launch_multi_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, sched, st); break;
-        case 3: launch_multi_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, sched, st); break;
-        case 4: launch_multi_t<TF, TD, IO, 16, 3>(hs, cds, ios, ios2, sched, st); break;
-        case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, ios2, sched, st); break;
-        case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, ios2, sched, st); break;
-        case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, ios2, sched, st); break;
-        case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, sched, st); break;
-        case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, sched, st); break;
-        case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, sched, st); break;
-        default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, sched, st); break;
+        case 1: launch_multi_t<TF, TD, IO, 8, 3>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 2: launch_multi_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 3: launch_multi_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 4: launch_multi_t<TF, TD, IO, 16, 3>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 5: launch_multi_t<TF, TD, IO, 4, 4>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 6: launch_multi_t<TF, TD, IO, 2, 4>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 7: launch_multi_t<TF, TD, IO, 16, 4>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, rng, sched, st); break;
+        default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }
 
@@ -2384,19 +2407,28 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
 extern "C" {
 
 int cng_banded_solve_batch2(int nh, cng_banded* const* hh, const void* const* b, void* const* x,
-                            const void* const* b2, void* const* x2, void* const* xt, void* const* xt2, int fp32,
-                            int accumulate, void* stream) {
+                            const void* const* b2, void* const* x2, void* const* xt, void* const* xt2,
+                            const int32_t* range, int fp32, int accumulate, void* stream) {
     CNG_TRY({
         if (nh < 1 || nh > kMaxMulti) throw InvalidArgument("1 to 8 handles per batched solve");
         if (!hh || !b || !x) throw InvalidArgument("null argument");
         if ((xt || xt2) && !fp32) throw InvalidArgument("the row-major copy of x is written by the FP32 solve only");
         std::vector<const Banded*> hs;
         std::vector<SolveIo> ios, ios2;
-        bool any_pair = false;
+        std::vector<int> rng(2 * nh, -1);
+        bool any_pair = false, any_range = false;
         for (int k = 0; k < nh; ++k) {
             const Banded* h = reinterpret_cast<const Banded*>(hh[k]);
             if (!h || !h->compact_ready || h->dtype != 1)
                 throw InvalidArgument("batched solve needs complex128 handles in compact form");
+            if (range && !(range[2 * k] == 0 && range[2 * k + 1] == h->batch)) {
+                const int s0 = range[2 * k], s1 = range[2 * k + 1];
+                if (s0 < 0 || s1 <= s0 || s1 > h->batch || s0 % h->cG || (s1 % h->cG && s1 != h->batch))
+                    throw InvalidArgument("system range: 0 <= s0 < s1 <= batch, on warp-group boundaries");
+                rng[2 * k] = s0;
+                rng[2 * k + 1] = s1;
+                any_range = true;
+            }
             if (fp32 && !h->fp32_ready) throw InvalidArgument("call cng_banded_make_fp32 first");
             if (!b[k] || !x[k] || b[k] == x[k]) throw InvalidArgument("b and x: device pointers, not aliased");
             const void* pb = b2 ? b2[k] : nullptr;
@@ -2423,6 +2455,7 @@ int cng_banded_solve_batch2(int nh, cng_banded* const* hh, const void* const* b,
         for (const Banded* h : hs) dense = dense && h->sched < 0;
         if (dense) {              // the band kernel, one launch per bucket
             if (any_pair) throw InvalidArgument("the band kernel does not solve shared pairs: a compact schedule");
+            if (any_range) throw InvalidArgument("the band kernel solves whole batches (no system range)");
             if (xt) throw InvalidArgument("the transposed copy of x: compact schedules only");
             for (size_t k = 0; k < hs.size(); ++k) {
                 if (fp32) launch_mixed_dense(*hs[k], b[k], x[k], accumulate, st);
@@ -2435,21 +2468,21 @@ int cng_banded_solve_batch2(int nh, cng_banded* const* hh, const void* const* b,
             for (const Banded* h : hs)
                 cds.push_back(CompactData<zf>{h->c_L32, h->c_U32, h->c_piv, h->c_V32, h->w32, h->slu32, h->spiv, h->perm,
                                               h->flip_r, h->flip_c});
-            launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, ios2, st);
+            launch_multi<zf, zd, IO_MIXED>(hs, cds, ios, ios2, rng, st);
         } else {
             std::vector<CompactData<zd>> cds;
             for (const Banded* h : hs)
                 cds.push_back(CompactData<zd>{static_cast<const zd*>(h->c_L), static_cast<const zd*>(h->c_U), h->c_piv,
                                               static_cast<const zd*>(h->c_V), static_cast<const zd*>(h->w),
                                               static_cast<const zd*>(h->slu), h->spiv, h->perm, h->flip_r, h->flip_c});
-            launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, ios2, st);
+            launch_multi<zd, zd, IO_MAPPED>(hs, cds, ios, ios2, rng, st);
         }
     })
 }
 
 int cng_banded_solve_batch(int nh, cng_banded* const* hh, const void* const* b, void* const* x, int fp32,
                            int accumulate, void* stream) {
-    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, nullptr, nullptr, fp32, accumulate, stream);
+    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, nullptr, nullptr, nullptr, fp32, accumulate, stream);
 }
 
 int cng_banded_solve_batch_xt(int nh, cng_banded* const* hh, const void* const* b, void* const* x,
@@ -2458,7 +2491,7 @@ int cng_banded_solve_batch_xt(int nh, cng_banded* const* hh, const void* const* 
         cng::set_error("null argument");
         return cng::CNG_EINVAL;
     }
-    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, xt, nullptr, 1, accumulate, stream);
+    return cng_banded_solve_batch2(nh, hh, b, x, nullptr, nullptr, xt, nullptr, nullptr, 1, accumulate, stream);
 }
 
 int cng_banded_share(cng_banded* hh, const int8_t* dr, const int8_t* dc, void* stream) {

@@ -171,20 +171,24 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
 constexpr int kMergedTerm = 63;          // an entry list shared by several terms: scale per (row, system)
 
 template <bool CONE>
-__global__ void k_split_residual(int nsys, int n, const int* __restrict__ ptr, const int* __restrict__ col,
+// Systems s0 .. s0 + cnt - 1 of a bucket of ld systems (rowscale and xT are [n][ld]).
+__global__ void k_split_residual(int cnt, int s0, int ld, int n, const int* __restrict__ ptr,
+                                 const int* __restrict__ col,
                                  const double* __restrict__ val, const signed char* __restrict__ code,
                                  const double* __restrict__ mono, int nmono, double a, double c,
                                  const double* __restrict__ rowscale, const double2* __restrict__ x,
                                  const double2* __restrict__ xT, const double2* __restrict__ b,
                                  double2* __restrict__ r) {
-    const unsigned sysw = ((unsigned)nsys + 31u) >> 5;             // warps of 32 systems per row
+    const int nsys = ld;
+    const unsigned sysw = ((unsigned)cnt + 31u) >> 5;              // warps of 32 systems per row
     const unsigned nwarps = sysw * (unsigned)n;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned wstride = (gridDim.x * blockDim.x) >> 5;
     for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
         const int i = (int)(w / sysw);
-        const unsigned m = (w - (unsigned)i * sysw) * 32u + lane;
-        if (m >= (unsigned)nsys) continue;
+        const unsigned ml = (w - (unsigned)i * sysw) * 32u + lane;
+        if (ml >= (unsigned)cnt) continue;
+        const unsigned m = ml + (unsigned)s0;
         const long long t = (long long)m * n + i;
         const double2* xm = x + (long long)m * n;
         const double* mv = mono + (long long)m * nmono;
@@ -281,29 +285,39 @@ int cng_poly_residual(int nsys, int n, const int32_t* indptr, const int32_t* ind
     })
 }
 
-int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
-                       const int8_t* code, const double* mono, int nmono, double a, double c,
-                       const double* rowscale, const void* x, const void* xT, const void* b, void* r,
-                       void* stream) {
+int cng_split_residual_range(int nsys, int s0, int s1, int n, const int32_t* ptr, const int32_t* col,
+                             const double* val, const int8_t* code, const double* mono, int nmono, double a,
+                             double c, const double* rowscale, const void* x, const void* xT, const void* b,
+                             void* r, void* stream) {
     CNG_TRY({
         if (!ptr || !col || !val || !code || (nmono > 0 && !mono) || !x || !b || !r)
             throw InvalidArgument("null device pointer");
         if (r == x || r == b) throw InvalidArgument("r must not alias x or b");
-        if (nsys <= 0 || n <= 0) return CNG_OK;
+        if (s0 < 0 || s1 > nsys || s0 > s1) throw InvalidArgument("split_residual: system range outside the batch");
+        const int cnt = s1 - s0;
+        if (cnt <= 0 || n <= 0) return CNG_OK;
         auto* sc = reinterpret_cast<const signed char*>(code);
-        if ((long long)((nsys + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("split_residual: batch too large");
-        const long long threads = (long long)((nsys + 31) / 32) * n * 32;
+        if ((long long)((cnt + 31) / 32) * n >= (1LL << 31)) throw InvalidArgument("split_residual: batch too large");
+        const long long threads = (long long)((cnt + 31) / 32) * n * 32;
         const int blk = (int)std::min<long long>((threads + 255) / 256, 152LL * 64);
         if (c == 1.0)
             k_split_residual<true><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-                nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
+                cnt, s0, nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
                 static_cast<const double2*>(xT), static_cast<const double2*>(b), static_cast<double2*>(r));
         else
             k_split_residual<false><<<blk, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-                nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
+                cnt, s0, nsys, n, ptr, col, val, sc, mono, nmono, a, c, rowscale, static_cast<const double2*>(x),
                 static_cast<const double2*>(xT), static_cast<const double2*>(b), static_cast<double2*>(r));
         CNG_LAUNCH("k_split_residual");
     })
+}
+
+int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, const double* val,
+                       const int8_t* code, const double* mono, int nmono, double a, double c,
+                       const double* rowscale, const void* x, const void* xT, const void* b, void* r,
+                       void* stream) {
+    return cng_split_residual_range(nsys, 0, nsys, n, ptr, col, val, code, mono, nmono, a, c, rowscale, x, xT, b,
+                                    r, stream);
 }
 
 int cng_lincomb(int64_t count, const void* base, int nterms, const double* coef, const int32_t* negate,

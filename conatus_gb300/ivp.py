@@ -516,19 +516,23 @@ class DeviceProblem:
             self._R2 = self.zeros()
 
     def residual(self, a, b_, x, rhs, out, stream=None, buckets=None, xT=None) -> None:
-        """out = rhs - (a M + b L) x per bucket (all, or the indices in ``buckets``), FP64; ``xT``:
-        x also row-major over the systems of each bucket (read by the split kernel instead)."""
+        """out = rhs - (a M + b L) x per bucket (all, or ``buckets``: bucket indices or (bucket,
+        first system, end system) parts), FP64; ``xT``: x also row-major over the systems of each
+        bucket (read by the split kernel instead)."""
         s = _stream_handle(stream)
-        for bi, b in enumerate(self.tpl.buckets):
-            if buckets is not None and bi not in buckets:
-                continue
+        if buckets is None:
+            parts = [(bi, 0, ns) for bi, ns in enumerate(self.nsys)]
+        else:
+            parts = [(g, 0, self.nsys[g]) if isinstance(g, (int, np.integer)) else tuple(g) for g in buckets]
+        for bi, s0, s1 in parts:
+            b = self.tpl.buckets[bi]
             kind, data = self._residual_data(bi)
             xb, rb, ob = self.bucket(x, bi), self.bucket(rhs, bi), self.bucket(out, bi)
             if kind == "split":
                 ptr, col, val, code, mv, nm = data[:6]
                 rs = self._rowscale(bi, a, b_)
-                call("cng_split_residual", self.nsys[bi], b.n, ptr.data_ptr(), col.data_ptr(), val.data_ptr(),
-                     code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_),
+                call("cng_split_residual_range", self.nsys[bi], int(s0), int(s1), b.n, ptr.data_ptr(), col.data_ptr(),
+                     val.data_ptr(), code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_),
                      rs.data_ptr() if rs is not None else None, xb.data_ptr(),
                      self.bucket(xT, bi).data_ptr() if xT is not None else None, rb.data_ptr(), ob.data_ptr(), s)
                 continue
@@ -541,7 +545,7 @@ class DeviceProblem:
                 _torch().cuda.current_stream(self.device).synchronize()   # made on torch's stream
             ip, ix = self._pat[bi]
             A = data[key]
-            for m in range(self.nsys[bi]):
+            for m in range(s0, s1):
                 sl = slice(m * b.n, (m + 1) * b.n)
                 call("cng_poly_residual", 1, b.n, ip.data_ptr(), ix.data_ptr(), A[m].data_ptr(), None, None, 0,
                      1.0, 0.0, xb[sl].data_ptr(), rb[sl].data_ptr(), ob[sl].data_ptr(), s)
@@ -569,7 +573,8 @@ class DeviceProblem:
             return
         if self._R2 is None:
             self._R2 = self.zeros()
-        groups = self._refine_groups() if self.overlap_refine else [list(range(nb))]
+        dense = all(getattr(h, "schedule", 0) < 0 for h in fs)
+        groups = self._refine_groups() if (self.overlap_refine and not dense) else [list(range(nb))]
         if len(groups) == 1:
             self._refine_chain(fs, groups[0], a, b_, rhs, out, s)
             return
@@ -591,43 +596,70 @@ class DeviceProblem:
         main.wait_event(join)
 
     def _refine_groups(self):
-        """Buckets split in two groups of about equal work (systems x length), largest first; a
-        shared pair (one factor set, both solved in one sweep) stays in one group."""
+        """Two groups of about equal work (systems x length) for the FP32 refinement on two streams,
+        as (bucket, first system, end system) parts; a shared pair's partner goes with its primary
+        (one sweep solves both). Whole buckets are placed largest first; when one bucket outweighs
+        all the others, it is split at a system boundary between the two groups."""
         if self._groups is None:
-            units = {}
-            for bi in range(len(self.nsys)):
-                units.setdefault(self.shared.get(bi, bi), []).append(bi)
-            work = lambda u: sum(self.nsys[bi] * self.tpl.buckets[bi].n for bi in units[u])
-            order = sorted(units, key=lambda u: -work(u))
-            g, w = [[], []], [0, 0]
-            for u in order:
-                k = 0 if w[0] <= w[1] else 1
-                g[k].extend(units[u])
-                w[k] += work(u)
-            self._groups = [sorted(x) for x in g if x]
+            partner_of = {i: j for j, i in self.shared.items()}
+            units = [bi for bi in range(len(self.nsys)) if bi not in self.shared]
+            per = {bi: self.tpl.buckets[bi].n * (2 if bi in partner_of else 1) for bi in units}
+            work = {bi: self.nsys[bi] * per[bi] for bi in units}
+            total = sum(work.values())
+            big = max(units, key=lambda bi: work[bi])
+            if len(units) > 0 and work[big] > total / 2 and self.nsys[big] >= 4:
+                align = 1 if big in partner_of else 2          # warp groups of the compact streams
+                rest = total - work[big]
+                h = int(round((work[big] - rest) / (2 * per[big])))
+                h = max(align, min(self.nsys[big] - align, h - h % align))
+                g0 = [(bi, 0, self.nsys[bi]) for bi in sorted(units) if bi != big] + [(big, 0, h)]
+                self._groups = [g0, [(big, h, self.nsys[big])]]
+            else:
+                g, w = [[], []], [0, 0]
+                for bi in sorted(units, key=lambda u: -work[u]):
+                    k = 0 if w[0] <= w[1] else 1
+                    g[k].append((bi, 0, self.nsys[bi]))
+                    w[k] += work[bi]
+                self._groups = [sorted(x) for x in g if x]
         return self._groups
 
+    def _with_partners(self, parts):
+        """Parts plus the same system range of each part's shared partner (the residual's list)."""
+        partner_of = {i: j for j, i in self.shared.items()}
+        out = []
+        for g in parts:
+            bi, s0, s1 = (g, 0, self.nsys[g]) if isinstance(g, (int, np.integer)) else tuple(g)
+            for e in ((bi, s0, s1), (partner_of[bi], s0, s1) if bi in partner_of else None):
+                if e is not None and e not in out:
+                    out.append(e)
+        return out
+
     def _batch_call(self, fs, group, rhs, out, xt, fp32, accumulate, s) -> None:
-        """One batched solve launch over the buckets in ``group``: every handle of the group, a
-        shared pair's partner solved in the same sweep as its primary (cng_banded_solve_batch2)."""
-        prim = [bi for bi in group if not isinstance(fs[bi], _Partner)]
-        part = {fs[bj].primary: bj for bj in group if isinstance(fs[bj], _Partner)}
-        if any(fs[bj].primary not in prim for bj in part.values()):
-            raise ValueError("a shared pair must be solved in one launch")
+        """One batched solve launch over ``group`` (bucket indices, or (bucket, first system, end
+        system) parts): a shared pair's partner is solved in the same sweep as its primary
+        (cng_banded_solve_batch2), over the same systems."""
+        parts = [(g, 0, self.nsys[g]) if isinstance(g, (int, np.integer)) else tuple(g) for g in group]
+        partner_of = {fs[bj].primary: bj for bj in range(len(fs)) if isinstance(fs[bj], _Partner)}
+        prim = [p for p in parts if not isinstance(fs[p[0]], _Partner)]
+        for p in parts:
+            if isinstance(fs[p[0]], _Partner) and not any(q[0] == fs[p[0]].primary for q in prim):
+                raise ValueError("a shared pair's partner is solved with its primary, in one launch")
         nb = len(prim)
         V = ctypes.c_void_p * nb
         ptr = lambda X, bi: self.bucket(X, bi).data_ptr() if bi is not None else None
-        hs = V(*[fs[bi].h.value for bi in prim])
-        bp, xp = V(*[ptr(rhs, bi) for bi in prim]), V(*[ptr(out, bi) for bi in prim])
-        b2 = x2 = xt1 = xt2 = None
-        if part:
-            b2 = V(*[ptr(rhs, part.get(bi)) for bi in prim])
-            x2 = V(*[ptr(out, part.get(bi)) for bi in prim])
+        hs = V(*[fs[bi].h.value for bi, _, _ in prim])
+        bp, xp = V(*[ptr(rhs, bi) for bi, _, _ in prim]), V(*[ptr(out, bi) for bi, _, _ in prim])
+        b2 = x2 = xt1 = xt2 = rng = None
+        if partner_of:
+            b2 = V(*[ptr(rhs, partner_of.get(bi)) for bi, _, _ in prim])
+            x2 = V(*[ptr(out, partner_of.get(bi)) for bi, _, _ in prim])
         if xt is not None:
-            xt1 = V(*[ptr(xt, bi) for bi in prim])
-            if part:
-                xt2 = V(*[ptr(xt, part.get(bi)) for bi in prim])
-        call("cng_banded_solve_batch2", nb, hs, bp, xp, b2, x2, xt1, xt2, fp32, accumulate, s)
+            xt1 = V(*[ptr(xt, bi) for bi, _, _ in prim])
+            if partner_of:
+                xt2 = V(*[ptr(xt, partner_of.get(bi)) for bi, _, _ in prim])
+        if any(s0 != 0 or s1 != self.nsys[bi] for bi, s0, s1 in prim):
+            rng = (ctypes.c_int32 * (2 * nb))(*[int(v) for _, s0, s1 in prim for v in (s0, s1)])
+        call("cng_banded_solve_batch2", nb, hs, bp, xp, b2, x2, xt1, xt2, rng, fp32, accumulate, s)
 
     def _refine_chain(self, fs, group, a, b_, rhs, out, s) -> None:
         """FP32 solve of the buckets in ``group``, then ``refine`` passes of FP64 residual and FP32
@@ -635,13 +667,13 @@ class DeviceProblem:
         # x also row-major over the systems (coalesced reads of the residual kernel), with the
         # compact schedules
         xt = None
-        if all(getattr(fs[bi], "schedule", 0) >= 0 for bi in group):
+        if all(getattr(fs[g if isinstance(g, (int, np.integer)) else g[0]], "schedule", 0) >= 0 for g in group):
             if self._XT is None:
                 self._XT = self.zeros()
             xt = self._XT
         self._batch_call(fs, group, rhs, out, xt, 1, 0, s)
         for p in range(self.refine):
-            self.residual(a, b_, out, rhs, self._R2, s, buckets=group, xT=xt)
+            self.residual(a, b_, out, rhs, self._R2, s, buckets=self._with_partners(group), xT=xt)
             self._batch_call(fs, group, self._R2, out, xt if p + 1 < self.refine else None, 1, 1, s)
 
     def solve_launch(self, fs, rhs, out, stream=None) -> None:
@@ -1234,9 +1266,12 @@ class IVPSolver:
         f = 2 * nb + 2 + 2 + (2 if d >= 2 else 0) + 1 + (1 if dev.has_b0 else 0)
         dense = bool(dev._factors) and all(getattr(h, "schedule", 0) < 0 for fs in dev._factors.values() for h in fs)
         one = (nb if dense else 1) if dev.compact else nb
+        res = nb                                      # residual launches per refinement pass
         if dev.precision == "fp32" and dev.compact and not dense and dev.overlap_refine:
-            one = len(dev._refine_groups())           # one batched launch per bucket group
-        solve = one if dev.precision == "fp64" else one + dev.refine * (one + nb)
+            groups = dev._refine_groups()
+            one = len(groups)                         # one batched launch per group
+            res = sum(len(dev._with_partners(g)) for g in groups)
+        solve = one if dev.precision == "fp64" else one + dev.refine * (one + res)
         if self.family == "sbdf":
             return nb + f + 1 + solve
         if self.family == "cn":

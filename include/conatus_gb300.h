@@ -135,11 +135,14 @@ int cng_banded_share(cng_banded* h, const int8_t* dr, const int8_t* dc, void* st
 /* The general batched solve: cng_banded_solve_batch, plus for a shared handle k (cng_banded_share)
  * the partner's right-hand side b2[k] and solution x2[k] (NULL entries, or NULL arrays: no partner),
  * solved in the same sweep over the factor streams; fp32 = 1 may also write x row-major over the
- * systems into xt[k] and xt2[k] (the refinement residual's coalesced copy; NULL: not written). The
- * band kernel (schedule -1) and the split-lane schedules do not solve partners (status 1). */
+ * systems into xt[k] and xt2[k] (the refinement residual's coalesced copy; NULL: not written).
+ * range (NULL: every system): systems [range[2k], range[2k+1]) of handle k only (pointers still
+ * address the whole batch), on warp-group boundaries (even for unshared handles), so that two
+ * launches on two streams can each take a part of one large bucket. The band kernel (schedule -1)
+ * and the split-lane schedules solve neither partners nor ranges (status 1). */
 int cng_banded_solve_batch2(int nh, cng_banded* const* h, const void* const* b, void* const* x,
                             const void* const* b2, void* const* x2, void* const* xt, void* const* xt2,
-                            int fp32, int accumulate, void* stream);
+                            const int32_t* range, int fp32, int accumulate, void* stream);
 
 /* Schedules of the compact solve (the batched-solve kernel of the step): count, and per schedule
  * the columns per staged chunk of the factor streams, the depth of the staging ring and whether it
@@ -316,6 +319,14 @@ int cng_split_residual(int nsys, int n, const int32_t* ptr, const int32_t* col, 
                        const int8_t* code, const double* mono, int nmono, double a, double c,
                        const double* rowscale, const void* x, const void* xT, const void* b, void* r,
                        void* stream);
+
+/* cng_split_residual over systems [s0, s1) of the bucket's nsys only (every pointer addresses the
+ * whole bucket): the refinement of one part of a bucket while another part is solved on another
+ * stream. No reference counterpart. */
+int cng_split_residual_range(int nsys, int s0, int s1, int n, const int32_t* ptr, const int32_t* col,
+                             const double* val, const int8_t* code, const double* mono, int nmono, double a,
+                             double c, const double* rowscale, const void* x, const void* xT, const void* b,
+                             void* r, void* stream);
 
 /* y = M x with one real value array shared by every system of the bucket (the mass matrices of the
  * tau systems are real). */

@@ -124,21 +124,43 @@ def test_environment_fixes_the_schedule(fake, monkeypatch):
 
 
 def test_refine_groups_balance_the_work():
-    """The FP32 form's two refinement groups (two streams): buckets split largest first into two
-    groups of about equal work (systems x length); every bucket in exactly one group."""
+    """The FP32 form's two refinement groups (two streams): (bucket, first system, end system)
+    parts of about equal work (systems x length), every system in exactly one group; a bucket that
+    outweighs all the others is split at a warp-group boundary, a shared pair's partner follows its
+    primary."""
     from conatus_gb300.ivp import DeviceProblem
     B = types.SimpleNamespace
-    stub = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None,
-             shared={})
-    g = DeviceProblem._refine_groups(stub)
-    assert sorted(sum(g, [])) == [0, 1, 2, 3, 4]
-    w = [sum(stub.nsys[b] * stub.tpl.buckets[b].n for b in grp) for grp in g]
-    assert len(g) == 2 and abs(w[0] - w[1]) <= 96 * 522
-    one = B(nsys=[127], tpl=B(buckets=[B(n=262)]), _groups=None, shared={})
-    assert DeviceProblem._refine_groups(one) == [[0]]
-    # a shared pair (bucket 4 solved with bucket 3's factors) stays in one group
-    pair = B(nsys=[1, 95, 95, 9025, 9025], tpl=B(buckets=[B(n=523)] + [B(n=522)] * 4), _groups=None,
-             shared={4: 3})
+
+    def stub(nsys, ns, shared):
+        st = B(nsys=nsys, tpl=B(buckets=[B(n=n) for n in ns]), _groups=None, shared=shared)
+        st._with_partners = lambda parts: DeviceProblem._with_partners(st, parts)
+        return st
+
+    def covered(st, g):
+        seen = {}
+        for part in sum((st._with_partners(grp) for grp in g), []):
+            bi, s0, s1 = part
+            seen.setdefault(bi, []).append((s0, s1))
+        for bi, ns in enumerate(st.nsys):
+            r = sorted(seen[bi])
+            assert r[0][0] == 0 and r[-1][1] == ns and all(a[1] == b[0] for a, b in zip(r, r[1:])), (bi, r)
+
+    def work(st, grp):
+        return sum((s1 - s0) * st.tpl.buckets[bi].n for bi, s0, s1 in st._with_partners(grp))
+
+    st = stub([1, 95, 95, 9025, 9025], [523, 522, 522, 522, 522], {})
+    g = DeviceProblem._refine_groups(st)
+    covered(st, g)
+    assert len(g) == 2 and abs(work(st, g[0]) - work(st, g[1])) <= 96 * 522
+    one = stub([127], [262], {})
+    g = DeviceProblem._refine_groups(one)
+    covered(one, g)
+    assert len(g) == 2 and abs(work(one, g[0]) - work(one, g[1])) <= 2 * 262     # split at an even system
+    assert all(s0 % 2 == 0 for grp in g for _, s0, _ in grp)
+    # a shared pair (bucket 4 solved with bucket 3's factors): bucket 3 split between the groups,
+    # its partner's residual over the same systems
+    pair = stub([1, 95, 95, 9025, 9025], [523, 522, 522, 522, 522], {4: 3})
     g = DeviceProblem._refine_groups(pair)
-    assert sorted(sum(g, [])) == [0, 1, 2, 3, 4]
-    assert any(3 in grp and 4 in grp for grp in g)
+    covered(pair, g)
+    assert all(bi != 4 for grp in g for bi, _, _ in grp)
+    assert abs(work(pair, g[0]) - work(pair, g[1])) <= 2 * 522

@@ -143,3 +143,37 @@ def test_planned_bytes_bound_the_shared_solver(cuda_lib):
         del s
         gc.collect()
     assert held[True] < held[False]
+
+
+@pytest.mark.parametrize("share", [True, False])
+def test_system_ranges_solve_alike(share, cuda_lib):
+    """A bucket solved in two launches over system ranges (the FP32 refinement's two streams)
+    gives the bits of one launch over the whole batch, and the ranged residual those of the whole."""
+    import torch
+    from conatus_gb300.ivp import DeviceProblem
+    P = template("channel_ny129").instantiate([24, 24])
+    dev = DeviceProblem(P, "fp32", share=share)
+    dev.autotune = False
+    a, b = 11 / 6 / 5e-3, 1.0
+    fs = dev.factor(a, b)
+    dev.ensure_residual(a, b)
+    rhs = dev.zeros()
+    rhs.real.normal_()
+    rhs.imag.normal_()
+    whole, parts = dev.zeros(), dev.zeros()
+    nb = len(fs)
+    dev._batch_call(fs, list(range(nb)), rhs, whole, None, 1, 0, 0)
+    big = 3
+    h = dev.nsys[big] // 2 & ~1
+    # shared: bucket 4 follows bucket 3's ranges; unshared: solved whole in the first launch
+    rest = [bi for bi in range(nb) if bi not in (big, 4)] + ([] if share else [4])
+    dev._batch_call(fs, rest + [(big, 0, h)], rhs, parts, None, 1, 0, 0)
+    dev._batch_call(fs, [(big, h, dev.nsys[big])], rhs, parts, None, 1, 0, 0)
+    torch.cuda.synchronize()
+    assert torch.equal(whole, parts)
+    r1, r2 = dev.zeros(), dev.zeros()
+    dev.residual(a, b, whole, rhs, r1)
+    dev.residual(a, b, whole, rhs, r2, buckets=[(bi, 0, dev.nsys[bi]) for bi in range(nb) if bi != big]
+                 + [(big, 0, h), (big, h, dev.nsys[big])])
+    torch.cuda.synchronize()
+    assert torch.equal(r1, r2)
