@@ -489,30 +489,45 @@ def cpu_baseline(args, P, C0, steps=1, warmup=1):
             "sample": desc}
 
 
+def serving_record(args, requests=None, rate=None, steps=None, budget=150e9):
+    """Serve a seeded Poisson stream (conatus_gb300.serving.ServingEngine: pools of requests of one
+    template, resolution and step advanced by shared launches, admission by planned bytes under the
+    HBM budget) and summarize it: served steps/s, p50/p99 completion latency, pools and members in
+    flight. A short warm stream first (templates, twiddles, the autotuner's schedules)."""
+    from conatus_gb300 import serving
+    requests = requests or args.requests
+    rate = rate or args.rate
+    lo, hi = steps or args.serve_steps
+    warm = serving.poisson_stream(24, rate=1e4, seed=1000, steps=(40, 60))
+    serving.ServingEngine(precision=args.precision).run(warm, realtime=False)
+    reqs = serving.poisson_stream(requests, rate=rate, seed=0, steps=(lo, hi))
+    eng = serving.ServingEngine(budget_bytes=budget, precision=args.precision, chunk=args.chunk,
+                                unroll=args.unroll)
+    with ClockSampler(0) as clk:
+        st = eng.run(reqs, realtime=True)
+    return {"metric": "served IMEX steps/s (Poisson mix Burgers/KS/RB, rate %g/s)" % rate,
+            "value": st["steps_per_s"], "unit": "steps/s", "requests": st["requests"],
+            "steps": st["steps"], "wall_s": st["wall_s"],
+            "latency_s": {"p50": st["p50_s"], "p99": st["p99_s"]},
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "config": {"workload": f"serving {requests} requests at {rate:g}/s, steps U[{lo},{hi}], SBDF2, "
+                                   "Burgers N 64..512 / KS N 64..256 / RB Nz 32..96 Nx 4Nz",
+                       "budget_gb": budget / 1e9, "chunk": args.chunk, "unroll": args.unroll,
+                       "slots": serving.POOL_SLOTS},
+            "serving": st, "clocks": clk.summary()}
+
+
 def run_serving(args):
     """The serving configuration: a seeded Poisson stream (rate 200/s) of Burgers / KS / RB requests
     served by conatus_gb300.serving.ServingEngine with a 150 GB admission budget."""
     import torch
-    from conatus_gb300 import serving
     torch.cuda.set_device(0)
-    lo, hi = args.serve_steps
-    warm = serving.poisson_stream(6, rate=1e4, seed=1000, steps=(40, 40))
-    serving.ServingEngine(precision=args.precision).run(warm, realtime=False)     # templates, twiddles, modules
-    reqs = serving.poisson_stream(args.requests, rate=args.rate, seed=0, steps=(lo, hi))
-    eng = serving.ServingEngine(budget_bytes=150e9, precision=args.precision, chunk=args.chunk,
-                                unroll=args.unroll)
-    with ClockSampler(0) as clk:
-        st = eng.run(reqs, realtime=True)
-    out = {"metric": "served IMEX steps/s (Poisson mix Burgers/KS/RB, rate %g/s)" % args.rate,
-           "value": st["steps_per_s"], "unit": "steps/s", "n_gpus": 1, "steps": st["steps"],
-           "warmup": 6, "ms_per_step": 1e3 / st["steps_per_s"], "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-           "data": "synthetic (seeded request stream and initial states)",
-           "config": {"workload": f"serving {args.requests} requests, steps U[{lo},{hi}], SBDF2, "
-                                  "Burgers N 64..512 / KS N 64..256 / RB Nz 32..96 Nx 4Nz",
-                      "budget_gb": 150, "chunk": args.chunk, "unroll": args.unroll},
-           "latency_s": {"p50": st["p50_s"], "p99": st["p99_s"]}, "serving": st, "clocks": clk.summary()}
+    rec = serving_record(args)
+    out = {"metric": rec["metric"], "value": rec["value"], "unit": "steps/s", "n_gpus": 1,
+           "steps": rec["steps"], "warmup": 24, "ms_per_step": 1e3 / max(rec["value"], 1e-30),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": rec["dtype"],
+           "data": "synthetic (seeded request stream and initial states)", "config": rec["config"],
+           "latency_s": rec["latency_s"], "serving": rec["serving"], "clocks": rec["clocks"]}
     print(json.dumps(out), flush=True)
 
 
@@ -663,8 +678,8 @@ def main():
     ap.add_argument("--requests", type=int, default=200, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--serve-steps", type=int, nargs=2, default=[1000, 20000], help="serving: step range")
-    ap.add_argument("--chunk", type=int, default=500, help="serving: steps per scheduling chunk")
-    ap.add_argument("--unroll", type=int, default=50, help="steps per CUDA graph (serving, ensemble)")
+    ap.add_argument("--chunk", type=int, default=500, help="serving: most steps per scheduling chunk")
+    ap.add_argument("--unroll", type=int, default=25, help="steps per CUDA graph (serving, ensemble)")
     ap.add_argument("--members", type=int, default=None, help="ensembles: members (KS 4096, RB 1024)")
     args = ap.parse_args()
     if args.warmup < 3:

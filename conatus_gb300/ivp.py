@@ -363,6 +363,17 @@ class DeviceProblem:
                 self.tuning = tune_solve(self, key, f, stream)
         return f
 
+    def reset_operators(self) -> None:
+        """The problem's operator values changed (a stacked problem's case parameters): drop the L
+        values, the factor sets and the residual data made from them; they are rebuilt on next use
+        (outside any capture). Solvers on this problem drop their captured graphs
+        (``IVPSolver.operators_changed``)."""
+        self._L = [None] * len(self.tpl.buckets)
+        self._factors = {}
+        self._resid = [None] * len(self.tpl.buckets)
+        self._groups = None
+        self.shared = {}
+
     def _check_pairs(self, vals_all) -> dict:
         """{partner: primary} of the structural pairs whose values satisfy the relation exactly at
         this (a, b): no zero entry in the primary (a zero carries no sign), and every entry of the
@@ -865,6 +876,11 @@ class IVPSolver:
         if self._flag is not None:
             self._flag.fill_(_FLAG_CLEAR)
         self._finite_ok = self._probed = None
+
+    def operators_changed(self) -> None:
+        """After ``DeviceProblem.reset_operators``: the captured graphs hold the old factor sets;
+        they are captured again on next use."""
+        self._graphs = {}
 
     def set_history(self, MX_list, F_list, LX_list=None) -> None:
         """History (newest first) of M X and F, and of L X for the CN family, e.g. to continue from

@@ -40,3 +40,20 @@ def cuda_lib():
 
 def golden(name):
     return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+
+
+def reference_python():
+    """The reference's Python package directory (holding ``conatus/``) where it is present: the
+    environment variable CONATUS_REFERENCE_PYTHON, else CONATUS_REFERENCE/python, else the tree
+    that built oracle/_ref (recorded in oracle/_ref/REFERENCE by the build); None otherwise."""
+    cands = [os.environ.get("CONATUS_REFERENCE_PYTHON")]
+    if os.environ.get("CONATUS_REFERENCE"):
+        cands.append(os.path.join(os.environ["CONATUS_REFERENCE"], "python"))
+    rec = os.path.join(ROOT, "oracle", "_ref", "REFERENCE")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            cands.append(os.path.join(f.read().strip(), "python"))
+    for c in cands:
+        if c and os.path.exists(os.path.join(c, "conatus", "__init__.py")):
+            return c
+    return None
