@@ -1,4 +1,4 @@
-"""Serving (CPU): the seeded Poisson request stream, host-side request preparation and the
+"""Serving (CPU): the seeded Poisson request stream, the pools' planned bytes and the
 device-memory planner (no device work)."""
 from __future__ import annotations
 
@@ -30,14 +30,29 @@ def test_stream_is_seeded_and_mixed():
 
 
 @pytest.mark.parametrize("kind", ["burgers", "ks", "rb"])
-def test_prepare_plans_bytes(kind):
+def test_pool_plans_bytes(kind):
+    """A pool's planned bytes: positive, growing with its slots, the FP32 form's copies on top of
+    the FP64 factors; the problem of a Burgers / RB pool stacks one case per slot."""
     reqs = [r for r in serving.poisson_stream(200, seed=3) if r.kind == kind][:3]
     for r in reqs:
-        p = serving.prepare(r, "fp64")
-        assert p.bytes > 0
+        key = serving.pool_key(r)
+        a = serving.plan_pool(key, 2, "fp64")
+        b = serving.plan_pool(key, 4, "fp64")
+        assert 0 < a < b
         if kind != "ks":
-            assert sum(c.size for c in p.state) == sum(ns * b.n for ns, b in zip(p.problem.nsys, p.problem.tpl.buckets))
-            assert serving.prepare(r, "fp32").bytes > p.bytes        # FP32 copies on top of FP64 factors
+            assert serving.plan_pool(key, 2, "fp32") > a
+            _, S = serving._pool_problem(key, 3)
+            assert S.ncase == 3 and S.n_total == 3 * sum(ns * bk.n for ns, bk in zip(S._nsys_case, S.tpl.buckets))
+
+
+def test_ks_state_is_one_member_of_the_ensemble_state():
+    """A KS request's initial state does not depend on its slot: one member of the ensemble's
+    seeded state."""
+    import types
+    from conatus_gb300.ensemble import FourierEnsemble
+    fake = types.SimpleNamespace(N=np.array([128]))
+    ref = FourierEnsemble.random_state(fake, seed=17)[0]
+    assert np.array_equal(serving.ks_state(128, 17), ref)
 
 
 def test_plan_parts_scale():
