@@ -48,21 +48,24 @@ BURGERS_N = tuple(range(64, 513, 32))     # resolutions with a parameter-linear 
 RB_NZ = (32, 48, 64, 80, 96)
 SCHEME = "SBDF2"
 DT = {"burgers": 1e-4, "ks": 1e-2, "rb": 1e-4}
-POOL_SLOTS = {"burgers": 32, "ks": 64, "rb": 8}
+# slots per pool: about the members a pool of the configured stream holds at once (measured: a
+# Burgers resolution sees ~6 requests in flight, a KS size ~20, an RB (Nz, dt) key ~2); every slot
+# is computed whether it holds a member or not
+POOL_SLOTS = {"burgers": 8, "ks": 32, "rb": 2}
 CHECK_EVERY = 100                         # steps between two finite-state checks of a member
 RB_LX = 2 * math.pi / 3.117
 
 
 def time_step(req) -> float:
-    """dt of a request: 1e-4 for Burgers, 1e-2 for KS; for RB the largest 1e-4 / 2^k below an
+    """dt of a request: 1e-4 for Burgers, 1e-2 for KS; for RB the largest 1e-4 / 4^k below an
     advective limit, a quarter of the grid spacing Lx/Nx over the free-fall velocity (Ra Pr)^(1/2)
     (thermal-diffusion units, Pr = 1): the explicit advection of SBDF2 at dt = 1e-4 diverges from
-    Ra ~ 1e5 up (the reference's own runs blow up), and steps on a 2^-k ladder let requests of
+    Ra ~ 1e5 up (the reference's own runs blow up), and steps on a 4^-k ladder let requests of
     nearby Ra share a pool."""
     if req.kind == "rb":
         limit = 0.25 * (RB_LX / req.params["Nx"]) / math.sqrt(req.params["Ra"])
-        k = max(0, math.ceil(math.log2(DT["rb"] / limit)))
-        return DT["rb"] * 2.0 ** -k
+        k = max(0, math.ceil(math.log(DT["rb"] / limit, 4)))
+        return DT["rb"] * 4.0 ** -k
     return DT[req.kind]
 
 

@@ -139,7 +139,7 @@ def test_chunks_end_on_checks_and_last_steps(fake_pools):
 
 
 def test_pool_keys_of_the_stream():
-    """Requests of one template, resolution and time step share a key; RB steps sit on the 1e-4 / 2^k
+    """Requests of one template, resolution and time step share a key; RB steps sit on the 1e-4 / 4^k
     ladder below the advective limit."""
     import math
     reqs = serving.poisson_stream(400, seed=3)
@@ -148,7 +148,7 @@ def test_pool_keys_of_the_stream():
         dt = k[-1]
         if r.kind == "rb":
             limit = 0.25 * (serving.RB_LX / r.params["Nx"]) / math.sqrt(r.params["Ra"])
-            assert dt <= limit < 2 * dt or (dt == 1e-4 and limit >= 1e-4)
+            assert dt <= limit * (1 + 1e-12) and (limit < 4 * dt or (dt == 1e-4 and limit >= 1e-4))
             assert k[:3] == ("rb", r.params["Nz"], r.params["Nx"])
         else:
             assert k == (r.kind, r.params["N"], serving.DT[r.kind])
