@@ -384,6 +384,8 @@ def run_gpu(args):
         del solver, dev, R, X2
         torch.cuda.empty_cache()
         out["forms"] = {"fp32": form_fp32(P, C0, cfg, args)}
+    if args.config == "channel" and ws == 1 and not args.no_forms:
+        out["subrecords"] = subrecords(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, P, C0)
     if rank == 0:
@@ -391,6 +393,38 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def subrecords(args):
+    """The other configurations, compact and time-bounded, beside the default line: the serving
+    stream (100 requests at 200/s, steps U[1000, 20000], FP64 and the FP32 form), the KS ensemble
+    (4096 members, 500 steps) and the RB ensemble (1024 cases, 50 steps) in the FP32 form."""
+    import copy
+    import torch
+    out = {}
+    for prec in ("fp64", "fp32"):
+        a = copy.copy(args)
+        a.precision, a.chunk, a.unroll = prec, 500, 25
+        rec = serving_record(a, requests=100, rate=200.0, steps=(1000, 20000))
+        st = rec["serving"]
+        out[f"serving_{prec}"] = {"metric": rec["metric"], "value": rec["value"], "unit": "steps/s",
+                                  "dtype": rec["dtype"], "latency_s": rec["latency_s"],
+                                  "requests": st["requests"], "steps": st["steps"], "wall_s": st["wall_s"],
+                                  "nonfinite": st["nonfinite"], "peak_pools": st["peak_pools"],
+                                  "peak_members": st["peak_members"],
+                                  "peak_planned_gb": st["peak_planned_bytes"] / 1e9, "budget_gb": 150,
+                                  "workload": rec["config"]["workload"]}
+        torch.cuda.empty_cache()
+    for name, fn, members, steps in (("ks_ensemble", ks_ensemble_record, 4096, 500),
+                                     ("rb_ensemble", rb_ensemble_record, 1024, 50)):
+        a = copy.copy(args)
+        a.precision, a.members, a.steps, a.warmup, a.unroll = "fp32", members, steps, 3, 25
+        rec = fn(a)
+        out[name] = {k: rec[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "dtype",
+                                          "member_steps_per_s", "mode_updates_per_s") if k in rec}
+        out[name]["workload"] = rec["config"]["workload"]
+        torch.cuda.empty_cache()
+    return out
 
 
 def form_fp32(P, C0, cfg, args):
@@ -532,12 +566,18 @@ def run_serving(args):
 
 
 def run_ks_ensemble(args):
+    """The KS ensemble line (see ``ks_ensemble_record``)."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(ks_ensemble_record(args)), flush=True)
+
+
+def ks_ensemble_record(args):
     """The KS ensemble: 4096 members (L ~ U[22, 100], N = next power of two >= 2L), SBDF2, dt = 0.01,
     one fused launch per step replayed as CUDA graphs."""
     import torch
     from conatus_gb300 import workloads as W
     from conatus_gb300.ensemble import FourierEnsemble, ks_members
-    torch.cuda.set_device(0)
     N, L = ks_members(args.members, seed=0)
     ens = FourierEnsemble(W.load_template("ks"), N, L, scheme="SBDF2", dt=0.01, precision=args.precision)
     ens.set_state(ens.random_state(seed=0))
@@ -563,10 +603,17 @@ def run_ks_ensemble(args):
                       "state_finite": bool(np.all(np.isfinite(x)))},
            "member_steps_per_s": value * args.members, "mode_updates_per_s": value * ens.mode_updates(),
            "gpu_launches": args.steps, "clocks": clk.summary()}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_rb_ensemble(args):
+    """The RB ensemble line (see ``rb_ensemble_record``)."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(rb_ensemble_record(args)), flush=True)
+
+
+def rb_ensemble_record(args):
     """The RB ensemble: ``--members`` 2D Rayleigh-Benard cases (default 1024), Nz uniform in {32, 48,
     64}, Nx = 4 Nz, Ra log-uniform in [1e4, 1e7], Pr = 1, seeded noise 1e-3. The cases of one Nz are
     stacked into one problem (one F pass and one solve launch for all of them per step); the three
@@ -577,7 +624,6 @@ def run_rb_ensemble(args):
     from conatus_gb300 import workloads as W
     from conatus_gb300.ivp import IVPSolver
     from conatus_gb300.template import StackedProblem
-    torch.cuda.set_device(0)
     rng = np.random.default_rng(0)
     nzs = (32, 48, 64)
     nz = rng.choice(nzs, args.members)
@@ -629,7 +675,7 @@ def run_rb_ensemble(args):
                       "l2": "inputs larger than L2 (factors of every case)"},
            "member_steps_per_s": value * args.members, "mode_updates_per_s": value * nu,
            "clocks": clk.summary()}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_reference(args):
