@@ -655,7 +655,7 @@ def rb_ensemble_record(args):
         e0.record(cur)
         for sv in groups:
             sv.stream.wait_event(e0)
-            sv.run_graph(args.steps, args.unroll)
+            sv.run_graph(args.steps, args.unroll, wait=False)    # the groups overlap; checks read below
         for sv in groups:
             cur.wait_stream(sv.stream)
         e1.record(cur)
