@@ -150,13 +150,14 @@ def step_bytes(dev, solver):
 
 
 # DRAM bytes per system of one batched solve launch, from the ncu captures of the channel solve
-# (64x129x64, 1985 systems; dram__bytes_read.sum + dram__bytes_write.sum): the compact solve reads
-# the union pattern of the factors, not the band, so its traffic is below the band-equivalent bytes
+# (64x129x64; dram__bytes_read.sum + dram__bytes_write.sum): the compact solve reads the union pattern
+# of the factors, not the band, and a shared pair's factors once for both systems, so its traffic is
+# below the band-equivalent bytes
 TRAFFIC_PER_SYSTEM = {
-    ("channel", "fp64"): ((325.293312 + 3.231488) * 1e6 / 1985,
+    ("channel", "fp64"): ((174.600192 + 3.016192) * 1e6 / 1985,
                           "profiles/k_solve_compact_multi_channel64x129x64_fp64.md"),
-    # the FP32 form solves its buckets in two groups: the captured launch is the group of 992
-    ("channel", "fp32"): ((86.345216 + 2.852096) * 1e6 / 992,
+    # the FP32 form solves in two groups: the captured launch is the group of 1024 paired systems
+    ("channel", "fp32"): ((47.700736 + 0.423936) * 1e6 / 1024,
                           "profiles/k_solve_compact_multi_channel64x129x64_fp32.md"),
 }
 
@@ -165,7 +166,7 @@ TRAFFIC_PER_SYSTEM = {
 # write; it reads the 9 z-groups, 32 modes x 19200 columns, and writes the 12 factor fields, 96
 # points x 19200 columns) and the algorithmic bytes of that launch; the full launch's traffic is
 # taken in the same proportion to its algorithmic bytes (the transform streams its fields once)
-RFFT_TRAFFIC = ((94.525440 + 125.520384) * 1e6, 9 * 19200 * 32 * 16 + 12 * 19200 * 96 * 8,
+RFFT_TRAFFIC = ((95.617024 + 126.273024) * 1e6, 9 * 19200 * 32 * 16 + 12 * 19200 * 96 * 8,
                 "profiles/k_rfft_axis_channel64x129x64_fp64.md")
 FP64_NOMINAL_TFLOPS = 1.25     # GB300 FP64 (2 DFMA per clock per SM): nominal, not measured
 
