@@ -65,6 +65,7 @@ _SIGS = {
     "cng_sbdf_rhs_fused": [c_int, P, P, P, P, P, ctypes.c_int64, c_int, P],
     "cng_lincomb": [ctypes.c_int64, P, c_int, P, P, P, P, P],
     "cng_check_finite": [P, ctypes.c_int64, ctypes.c_int64, P, P],
+    "cng_dfma_probe": [ctypes.c_int64, c_int, P, P, P],
     "cng_split_residual": [c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P, P, P, P],
     "cng_split_residual_range": [c_int, c_int, c_int, c_int, P, P, P, P, P, c_int, c_double, c_double, P, P, P,
                                  P, P, P],

@@ -1059,10 +1059,7 @@ static void check_smem(const Banded& h) {
 
 template <class T, int IO>
 static void launch_solve_t(const Banded& h, const SolveIo& io, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve<T, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
-    });
+    ensure_smem_attr((const void*)k_solve<T, IO>, (int)kMaxSolveSmem);
     const int blocks = ceil_div(h.batch, kWarpsPerBlock);
     k_solve<T, IO><<<blocks, 32 * kWarpsPerBlock, h.solve_smem(), st>>>(h.view<T>(), io);
     CNG_LAUNCH("k_solve");
@@ -1087,10 +1084,7 @@ static void demote_compact(Banded& h, cudaStream_t st);
 
 // FP32 band-kernel solve (one warp per system) of the mixed form: x (+)= A^{-1} b, complex128 data
 static void launch_mixed_dense(const Banded& h, const void* b, void* x, int accumulate, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
-    });
+    ensure_smem_attr((const void*)k_solve_mixed, (int)kMaxSolveSmem);
     MixedView v{h.batch, h.n, h.r, h.kl, h.ku, h.ldab, h.ab32, h.ipiv, h.vt32, h.w32, h.slu32, h.spiv, h.perm};
     const size_t smem = h.solve_smem(sizeof(zf));
     k_solve_mixed<<<ceil_div(h.batch, kWarpsPerBlock), 32 * kWarpsPerBlock, smem, st>>>(
@@ -1137,10 +1131,7 @@ static void prepare_transpose(Banded& h, cudaStream_t st) {
 
 template <class T>
 static void launch_solve_T_t(const Banded& h, void* b, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_T<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSolveSmem);
-    });
+    ensure_smem_attr((const void*)k_solve_T<T>, (int)kMaxSolveSmem);
     const int blocks = ceil_div(h.batch, kWarpsPerBlock);
     k_solve_T<T><<<blocks, 32 * kWarpsPerBlock, (size_t)kWarpsPerBlock * (h.n + 64) * sizeof(T), st>>>(
         h.view<T>(), static_cast<T*>(b));
@@ -2204,10 +2195,7 @@ static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
 
 template <class TF, class TD, int IO>
 static void launch_compact(const Banded& h, const CompactData<TF>& cd, const SolveIo& io, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_compact<TF, TD, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    });
+    ensure_smem_attr((const void*)k_solve_compact<TF, TD, IO>, 220 * 1024);
     int nw = 8;
     while (nw > 1 && compact_smem<TF>(h, nw) > 220 * 1024) --nw;
     nw = std::min(nw, std::max(1, ceil_div(h.cWg, sm_count())));
@@ -2249,11 +2237,7 @@ template <class TF, class TD, int IO, int CH, int ST>
 static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
                            const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2,
                            const std::vector<int>& rng, int sched, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_compact_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024);
-    });
+    ensure_smem_attr((const void*)k_solve_compact_multi<TF, TD, IO, CH, ST>, 220 * 1024);
     // one warp count for all blocks: the one that keeps the most warps resident per SM (blocks per
     // SM are bounded by their shared memory: eight warps in one block can lose to seven in two),
     // and no more than it takes to give every SM a block (a small batch spreads over the SMs: each
@@ -2324,11 +2308,7 @@ static void launch_split_t(const std::vector<const Banded*>& hs, const std::vect
     for (const Banded* h : hs)
         if (h->cG != kGroup)
             throw InvalidArgument("the split-lane schedules do not solve shared pairs: a compact two-system schedule");
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaFuncSetAttribute(k_solve_split_multi<TF, TD, IO, CH, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024);
-    });
+    ensure_smem_attr((const void*)k_solve_split_multi<TF, TD, IO, CH, ST>, 220 * 1024);
     // warps per block as launch_multi_t: the most resident warps per SM, and a block for every SM
     // when the batch is small
     auto smem_of = [&](int w) {

@@ -7,8 +7,11 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
+#include <set>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 namespace cng {
 
@@ -46,6 +49,20 @@ inline void cuda_check(cudaError_t e, const char* what) {
 }
 #define CNG_CUDA(call) ::cng::cuda_check((call), #call)
 #define CNG_LAUNCH(what) ::cng::cuda_check(cudaGetLastError(), what)
+
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current device, once per (kernel,
+// device): the attribute belongs to the device's context, so a second device needs its own call.
+inline void ensure_smem_attr(const void* fn, int bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({fn, dev})) return;
+    cuda_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+               "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
+    done.insert({fn, dev});
+}
 
 // Two timing events, destroyed on every exit path (a failed second creation frees the first).
 struct EventPair {

@@ -219,16 +219,10 @@ int cng_fourier_ensemble_step(const cng_fourier_ensemble_desc* D, void* X, void*
         const size_t smem = cs * 3 * (size_t)maxM + rs * ((size_t)(a.nfactors * maxM + 3) & ~(size_t)3) +
                             sizeof(double2) * (size_t)maxM + 64;
         if (D->precision) {
-            static std::once_flag f;
-            std::call_once(f, [] {
-                cudaFuncSetAttribute(k_fourier_ensemble_step<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            });
+            ensure_smem_attr((const void*)k_fourier_ensemble_step<float>, 200 * 1024);
             k_fourier_ensemble_step<float><<<a.nmem, 128, smem, st>>>(a);
         } else {
-            static std::once_flag f;
-            std::call_once(f, [] {
-                cudaFuncSetAttribute(k_fourier_ensemble_step<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            });
+            ensure_smem_attr((const void*)k_fourier_ensemble_step<double>, 200 * 1024);
             k_fourier_ensemble_step<double><<<a.nmem, 128, smem, st>>>(a);
         }
         CNG_LAUNCH("k_fourier_ensemble_step");

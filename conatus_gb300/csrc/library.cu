@@ -170,3 +170,34 @@ int cng_graph_destroy(cng_graph* g) {
 }
 
 }  // extern "C"
+
+// FP64 arithmetic rate probe: every thread runs `iters` rounds of 8 independent fused multiply-adds
+// on registers (8 chains hide the pipe's latency), then folds them into one store so that nothing
+// is removed. 16 flops per thread and round.
+namespace cng {
+__global__ void k_dfma_probe(long long iters, double a, double b, double* __restrict__ sink) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (threadIdx.x + k) * 1e-3;
+    for (long long i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 12345.6789) sink[0] = s;          // never true for the probe's inputs; keeps the chains
+}
+}  // namespace cng
+
+extern "C" int cng_dfma_probe(int64_t iters, int blocks_per_sm, void* sink, double* flops, void* stream) {
+    CNG_TRY({
+        if (iters <= 0 || blocks_per_sm <= 0 || !sink || !flops) throw cng::InvalidArgument("dfma_probe: bad argument");
+        const int blocks = cng::sm_count() * blocks_per_sm, threads = 256;
+        cng::k_dfma_probe<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(iters, 0.999999, 1e-7,
+                                                                                      static_cast<double*>(sink));
+        CNG_LAUNCH("k_dfma_probe");
+        *flops = 16.0 * (double)iters * (double)blocks * threads;
+    })
+}
+

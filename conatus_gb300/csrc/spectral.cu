@@ -757,9 +757,7 @@ void complexify_kernel_launch(const R* in, void* out, long long n, cudaStream_t 
 // host: transform launchers
 
 template <class R>
-static void set_smem_attr(const void* fn) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax);
-}
+static void set_smem_attr(const void* fn) { ensure_smem_attr(fn, (int)kFftSmemMax); }
 
 // Sequences per block of the shared-memory transforms: at most 8 in FP32 and 4 in FP64 (measured
 // on the channel's F: fewer sequences per block, more blocks per SM; 16 was 6 % slower in FP32 and
@@ -781,9 +779,8 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
         CNG_CUDA(cudaMemcpyAsync(out, in, sizeof(c2<R>) * (size_t)ncols, cudaMemcpyDeviceToDevice, st));
         return;
     }
-    static std::once_flag f1, f2;
-    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_cheb_bwd<R>); });
-    std::call_once(f2, [] { set_smem_attr<R>((const void*)k_cheb_fwd<R>); });
+        set_smem_attr<R>((const void*)k_cheb_bwd<R>);
+    set_smem_attr<R>((const void*)k_cheb_fwd<R>);
     if (M % 2) throw InvalidArgument("Chebyshev grid size must be even");
     FftPlan plan = make_plan(M);
     const c2<R>* tw = twiddles<R>().get(M, 0);
@@ -801,8 +798,7 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
                      cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
-    static std::once_flag f1;
-    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_fft_axis<R>); });
+        set_smem_attr<R>((const void*)k_fft_axis<R>);
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
@@ -817,8 +813,7 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
                       cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
-    static std::once_flag f1;
-    std::call_once(f1, [] { set_smem_attr<R>((const void*)k_rfft_axis<R>); });
+        set_smem_attr<R>((const void*)k_rfft_axis<R>);
     FftPlan plan = make_plan(L);
     const c2<R>* tw = twiddles<R>().get(L, 0);
     const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
@@ -1171,13 +1166,11 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     CNG_CUDA(cudaMemset(h->S, 0, h->S_bytes));
     CNG_CUDA(cudaMemset(h->W1, 0, w));
     CNG_CUDA(cudaMemset(h->W2, 0, w));
-    static std::once_flag f;
-    std::call_once(f, [] {
-        cudaFuncSetAttribute(k_unpack<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_unpack<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_pack<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_pack<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    });
+    // on the device current at creation (the handle's device)
+    ensure_smem_attr((const void*)k_unpack<double>, 200 * 1024);
+    ensure_smem_attr((const void*)k_unpack<float>, 200 * 1024);
+    ensure_smem_attr((const void*)k_pack<double>, 200 * 1024);
+    ensure_smem_attr((const void*)k_pack<float>, 200 * 1024);
     return h.release();
 }
 

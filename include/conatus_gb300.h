@@ -32,8 +32,10 @@ int cng_device_name(int dev, char* buf, int buflen);
  * python/conatus/runtime/memory.py predicts the same quantity). */
 int cng_mem_info(uint64_t* free_bytes, uint64_t* total_bytes);
 /* Device memory held by the library's handles: live bytes and allocations so far; cached bytes and
- * reuses are 0 (freed memory goes back to the driver at once, there is no pool). Replaces
- * cuda.pool_stats (core/bindings/module.cpp:450-453). Any argument may be NULL. */
+ * reuses are 0 (freed memory goes back to the driver at once, there is no pool). Not counted: the
+ * fixed 8 MiB staging array of cng_banded_solve_host_static, resident on every device that loaded
+ * the library. Replaces cuda.pool_stats (core/bindings/module.cpp:450-453). Any argument may be
+ * NULL. */
 int cng_pool_stats(uint64_t* live_bytes, uint64_t* cached_bytes, uint64_t* n_alloc, uint64_t* n_reuse);
 /* Nothing is cached, so nothing to return to the driver: 0. Replaces cuda.pool_trim
  * (core/bindings/module.cpp:454). */
@@ -165,7 +167,10 @@ int cng_banded_make_fp32(cng_banded* h, void* stream);
 int cng_banded_solve_fp32(const cng_banded* h, const void* b, void* x, int accumulate, void* stream);
 
 /* Host buffers: x = A^{-1} b (or A^{-T} b) with the copies inside the call, (batch, n) C-order.
- * Replaces _core.BorderedBandedBatch{D,Z}.solve (core/bindings/module.cpp:184-206). */
+ * The copies and kernels run on the legacy default stream and the call returns when x is on the
+ * host; work the caller queued on non-blocking streams (a refactorization, a transpose preparation)
+ * is not ordered before it: synchronize those streams first. Replaces
+ * _core.BorderedBandedBatch{D,Z}.solve (core/bindings/module.cpp:184-206). */
 int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int transpose);
 
 /* As cng_banded_solve_host, but allocates no device memory: the right-hand sides are staged in a
@@ -177,7 +182,9 @@ int cng_banded_solve_host(cng_banded* h, const void* b_host, void* x_host, int t
  * whole device, which stalls every other stream (other runs in flight in a serving loop); a
  * caller under a planned device-memory budget must not grow its footprint either. The first call
  * on a device looks up the array's address. Every call on a device shares the one array, so
- * calls on one device take turns (a per-device lock, held from the copy in to the copy out). */
+ * calls on one device take turns (a per-device lock, held from the copy in to the copy out). Like
+ * cng_banded_solve_host it runs on the legacy default stream: synchronize the caller's own
+ * non-blocking streams first. */
 int cng_banded_solve_host_static(cng_banded* h, const void* b_host, void* x_host, int transpose);
 
 /* ---- pseudospectral explicit right-hand side F(X) ------------------------------------------ */
@@ -356,6 +363,13 @@ int cng_sbdf_rhs_fused(int q, const double* c, const double* d, const void* cons
  * IVPSolver.run every FINITE_CHECK_EVERY = 100 steps and at the end of a run
  * (run_checks.py:15-20, python/conatus/timestep/integrator.py:764-767,1306-1312). */
 int cng_check_finite(const void* x, int64_t count, int64_t iteration, int64_t* flag, void* stream);
+
+/* Measurement: launch an FP64 fused-multiply-add loop (iters rounds of 8 independent chains per
+ * thread, blocks_per_sm blocks of 256 threads on every SM) on `stream` and return its flop count in
+ * *flops (16 per thread and round); the caller times it with events. sink: one device double (never
+ * written for the probe's inputs). The FP64 peak the transforms' roofline is measured against. No
+ * reference counterpart. */
+int cng_dfma_probe(int64_t iters, int blocks_per_sm, void* sink, double* flops, void* stream);
 
 /* ---- CUDA graphs of whole steps ------------------------------------------------------------- */
 

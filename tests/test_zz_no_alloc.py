@@ -77,3 +77,60 @@ def test_static_host_solve_refuses_oversize(cuda_lib):
     got = _solve("cng_banded_solve_host_static", small._h.h, b[:4], False)
     ref = _solve("cng_banded_solve_host", small._h.h, b[:4], False)
     assert rel(got, ref) <= 1e-15
+
+
+def _batch(n=96, batch=24, seed=1):
+    import scipy.sparse as sp
+    from conatus_gb300 import core
+    rng = np.random.default_rng(seed)
+    mats = []
+    for _ in range(batch):
+        A = sp.diags([rng.standard_normal(n - 2), rng.standard_normal(n - 1), 6 + rng.standard_normal(n),
+                      rng.standard_normal(n - 1)], [-2, -1, 0, 1], format="lil")
+        A[0, :] = rng.standard_normal(n)               # a border row
+        A = A.tocsr().astype(np.complex128)
+        mats.append((n, A.indptr, A.indices, A.data))
+    return core.BandedBatchZ(mats, [0]), rng
+
+
+def test_static_host_solve_allocates_nothing(cuda_lib):
+    """After the first call (which looks up the array's address), further calls leave the device's
+    free memory and the library's allocation counters unchanged."""
+    import torch
+    from conatus_gb300 import core
+    B, rng = _batch()
+    b = rng.standard_normal((24, 96)) + 1j * rng.standard_normal((24, 96))
+    _solve("cng_banded_solve_host_static", B._h.h, b, False)
+    torch.cuda.synchronize()
+    free0, stats0 = torch.cuda.mem_get_info()[0], core.pool_stats()
+    for _ in range(20):
+        _solve("cng_banded_solve_host_static", B._h.h, b, False)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert core.pool_stats() == stats0
+
+
+def test_static_host_solve_from_two_threads(cuda_lib):
+    """Two host threads solving different right-hand sides on one device take turns on the shared
+    array: each result equals its own plain host solve."""
+    import threading
+    B, rng = _batch(seed=2)
+    rhs = [rng.standard_normal((24, 96)) + 1j * rng.standard_normal((24, 96)) for _ in range(2)]
+    refs = [_solve("cng_banded_solve_host", B._h.h, r, False) for r in rhs]
+    errors = []
+
+    def work(k):
+        try:
+            for _ in range(25):
+                got = _solve("cng_banded_solve_host_static", B._h.h, rhs[k], False)
+                if rel(got, refs[k]) > 1e-15:
+                    errors.append((k, rel(got, refs[k])))
+        except Exception as e:              # noqa: BLE001 -- reported below
+            errors.append((k, repr(e)))
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
