@@ -20,6 +20,19 @@ _lock = threading.Lock()
 c_int, c_void_p, c_double, c_char_p = ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_char_p
 P = ctypes.c_void_p
 
+
+class MatvecPart(ctypes.Structure):
+    """cng_matvec_part: one bucket of a grouped M X launch."""
+    _fields_ = [("nsys", ctypes.c_int32), ("n", ctypes.c_int32), ("indptr", P), ("indices", P), ("values", P),
+                ("x", P), ("y", P)]
+
+
+class ResidualPart(ctypes.Structure):
+    """cng_residual_part: systems s0 .. s1 - 1 of one bucket of a grouped residual launch."""
+    _fields_ = [("nsys", ctypes.c_int32), ("s0", ctypes.c_int32), ("s1", ctypes.c_int32), ("n", ctypes.c_int32),
+                ("ptr", P), ("col", P), ("val", P), ("code", P), ("mono", P), ("nmono", ctypes.c_int32),
+                ("rowscale", P), ("x", P), ("xT", P), ("b", P), ("r", P)]
+
 # name -> argtypes (all return int status unless listed in _RESTYPES)
 _SIGS = {
     "cng_last_error": [],
@@ -54,6 +67,9 @@ _SIGS = {
     "cng_rhs_create": [P, P],
     "cng_rhs_destroy": [P],
     "cng_rhs_evaluate": [P, P, P, P],
+    "cng_rhs_evaluate_group": [c_int, P, P, P, P],
+    "cng_csr_matvec_real_group": [c_int, P, P],
+    "cng_split_residual_group": [c_int, P, c_double, c_double, P],
     "cng_rhs_workspace_bytes": [P, P],
     "cng_rhs_set_tuning": [P, c_int, c_int],
     "cng_cheb_transform": [c_int, P, P, ctypes.c_int64, c_int, c_int, P],

@@ -112,6 +112,12 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
 _RHS_CACHE: dict = {}
 
 
+def _set_rhs_tuning(dev, q, t) -> None:
+    """One launch shape for every F evaluator of ``dev`` (a grouped problem's handles share it)."""
+    for h in dev._rhs_all:
+        call("cng_rhs_set_tuning", h, int(q), int(t))
+
+
 def tune_rhs(dev, reps: int = 2, candidates=((2, 128), (4, 128), (8, 128), (2, 256), (4, 256), (8, 256),
                                                (16, 256))) -> dict:
     """Time the F evaluation of ``dev`` (a DeviceProblem) with each launch shape of its shared-memory
@@ -124,18 +130,18 @@ def tune_rhs(dev, reps: int = 2, candidates=((2, 128), (4, 128), (8, 128), (2, 2
     fixed = os.environ.get("CONATUS_GB300_RHS_TUNING")
     if fixed is not None:                 # "sequences,threads" instead of timing (reproducible runs)
         q, t = (int(v) for v in fixed.split(","))
-        call("cng_rhs_set_tuning", dev._rhs, q, t)
+        _set_rhs_tuning(dev, q, t)
         return {f"{q}x{t}": None}
     key = (dev.precision, dev.tpl.name, tuple(P.fourier_sizes), int(getattr(P, "ncase", 1)),
            tuple(dev.nsys))
     if key in _RHS_CACHE:
-        call("cng_rhs_set_tuning", dev._rhs, *_RHS_CACHE[key][0])
+        _set_rhs_tuning(dev, *_RHS_CACHE[key][0])
         return _RHS_CACHE[key][1]
     st = torch.cuda.Stream()
     x, out = dev.zeros(), dev.zeros()
     times = {}
     for q, t in candidates:
-        call("cng_rhs_set_tuning", dev._rhs, int(q), int(t))
+        _set_rhs_tuning(dev, int(q), int(t))
         dev.F(x, out, st)                                 # warm-up (first-use set-up)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
@@ -145,7 +151,7 @@ def tune_rhs(dev, reps: int = 2, candidates=((2, 128), (4, 128), (8, 128), (2, 2
         e1.synchronize()
         times[(q, t)] = e0.elapsed_time(e1) / reps
     best = min(times, key=times.get)
-    call("cng_rhs_set_tuning", dev._rhs, *best)
+    _set_rhs_tuning(dev, *best)
     report = {f"{q}x{t}": v for (q, t), v in times.items()}
     _RHS_CACHE[key] = (best, report)
     return report

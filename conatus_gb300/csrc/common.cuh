@@ -12,6 +12,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <vector>
 
 namespace cng {
 
@@ -62,6 +63,44 @@ inline void ensure_smem_attr(const void* fn, int bytes) {
     cuda_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
                "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
     done.insert({fn, dev});
+}
+
+// Grouped launches: one launch runs a kernel body over up to kMaxGrp argument sets (problems of
+// different sizes), each over its own range of blocks [start[k], start[k + 1]). The body sees its
+// block index and block count within its range. Passed as a __grid_constant__ kernel parameter.
+constexpr int kMaxGrp = 8;
+template <class A>
+struct Grp {
+    int n = 0;
+    unsigned start[kMaxGrp + 1] = {};
+    A a[kMaxGrp];
+    __device__ __forceinline__ int find(unsigned b) const {
+        int k = 0;
+        while (k + 1 < n && b >= start[k + 1]) ++k;
+        return k;
+    }
+};
+
+// Launch fn(table, total blocks) over `args` (blocks[i] blocks each; empty entries dropped), in as
+// few launches as kMaxGrp entries per launch allow.
+template <class A, class Fn>
+void launch_groups(const std::vector<A>& args, const std::vector<unsigned>& blocks, Fn fn) {
+    Grp<A> g{};
+    unsigned total = 0;
+    for (size_t i = 0; i < args.size(); ++i) {
+        if (blocks[i] == 0) continue;
+        if (blocks[i] > 0x7fffffffu - total) throw InvalidArgument("grouped launch: too many blocks");
+        g.start[g.n] = total;
+        g.a[g.n] = args[i];
+        total += blocks[i];
+        g.start[++g.n] = total;
+        if (g.n == kMaxGrp) {
+            fn(g, total);
+            g = Grp<A>{};
+            total = 0;
+        }
+    }
+    if (g.n) fn(g, total);
 }
 
 // Two timing events, destroyed on every exit path (a failed second creation frees the first).

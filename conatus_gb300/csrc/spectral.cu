@@ -107,11 +107,24 @@ TwiddleCache<R>& twiddles() {
 // Chebyshev transforms of contiguous complex columns (Makhoul; conventions of the reference's
 // reference/transforms.py:117-121,158-164: Gauss nodes t_j = -cos(pi (j + 1/2) / M)).
 
-// backward: c[0..N) -> f[0..M): f_j = sum_n c_n T_n(t_j).
+// Arguments of one Chebyshev transform launch (a grouped launch holds one set per problem).
 template <class R>
-__global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
-                           FftPlan plan, int B, const c2<R>* __restrict__ tw_g,
-                           const c2<R>* __restrict__ tq_g) {
+struct ChebArgs {
+    const c2<R>* in;
+    c2<R>* out;
+    long long ncols;
+    int N;
+    FftPlan plan;
+    int B;
+    const c2<R>* tw;
+    const c2<R>* tq;
+};
+
+// backward: c[0..N) -> f[0..M): f_j = sum_n c_n T_n(t_j). Block `bid` takes columns bid B ...
+template <class R>
+__device__ __forceinline__ void cheb_bwd_body(unsigned bid, const c2<R>* __restrict__ in, c2<R>* __restrict__ out,
+                                              long long ncols, int N, const FftPlan& plan, int B,
+                                              const c2<R>* __restrict__ tw_g, const c2<R>* __restrict__ tq_g) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int M = plan.L;
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -125,7 +138,7 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         tw[q] = tw_g[q];
         tq[q] = tq_g[q];
     }
-    const long long col0 = (long long)blockIdx.x * B;
+    const long long col0 = (long long)bid * B;
     for (int e = tid; e < B * (M + 1); e += nt) {
         const int t = dM1.div(e), k = e - t * (M + 1);
         const long long col = col0 + t;
@@ -161,11 +174,25 @@ __global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     }
 }
 
-// forward: f[0..M) -> c[0..N): c_k = (2/M) sum_j f_j T_k(t_j), halved at k = 0 (DCT-II / M).
 template <class R>
-__global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
+__global__ void k_cheb_bwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
                            FftPlan plan, int B, const c2<R>* __restrict__ tw_g,
                            const c2<R>* __restrict__ tq_g) {
+    cheb_bwd_body<R>(blockIdx.x, in, out, ncols, N, plan, B, tw_g, tq_g);
+}
+
+template <class R>
+__global__ void k_cheb_bwd_grp(const __grid_constant__ Grp<ChebArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const ChebArgs<R>& a = g.a[k];
+    cheb_bwd_body<R>(blockIdx.x - g.start[k], a.in, a.out, a.ncols, a.N, a.plan, a.B, a.tw, a.tq);
+}
+
+// forward: f[0..M) -> c[0..N): c_k = (2/M) sum_j f_j T_k(t_j), halved at k = 0 (DCT-II / M).
+template <class R>
+__device__ __forceinline__ void cheb_fwd_body(unsigned bid, const c2<R>* __restrict__ in, c2<R>* __restrict__ out,
+                                              long long ncols, int N, const FftPlan& plan, int B,
+                                              const c2<R>* __restrict__ tw_g, const c2<R>* __restrict__ tq_g) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int M = plan.L;
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -178,7 +205,7 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         tw[q] = tw_g[q];
         tq[q] = tq_g[q];
     }
-    const long long col0 = (long long)blockIdx.x * B;
+    const long long col0 = (long long)bid * B;
     // v_j = f_{2j}, v_{M-1-j} = f_{2j+1}
     for (int e = tid; e < B * M; e += nt) {
         const int t = dM.div(e), i = e - t * M;
@@ -203,6 +230,20 @@ __global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
         const R sg = k == 0 ? invMh : ((k & 1) ? -invM : invM);
         out[col * N + k] = mk<R>(re * sg, im * sg);
     }
+}
+
+template <class R>
+__global__ void k_cheb_fwd(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long ncols, int N,
+                           FftPlan plan, int B, const c2<R>* __restrict__ tw_g,
+                           const c2<R>* __restrict__ tq_g) {
+    cheb_fwd_body<R>(blockIdx.x, in, out, ncols, N, plan, B, tw_g, tq_g);
+}
+
+template <class R>
+__global__ void k_cheb_fwd_grp(const __grid_constant__ Grp<ChebArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const ChebArgs<R>& a = g.a[k];
+    cheb_fwd_body<R>(blockIdx.x - g.start[k], a.in, a.out, a.ncols, a.N, a.plan, a.B, a.tw, a.tq);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -244,9 +285,24 @@ __device__ __forceinline__ c2<R> ikmul(c2<R> w, c2<R> v) {
 // complex FFT along a strided axis: data [outer][len][inner]. Backward: compact spectrum of Nc
 // entries (fftfreq order, Nyquist entry Nc/2 ignored) -> L grid points, unnormalized inverse.
 // Forward: L points -> compact Nc (|k| < Nc/2, Nyquist set to 0), scaled 1/L.
+// Arguments of one strided-axis transform launch (complex or real; a grouped launch holds one set
+// per problem).
 template <class R>
-__global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long outer, int inner,
-                           int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g, Expand<R> ex) {
+struct AxisArgs {
+    const void* in;
+    void* out;
+    long long outer;
+    int inner, ncompact;       // ncompact: Nc (complex transform) or K (real transform)
+    FftPlan plan;
+    int B, forward;
+    const c2<R>* tw;
+    Expand<R> ex;
+};
+
+template <class R>
+__device__ __forceinline__ void fft_axis_body(unsigned bid, const c2<R>* __restrict__ in, c2<R>* __restrict__ out,
+                                              long long outer, int inner, int Nc, const FftPlan& plan, int B,
+                                              int forward, const c2<R>* __restrict__ tw_g, const Expand<R>& ex) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int L = plan.L, LS = L + 1;        // padded rows: the column-wise staging is conflict-free
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -256,8 +312,8 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     const FastDiv dB(B);
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int chunks = (inner + B - 1) / B;
-    const long long o = blockIdx.x / chunks;
-    const int i0 = (blockIdx.x - o * chunks) * B;
+    const long long o = bid / chunks;
+    const int i0 = (bid - o * chunks) * B;
     const int K = Nc / 2;
     const int lin = forward ? L : Nc;
     const int lout = forward ? Nc : L;
@@ -299,14 +355,28 @@ __global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out
     }
 }
 
+template <class R>
+__global__ void k_fft_axis(const c2<R>* __restrict__ in, c2<R>* __restrict__ out, long long outer, int inner,
+                           int Nc, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g, Expand<R> ex) {
+    fft_axis_body<R>(blockIdx.x, in, out, outer, inner, Nc, plan, B, forward, tw_g, ex);
+}
+
+template <class R>
+__global__ void k_fft_axis_grp(const __grid_constant__ Grp<AxisArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const AxisArgs<R>& a = g.a[k];
+    fft_axis_body<R>(blockIdx.x - g.start[k], static_cast<const c2<R>*>(a.in), static_cast<c2<R>*>(a.out), a.outer,
+                     a.inner, a.ncompact, a.plan, a.B, a.forward, a.tw, a.ex);
+}
+
 // Real FFT along the outer axis of [outer][len][inner]: two adjacent inner columns per complex FFT
 // (an odd last column is paired with zero). Backward (c2r): half spectrum [outer][K][inner] complex (modes 0..K-1,
 // Hermitian continuation, zero padding) -> [outer][L][inner] real, unnormalized. Forward (r2c):
 // real -> modes 0..K-1, scaled 1/L.
 template <class R>
-__global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out_, long long outer, int inner,
-                            int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g,
-                            Expand<R> ex) {
+__device__ __forceinline__ void rfft_axis_body(unsigned bid, const void* __restrict__ in_, void* __restrict__ out_,
+                                               long long outer, int inner, int K, const FftPlan& plan, int B,
+                                               int forward, const c2<R>* __restrict__ tw_g, const Expand<R>& ex) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int L = plan.L, LS = L + 1;
     c2<R>* tw = reinterpret_cast<c2<R>*>(sm);
@@ -317,8 +387,8 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     for (int q = tid; q < L; q += nt) tw[q] = tw_g[q];
     const int pairs = (inner + 1) / 2;             // an odd last column is paired with zero
     const int chunks = (pairs + B - 1) / B;
-    const long long o = blockIdx.x / chunks;
-    const int p0 = (blockIdx.x - o * chunks) * B;     // first pair
+    const long long o = bid / chunks;
+    const int p0 = (bid - o * chunks) * B;     // first pair
     if (!forward) {
         const c2<R>* wt;
         const c2<R>* src = static_cast<const c2<R>*>(in_) + expand_row<R>(ex, o, &wt) * (long long)K * inner;
@@ -386,6 +456,20 @@ __global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out
     }
 }
 
+template <class R>
+__global__ void k_rfft_axis(const void* __restrict__ in_, void* __restrict__ out_, long long outer, int inner,
+                            int K, FftPlan plan, int B, int forward, const c2<R>* __restrict__ tw_g,
+                            Expand<R> ex) {
+    rfft_axis_body<R>(blockIdx.x, in_, out_, outer, inner, K, plan, B, forward, tw_g, ex);
+}
+
+template <class R>
+__global__ void k_rfft_axis_grp(const __grid_constant__ Grp<AxisArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const AxisArgs<R>& a = g.a[k];
+    rfft_axis_body<R>(blockIdx.x - g.start[k], a.in, a.out, a.outer, a.inner, a.ncompact, a.plan, a.B, a.forward,
+                      a.tw, a.ex);
+}
 
 // ------------------------------------------------------------------------------------------------
 // F pipeline: descriptors on the device
@@ -472,12 +556,22 @@ __device__ __forceinline__ void cheb_der_warp(const c2<R>* __restrict__ c, c2<R>
     }
 }
 
+// Arguments of the per-bucket stages (unpack, pack; a grouped launch holds one set per bucket).
 template <class R>
-__global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ state, c2<R>* __restrict__ S) {
+struct BucketArgs {
+    RhsDev d;
+    BucketDev b;
+    const void* in;
+    void* out;
+};
+
+template <class R>
+__device__ __forceinline__ void unpack_body(unsigned bid, const RhsDev& d, const BucketDev& b,
+                                            const double2* __restrict__ state, c2<R>* __restrict__ S) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
-    const int m = blockIdx.x * nw + wib;
+    const int m = bid * nw + wib;
     if (m >= b.nsys) return;
     const int Ny = d.Ny;
     // the system's state, rounded once to the transform precision R
@@ -552,6 +646,18 @@ __global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ stat
     }
 }
 
+template <class R>
+__global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ state, c2<R>* __restrict__ S) {
+    unpack_body<R>(blockIdx.x, d, b, state, S);
+}
+
+template <class R>
+__global__ void k_unpack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const BucketArgs<R>& a = g.a[k];
+    unpack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const double2*>(a.in), static_cast<c2<R>*>(a.out));
+}
+
 // products on the grid: out_o = sum_m c_m prod_j G_j. The monomial tables are staged in shared
 // memory; a thread takes V consecutive points (one 16-byte load per factor field: V = 4 in FP32,
 // 2 in FP64), which needs P % V == 0 (else V = 1).
@@ -584,8 +690,18 @@ __device__ __forceinline__ void store_v(R* p, const R* v) {
     }
 }
 
+// Arguments of one products launch (a grouped launch holds one set per problem).
+template <class R>
+struct ProductArgs {
+    RhsDev d;
+    const R* G;
+    R* O;
+    long long P;
+};
+
 template <class R, int V>
-__global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
+__device__ __forceinline__ void products_body(unsigned bid, unsigned nblk, const RhsDev& d, const R* __restrict__ G,
+                                              R* __restrict__ O, long long P) {
     __shared__ int s_ptr[17];
     __shared__ R s_coef[kMaxMono];
     __shared__ int s_kind[kMaxMono];         // 1: coefficient +1, -1: coefficient -1, 0: other
@@ -601,8 +717,8 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
     for (int q = threadIdx.x; q < 4 * nm; q += blockDim.x) s_fac[q] = d.mono_fac[q];
     __syncthreads();
     const long long total = P * d.ncase;
-    for (long long t0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * V; t0 < total;
-         t0 += (long long)gridDim.x * blockDim.x * V) {
+    for (long long t0 = ((long long)bid * blockDim.x + threadIdx.x) * V; t0 < total;
+         t0 += (long long)nblk * blockDim.x * V) {
         const long long c = t0 / P, p = t0 - c * P;
         const R* Gc = G + c * d.nfactors * P + p;
         R* Oc = O + c * no * P + p;
@@ -665,14 +781,27 @@ __global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O,
     }
 }
 
+template <class R, int V>
+__global__ void k_products(RhsDev d, const R* __restrict__ G, R* __restrict__ O, long long P) {
+    products_body<R, V>(blockIdx.x, gridDim.x, d, G, O, P);
+}
+
+template <class R, int V>
+__global__ void k_products_grp(const __grid_constant__ Grp<ProductArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const ProductArgs<R>& a = g.a[k];
+    products_body<R, V>(blockIdx.x - g.start[k], g.start[k + 1] - g.start[k], a.d, a.G, a.O, a.P);
+}
+
 // one warp per system: output spectra -> rows (C^(lambda) conversion, 2^d_act, real buckets real)
 template <class R>
-__global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, double2* __restrict__ rows) {
+__device__ __forceinline__ void pack_body(unsigned bid, const RhsDev& d, const BucketDev& b,
+                                          const c2<R>* __restrict__ H, double2* __restrict__ rows) {
     // the system's output spectra are staged in shared memory (coalesced), then gathered by row
     extern __shared__ __align__(16) unsigned char sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
-    const int m = blockIdx.x * nw + wib;
+    const int m = bid * nw + wib;
     if (m >= b.nsys) return;
     const int Ny = d.Ny;
     const int jx = b.modes[2 * m], jz = b.modes[2 * m + 1];
@@ -724,12 +853,42 @@ __global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, doubl
     }
 }
 
+template <class R>
+__global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, double2* __restrict__ rows) {
+    pack_body<R>(blockIdx.x, d, b, H, rows);
+}
+
+template <class R>
+__global__ void k_pack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
+    const int k = g.find(blockIdx.x);
+    const BucketArgs<R>& a = g.a[k];
+    pack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const c2<R>*>(a.in), static_cast<double2*>(a.out));
+}
+
 // constant part of F: rows[idx] += value
-__global__ void k_add_sparse(double2* rows, const long long* idx, const double2* val, long long n) {
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void add_sparse_body(unsigned bid, unsigned nblk, double2* rows, const long long* idx,
+                                                const double2* val, long long n) {
+    for (long long q = (long long)bid * blockDim.x + threadIdx.x; q < n; q += (long long)nblk * blockDim.x) {
         double2 r = rows[idx[q]];
         rows[idx[q]] = make_double2(r.x + val[q].x, r.y + val[q].y);
     }
+}
+
+__global__ void k_add_sparse(double2* rows, const long long* idx, const double2* val, long long n) {
+    add_sparse_body(blockIdx.x, gridDim.x, rows, idx, val, n);
+}
+
+struct SparseArgs {
+    double2* rows;
+    const long long* idx;
+    const double2* val;
+    long long n;
+};
+
+__global__ void k_add_sparse_grp(const __grid_constant__ Grp<SparseArgs> g) {
+    const int k = g.find(blockIdx.x);
+    const SparseArgs& a = g.a[k];
+    add_sparse_body(blockIdx.x - g.start[k], g.start[k + 1] - g.start[k], a.rows, a.idx, a.val, a.n);
 }
 
 template <class R>
@@ -770,6 +929,40 @@ static int pick_B(int L, int extra_per_col, int maxB) {
     return std::max(1, std::min(B, maxB));
 }
 
+// A transform launch's arguments with its dynamic shared memory and block count.
+template <class A>
+struct Planned {
+    A a;
+    size_t smem = 0;
+    unsigned blocks = 0;
+};
+
+template <class R>
+static Planned<ChebArgs<R>> plan_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward,
+                                      int maxseq) {
+    if (M % 2) throw InvalidArgument("Chebyshev grid size must be even");
+    Planned<ChebArgs<R>> p;
+    const int B = pick_B<R>(M, forward ? 0 : M + 1, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
+    p.a = ChebArgs<R>{in, out, ncols, N, make_plan(M), B, twiddles<R>().get(M, 0),
+                      twiddles<R>().get(M, forward ? 1 : 2)};
+    p.smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
+    p.blocks = (unsigned)((ncols + B - 1) / B);
+    return p;
+}
+
+// complex (real = false) or real (real = true) transform along the strided axis
+template <class R>
+static Planned<AxisArgs<R>> plan_axis(bool real, const void* in, void* out, long long outer, int inner, int ncompact,
+                                      int L, bool forward, int maxseq, const Expand<R>& ex) {
+    Planned<AxisArgs<R>> p;
+    const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
+    p.a = AxisArgs<R>{in, out, outer, inner, ncompact, make_plan(L), B, forward ? 1 : 0, twiddles<R>().get(L, 0), ex};
+    p.smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
+    const long long cols = real ? (inner + 1) / 2 : inner;
+    p.blocks = (unsigned)(outer * ((cols + B - 1) / B));
+    return p;
+}
+
 template <class R>
 void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, bool forward, cudaStream_t st,
                  int maxseq = 0, int threads = 0) {
@@ -779,17 +972,12 @@ void launch_cheb(const c2<R>* in, c2<R>* out, long long ncols, int N, int M, boo
         CNG_CUDA(cudaMemcpyAsync(out, in, sizeof(c2<R>) * (size_t)ncols, cudaMemcpyDeviceToDevice, st));
         return;
     }
-        set_smem_attr<R>((const void*)k_cheb_bwd<R>);
+    set_smem_attr<R>((const void*)k_cheb_bwd<R>);
     set_smem_attr<R>((const void*)k_cheb_fwd<R>);
-    if (M % 2) throw InvalidArgument("Chebyshev grid size must be even");
-    FftPlan plan = make_plan(M);
-    const c2<R>* tw = twiddles<R>().get(M, 0);
-    const c2<R>* tq = twiddles<R>().get(M, forward ? 1 : 2);
-    const int B = pick_B<R>(M, forward ? 0 : M + 1, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
-    const size_t smem = sizeof(c2<R>) * ((size_t)2 * M + (size_t)B * (2 * M + (forward ? 0 : M + 1)));
-    const long long blocks = (ncols + B - 1) / B;
-    if (forward) k_cheb_fwd<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
-    else k_cheb_bwd<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, ncols, N, plan, B, tw, tq);
+    const auto p = plan_cheb<R>(in, out, ncols, N, M, forward, maxseq);
+    const ChebArgs<R>& a = p.a;
+    if (forward) k_cheb_fwd<R><<<p.blocks, threads, p.smem, st>>>(a.in, a.out, a.ncols, a.N, a.plan, a.B, a.tw, a.tq);
+    else k_cheb_bwd<R><<<p.blocks, threads, p.smem, st>>>(a.in, a.out, a.ncols, a.N, a.plan, a.B, a.tw, a.tq);
     CNG_LAUNCH("k_cheb");
 }
 
@@ -798,13 +986,10 @@ void launch_fft_axis(const c2<R>* in, c2<R>* out, long long outer, int inner, in
                      cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
-        set_smem_attr<R>((const void*)k_fft_axis<R>);
-    FftPlan plan = make_plan(L);
-    const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
-    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
-    const long long blocks = outer * ((inner + B - 1) / B);
-    k_fft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, Nc, plan, B, forward ? 1 : 0, tw, ex);
+    set_smem_attr<R>((const void*)k_fft_axis<R>);
+    const auto p = plan_axis<R>(false, in, out, outer, inner, Nc, L, forward, maxseq, ex);
+    k_fft_axis<R><<<p.blocks, threads, p.smem, st>>>(in, out, outer, inner, Nc, p.a.plan, p.a.B, p.a.forward,
+                                                      p.a.tw, ex);
     CNG_LAUNCH("k_fft_axis");
 }
 
@@ -813,14 +998,30 @@ void launch_rfft_axis(const void* in, void* out, long long outer, int inner, int
                       cudaStream_t st, int maxseq = 0, int threads = 0, Expand<R> ex = Expand<R>{}) {
     if (threads <= 0) threads = kFftThreads;
     if (outer <= 0 || inner <= 0) return;
-        set_smem_attr<R>((const void*)k_rfft_axis<R>);
-    FftPlan plan = make_plan(L);
-    const c2<R>* tw = twiddles<R>().get(L, 0);
-    const int B = pick_B<R>(L + 1, 0, maxseq > 0 ? maxseq : (sizeof(R) == 4 ? kMaxSeq32 : kMaxSeq64));
-    const size_t smem = sizeof(c2<R>) * ((size_t)L + (size_t)B * 2 * (L + 1));
-    const long long blocks = outer * (((inner + 1) / 2 + B - 1) / B);
-    k_rfft_axis<R><<<(unsigned)blocks, threads, smem, st>>>(in, out, outer, inner, K, plan, B, forward ? 1 : 0, tw, ex);
+    set_smem_attr<R>((const void*)k_rfft_axis<R>);
+    const auto p = plan_axis<R>(true, in, out, outer, inner, K, L, forward, maxseq, ex);
+    k_rfft_axis<R><<<p.blocks, threads, p.smem, st>>>(in, out, outer, inner, K, p.a.plan, p.a.B, p.a.forward,
+                                                       p.a.tw, ex);
     CNG_LAUNCH("k_rfft_axis");
+}
+
+// Grouped launches of planned stages: one launch per kMaxGrp argument sets, dynamic shared memory
+// the largest of the group's.
+template <class A, class Kernel>
+static void launch_planned(const std::vector<Planned<A>>& ps, Kernel kernel, int threads, cudaStream_t st,
+                           const char* what) {
+    std::vector<A> args;
+    std::vector<unsigned> blocks;
+    size_t smem = 0;
+    for (const auto& p : ps) {
+        args.push_back(p.a);
+        blocks.push_back(p.blocks);
+        if (p.blocks) smem = std::max(smem, p.smem);
+    }
+    launch_groups(args, blocks, [&](const Grp<A>& g, unsigned total) {
+        kernel<<<total, threads, smem, st>>>(g);
+        CNG_LAUNCH(what);
+    });
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -976,6 +1177,166 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     if (nb0) {
         k_add_sparse<<<ceil_div(nb0, 256), 256, 0, st>>>(rows, b0_idx, b0_val, nb0);
         CNG_LAUNCH("k_add_sparse");
+    }
+}
+
+// F of several problems (templates and sizes may differ; one precision, the same Fourier
+// directions) with one launch per stage: each stage's grouped kernel runs every problem's
+// arguments over its own block range. The problems read one state and write one set of rows
+// (their bucket offsets place them in it). The arithmetic of each problem is that of Rhs::run.
+template <class R>
+void run_group(Rhs* const* hs, int n, const double2* state, double2* rows, cudaStream_t st) {
+    using C = c2<R>;
+    const int threads = hs[0]->threads > 0 ? hs[0]->threads : kFftThreads;
+    const int ndir = hs[0]->ndir;
+    for (int i = 0; i < n; ++i) {
+        if (hs[i]->ndir != ndir || hs[i]->precision != hs[0]->precision)
+            throw InvalidArgument("grouped F: every problem needs the same precision and Fourier directions");
+        if ((hs[i]->threads > 0 ? hs[i]->threads : kFftThreads) != threads)
+            throw InvalidArgument("grouped F: every problem needs the same transform block size");
+    }
+    if (ndir < 1) throw InvalidArgument("grouped F: at least one Fourier direction");
+    constexpr int nw = 4;
+    // 1. unpack
+    {
+        std::vector<BucketArgs<R>> args;
+        std::vector<unsigned> blocks;
+        size_t smem = 0;
+        for (int i = 0; i < n; ++i)
+            for (const auto& b : hs[i]->buckets) {
+                args.push_back(BucketArgs<R>{hs[i]->dev, b, state, hs[i]->S});
+                blocks.push_back((unsigned)ceil_div(b.nsys, nw));
+                if (b.nsys) smem = std::max(smem, (size_t)nw * (b.n + 2 * hs[i]->ny) * sizeof(C));
+            }
+        ensure_smem_attr((const void*)k_unpack_grp<R>, 200 * 1024);
+        launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
+            k_unpack_grp<R><<<total, 32 * nw, smem, st>>>(g);
+            CNG_LAUNCH("k_unpack_grp");
+        });
+    }
+    // the stages' buffers per problem, as Rhs::run rotates them
+    std::vector<C*> cur(n), other(n);
+    std::vector<Planned<ChebArgs<R>>> cheb;
+    for (int i = 0; i < n; ++i) {
+        const Rhs& h = *hs[i];
+        cur[i] = static_cast<C*>(h.W1);
+        other[i] = static_cast<C*>(h.W2);
+        const long long cols = h.spec_cols(h.dev.ngy * h.ncase);
+        if (h.ny == 1 && h.my == 1) throw InvalidArgument("grouped F: a Chebyshev direction is needed");
+        cheb.push_back(plan_cheb<R>(static_cast<const C*>(h.S), cur[i], cols, h.ny, h.my, false, h.maxseq));
+    }
+    set_smem_attr<R>((const void*)k_cheb_bwd_grp<R>);
+    launch_planned(cheb, k_cheb_bwd_grp<R>, threads, st, "k_cheb_bwd_grp");
+    if (ndir == 2) {
+        std::vector<Planned<AxisArgs<R>>> z;
+        for (int i = 0; i < n; ++i) {
+            const Rhs& h = *hs[i];
+            Expand<R> ez{};
+            if (h.dev.share) {
+                ez.nout = h.dev.ngz; ez.nin = h.dev.ngy; ez.per = h.Kx; ez.nidx = h.Nzc;
+                ez.src = h.dev.zg_y; ez.ord = h.dev.zg_oz; ez.tab = static_cast<const C*>(h.ktab_z);
+            }
+            z.push_back(plan_axis<R>(false, cur[i], other[i], (long long)h.dev.ngz * h.ncase * h.Kx, h.my, h.Nzc,
+                                     h.mz, false, h.maxseq, ez));
+            std::swap(cur[i], other[i]);
+        }
+        set_smem_attr<R>((const void*)k_fft_axis_grp<R>);
+        launch_planned(z, k_fft_axis_grp<R>, threads, st, "k_fft_axis_grp");
+    }
+    // x backward (c2r) with the x expansions
+    std::vector<Planned<AxisArgs<R>>> xb;
+    std::vector<R*> G(n);
+    for (int i = 0; i < n; ++i) {
+        const Rhs& h = *hs[i];
+        const long long inner = (long long)(ndir == 2 ? h.mz : 1) * h.my;
+        Expand<R> exx{};
+        if (h.dev.share) {
+            exx.nout = h.nfactors; exx.nin = h.dev.ngz; exx.per = 1; exx.nidx = h.Kx;
+            exx.src = h.dev.f_z; exx.ord = h.f_ox; exx.tab = static_cast<const C*>(h.ktab_x);
+        }
+        xb.push_back(plan_axis<R>(true, cur[i], other[i], (long long)h.nfactors * h.ncase, (int)inner, h.Kx, h.mx,
+                                  false, h.maxseq, exx));
+        G[i] = reinterpret_cast<R*>(other[i]);
+        std::swap(cur[i], other[i]);
+    }
+    set_smem_attr<R>((const void*)k_rfft_axis_grp<R>);
+    launch_planned(xb, k_rfft_axis_grp<R>, threads, st, "k_rfft_axis_grp(backward)");
+    // products
+    {
+        constexpr int VV = sizeof(R) == 4 ? 4 : 2;
+        bool vec = true;
+        for (int i = 0; i < n; ++i) vec = vec && hs[i]->grid_points() % VV == 0;
+        std::vector<ProductArgs<R>> args;
+        std::vector<unsigned> blocks;
+        for (int i = 0; i < n; ++i) {
+            const Rhs& h = *hs[i];
+            const long long P = h.grid_points();
+            args.push_back(ProductArgs<R>{h.dev, G[i], reinterpret_cast<R*>(other[i]), P});
+            const long long per = vec ? P * h.ncase / VV : P * h.ncase;
+            blocks.push_back((unsigned)std::min<long long>((per + 255) / 256, 152LL * 16));
+            std::swap(cur[i], other[i]);       // cur = the products
+        }
+        launch_groups(args, blocks, [&](const Grp<ProductArgs<R>>& g, unsigned total) {
+            if (vec) k_products_grp<R, VV><<<total, 256, 0, st>>>(g);
+            else k_products_grp<R, 1><<<total, 256, 0, st>>>(g);
+            CNG_LAUNCH("k_products_grp");
+        });
+    }
+    // x forward (r2c)
+    std::vector<Planned<AxisArgs<R>>> xf;
+    for (int i = 0; i < n; ++i) {
+        const Rhs& h = *hs[i];
+        const long long inner = (long long)(ndir == 2 ? h.mz : 1) * h.my;
+        xf.push_back(plan_axis<R>(true, cur[i], other[i], (long long)h.noutputs * h.ncase, (int)inner, h.Kx, h.mx,
+                                  true, h.maxseq, Expand<R>{}));
+        std::swap(cur[i], other[i]);
+    }
+    launch_planned(xf, k_rfft_axis_grp<R>, threads, st, "k_rfft_axis_grp(forward)");
+    if (ndir == 2) {
+        std::vector<Planned<AxisArgs<R>>> z;
+        for (int i = 0; i < n; ++i) {
+            const Rhs& h = *hs[i];
+            z.push_back(plan_axis<R>(false, cur[i], other[i], (long long)h.noutputs * h.ncase * h.Kx, h.my, h.Nzc,
+                                     h.mz, true, h.maxseq, Expand<R>{}));
+            std::swap(cur[i], other[i]);
+        }
+        launch_planned(z, k_fft_axis_grp<R>, threads, st, "k_fft_axis_grp(forward)");
+    }
+    // Chebyshev forward into S
+    cheb.clear();
+    for (int i = 0; i < n; ++i) {
+        const Rhs& h = *hs[i];
+        cheb.push_back(plan_cheb<R>(cur[i], static_cast<C*>(h.S), h.spec_cols(h.noutputs * h.ncase), h.ny, h.my,
+                                    true, h.maxseq));
+    }
+    set_smem_attr<R>((const void*)k_cheb_fwd_grp<R>);
+    launch_planned(cheb, k_cheb_fwd_grp<R>, threads, st, "k_cheb_fwd_grp");
+    // pack and the constant parts
+    {
+        std::vector<BucketArgs<R>> args;
+        std::vector<unsigned> blocks;
+        size_t smem = 0;
+        for (int i = 0; i < n; ++i)
+            for (const auto& b : hs[i]->buckets) {
+                args.push_back(BucketArgs<R>{hs[i]->dev, b, hs[i]->S, rows});
+                blocks.push_back((unsigned)ceil_div(b.nsys, nw));
+                if (b.nsys) smem = std::max(smem, (size_t)nw * hs[i]->noutputs * hs[i]->ny * sizeof(double2));
+            }
+        ensure_smem_attr((const void*)k_pack_grp<R>, 200 * 1024);
+        launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
+            k_pack_grp<R><<<total, 32 * nw, smem, st>>>(g);
+            CNG_LAUNCH("k_pack_grp");
+        });
+        std::vector<SparseArgs> sp;
+        std::vector<unsigned> sb;
+        for (int i = 0; i < n; ++i) {
+            sp.push_back(SparseArgs{rows, hs[i]->b0_idx, hs[i]->b0_val, hs[i]->nb0});
+            sb.push_back((unsigned)ceil_div(hs[i]->nb0, 256));
+        }
+        launch_groups(sp, sb, [&](const Grp<SparseArgs>& g, unsigned total) {
+            k_add_sparse_grp<<<total, 256, 0, st>>>(g);
+            CNG_LAUNCH("k_add_sparse_grp");
+        });
     }
 }
 
@@ -1206,6 +1567,26 @@ int cng_rhs_evaluate(cng_rhs* hh, const void* state, void* rows, void* stream) {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         if (h->precision == 0) h->run<double>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
         else h->run<float>(static_cast<const double2*>(state), static_cast<double2*>(rows), st);
+    })
+}
+
+int cng_rhs_evaluate_group(int n, cng_rhs* const* hh, const void* state, void* rows, void* stream) {
+    CNG_TRY({
+        if (n <= 0 || !hh) throw InvalidArgument("grouped F: no handles");
+        if (!state || !rows) throw InvalidArgument("null device pointer");
+        if (state == rows) throw InvalidArgument("state and rows must not alias");
+        std::vector<Rhs*> hs(n);
+        for (int i = 0; i < n; ++i) {
+            hs[i] = reinterpret_cast<Rhs*>(hh[i]);
+            if (!hs[i]) throw InvalidArgument("null RHS handle");
+            for (int j = 0; j < i; ++j)
+                if (hs[j] == hs[i]) throw InvalidArgument("grouped F: a handle appears twice (shared work buffers)");
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const double2* s = static_cast<const double2*>(state);
+        double2* r = static_cast<double2*>(rows);
+        if (hs[0]->precision == 0) run_group<double>(hs.data(), n, s, r, st);
+        else run_group<float>(hs.data(), n, s, r, st);
     })
 }
 

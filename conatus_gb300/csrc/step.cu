@@ -31,15 +31,16 @@ __global__ void k_csr_matvec(int nsys, int n, const int* __restrict__ ip, const 
 // y = M x with real M values (M of the tau systems is real: conversions between Chebyshev and
 // ultraspherical bases). A warp takes one row i for 32 systems (lane = system): uniform trip
 // counts across the warp, the row's entries as broadcast loads, x gathered per lane.
-__global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
-                                  const double* __restrict__ val, const double2* __restrict__ x,
-                                  double2* __restrict__ y) {
+__device__ __forceinline__ void csr_matvec_real_body(unsigned bid, unsigned nblk, int nsys, int n,
+                                                     const int* __restrict__ ip, const int* __restrict__ ix,
+                                                     const double* __restrict__ val, const double2* __restrict__ x,
+                                                     double2* __restrict__ y) {
     // one thread per (system, row), rows fastest: a warp reads a contiguous stretch of one
     // system's vector (the band around its rows) and writes 32 consecutive rows; the row pattern
     // and values, shared by every system, stay in L1
     const unsigned total = (unsigned)nsys * (unsigned)n;
-    const unsigned stride = gridDim.x * blockDim.x;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const unsigned stride = nblk * blockDim.x;
+    for (unsigned t = bid * blockDim.x + threadIdx.x; t < total; t += stride) {
         const unsigned m = t / (unsigned)n;
         const int i = (int)(t - m * (unsigned)n);
         const double2* xm = x + (size_t)m * n;
@@ -53,6 +54,19 @@ __global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, c
         }
         y[t] = make_double2(ar[0] + ar[1], ai[0] + ai[1]);
     }
+}
+
+__global__ void k_csr_matvec_real(int nsys, int n, const int* __restrict__ ip, const int* __restrict__ ix,
+                                  const double* __restrict__ val, const double2* __restrict__ x,
+                                  double2* __restrict__ y) {
+    csr_matvec_real_body(blockIdx.x, gridDim.x, nsys, n, ip, ix, val, x, y);
+}
+
+__global__ void k_csr_matvec_real_grp(const __grid_constant__ Grp<cng_matvec_part> g) {
+    const int k = g.find(blockIdx.x);
+    const cng_matvec_part& a = g.a[k];
+    csr_matvec_real_body(blockIdx.x - g.start[k], g.start[k + 1] - g.start[k], a.nsys, a.n, a.indptr, a.indices,
+                         a.values, static_cast<const double2*>(a.x), static_cast<double2*>(a.y));
 }
 
 struct SbdfArgs {
@@ -170,21 +184,22 @@ __global__ void k_poly_residual(int nsys, int n, const int* __restrict__ ip, con
 // a dozen) and the entry data is one broadcast load per warp; x is gathered per lane.
 constexpr int kMergedTerm = 63;          // an entry list shared by several terms: scale per (row, system)
 
-template <bool CONE>
 // Systems s0 .. s0 + cnt - 1 of a bucket of ld systems (rowscale and xT are [n][ld]).
-__global__ void k_split_residual(int cnt, int s0, int ld, int n, const int* __restrict__ ptr,
-                                 const int* __restrict__ col,
-                                 const double* __restrict__ val, const signed char* __restrict__ code,
-                                 const double* __restrict__ mono, int nmono, double a, double c,
-                                 const double* __restrict__ rowscale, const double2* __restrict__ x,
-                                 const double2* __restrict__ xT, const double2* __restrict__ b,
-                                 double2* __restrict__ r) {
+template <bool CONE>
+__device__ __forceinline__ void split_residual_body(unsigned bid, unsigned nblk, int cnt, int s0, int ld, int n,
+                                                    const int* __restrict__ ptr, const int* __restrict__ col,
+                                                    const double* __restrict__ val,
+                                                    const signed char* __restrict__ code,
+                                                    const double* __restrict__ mono, int nmono, double a, double c,
+                                                    const double* __restrict__ rowscale,
+                                                    const double2* __restrict__ x, const double2* __restrict__ xT,
+                                                    const double2* __restrict__ b, double2* __restrict__ r) {
     const int nsys = ld;
     const unsigned sysw = ((unsigned)cnt + 31u) >> 5;              // warps of 32 systems per row
     const unsigned nwarps = sysw * (unsigned)n;
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned wstride = (gridDim.x * blockDim.x) >> 5;
-    for (unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
+    const unsigned wstride = (nblk * blockDim.x) >> 5;
+    for (unsigned w = (bid * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
         const int i = (int)(w / sysw);
         const unsigned ml = (w - (unsigned)i * sysw) * 32u + lane;
         if (ml >= (unsigned)cnt) continue;
@@ -231,6 +246,28 @@ __global__ void k_split_residual(int cnt, int s0, int ld, int n, const int* __re
     }
 }
 
+template <bool CONE>
+__global__ void k_split_residual(int cnt, int s0, int ld, int n, const int* __restrict__ ptr,
+                                 const int* __restrict__ col,
+                                 const double* __restrict__ val, const signed char* __restrict__ code,
+                                 const double* __restrict__ mono, int nmono, double a, double c,
+                                 const double* __restrict__ rowscale, const double2* __restrict__ x,
+                                 const double2* __restrict__ xT, const double2* __restrict__ b,
+                                 double2* __restrict__ r) {
+    split_residual_body<CONE>(blockIdx.x, gridDim.x, cnt, s0, ld, n, ptr, col, val, code, mono, nmono, a, c,
+                              rowscale, x, xT, b, r);
+}
+
+template <bool CONE>
+__global__ void k_split_residual_grp(const __grid_constant__ Grp<cng_residual_part> g, double a, double c) {
+    const int k = g.find(blockIdx.x);
+    const cng_residual_part& p = g.a[k];
+    split_residual_body<CONE>(blockIdx.x - g.start[k], g.start[k + 1] - g.start[k], p.s1 - p.s0, p.s0, p.nsys, p.n,
+                              p.ptr, p.col, p.val, reinterpret_cast<const signed char*>(p.code), p.mono, p.nmono, a, c,
+                              p.rowscale, static_cast<const double2*>(p.x), static_cast<const double2*>(p.xT),
+                              static_cast<const double2*>(p.b), static_cast<double2*>(p.r));
+}
+
 }  // namespace cng
 
 using namespace cng;
@@ -264,6 +301,55 @@ int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* i
         k_csr_matvec_real<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
             nsys, n, indptr, indices, values, static_cast<const double2*>(x), static_cast<double2*>(y));
         CNG_LAUNCH("k_csr_matvec_real");
+    })
+}
+
+int cng_csr_matvec_real_group(int nparts, const cng_matvec_part* parts, void* stream) {
+    CNG_TRY({
+        if (nparts < 0 || (nparts > 0 && !parts)) throw InvalidArgument("null argument");
+        std::vector<cng_matvec_part> args;
+        std::vector<unsigned> blocks;
+        for (int k = 0; k < nparts; ++k) {
+            const cng_matvec_part& p = parts[k];
+            if (!p.indptr || !p.indices || !p.values || !p.x || !p.y) throw InvalidArgument("null device pointer");
+            if (p.x == p.y) throw InvalidArgument("x and y must not alias");
+            if (p.nsys < 0 || p.n < 0) throw InvalidArgument("csr_matvec_real: negative size");
+            const long long threads = (long long)p.nsys * p.n;
+            if (threads >= (1LL << 32) - (1LL << 24)) throw InvalidArgument("csr_matvec_real: batch too large");
+            args.push_back(p);
+            blocks.push_back((unsigned)std::min<long long>((threads + 255) / 256, 152LL * 64));
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        launch_groups(args, blocks, [&](const Grp<cng_matvec_part>& g, unsigned total) {
+            k_csr_matvec_real_grp<<<total, 256, 0, st>>>(g);
+            CNG_LAUNCH("k_csr_matvec_real_grp");
+        });
+    })
+}
+
+int cng_split_residual_group(int nparts, const cng_residual_part* parts, double a, double c, void* stream) {
+    CNG_TRY({
+        if (nparts < 0 || (nparts > 0 && !parts)) throw InvalidArgument("null argument");
+        std::vector<cng_residual_part> args;
+        std::vector<unsigned> blocks;
+        for (int k = 0; k < nparts; ++k) {
+            const cng_residual_part& p = parts[k];
+            if (!p.ptr || !p.col || !p.val || !p.code || (p.nmono > 0 && !p.mono) || !p.x || !p.b || !p.r)
+                throw InvalidArgument("null device pointer");
+            if (p.r == p.x || p.r == p.b) throw InvalidArgument("r must not alias x or b");
+            if (p.s0 < 0 || p.s1 > p.nsys || p.s0 > p.s1 || p.n < 0)
+                throw InvalidArgument("split_residual: system range outside the batch");
+            const long long w = (long long)((p.s1 - p.s0 + 31) / 32) * p.n;
+            if (w >= (1LL << 31)) throw InvalidArgument("split_residual: batch too large");
+            args.push_back(p);
+            blocks.push_back((unsigned)std::min<long long>((w * 32 + 255) / 256, 152LL * 64));
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        launch_groups(args, blocks, [&](const Grp<cng_residual_part>& g, unsigned total) {
+            if (c == 1.0) k_split_residual_grp<true><<<total, 256, 0, st>>>(g, a, c);
+            else k_split_residual_grp<false><<<total, 256, 0, st>>>(g, a, c);
+            CNG_LAUNCH("k_split_residual_grp");
+        });
     })
 }
 

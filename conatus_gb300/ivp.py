@@ -164,7 +164,22 @@ class DeviceProblem:
 
     # ------------------------------------------------------------------ F
     def _build_rhs(self):
-        tpl, P = self.tpl, self.P
+        """The F evaluator: one handle, or one per group of a GroupedProblem (each placed at its
+        buckets' offsets in the joint layout, evaluated together by cng_rhs_evaluate_group)."""
+        P = self.P
+        parts = getattr(P, "parts", None)
+        self._has_b0 = []
+        if parts is None:
+            self._rhs_all = [self._make_rhs(P, self.offsets)]
+        else:
+            self._rhs_all = [self._make_rhs(p, [self.offsets[k] for k in P.group_buckets[g]])
+                             for g, p in enumerate(parts)]
+        self._rhs = self._rhs_all[0]
+        self._rhs_arr = (ctypes.c_void_p * len(self._rhs_all))(*[h.value for h in self._rhs_all])
+        self.has_b0 = any(self._has_b0)
+
+    def _make_rhs(self, P, offsets):
+        tpl = P.tpl
         d = self.d
         ax = tpl.axes
         fa = tpl.fourier_axes
@@ -193,7 +208,8 @@ class DeviceProblem:
             desc.ly = ax[ca]["L"]
         else:
             desc.ny, desc.my, desc.ly = 1, 1, 1.0
-        self.grid = dict(mx=desc.mx, mz=desc.mz, my=desc.my)
+        if not self._has_b0:               # the first (or only) problem's grids
+            self.grid = dict(mx=desc.mx, mz=desc.mz, my=desc.my)
 
         def axis_orders(orders):
             ox = orders[fa[0]] if d >= 1 else 0
@@ -256,7 +272,7 @@ class DeviceProblem:
                     rm[i] = (-1, 0)
             row_p.append(arr(rm, np.int32))
         desc.buckets = arr(bd, np.int32)
-        desc.bucket_offset = arr(self.offsets, np.int64)
+        desc.bucket_offset = arr(offsets, np.int64)
         ptrs = [(ctypes.c_void_p * nb)(*modes_p), (ctypes.c_void_p * nb)(*col_p), (ctypes.c_void_p * nb)(*row_p)]
         keep.extend(ptrs)
         desc.modes, desc.colpos, desc.rowmap = (ctypes.cast(p, ctypes.c_void_p).value for p in ptrs)
@@ -276,24 +292,67 @@ class DeviceProblem:
         for bi, B0 in enumerate(b0):
             m, i = np.nonzero(B0)
             for mm, ii in zip(m, i):
-                idx.append(self.offsets[bi] + mm * tpl.buckets[bi].n + ii)
+                idx.append(offsets[bi] + mm * tpl.buckets[bi].n + ii)
                 val.append([B0[mm, ii].real, B0[mm, ii].imag])
         desc.nb0 = len(idx)
-        self.has_b0 = len(idx) > 0
+        self._has_b0.append(len(idx) > 0)
         desc.b0_index = arr(idx if idx else [0], np.int64)
         desc.b0_value = arr(val if val else [[0.0, 0.0]], np.float64)
         h = ctypes.c_void_p()
         call("cng_rhs_create", ctypes.byref(desc), ctypes.byref(h))
-        self._rhs = h
+        return h
 
     def F(self, X, out, stream=None) -> None:
-        """out = F(X) (mode layout, complex128 device tensors)."""
-        call("cng_rhs_evaluate", self._rhs, X.data_ptr(), out.data_ptr(), _stream_handle(stream))
+        """out = F(X) (mode layout, complex128 device tensors); a GroupedProblem's groups in one
+        launch per stage."""
+        if len(self._rhs_all) == 1:
+            call("cng_rhs_evaluate", self._rhs, X.data_ptr(), out.data_ptr(), _stream_handle(stream))
+        else:
+            call("cng_rhs_evaluate_group", len(self._rhs_all), self._rhs_arr, X.data_ptr(), out.data_ptr(),
+                 _stream_handle(stream))
+
+    # kernel launches of the step's pieces (the count a step reports; a grouped launch takes at
+    # most 8 argument sets)
+    _GRP = 8
+
+    def f_launches(self) -> int:
+        """Launches of one F evaluation."""
+        g8 = lambda k: -(-k // self._GRP)
+        nbk = sum(1 for ns in self.nsys if ns > 0)
+        stages = 2 + 2 + (2 if self.d >= 2 else 0) + 1        # Chebyshev, x (or real parts), z, products
+        if len(self._rhs_all) == 1:
+            return 2 * nbk + stages + (1 if self.has_b0 else 0)
+        ng = len(self._rhs_all)
+        return 2 * g8(nbk) + stages * g8(ng) + g8(sum(self._has_b0))
+
+    def mx_launches(self) -> int:
+        """Launches of one M X."""
+        real = [len(self._M[bi]) == 4 for bi in range(len(self.nsys))]
+        return -(-sum(1 for r, ns in zip(real, self.nsys) if r and ns > 0) // self._GRP) + \
+            sum(1 for r, ns in zip(real, self.nsys) if not r and ns > 0)
+
+    def residual_launches(self, parts=None) -> int:
+        """Launches of one residual() over ``parts`` (default: every bucket): one grouped launch for
+        the split-form parts (per 8 of them), one per system for the others."""
+        if parts is None:
+            parts = [(bi, 0, ns) for bi, ns in enumerate(self.nsys)]
+        nsplit, nvals = 0, 0
+        for g in parts:
+            bi, s0, s1 = (g, 0, self.nsys[g]) if isinstance(g, (int, np.integer)) else tuple(g)
+            r = self._resid[bi]
+            if r is not None and r[0] == "values":
+                nvals += s1 - s0
+            elif s1 > s0:
+                nsplit += 1
+        return -(-nsplit // self._GRP) + nvals
 
     def workspace_bytes(self) -> int:
-        v = ctypes.c_uint64()
-        call("cng_rhs_workspace_bytes", self._rhs, ctypes.byref(v))
-        return int(v.value)
+        tot = 0
+        for h in self._rhs_all:
+            v = ctypes.c_uint64()
+            call("cng_rhs_workspace_bytes", h, ctypes.byref(v))
+            tot += int(v.value)
+        return tot
 
     # ------------------------------------------------------------------ linear algebra
     def bucket(self, X, bi):
@@ -302,13 +361,20 @@ class DeviceProblem:
         return X[o:o + self.nsys[bi] * b.n]
 
     def MX(self, X, out, stream=None) -> None:
+        """out = M X per bucket: the buckets with one real M (shared by their systems) in one
+        grouped launch, the others one launch each."""
         s = _stream_handle(stream)
+        real = [bi for bi in range(len(self.nsys)) if len(self._M[bi]) == 4 and self.nsys[bi] > 0]
+        if real:
+            parts = (_lib.MatvecPart * len(real))()
+            for k, bi in enumerate(real):
+                _, mv, ipM, ixM = self._M[bi]
+                parts[k] = _lib.MatvecPart(self.nsys[bi], self.tpl.buckets[bi].n, ipM.data_ptr(), ixM.data_ptr(),
+                                           mv.data_ptr(), self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr())
+            call("cng_csr_matvec_real_group", len(real), parts, s)
         for bi, b in enumerate(self.tpl.buckets):
             ip, ix = self._pat[bi]
-            if len(self._M[bi]) == 4:                    # shared real values on M's own pattern
-                _, mv, ipM, ixM = self._M[bi]
-                call("cng_csr_matvec_real", self.nsys[bi], b.n, ipM.data_ptr(), ixM.data_ptr(), mv.data_ptr(),
-                     self.bucket(X, bi).data_ptr(), self.bucket(out, bi).data_ptr(), s)
+            if len(self._M[bi]) == 4:                    # shared real values on M's own pattern: above
                 continue
             vals, per = self._M[bi]
             call("cng_csr_matvec", self.nsys[bi], b.n, ip.data_ptr(), ix.data_ptr(), vals.data_ptr(), per,
@@ -535,17 +601,20 @@ class DeviceProblem:
             parts = [(bi, 0, ns) for bi, ns in enumerate(self.nsys)]
         else:
             parts = [(g, 0, self.nsys[g]) if isinstance(g, (int, np.integer)) else tuple(g) for g in buckets]
+        split = []                     # the split-form parts: one grouped launch
         for bi, s0, s1 in parts:
             b = self.tpl.buckets[bi]
             kind, data = self._residual_data(bi)
             xb, rb, ob = self.bucket(x, bi), self.bucket(rhs, bi), self.bucket(out, bi)
             if kind == "split":
+                if s1 <= s0:
+                    continue
                 ptr, col, val, code, mv, nm = data[:6]
                 rs = self._rowscale(bi, a, b_)
-                call("cng_split_residual_range", self.nsys[bi], int(s0), int(s1), b.n, ptr.data_ptr(), col.data_ptr(),
-                     val.data_ptr(), code.data_ptr(), mv.data_ptr(), nm, float(a), float(b_),
-                     rs.data_ptr() if rs is not None else None, xb.data_ptr(),
-                     self.bucket(xT, bi).data_ptr() if xT is not None else None, rb.data_ptr(), ob.data_ptr(), s)
+                split.append(_lib.ResidualPart(
+                    self.nsys[bi], int(s0), int(s1), b.n, ptr.data_ptr(), col.data_ptr(), val.data_ptr(),
+                    code.data_ptr(), mv.data_ptr(), nm, rs.data_ptr() if rs is not None else None, xb.data_ptr(),
+                    self.bucket(xT, bi).data_ptr() if xT is not None else None, rb.data_ptr(), ob.data_ptr()))
                 continue
             key = (float(a), float(b_))
             if key not in data:
@@ -560,6 +629,9 @@ class DeviceProblem:
                 sl = slice(m * b.n, (m + 1) * b.n)
                 call("cng_poly_residual", 1, b.n, ip.data_ptr(), ix.data_ptr(), A[m].data_ptr(), None, None, 0,
                      1.0, 0.0, xb[sl].data_ptr(), rb[sl].data_ptr(), ob[sl].data_ptr(), s)
+        if split:
+            arr = (_lib.ResidualPart * len(split))(*split)
+            call("cng_split_residual_group", len(split), arr, float(a), float(b_), s)
 
     def solve(self, a: float, b_: float, rhs, out, stream=None) -> None:
         """out = (a M + b L)^{-1} rhs per bucket (rhs and out must not alias), every bucket in one
@@ -708,12 +780,12 @@ class DeviceProblem:
         return [x[o:o + ns * b.n].reshape(ns, b.n) for o, ns, b in zip(self.offsets, self.nsys, self.tpl.buckets)]
 
     def __del__(self):
-        h = getattr(self, "_rhs", None)
-        if h is not None and h.value:
-            try:
-                _lib.lib().cng_rhs_destroy(h)
-            except Exception:
-                pass
+        for h in getattr(self, "_rhs_all", []):
+            if h is not None and h.value:
+                try:
+                    _lib.lib().cng_rhs_destroy(h)
+                except Exception:
+                    pass
 
 
 class _Partner:
@@ -1278,23 +1350,24 @@ class IVPSolver:
         residual per bucket and a second solve)."""
         dev = self.dev
         nb = len(dev.tpl.buckets)
-        d = dev.d
-        f = 2 * nb + 2 + 2 + (2 if d >= 2 else 0) + 1 + (1 if dev.has_b0 else 0)
+        f = dev.f_launches()
+        mx = dev.mx_launches()
+        lx = dev.residual_launches()                  # -L X: the residual with a = 0
         dense = bool(dev._factors) and all(getattr(h, "schedule", 0) < 0 for fs in dev._factors.values() for h in fs)
         one = (nb if dense else 1) if dev.compact else nb
-        res = nb                                      # residual launches per refinement pass
+        res = dev.residual_launches()                 # residual launches per refinement pass
         if dev.precision == "fp32" and dev.compact and not dense and dev.overlap_refine:
             groups = dev._refine_groups()
             one = len(groups)                         # one batched launch per group
-            res = sum(len(dev._with_partners(g)) for g in groups)
+            res = sum(dev.residual_launches(dev._with_partners(g)) for g in groups)
         solve = one if dev.precision == "fp64" else one + dev.refine * (one + res)
         if self.family == "sbdf":
-            return nb + f + 1 + solve
+            return mx + f + 1 + solve
         if self.family == "cn":
-            return nb + nb + f + 1 + solve
+            return mx + lx + f + 1 + solve
         A, H, c = self._rk
         S = len(c) - 1
-        return nb + sum(f for x in self._Fs if x is not None) + sum(nb for x in self._LXs if x is not None) \
+        return mx + sum(f for x in self._Fs if x is not None) + sum(lx for x in self._LXs if x is not None) \
             + S * (1 + solve) + 1
 
     def synchronize(self) -> None:

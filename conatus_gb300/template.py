@@ -453,3 +453,115 @@ class StackedProblem:
     def stack_states(self, states):
         """Per-bucket stacked arrays from the cases' mode-layout states."""
         return [np.concatenate([st[bi] for st in states]) for bi in range(len(self._nsys_case))]
+
+
+class _GroupedTemplate:
+    """The bucket list of a GroupedProblem (its groups' buckets side by side) with the template
+    attributes the device solver reads; F stays per group."""
+
+    def __init__(self, tpls):
+        t0 = tpls[0]
+        for t in tpls[1:]:
+            if (len(t.fourier_axes) != len(t0.fourier_axes) or (t.cheb_axis >= 0) != (t0.cheb_axis >= 0)
+                    or [v["name"] for v in t.variables] != [v["name"] for v in t0.variables]):
+                raise ValueError("grouped problems need the same variables and the same kinds of axes")
+        self.parts = list(tpls)
+        self.name = "+".join(t.name for t in tpls)
+        self.variables = t0.variables
+        self.fourier_axes = t0.fourier_axes
+        self.cheb_axis = t0.cheb_axis
+        self.axes = t0.axes
+        self.buckets = [b for t in tpls for b in t.buckets]
+        self.linear_params = list(t0.linear_params)
+
+    def sign_pairs(self) -> dict:
+        out, base = {}, 0
+        for t in self.parts:
+            for j, (i, dr, dc) in t.sign_pairs().items():
+                out[base + j] = (base + i, dr, dc)
+            base += len(t.buckets)
+        return out
+
+
+class GroupedProblem:
+    """Problems of different sizes (or templates with the same variables) advanced as one: their
+    buckets side by side in one mode layout, so that every kernel of a step is one launch for all
+    of them — F by grouped launches (one per stage, each problem over its own block range), M X and
+    the refinement residual by grouped launches, the solves by the batched multi-bucket launch, the
+    right-hand side and the finite-state check over the joint vector. Each problem keeps its own
+    arithmetic: a group member's trajectory is bit for bit the one it has alone. The groups are
+    typically ``StackedProblem`` ensembles of one resolution each (Rayleigh-Benard cases of several
+    Nz).
+
+    The reference batches ensemble members of one discretization only
+    (python/conatus/ensembles/batched.py:442-613)."""
+
+    def __init__(self, problems):
+        if not problems:
+            raise ValueError("at least one problem")
+        self.parts = list(problems)
+        self.tpl = _GroupedTemplate([p.tpl for p in self.parts])
+        self.bucket_of = [(g, bi) for g, p in enumerate(self.parts) for bi in range(len(p.tpl.buckets))]
+        self.group_buckets = []
+        k = 0
+        for p in self.parts:
+            nb = len(p.tpl.buckets)
+            self.group_buckets.append(list(range(k, k + nb)))
+            k += nb
+        self.modes = [self.parts[g].modes[bi] for g, bi in self.bucket_of]
+        self.offsets, off = [], 0
+        for (g, bi), b in zip(self.bucket_of, self.tpl.buckets):
+            self.offsets.append(off)
+            off += self.parts[g].nsys[bi] * b.n
+        self.n_total = off
+
+    @property
+    def nsys(self):
+        return [self.parts[g].nsys[bi] for g, bi in self.bucket_of]
+
+    @property
+    def ncase(self) -> int:
+        return sum(int(getattr(p, "ncase", 1)) for p in self.parts)
+
+    @property
+    def fourier_sizes(self):
+        return tuple(tuple(p.fourier_sizes) for p in self.parts)
+
+    def _part(self, bi):
+        g, lb = self.bucket_of[bi]
+        return self.parts[g], lb
+
+    def mono_values(self, bi: int) -> np.ndarray:
+        p, lb = self._part(bi)
+        return p.mono_values(lb)
+
+    def values(self, bi: int, which: str) -> np.ndarray:
+        p, lb = self._part(bi)
+        return p.values(lb, which)
+
+    def split_terms(self, bi: int):
+        p, lb = self._part(bi)
+        if hasattr(p, "split_terms"):
+            return p.split_terms(lb)
+        b = p.tpl.buckets[lb]
+        return [(b.Lc[t], p.mono_values(lb)[:, t]) for t in range(b.monos.shape[0]) if np.any(b.Lc[t] != 0)]
+
+    def d_active(self, bi: int) -> int:
+        p, lb = self._part(bi)
+        return p.d_active(lb)
+
+    def real_unknowns(self) -> int:
+        return sum(p.real_unknowns() for p in self.parts)
+
+    def b0_dense(self):
+        return [x for p in self.parts for x in p.b0_dense()]
+
+    def stack_states(self, states):
+        """The joint per-bucket list from one mode-layout state per group."""
+        if len(states) != len(self.parts):
+            raise ValueError("one state per group")
+        return [np.asarray(c) for st in states for c in st]
+
+    def group_state(self, C, g: int):
+        """Group g's per-bucket arrays out of the joint list."""
+        return [C[bi] for bi in self.group_buckets[g]]

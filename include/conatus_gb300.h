@@ -240,6 +240,13 @@ int cng_rhs_destroy(cng_rhs* h);
 /* rows = F(state) on the mode layout (complex128 device arrays; must not alias). Capturable.
  * Replaces IVPSolver.F (python/conatus/timestep/integrator.py:308-348). */
 int cng_rhs_evaluate(cng_rhs* h, const void* state, void* rows, void* stream);
+/* F of n problems of different sizes (or templates) in one launch per stage: every handle reads
+ * `state` and writes `rows` at its own bucket offsets (set at creation: the problems share one mode
+ * layout), with the arithmetic of cng_rhs_evaluate. The handles share one precision, the same
+ * Fourier directions (at least one), a Chebyshev direction and one transform block size; each
+ * appears once. Capturable. No reference counterpart: the reference advances ensemble members of
+ * one discretization together (python/conatus/ensembles/batched.py:442-613), one size per batch. */
+int cng_rhs_evaluate_group(int n, cng_rhs* const* h, const void* state, void* rows, void* stream);
 /* Launch shape of the evaluator's shared-memory transforms: sequences per block (0: the default, 8
  * in FP32 and 4 in FP64; at most 32) and threads per block (0: 256; else a multiple of 32 in
  * 64..512). Knobs of the autotuner (conatus_gb300.autotune); no reference counterpart. */
@@ -339,6 +346,36 @@ int cng_split_residual_range(int nsys, int s0, int s1, int n, const int32_t* ptr
  * tau systems are real). */
 int cng_csr_matvec_real(int nsys, int n, const int32_t* indptr, const int32_t* indices, const double* values,
                         const void* x, void* y, void* stream);
+
+/* Grouped forms: the buckets of several problems of different sizes in one launch, each part with
+ * the arithmetic of its single-bucket call (cng_csr_matvec_real, cng_split_residual_range with a
+ * common a and c). No reference counterpart (the reference advances one size per batch,
+ * python/conatus/ensembles/batched.py:442-613). */
+typedef struct cng_matvec_part {
+    int32_t nsys, n;
+    const int32_t* indptr;
+    const int32_t* indices;
+    const double* values;
+    const void* x;
+    void* y;
+} cng_matvec_part;
+int cng_csr_matvec_real_group(int nparts, const cng_matvec_part* parts, void* stream);
+
+typedef struct cng_residual_part {
+    int32_t nsys, s0, s1, n;
+    const int32_t* ptr;
+    const int32_t* col;
+    const double* val;
+    const int8_t* code;
+    const double* mono;
+    int32_t nmono;
+    const double* rowscale;
+    const void* x;
+    const void* xT;
+    const void* b;
+    void* r;
+} cng_residual_part;
+int cng_split_residual_group(int nparts, const cng_residual_part* parts, double a, double c, void* stream);
 
 /* out = base + sum_k (negate[k] ? -1 : +1) coef[k] vecs[k] over count complex128 entries, the terms
  * applied in order with explicit roundings (base NULL: start from 0); out may alias base. The
