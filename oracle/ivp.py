@@ -74,9 +74,15 @@ RK = _rk_tables()
 # ------------------------------------------------------------------------------------------------
 # reference transforms (reference/transforms.py:103-187), along axis 0
 
+def _workers(a):
+    """scipy.fft threads for array ``a``: the CPU baseline's WORKERS for large arrays, one for small
+    ones (starting the threads costs more than they save); None (the default) outside it."""
+    return WORKERS if (WORKERS is None or a.size >= 1 << 16) else 1
+
+
 def cheb_forward(f, N):
     M = f.shape[0]
-    y = sfft.dct(f, type=2, axis=0, workers=WORKERS) / M
+    y = sfft.dct(f, type=2, axis=0, workers=_workers(f)) / M
     y[0] /= 2
     sign = (-1.0) ** np.arange(M)
     return (y * sign.reshape((M,) + (1,) * (f.ndim - 1)))[:N]
@@ -89,18 +95,18 @@ def cheb_backward(c, M):
     y[:N] = c * sign.reshape((N,) + (1,) * (c.ndim - 1))
     y[0] *= 2
     y *= M
-    return sfft.idct(y, type=2, axis=0, workers=WORKERS)
+    return sfft.idct(y, type=2, axis=0, workers=_workers(y))
 
 
 WORKERS = None      # scipy.fft worker threads for the CPU baseline (None: NumPy's transforms)
 
 
 def _rfft(f):
-    return np.fft.rfft(f, axis=0) if WORKERS is None else sfft.rfft(f, axis=0, workers=WORKERS)
+    return np.fft.rfft(f, axis=0) if WORKERS is None else sfft.rfft(f, axis=0, workers=_workers(f))
 
 
 def _irfft(F, n):
-    return np.fft.irfft(F, n=n, axis=0) if WORKERS is None else sfft.irfft(F, n=n, axis=0, workers=WORKERS)
+    return np.fft.irfft(F, n=n, axis=0) if WORKERS is None else sfft.irfft(F, n=n, axis=0, workers=_workers(F))
 
 
 def rf_forward(f, N):
@@ -617,12 +623,13 @@ class ParallelStepper:
                 mv = self.P.mono_values(bi)[:1].astype(np.complex128) @ b.Mc
                 A = sp.csr_matrix((mv[0], b.indices, b.indptr), shape=(b.n, b.n))
                 out.append(np.asarray(C[bi] @ A.T))
-            else:
-                V = self._Mcsr[bi]
-                rows = b.coo_rows()
+            else:                                    # per-system values on the bucket's pattern:
+                V = self._Mcsr[bi]                   # row sums of the products, all systems at once
+                prod = V * C[bi][:, b.indices]
                 Y = np.zeros_like(C[bi])
-                for m in range(C[bi].shape[0]):
-                    np.add.at(Y[m], rows, V[m] * C[bi][m, b.indices])
+                full = np.diff(b.indptr) > 0
+                if prod.shape[1]:
+                    Y[:, full] = np.add.reduceat(prod, b.indptr[:-1][full], axis=1)
                 out.append(Y)
         return out
 

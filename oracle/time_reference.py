@@ -66,6 +66,9 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--threads", type=int, default=len(os.sched_getaffinity(0)))
     ap.add_argument("--f-backend", default="both", choices=["both", "evaluator", "fused"])
+    ap.add_argument("--fourier", type=int, nargs="*", default=None,
+                    help="Fourier sizes instead of the configuration's (the channel's CPU run at 192 x 192 "
+                         "needs more host memory than 64 GB)")
     args = ap.parse_args()
     if not args.ref:
         ap.error("the reference source tree is needed: pass --ref or set CONATUS_REFERENCE")
@@ -76,7 +79,14 @@ def main():
     from oracle.ref import install_compiled_core
     install_compiled_core()
     import conatus as cn
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.fourier:
+        N = list(cfg["N"]) if isinstance(cfg["N"], tuple) else [cfg["N"]]
+        if args.config == "channel":
+            N[0], N[2] = args.fourier[0], args.fourier[-1]
+        elif args.config == "rayleigh_benard":
+            N[0] = args.fourier[0]
+        cfg["N"] = tuple(N) if len(N) > 1 else N[0]
     backends = ["evaluator", "fused"] if args.f_backend == "both" else [args.f_backend]
     res = {}
     for fb in backends:
