@@ -523,38 +523,48 @@ class RKStepper:
         return X[-1]
 
 
+def _factor_batches(jobs):
+    """Factorizations (the oracle restatement of banded.hpp) of a share of every bucket's systems:
+    one batch per bucket, None where the share is empty."""
+    from .banded import BorderedBandedBatch
+    batches = []
+    for n, r, real, indptr, indices, monos_val, Mc, Lc, a, b_ in jobs:
+        if monos_val.shape[0] == 0:
+            batches.append(None)
+            continue
+        Vm = monos_val.astype(np.complex128) @ Mc
+        Vl = monos_val.astype(np.complex128) @ Lc
+        vals = a * Vm + b_ * Vl
+        if real:
+            vals = vals.real
+        mats = [(n, indptr, indices, v) for v in vals]
+        batches.append(BorderedBandedBatch(mats, list(range(r)), dtype=np.float64 if real else np.complex128))
+    return batches
+
+
+def _solve_batches(batches, rhs):
+    out = []
+    for B, b in zip(batches, rhs):
+        if B is None:
+            out.append(None)
+        elif B.sys[0].dtype == np.float64:
+            out.append(B.solve(b.real).astype(np.complex128))
+        else:
+            out.append(B.solve(b))
+    return out
+
+
 def _solve_worker(conn):
     """A worker process of ``ParallelStepper``: holds the factorizations of its share of the systems
-    of every bucket (the oracle restatement of banded.hpp) and solves them on request."""
-    from .banded import BorderedBandedBatch
+    of every bucket and solves them on request."""
     batches = []
     while True:
         msg = conn.recv()
         if msg[0] == "factor":
-            batches = []
-            for n, r, real, indptr, indices, monos_val, Mc, Lc, a, b_ in msg[1]:
-                if monos_val.shape[0] == 0:
-                    batches.append(None)
-                    continue
-                Vm = monos_val.astype(np.complex128) @ Mc
-                Vl = monos_val.astype(np.complex128) @ Lc
-                vals = a * Vm + b_ * Vl
-                if real:
-                    vals = vals.real
-                mats = [(n, indptr, indices, v) for v in vals]
-                batches.append(BorderedBandedBatch(mats, list(range(r)),
-                                                   dtype=np.float64 if real else np.complex128))
+            batches = _factor_batches(msg[1])
             conn.send("ok")
         elif msg[0] == "solve":
-            out = []
-            for B, rhs in zip(batches, msg[1]):
-                if B is None:
-                    out.append(None)
-                elif B.sys[0].dtype == np.float64:
-                    out.append(B.solve(rhs.real).astype(np.complex128))
-                else:
-                    out.append(B.solve(rhs))
-            conn.send(out)
+            conn.send(_solve_batches(batches, msg[1]))
         else:
             conn.close()
             return
@@ -563,9 +573,13 @@ def _solve_worker(conn):
 class ParallelStepper:
     """The oracle's SBDF-q step on a whole workload, timed as the CPU baseline: F (transforms on
     ``workers`` scipy.fft threads), M X, the right-hand side of ``SBDFStepper.step`` and the solves
-    of every system of every bucket, spread over ``workers`` processes (started with ``spawn``),
-    each holding the factorizations of its share (made before the timing: the reference times
-    steps after a warm-up that factors, examples/benchmarks/cases.py:27-43)."""
+    of every system of every bucket, spread over up to ``workers`` processes (started with
+    ``spawn``; at least 64 systems each, so a few dozen systems are solved in this process: the
+    messages cost more than the solves of a small share), each
+    holding the factorizations of its share (made before the timing: the reference times steps
+    after a warm-up that factors, examples/benchmarks/cases.py:27-43)."""
+
+    SYSTEMS_PER_PROCESS = 64
 
     def __init__(self, problem, order, dt, workers=None):
         import multiprocessing as mp
@@ -577,28 +591,40 @@ class ParallelStepper:
         self.order, self.dt = int(order), float(dt)
         self.workers = workers
         a0 = SBDF[self.order][0][0] / self.dt
-        ctx = mp.get_context("spawn")
-        self._procs, self._conns, self._shares = [], [], []
+        self._procs, self._conns, self._shares, self._local = [], [], [], None
         nb = len(problem.tpl.buckets)
-        bounds = [np.linspace(0, ns, workers + 1).round().astype(int) for ns in problem.nsys]
-        for w in range(workers):
-            parent, child = ctx.Pipe()
-            pr = ctx.Process(target=_solve_worker, args=(child,), daemon=True)
-            pr.start()
-            child.close()
+        nproc = max(1, min(workers, -(-sum(problem.nsys) // self.SYSTEMS_PER_PROCESS)))
+        self.processes = nproc if nproc > 1 else 0
+        bounds = [np.linspace(0, ns, nproc + 1).round().astype(int) for ns in problem.nsys]
+
+        def jobs_of(w):
             jobs, share = [], []
             for bi, b in enumerate(problem.tpl.buckets):
                 lo, hi = int(bounds[bi][w]), int(bounds[bi][w + 1])
                 mv = problem.mono_values(bi)[lo:hi]
                 jobs.append((b.n, b.r, b.kind == "real", b.indptr, b.indices, mv, b.Mc, b.Lc, a0, 1.0))
                 share.append((lo, hi))
-            parent.send(("factor", jobs))
-            self._procs.append(pr)
-            self._conns.append(parent)
+            return jobs, share
+
+        if nproc == 1:
+            jobs, share = jobs_of(0)
+            self._local = _factor_batches(jobs)
             self._shares.append(share)
-        for c in self._conns:
-            if c.recv() != "ok":
-                raise RuntimeError("oracle worker failed to factor")
+        else:
+            ctx = mp.get_context("spawn")
+            for w in range(nproc):
+                parent, child = ctx.Pipe()
+                pr = ctx.Process(target=_solve_worker, args=(child,), daemon=True)
+                pr.start()
+                child.close()
+                jobs, share = jobs_of(w)
+                parent.send(("factor", jobs))
+                self._procs.append(pr)
+                self._conns.append(parent)
+                self._shares.append(share)
+            for c in self._conns:
+                if c.recv() != "ok":
+                    raise RuntimeError("oracle worker failed to factor")
         self._Mcsr = [self.op._vals(bi, "M") if not problem.tpl.buckets[bi].m_is_constant() else None
                       for bi in range(nb)]
 
@@ -634,6 +660,9 @@ class ParallelStepper:
         return out
 
     def _solve(self, rhs):
+        if self._local is not None:                  # a handful of systems: this process
+            xs = _solve_batches(self._local, rhs)
+            return [x if x is not None else np.empty_like(r) for x, r in zip(xs, rhs)]
         for c, share in zip(self._conns, self._shares):
             c.send(("solve", [np.ascontiguousarray(r[lo:hi]) for r, (lo, hi) in zip(rhs, share)]))
         out = [np.empty_like(r) for r in rhs]
@@ -675,5 +704,6 @@ class ParallelStepper:
         self.state = C
         desc = (f"{steps} full step(s) after {warmup} untimed: F, M X, right-hand side and the "
                 f"banded solves of all {sum(self.P.nsys)} systems ({self.P.real_unknowns()} unknowns) "
-                f"on {self.workers} processes; factorizations untimed; scipy.fft workers={WORKERS}")
+                + (f"on {self.processes} processes" if self.processes else "in one process")
+                + f"; factorizations untimed; scipy.fft workers={WORKERS} (one thread for small arrays)")
         return float(np.mean(times)), desc

@@ -11,8 +11,10 @@ run on ``CN_FFT_WORKERS`` scipy.fft threads. The solver is ``Model.simulate(...)
 configuration's resolution, scheme and step (python/conatus/model/model.py:912-935,
 model/run.py:116-144); ``f_backend`` is the reference's default evaluator and its fused
 polynomial form, the faster one reported, as in the reference's own GPU table
-(docs/site/guide/benchmarks.md:271-275). Steps are timed in blocks, after one warm-up step that
-makes the factorizations (examples/benchmarks/cases.py:27-43). Prints one JSON line.
+(docs/site/guide/benchmarks.md:271-275). Steps are timed one by one (median reported) after
+warm-up steps that make the factorizations: the lower-order start-up takes one per order, so an
+SBDF-q run warms up q steps (examples/benchmarks/cases.py:27-43 warms up before timing). Prints one
+JSON line.
 
 This is the measurement behind the CPU baseline that the port (oracle/ivp.py) is compared with.
 """
@@ -96,8 +98,11 @@ def main():
         X = sim.solver.X
         rng = np.random.default_rng(0)
         sim.solver.X = X + 1e-3 * rng.standard_normal(X.shape)       # a generic state
+        # the lower-order start-up: one factorization per order (SBDF1, 2, .. q); the steady steps
+        # after it reuse the last one
+        order = int(cfg["scheme"][-1])
         t0 = time.perf_counter()
-        sim.run(steps=1)                                            # factorizations
+        sim.run(steps=order)
         t_first = time.perf_counter() - t0
         per = []
         for _ in range(args.steps):

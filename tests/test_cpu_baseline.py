@@ -11,7 +11,8 @@ import pytest
 
 from _step_cases import template
 
-CASES = [("rb_nz16", [32], 2, 1e-3), ("channel_ny17", [8, 8], 3, 5e-3)]
+# a handful of systems (solved in this process) and 265 systems (two worker processes)
+CASES = [("rb_nz16", [32], 2, 1e-3), ("channel_ny17", [8, 8], 3, 5e-3), ("channel_ny17", [24, 24], 3, 5e-3)]
 
 
 @pytest.mark.parametrize("tname,sizes,order,dt", CASES)
