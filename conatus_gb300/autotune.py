@@ -118,8 +118,8 @@ def _set_rhs_tuning(dev, q, t) -> None:
         call("cng_rhs_set_tuning", h, int(q), int(t))
 
 
-def tune_rhs(dev, reps: int = 2, candidates=((2, 128), (4, 128), (8, 128), (2, 256), (4, 256), (8, 256),
-                                               (16, 256))) -> dict:
+def tune_rhs(dev, reps: int = 2, candidates=((1, 64), (2, 64), (1, 128), (2, 128), (4, 128), (8, 128), (2, 256),
+                                               (4, 256), (8, 256), (16, 256))) -> dict:
     """Time the F evaluation of ``dev`` (a DeviceProblem) with each launch shape of its shared-memory
     transforms (sequences per block, threads per block) and keep the fastest
     (``cng_rhs_set_tuning``). Cached per precision, template, Fourier sizes and case count. Returns

@@ -646,11 +646,7 @@ __device__ __forceinline__ void unpack_body(unsigned bid, const RhsDev& d, const
     }
 }
 
-template <class R>
-__global__ void k_unpack(RhsDev d, BucketDev b, const double2* __restrict__ state, c2<R>* __restrict__ S) {
-    unpack_body<R>(blockIdx.x, d, b, state, S);
-}
-
+// every bucket of one or more evaluators in one launch (launch_unpack)
 template <class R>
 __global__ void k_unpack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
     const int k = g.find(blockIdx.x);
@@ -853,11 +849,7 @@ __device__ __forceinline__ void pack_body(unsigned bid, const RhsDev& d, const B
     }
 }
 
-template <class R>
-__global__ void k_pack(RhsDev d, BucketDev b, const c2<R>* __restrict__ H, double2* __restrict__ rows) {
-    pack_body<R>(blockIdx.x, d, b, H, rows);
-}
-
+// every bucket of one or more evaluators in one launch (launch_pack)
 template <class R>
 __global__ void k_pack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
     const int k = g.find(blockIdx.x);
@@ -1079,19 +1071,54 @@ struct Rhs {
     void run(const double2* state, double2* rows, cudaStream_t st);
 };
 
+// The per-bucket stages of one or more evaluators, every bucket in one grouped launch (one warp per
+// system; buckets of different lengths run side by side instead of one after the other).
+constexpr int kBucketWarps = 4;
+
+template <class R>
+static void launch_unpack(Rhs* const* hs, int n, const double2* state, cudaStream_t st) {
+    std::vector<BucketArgs<R>> args;
+    std::vector<unsigned> blocks;
+    size_t smem = 0;
+    for (int i = 0; i < n; ++i)
+        for (const auto& b : hs[i]->buckets) {
+            args.push_back(BucketArgs<R>{hs[i]->dev, b, state, hs[i]->S});
+            blocks.push_back((unsigned)ceil_div(b.nsys, kBucketWarps));
+            if (b.nsys) smem = std::max(smem, (size_t)kBucketWarps * (b.n + 2 * hs[i]->ny) * sizeof(c2<R>));
+        }
+    ensure_smem_attr((const void*)k_unpack_grp<R>, 200 * 1024);
+    launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
+        k_unpack_grp<R><<<total, 32 * kBucketWarps, smem, st>>>(g);
+        CNG_LAUNCH("k_unpack_grp");
+    });
+}
+
+template <class R>
+static void launch_pack(Rhs* const* hs, int n, double2* rows, cudaStream_t st) {
+    std::vector<BucketArgs<R>> args;
+    std::vector<unsigned> blocks;
+    size_t smem = 0;
+    for (int i = 0; i < n; ++i)
+        for (const auto& b : hs[i]->buckets) {
+            args.push_back(BucketArgs<R>{hs[i]->dev, b, hs[i]->S, rows});
+            blocks.push_back((unsigned)ceil_div(b.nsys, kBucketWarps));
+            if (b.nsys) smem = std::max(smem, (size_t)kBucketWarps * hs[i]->noutputs * hs[i]->ny * sizeof(double2));
+        }
+    ensure_smem_attr((const void*)k_pack_grp<R>, 200 * 1024);
+    launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
+        k_pack_grp<R><<<total, 32 * kBucketWarps, smem, st>>>(g);
+        CNG_LAUNCH("k_pack_grp");
+    });
+}
+
 template <class R>
 void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     using C = c2<R>;
     const int nf = nfactors * ncase, no = noutputs * ncase;     // fields of every case
     C* Sp = static_cast<C*>(S);
-    // 1. unpack (one warp per system)
-    for (const auto& b : buckets) {
-        if (b.nsys == 0) continue;
-        const int nw = 4;
-        const size_t smem = (size_t)nw * (b.n + 2 * ny) * sizeof(C);
-        k_unpack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, state, Sp);
-        CNG_LAUNCH("k_unpack");
-    }
+    Rhs* self = this;
+    // 1. unpack (one warp per system, every bucket in one launch)
+    launch_unpack<R>(&self, 1, state, st);
     // 2. Chebyshev backward along y of the y-groups: S [cols][ny] -> W1 [cols][my]
     C* A = static_cast<C*>(W1);
     C* Bf = static_cast<C*>(W2);
@@ -1166,14 +1193,8 @@ void Rhs::run(const double2* state, double2* rows, cudaStream_t st) {
     }
     // 8. Chebyshev forward: [cols][my] -> S [cols][ny]
     launch_cheb<R>(cur, Sp, spec_cols(no), ny, my, true, st, maxseq, threads);
-    // 9. pack rows and add the constant part
-    for (const auto& b : buckets) {
-        if (b.nsys == 0) continue;
-        const int nw = 4;
-        const size_t smem = (size_t)nw * noutputs * ny * sizeof(double2);
-        k_pack<R><<<ceil_div(b.nsys, nw), 32 * nw, smem, st>>>(dev, b, Sp, rows);
-        CNG_LAUNCH("k_pack");
-    }
+    // 9. pack rows (every bucket in one launch) and add the constant part
+    launch_pack<R>(&self, 1, rows, st);
     if (nb0) {
         k_add_sparse<<<ceil_div(nb0, 256), 256, 0, st>>>(rows, b0_idx, b0_val, nb0);
         CNG_LAUNCH("k_add_sparse");
@@ -1196,24 +1217,8 @@ void run_group(Rhs* const* hs, int n, const double2* state, double2* rows, cudaS
             throw InvalidArgument("grouped F: every problem needs the same transform block size");
     }
     if (ndir < 1) throw InvalidArgument("grouped F: at least one Fourier direction");
-    constexpr int nw = 4;
     // 1. unpack
-    {
-        std::vector<BucketArgs<R>> args;
-        std::vector<unsigned> blocks;
-        size_t smem = 0;
-        for (int i = 0; i < n; ++i)
-            for (const auto& b : hs[i]->buckets) {
-                args.push_back(BucketArgs<R>{hs[i]->dev, b, state, hs[i]->S});
-                blocks.push_back((unsigned)ceil_div(b.nsys, nw));
-                if (b.nsys) smem = std::max(smem, (size_t)nw * (b.n + 2 * hs[i]->ny) * sizeof(C));
-            }
-        ensure_smem_attr((const void*)k_unpack_grp<R>, 200 * 1024);
-        launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
-            k_unpack_grp<R><<<total, 32 * nw, smem, st>>>(g);
-            CNG_LAUNCH("k_unpack_grp");
-        });
-    }
+    launch_unpack<R>(hs, n, state, st);
     // the stages' buffers per problem, as Rhs::run rotates them
     std::vector<C*> cur(n), other(n);
     std::vector<Planned<ChebArgs<R>>> cheb;
@@ -1313,20 +1318,7 @@ void run_group(Rhs* const* hs, int n, const double2* state, double2* rows, cudaS
     launch_planned(cheb, k_cheb_fwd_grp<R>, threads, st, "k_cheb_fwd_grp");
     // pack and the constant parts
     {
-        std::vector<BucketArgs<R>> args;
-        std::vector<unsigned> blocks;
-        size_t smem = 0;
-        for (int i = 0; i < n; ++i)
-            for (const auto& b : hs[i]->buckets) {
-                args.push_back(BucketArgs<R>{hs[i]->dev, b, hs[i]->S, rows});
-                blocks.push_back((unsigned)ceil_div(b.nsys, nw));
-                if (b.nsys) smem = std::max(smem, (size_t)nw * hs[i]->noutputs * hs[i]->ny * sizeof(double2));
-            }
-        ensure_smem_attr((const void*)k_pack_grp<R>, 200 * 1024);
-        launch_groups(args, blocks, [&](const Grp<BucketArgs<R>>& g, unsigned total) {
-            k_pack_grp<R><<<total, 32 * nw, smem, st>>>(g);
-            CNG_LAUNCH("k_pack_grp");
-        });
+        launch_pack<R>(hs, n, rows, st);
         std::vector<SparseArgs> sp;
         std::vector<unsigned> sb;
         for (int i = 0; i < n; ++i) {
@@ -1528,10 +1520,10 @@ static Rhs* build_rhs(const cng_rhs_desc* D) {
     CNG_CUDA(cudaMemset(h->W1, 0, w));
     CNG_CUDA(cudaMemset(h->W2, 0, w));
     // on the device current at creation (the handle's device)
-    ensure_smem_attr((const void*)k_unpack<double>, 200 * 1024);
-    ensure_smem_attr((const void*)k_unpack<float>, 200 * 1024);
-    ensure_smem_attr((const void*)k_pack<double>, 200 * 1024);
-    ensure_smem_attr((const void*)k_pack<float>, 200 * 1024);
+    ensure_smem_attr((const void*)k_unpack_grp<double>, 200 * 1024);
+    ensure_smem_attr((const void*)k_unpack_grp<float>, 200 * 1024);
+    ensure_smem_attr((const void*)k_pack_grp<double>, 200 * 1024);
+    ensure_smem_attr((const void*)k_pack_grp<float>, 200 * 1024);
     return h.release();
 }
 

@@ -320,8 +320,8 @@ class DeviceProblem:
         g8 = lambda k: -(-k // self._GRP)
         nbk = sum(1 for ns in self.nsys if ns > 0)
         stages = 2 + 2 + (2 if self.d >= 2 else 0) + 1        # Chebyshev, x (or real parts), z, products
-        if len(self._rhs_all) == 1:
-            return 2 * nbk + stages + (1 if self.has_b0 else 0)
+        if len(self._rhs_all) == 1:                  # unpack and pack: every bucket in one launch
+            return 2 * g8(nbk) + stages + (1 if self.has_b0 else 0)
         ng = len(self._rhs_all)
         return 2 * g8(nbk) + stages * g8(ng) + g8(sum(self._has_b0))
 
@@ -1343,11 +1343,13 @@ class IVPSolver:
         return self.dev.to_host(self.X)
 
     def launches_per_step(self) -> int:
-        """Kernels of this library launched by one steady step: M X (one per bucket), F (unpack and
-        pack per bucket, 2 Chebyshev transforms, 2 or 4 Fourier transforms, products, constant
-        part), -L X (one per bucket, CN and Runge-Kutta), the right-hand side combination and the
-        solves (one batched launch, or one per bucket with the band kernel; the FP32 form adds the
-        residual per bucket and a second solve)."""
+        """Kernels of this library launched by one steady step: M X (one grouped launch for the
+        buckets with a shared real M), F (``DeviceProblem.f_launches``: unpack and pack of every
+        bucket in one launch each, 2 Chebyshev transforms, 2 or 4 Fourier transforms, products,
+        constant part), -L X (the residual with a = 0, CN and Runge-Kutta), the right-hand side
+        combination and the solves (one batched launch, or one per bucket with the band kernel; the
+        FP32 form adds the residual and a second solve per refinement group). Grouped launches take
+        at most 8 argument sets each."""
         dev = self.dev
         nb = len(dev.tpl.buckets)
         f = dev.f_launches()
