@@ -424,23 +424,28 @@ def run_gpu(args):
 
 def subrecords(args):
     """The other configurations, compact and time-bounded, beside the default line: the serving
-    stream (100 requests at 200/s, steps U[1000, 20000], FP64 and the FP32 form), the KS ensemble
-    (4096 members, 500 steps) and the RB ensemble (1024 cases, 50 steps) in the FP32 form."""
+    stream (100 requests at 200/s, steps U[1000, 20000]; FP64 and the FP32 form under the 150 GB
+    budget, FP64 under a 1.5 GB budget that binds), the KS ensemble (4096 members, 500 steps) and the
+    RB ensemble (1024 cases of three Nz, 50 steps) in the FP32 form."""
     import copy
     import torch
     out = {}
-    for prec in ("fp64", "fp32"):
+    # the configured 150 GB budget (the stream's pools plan about 4-8 GB together: it does not
+    # bind), and the same FP64 stream under a 1.5 GB budget (about two of its largest pools), where
+    # admission waits for pools to empty
+    for name, prec, budget in (("serving_fp64", "fp64", 150e9), ("serving_fp32", "fp32", 150e9),
+                               ("serving_fp64_budget_1.5gb", "fp64", 1.5e9)):
         a = copy.copy(args)
         a.precision, a.chunk, a.unroll = prec, 500, 25
-        rec = serving_record(a, requests=100, rate=200.0, steps=(1000, 20000))
+        rec = serving_record(a, requests=100, rate=200.0, steps=(1000, 20000), budget=budget)
         st = rec["serving"]
-        out[f"serving_{prec}"] = {"metric": rec["metric"], "value": rec["value"], "unit": "steps/s",
-                                  "dtype": rec["dtype"], "latency_s": rec["latency_s"],
-                                  "requests": st["requests"], "steps": st["steps"], "wall_s": st["wall_s"],
-                                  "nonfinite": st["nonfinite"], "peak_pools": st["peak_pools"],
-                                  "peak_members": st["peak_members"],
-                                  "peak_planned_gb": st["peak_planned_bytes"] / 1e9, "budget_gb": 150,
-                                  "workload": rec["config"]["workload"]}
+        out[name] = {"metric": rec["metric"], "value": rec["value"], "unit": "steps/s",
+                     "dtype": rec["dtype"], "latency_s": rec["latency_s"],
+                     "requests": st["requests"], "steps": st["steps"], "wall_s": st["wall_s"],
+                     "nonfinite": st["nonfinite"], "peak_pools": st["peak_pools"],
+                     "peak_members": st["peak_members"], "budget_waits": st["budget_waits"],
+                     "peak_planned_gb": st["peak_planned_bytes"] / 1e9, "budget_gb": budget / 1e9,
+                     "workload": rec["config"]["workload"]}
         torch.cuda.empty_cache()
     for name, fn, members, steps in (("ks_ensemble", ks_ensemble_record, 4096, 500),
                                      ("rb_ensemble", rb_ensemble_record, 1024, 50)):

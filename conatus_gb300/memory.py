@@ -67,8 +67,11 @@ def _factor_bytes(b, nsys, precision, compact, shared=False):
 
 
 def _rhs_bytes(problem, precision):
-    """Work buffers of the F pipeline (the sizes ``cng_rhs_create`` allocates)."""
+    """Work buffers of the F pipeline (the sizes ``cng_rhs_create`` allocates; a grouped problem has
+    one evaluator per group)."""
     from .ivp import smooth_size
+    if hasattr(problem, "parts"):
+        return sum(_rhs_bytes(p, precision) for p in problem.parts)
     tpl = problem.tpl
     cs = _C if precision == "fp32" else _Z
     rs = cs // 2

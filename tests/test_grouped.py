@@ -65,6 +65,20 @@ def test_sign_pairs_carry_offsets():
         assert np.array_equal(got[j + nb][1], dr) and np.array_equal(got[j + nb][2], dc)
 
 
+def test_planner_counts_every_group():
+    """The memory planner of a grouped problem: one F evaluator per group, the joint vectors and
+    every bucket's operators and factors; no more than the groups planned apart."""
+    from conatus_gb300 import memory
+    from conatus_gb300.template import GroupedProblem
+    a, b = _groups()
+    G = GroupedProblem([a, b])
+    for prec in ("fp64", "fp32"):
+        pg, pa, pb = (memory.plan_ivp(x, "SBDF2", prec) for x in (G, a, b))
+        for part in ("rhs_work", "state", "history", "operators", "factors"):
+            assert pg[part] == pa[part] + pb[part], (prec, part)
+        assert max(pa["total"], pb["total"]) < pg["total"] <= pa["total"] + pb["total"]
+
+
 def test_other_variables_refused():
     from conatus_gb300.template import GroupedProblem
     a, _ = _groups()

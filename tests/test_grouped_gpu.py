@@ -34,8 +34,9 @@ def _device(P, precision):
     return d
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_grouped_steps_are_each_problem_alone(precision, cuda_lib):
+@pytest.mark.parametrize("precision,scheme", [("fp64", "SBDF2"), ("fp32", "SBDF2"), ("fp64", "RK443"),
+                                              ("fp64", "CNAB2")])
+def test_grouped_steps_are_each_problem_alone(precision, scheme, cuda_lib):
     import torch
     from conatus_gb300.ivp import IVPSolver
     from conatus_gb300.template import GroupedProblem
@@ -43,13 +44,13 @@ def test_grouped_steps_are_each_problem_alone(precision, cuda_lib):
     stacks = _stacks()
     alone = []
     for S, C0 in stacks:
-        s = IVPSolver(S, scheme="SBDF2", dt=dt, device_problem=_device(S, precision))
+        s = IVPSolver(S, scheme=scheme, dt=dt, device_problem=_device(S, precision))
         s.set_state(C0)
         s.run_graph(6)
         torch.cuda.synchronize()
         alone.append([torch.as_tensor(x) for x in s.state_to_host()])
     G = GroupedProblem([S for S, _ in stacks])
-    g = IVPSolver(G, scheme="SBDF2", dt=dt, device_problem=_device(G, precision))
+    g = IVPSolver(G, scheme=scheme, dt=dt, device_problem=_device(G, precision))
     g.set_state(G.stack_states([C0 for _, C0 in stacks]))
     g.run_graph(6)
     torch.cuda.synchronize()
@@ -57,10 +58,10 @@ def test_grouped_steps_are_each_problem_alone(precision, cuda_lib):
     for k, ref in enumerate(alone):
         mine = G.group_state(got, k)
         assert all(np.isfinite(x).all() for x in mine)
-        assert all(torch.equal(torch.as_tensor(x), y) for x, y in zip(mine, ref)), (precision, k)
+        assert all(torch.equal(torch.as_tensor(x), y) for x, y in zip(mine, ref)), (precision, scheme, k)
     # one launch per kernel for all groups: the grouped step launches no more kernels than one
     # group's step, and fewer than the groups' steps together
-    one = IVPSolver(stacks[0][0], scheme="SBDF2", dt=dt, device_problem=_device(stacks[0][0], precision))
+    one = IVPSolver(stacks[0][0], scheme=scheme, dt=dt, device_problem=_device(stacks[0][0], precision))
     one.set_state(stacks[0][1])
     one.run(2)
     assert g.launches_per_step() <= one.launches_per_step()
@@ -105,3 +106,37 @@ def test_grouped_entry_refuses(cuda_lib):
         call("cng_rhs_evaluate_group", 2, mixed, x.data_ptr(), out.data_ptr(), None)
     with pytest.raises(ValueError, match="alias"):
         call("cng_rhs_evaluate_group", 2, d64._rhs_arr, x.data_ptr(), x.data_ptr(), None)
+
+
+def test_planned_bytes_bound_the_grouped_solver(cuda_lib):
+    """The planner's prediction for a grouped problem bounds the device bytes its solver holds
+    (driver free-memory drop plus torch's allocations, after the steady state)."""
+    import gc
+    import torch
+    from conatus_gb300 import memory
+    from conatus_gb300._lib import lib
+    from conatus_gb300.ivp import IVPSolver
+    from conatus_gb300.template import GroupedProblem
+
+    def free_bytes():
+        f, t = ctypes.c_uint64(), ctypes.c_uint64()
+        lib().cng_mem_info(ctypes.byref(f), ctypes.byref(t))
+        return int(f.value)
+
+    stacks = _stacks(4)
+    G = GroupedProblem([S for S, _ in stacks])
+    for precision in ("fp64", "fp32"):
+        gc.collect()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        f0, a0, r0 = free_bytes(), torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+        s = IVPSolver(G, scheme="SBDF2", dt=2e-6, precision=precision, factor_sets=1)
+        s.set_state(G.stack_states([C0 for _, C0 in stacks]))
+        s.run(4)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        f1, a1, r1 = free_bytes(), torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+        held = (f0 - f1) - (r1 - r0) + (a1 - a0)
+        plan = memory.plan_ivp(G, "SBDF2", precision, factor_sets=1)["total"]
+        assert held <= plan + (8 << 20), (precision, held, plan)
+        del s
