@@ -933,6 +933,8 @@ class IVPSolver:
         # default). A caller that keeps many solvers in flight on their own streams (the serving
         # loop) turns it off after one explicit wait, so that independent runs do not serialize.
         self.join = True
+        self._shadow = None                  # FP32 form: the FP64 shadow of monitor_fp64
+        self.mixed_error, self.mixed_error_last = {}, None
 
     def set_state(self, X, t: float = 0.0) -> None:
         """Initial state (mode layout tensor or list of per-bucket arrays); resets the history."""
@@ -942,6 +944,75 @@ class IVPSolver:
         self.t, self.iteration = float(t), 0
         self.filled, self.head = 0, self.ring - 1
         self._reset_finite()
+        if self._shadow is not None:
+            self._shadow.set_state(self.X, t)
+            self.mixed_error, self.mixed_error_last = {}, None
+
+    # ------------------------------------------------------------------ FP32 form: error monitor
+    def monitor_fp64(self, every: int = 100, bound: float = 1e-6) -> None:
+        """FP32 form: advance a plain FP64 shadow of this solver in lockstep (its own device problem)
+        and record the relative L2 error per field (tau variables left out) of this run against it
+        every ``every`` steps and at the end of every ``step`` / ``run`` / ``run_graph`` call, in
+        ``self.mixed_error`` ({iteration: {field: error}}; the latest in ``mixed_error_last``). An
+        error above ``bound`` warns (RuntimeWarning). The FP64 drop-in matches the reference step
+        by step, so this is the mixed form's error against the FP64 path, at the cost of running it
+        beside. Call after ``set_state`` and before the first step (the shadow starts from the same
+        state and an empty history)."""
+        if self.dev.precision != "fp32":
+            raise ValueError("monitor_fp64: the solver is not the FP32 form")
+        if self.iteration != 0 or self.filled != 0:
+            raise ValueError("monitor_fp64: call it after set_state, before the first step")
+        torch = _torch()
+        self._shadow = IVPSolver(self.dev.P, scheme=self.scheme, dt=self.dt, precision="fp64",
+                                 check_finite=self._finite_every or False)
+        self._shadow.set_state(self.X, self.t)
+        self._mon_every, self._mon_bound = max(1, int(every)), float(bound)
+        tpl = self.dev.tpl
+        self._mon_masks = {}
+        for v, var in enumerate(tpl.variables):
+            if var["name"].startswith("tau"):
+                continue
+            self._mon_masks[var["name"]] = [torch.as_tensor(b.col[:, 0] == v, device=self.X.device)
+                                            for b in tpl.buckets]
+        self.mixed_error, self.mixed_error_last = {}, None
+
+    def _record_error(self) -> None:
+        torch = _torch()
+        self.stream.synchronize()
+        self._shadow.stream.synchronize()
+        dev = self.dev
+        errs = {}
+        for name, masks in self._mon_masks.items():
+            num = den = 0.0
+            for bi, (b, mask) in enumerate(zip(dev.tpl.buckets, masks)):
+                ns = dev.nsys[bi]
+                if ns == 0:
+                    continue
+                a = dev.bucket(self.X, bi).view(ns, b.n)[:, mask]
+                r = dev.bucket(self._shadow.X, bi).view(ns, b.n)[:, mask]
+                num += float(torch.sum(torch.abs(a - r) ** 2))
+                den += float(torch.sum(torch.abs(r) ** 2))
+            errs[name] = (num / den) ** 0.5 if den > 0 else 0.0
+        self.mixed_error[int(self.iteration)] = errs
+        self.mixed_error_last = errs
+        worst = max(errs.values()) if errs else 0.0
+        if worst > self._mon_bound:
+            import warnings
+            warnings.warn(f"FP32 form: relative L2 error {worst:.3g} against the FP64 shadow at iteration "
+                          f"{self.iteration} (bound {self._mon_bound:g}; per field {errs})", RuntimeWarning,
+                          stacklevel=3)
+
+    def _monitored(self, fn, shadow_fn, steps: int) -> None:
+        """Run ``steps`` steps through fn and the shadow through shadow_fn in chunks that end on the
+        monitor's iterations; record the error there and at the end of the call."""
+        left = int(steps)
+        while left > 0:
+            n = min(left, self._mon_every - self.iteration % self._mon_every)
+            fn(n)
+            shadow_fn(n)
+            left -= n
+            if self.iteration % self._mon_every == 0 or left == 0:
+                self._record_error()
 
     def _reset_finite(self) -> None:
         """A new state: forget the finite-state checks of the previous one."""
@@ -1114,6 +1185,11 @@ class IVPSolver:
             _torch().cuda.current_stream().wait_stream(self.stream)
 
     def step(self) -> None:
+        if self._shadow is not None:
+            return self._monitored(lambda n: self._plain_step(), lambda n: self._shadow.step(), 1)
+        self._plain_step()
+
+    def _plain_step(self) -> None:
         self._enter()
         self._step()
         self._leave()
@@ -1130,6 +1206,11 @@ class IVPSolver:
         """``steps`` plain steps; with the finite-state check on, the state is checked every
         ``check_finite`` steps and at the end of the call, and a blown-up run stops with
         NumericalError (integrator.py:745-767)."""
+        if self._shadow is not None:
+            return self._monitored(self._run, self._shadow.run, steps)
+        self._run(steps)
+
+    def _run(self, steps: int) -> None:
         self._enter()
         fe = self._finite_every
         s = _stream_handle(self.stream)
@@ -1195,6 +1276,12 @@ class IVPSolver:
         and at the end of the call (graphs end on those iterations); ``wait``: wait for it at the
         end and raise NumericalError on a blown-up state, else leave the result to
         :meth:`finite_status` (a caller that keeps many runs in flight)."""
+        if self._shadow is not None:
+            return self._monitored(lambda n: self._run_graph(n, unroll, wait),
+                                   lambda n: self._shadow.run_graph(n, unroll), steps)
+        self._run_graph(steps, unroll, wait)
+
+    def _run_graph(self, steps: int, unroll: int = 1, wait: bool = True) -> None:
         s = _stream_handle(self.stream)
         steps = int(steps)
         unroll = max(1, int(unroll))

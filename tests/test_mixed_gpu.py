@@ -70,3 +70,43 @@ def test_fp32_F_error(tname, sizes, rng, cuda_lib):
         outs[prec] = o.cpu().numpy()
     err = np.linalg.norm(outs["fp32"] - outs["fp64"]) / np.linalg.norm(outs["fp64"])
     assert err < 1e-5, err
+
+
+def test_monitor_fp64_reports_the_error_of_every_run(rng, cuda_lib):
+    """IVPSolver.monitor_fp64: the FP32 form records its error against an FP64 shadow every
+    ``every`` steps and at the end of each call; the recorded error is the one against a separate
+    FP64 run, the shadow leaves the FP32 trajectory unchanged, and an error above the bound warns."""
+    import warnings
+    import torch
+    from conatus_gb300.ivp import IVPSolver
+    P = template("channel_ny129").instantiate([16, 16])
+    C0 = _workload_state("channel_ny129", P, rng)
+    plain = IVPSolver(P, scheme="SBDF3", dt=5e-3, precision="fp32")
+    plain.set_state(C0)
+    plain.run_graph(12)
+    ref = IVPSolver(P, scheme="SBDF3", dt=5e-3, precision="fp64")
+    ref.set_state(C0)
+    ref.run_graph(12)
+    mon = IVPSolver(P, scheme="SBDF3", dt=5e-3, precision="fp32")
+    mon.set_state(C0)
+    mon.monitor_fp64(every=5)
+    mon.run_graph(7)
+    mon.run(3)
+    mon.step()
+    mon.step()
+    torch.cuda.synchronize()
+    assert sorted(mon.mixed_error) == [5, 7, 10, 11, 12]
+    assert torch.equal(mon.X, plain.X)                      # the shadow does not touch the run
+    got = mon.mixed_error[12]
+    want = field_errors(P, mon.dev.to_host(mon.X), ref.dev.to_host(ref.X))
+    for k, v in got.items():
+        assert abs(v - want[k]) <= 1e-6 * want[k] + 1e-300, (k, v, want[k])
+    assert max(got.values()) < 1e-6 and mon.mixed_error_last == got
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        mon._mon_bound = 1e-30
+        mon.step()
+    assert any(issubclass(x.category, RuntimeWarning) and "FP64 shadow" in str(x.message) for x in w)
+    fp64 = IVPSolver(P, scheme="SBDF3", dt=5e-3, precision="fp64")
+    with pytest.raises(ValueError):
+        fp64.monitor_fp64()
