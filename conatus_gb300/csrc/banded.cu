@@ -1806,10 +1806,21 @@ __device__ __forceinline__ double fm(double a, double b, double c) { return fma(
 __device__ __forceinline__ float fm(float a, float b, float c) { return fmaf(a, b, c); }
 template <class TF>
 __device__ __forceinline__ typename CompT<TF>::T comp(const TF& v, int c) { return c ? v.im : v.re; }
-// component c of v - a b, in the order of cfms (the two-systems sweep's arithmetic)
+// component c of v - a b, in the order of cfms (the two-systems sweep's arithmetic): with the lane's
+// operands of b picked once per column, B0 = b.re (c = 0) or b.im (c = 1) and B1 = b.im or -b.re,
+// it is fma(a.im, B1, fma(-a.re, B0, v)) -- the products are exact sign flips of cfms's, so the
+// roundings are the same
 template <class TF>
-__device__ __forceinline__ typename CompT<TF>::T cfms_comp(typename CompT<TF>::T vc, const TF& a, const TF& b, int c) {
-    return c ? fm(-a.im, b.re, fm(-a.re, b.im, vc)) : fm(a.im, b.im, fm(-a.re, b.re, vc));
+struct CompB {
+    typename CompT<TF>::T b0, b1;
+};
+template <class TF>
+__device__ __forceinline__ CompB<TF> comp_b(const TF& b, int c) {
+    return c ? CompB<TF>{b.im, -b.re} : CompB<TF>{b.re, b.im};
+}
+template <class TF>
+__device__ __forceinline__ typename CompT<TF>::T cfms_comp(typename CompT<TF>::T vc, const TF& a, const CompB<TF>& b) {
+    return fm(a.im, b.b1, fm(-a.re, b.b0, vc));
 }
 
 template <class TF, class TD, int IO, int CH, int ST>
@@ -1901,11 +1912,13 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
                 const int e0 = e1;
                 e1 = s_offL[j + 1];
                 __syncwarp();
+                const CompB<TF> bq = comp_b(bj, c);
+                const T yj0c = comp(yj0, c);
                 for (int e = e0 + es; e < e1; e += 16) {
                     const int i = j + 1 + s_Lrow[e];
                     T* yi = reinterpret_cast<T*>(&y[i]) + c;
-                    const T vc = (i == l) ? comp(yj0, c) : *yi;
-                    *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bj, c);
+                    const T vc = (i == l) ? yj0c : *yi;
+                    *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bq);
                 }
                 if (lane == 0) {
                     y[j] = bj;
@@ -1942,11 +1955,12 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
                 e1 = s_offU[s + 1];
                 const TF yj = y[j];
                 __syncwarp();
+                const CompB<TF> bq = comp_b(yj, c);
                 for (int e = e0 + es; e < e1; e += 16) {
                     const int i = j - s_Udist[e];
                     T* yi = reinterpret_cast<T*>(&y[i]) + c;
                     const T vc = e == e0 ? T(0) : *yi;
-                    *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], yj, c);
+                    *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], bq);
                 }
                 __syncwarp();
             }
@@ -1959,9 +1973,23 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
             for (int q = lane; q < r * r; q += 32) sl[q] = cd.slu[(size_t)sys * r * r + q];
         const TF* Vg = cd.V + (size_t)wgs * ix.nV * 2;
         for (int a = 0; a < r; ++a) {
+            // kU entries per lane in flight (their column ids and values loaded together), in the
+            // order of one entry per lane and pass
             TF acc = TF(0.0);
-            for (int e = ix.offV[a] + lane; e < ix.offV[a + 1]; e += 32)
-                acc = cfma(acc, Vg[(size_t)e * 2 + gs], y[ix.Vcol[e]]);
+            const int ea = ix.offV[a], eb = ix.offV[a + 1];
+            for (int e0 = ea + lane; e0 < eb; e0 += kU * 32) {
+                int cix[kU];
+                TF v[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int e = e0 + u * 32;
+                    cix[u] = e < eb ? ix.Vcol[e] : -1;
+                    v[u] = e < eb ? Vg[(size_t)e * 2 + gs] : TF(0.0);
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                    if (cix[u] >= 0) acc = cfma(acc, v[u], y[cix[u]]);
+            }
             for (int m = 16; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
             if (lane == 0) zb[a] = acc;
         }
@@ -1972,10 +2000,25 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
         }
         __syncwarp();
         const TF* Ws = cd.W + (size_t)sys * r * n;
-        for (int i = lane; i < n; i += 32) {
-            TF acc = y[i];
-            for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
-            y[i] = acc;
+        if (r <= kMaxRUnroll) {
+            // the r entries of W for a row loaded together, then the r updates in order
+            for (int i = lane; i < n; i += 32) {
+                TF w[kMaxRUnroll];
+#pragma unroll
+                for (int k = 0; k < kMaxRUnroll; ++k)
+                    if (k < r) w[k] = Ws[(size_t)k * n + i];
+                TF acc = y[i];
+#pragma unroll
+                for (int k = 0; k < kMaxRUnroll; ++k)
+                    if (k < r) acc = cfms(acc, w[k], zb[k]);
+                y[i] = acc;
+            }
+        } else {
+            for (int i = lane; i < n; i += 32) {
+                TF acc = y[i];
+                for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
+                y[i] = acc;
+            }
         }
         __syncwarp();
     }
