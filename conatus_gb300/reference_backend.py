@@ -152,6 +152,18 @@ class GB300IVPSolver:
         self._gpu.stream.synchronize()
         self._gpu.X.copy_(dev.to_device(self._modes(value)))
         self._gpu._reset_finite()
+        if self._gpu._shadow is not None:             # the FP64 shadow of monitor_fp64 follows
+            self._gpu._shadow.stream.synchronize()
+            self._gpu._shadow.X.copy_(self._gpu.X)
+            self._gpu._shadow._reset_finite()
+
+    def monitor_fp64(self, every: int = 100, bound: float = 1e-6) -> None:
+        """The FP32 form (``install(precision="fp32")``): record the run's per-field error against
+        an FP64 shadow every ``every`` steps and at the end of every call, in ``mixed_error``
+        (``conatus_gb300.ivp.IVPSolver.monitor_fp64``). Call after ``set_state``, before stepping."""
+        self._gpu.monitor_fp64(every, bound)
+
+    mixed_error = property(lambda self: self._gpu.mixed_error)
 
     t = property(lambda self: self._gpu.t, lambda self, v: setattr(self._gpu, "t", float(v)))
     iteration = property(lambda self: self._gpu.iteration,

@@ -87,9 +87,13 @@ def main():
         out["solver"] = type(sim.solver).__name__
         sim.initial(u=lambda x: -np.sin(np.pi * x))
         u0 = sim.coeffs("u")
+        if case.endswith("fp32"):                     # the run reports its error against FP64
+            sim.solver.monitor_fp64(every=250)
         sim.run(steps=1000)
         out["t"], out["iteration"] = float(sim.t), int(sim.solver.iteration)
         out["u1000"] = sim.coeffs("u").tolist()
+        if case.endswith("fp32"):
+            out["mixed_error"] = {str(k): v for k, v in sim.solver.mixed_error.items()}
         # the reference's own CPU path on the same script, its banded solves on this package's
         # GPU core (conatus._core = conatus_gb300.core)
         cpu = burgers(cn).simulate(N=128, scheme="SBDF2", dt=1e-4)

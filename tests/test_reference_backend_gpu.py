@@ -44,7 +44,12 @@ def test_burgers_script_fp32_form(cuda_lib):
     fp64 = np.asarray(run_case("burgers")["u1000"])
     out = run_case("burgers_fp32")
     u = np.asarray(out["u1000"])
-    assert np.linalg.norm(u - fp64) / np.linalg.norm(fp64) < 1e-6
+    err = np.linalg.norm(u - fp64) / np.linalg.norm(fp64)
+    assert err < 1e-6
+    # the run's own report (monitor_fp64, every 250 steps): its last entry is this error
+    me = out["mixed_error"]
+    assert sorted(int(k) for k in me) == [250, 500, 750, 1000]
+    assert abs(me["1000"]["u"] - err) <= 1e-3 * err + 1e-15, (me["1000"], err)
 
 
 def test_channel_script_and_checkpoints_both_ways(cuda_lib):
