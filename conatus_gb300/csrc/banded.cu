@@ -746,6 +746,7 @@ struct Banded {
     bool compact_ready = false;
     int cL = 0, cU = 0, cV = 0, cWg = 0;
     int cMaxLk[4] = {0, 0, 0, 0}, cMaxUk[4] = {0, 0, 0, 0};   // largest stream chunk per chunk size 2, 4, 8, 16
+    int cMaxLcol = 0, cMaxUcol = 0;                            // most entries of one column (L, U)
     int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
     int cG = 2;                     // systems per warp group of the compact streams (1: shared pair)
     bool shared = false;            // factors shared with a sign-similar partner bucket
@@ -1469,6 +1470,7 @@ struct CompactIdx {
                                         // shared pair (both halves of the warp read one system's factors)
     int wg0;                            // first warp group solved (wgroups: one past the last)
     int maxLc, maxUc;                   // largest chunk of the L / U streams (entries)
+    int maxLcol, maxUcol;               // most entries of one column of the L / U streams
     const int* offL;                    // n + 1
     const unsigned char* Lrow;          // nL: t (row kv + 1 + t of the column)
     const unsigned* Lmask;              // n: bit t set if row t is in the union
@@ -1823,6 +1825,139 @@ __device__ __forceinline__ typename CompT<TF>::T cfms_comp(typename CompT<TF>::T
     return fm(a.im, b.b1, fm(-a.re, b.b0, vc));
 }
 
+// The sweeps of the split-lane solve (one system per warp; lane = entry slot es, component c).
+template <class TF>
+struct SplitSweep {
+    TF* y;
+    const int* s_offL;
+    const int* s_offU;
+    const unsigned* s_Lmask;
+    const unsigned char* s_Lrow;
+    const unsigned char* s_Udist;
+    TF* Lb;
+    TF* Ub;
+    int* Pb;
+    const TF* Lg;
+    const TF* Ug;
+    const int* Pg;
+    int n, maxLc, maxUc, gs, es, c, lane;
+};
+
+// One pass of a column's entries (slots es, es + 16, ...): NP > 0 unrolls NP predicated passes
+// (every column holds at most 16 NP entries), NP = 0 loops over any count. The same updates in the
+// same order either way.
+template <int NP, class F>
+__device__ __forceinline__ void column_passes(int e0, int e1, int es, F&& f) {
+    if constexpr (NP > 0) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const int e = e0 + es + 16 * p;
+            if (e < e1) f(e);
+        }
+    } else {
+        for (int e = e0 + es; e < e1; e += 16) f(e);
+    }
+}
+
+// forward: L with the row interchanges
+template <class TF, int CH, int ST, int NP>
+__device__ __forceinline__ void split_forward(const SplitSweep<TF>& w) {
+    using T = typename CompT<TF>::T;
+    TF* y = w.y;
+    const int n = w.n, gs = w.gs, c = w.c;
+    const int nch = (n - 1 + CH - 1) / CH;
+    auto issue = [&](int ch) {
+        if (ch < nch) {
+            const int buf = ch % ST;
+            const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+            warp_stage(w.Lb + (size_t)buf * w.maxLc * 2, w.Lg + (size_t)w.s_offL[j0] * 2,
+                       (w.s_offL[j1] - w.s_offL[j0]) * 2);
+            warp_stage(w.Pb + (size_t)buf * CH * 2, w.Pg + (size_t)j0 * 2, (j1 - j0) * 2);
+        }
+        cp_async_commit();
+    };
+    for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
+    for (int ch = 0; ch < nch; ++ch) {
+        issue(ch + ST - 1);
+        cp_async_wait<ST - 1>();
+        __syncwarp();
+        const TF* Lc = w.Lb + (size_t)(ch % ST) * w.maxLc * 2;
+        const int* Pc = w.Pb + (size_t)(ch % ST) * CH * 2;
+        const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+        const int base = w.s_offL[j0];
+        int e1 = base;
+#pragma unroll
+        for (int jj = 0; jj < CH; ++jj) {
+            const int j = j0 + jj;
+            if (j >= j1) break;
+            const int l = Pc[jj * 2 + gs];
+            const TF bj = y[l];
+            const TF yj0 = y[j];
+            const int e0 = e1;
+            e1 = w.s_offL[j + 1];
+            __syncwarp();
+            const CompB<TF> bq = comp_b(bj, c);
+            const T yj0c = comp(yj0, c);
+            column_passes<NP>(e0, e1, w.es, [&](int e) {
+                const int i = j + 1 + w.s_Lrow[e];
+                T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                const T vc = (i == l) ? yj0c : *yi;
+                *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bq);
+            });
+            if (w.lane == 0) {
+                y[j] = bj;
+                if (l != j && !((w.s_Lmask[j] >> (l - j - 1)) & 1u)) y[l] = yj0;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// backward: U (each column's first entry is its diagonal, held as -1/u_jj)
+template <class TF, int CH, int ST, int NP>
+__device__ __forceinline__ void split_backward(const SplitSweep<TF>& w) {
+    using T = typename CompT<TF>::T;
+    TF* y = w.y;
+    const int n = w.n, gs = w.gs, c = w.c;
+    const int nch = (n + CH - 1) / CH;
+    auto issue = [&](int ch) {
+        if (ch < nch) {
+            const int s0 = ch * CH, s1 = min(s0 + CH, n);
+            warp_stage(w.Ub + (size_t)(ch % ST) * w.maxUc * 2, w.Ug + (size_t)w.s_offU[s0] * 2,
+                       (w.s_offU[s1] - w.s_offU[s0]) * 2);
+        }
+        cp_async_commit();
+    };
+    for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
+    for (int ch = 0; ch < nch; ++ch) {
+        issue(ch + ST - 1);
+        cp_async_wait<ST - 1>();
+        __syncwarp();
+        const TF* Uc = w.Ub + (size_t)(ch % ST) * w.maxUc * 2;
+        const int s0 = ch * CH, s1 = min(s0 + CH, n);
+        const int base = w.s_offU[s0];
+        int e1 = base;
+#pragma unroll
+        for (int ss = 0; ss < CH; ++ss) {
+            const int s = s0 + ss;
+            if (s >= s1) break;
+            const int j = n - 1 - s;
+            const int e0 = e1;
+            e1 = w.s_offU[s + 1];
+            const TF yj = y[j];
+            __syncwarp();
+            const CompB<TF> bq = comp_b(yj, c);
+            column_passes<NP>(e0, e1, w.es, [&](int e) {
+                const int i = j - w.s_Udist[e];
+                T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                const T vc = e == e0 ? T(0) : *yi;
+                *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], bq);
+            });
+            __syncwarp();
+        }
+    }
+}
+
 template <class TF, class TD, int IO, int CH, int ST>
 __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const CompactData<TF>& cd,
                                                  const SolveIo& io, int block) {
@@ -1881,91 +2016,17 @@ __device__ __forceinline__ void solve_split_body(const CompactIdx& ix, const Com
     const TF* Lg = cd.L + (size_t)wgs * ix.nL * 2;
     const TF* Ug = cd.U + (size_t)wgs * ix.nU * 2;
     const int* Pg = cd.piv + (size_t)wgs * n * 2;
+    const SplitSweep<TF> sw{y, s_offL, s_offU, s_Lmask, s_Lrow, s_Udist, Lb, Ub, Pb, Lg, Ug, Pg,
+                            n, ix.maxLc, ix.maxUc, gs, es, c, lane};
+    // the column passes unrolled and predicated where every column fits 16 or 32 entry slots
     if (ix.kl > 0 && n > 1) {
-        const int nch = (n - 1 + CH - 1) / CH;
-        auto issue = [&](int ch) {
-            if (ch < nch) {
-                const int buf = ch % ST;
-                const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
-                warp_stage(Lb + (size_t)buf * ix.maxLc * 2, Lg + (size_t)s_offL[j0] * 2, (s_offL[j1] - s_offL[j0]) * 2);
-                warp_stage(Pb + (size_t)buf * CH * 2, Pg + (size_t)j0 * 2, (j1 - j0) * 2);
-            }
-            cp_async_commit();
-        };
-        for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
-        for (int ch = 0; ch < nch; ++ch) {
-            issue(ch + ST - 1);
-            cp_async_wait<ST - 1>();
-            __syncwarp();
-            const TF* Lc = Lb + (size_t)(ch % ST) * ix.maxLc * 2;
-            const int* Pc = Pb + (size_t)(ch % ST) * CH * 2;
-            const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
-            const int base = s_offL[j0];
-            int e1 = base;
-#pragma unroll
-            for (int jj = 0; jj < CH; ++jj) {
-                const int j = j0 + jj;
-                if (j >= j1) break;
-                const int l = Pc[jj * 2 + gs];
-                const TF bj = y[l];
-                const TF yj0 = y[j];
-                const int e0 = e1;
-                e1 = s_offL[j + 1];
-                __syncwarp();
-                const CompB<TF> bq = comp_b(bj, c);
-                const T yj0c = comp(yj0, c);
-                for (int e = e0 + es; e < e1; e += 16) {
-                    const int i = j + 1 + s_Lrow[e];
-                    T* yi = reinterpret_cast<T*>(&y[i]) + c;
-                    const T vc = (i == l) ? yj0c : *yi;
-                    *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bq);
-                }
-                if (lane == 0) {
-                    y[j] = bj;
-                    if (l != j && !((s_Lmask[j] >> (l - j - 1)) & 1u)) y[l] = yj0;
-                }
-                __syncwarp();
-            }
-        }
+        if (ix.maxLcol <= 16) split_forward<TF, CH, ST, 1>(sw);
+        else if (ix.maxLcol <= 32) split_forward<TF, CH, ST, 2>(sw);
+        else split_forward<TF, CH, ST, 0>(sw);
     }
-    {
-        const int nch = (n + CH - 1) / CH;
-        auto issue = [&](int ch) {
-            if (ch < nch) {
-                const int s0 = ch * CH, s1 = min(s0 + CH, n);
-                warp_stage(Ub + (size_t)(ch % ST) * ix.maxUc * 2, Ug + (size_t)s_offU[s0] * 2, (s_offU[s1] - s_offU[s0]) * 2);
-            }
-            cp_async_commit();
-        };
-        for (int ch = 0; ch < ST - 1; ++ch) issue(ch);
-        for (int ch = 0; ch < nch; ++ch) {
-            issue(ch + ST - 1);
-            cp_async_wait<ST - 1>();
-            __syncwarp();
-            const TF* Uc = Ub + (size_t)(ch % ST) * ix.maxUc * 2;
-            const int s0 = ch * CH, s1 = min(s0 + CH, n);
-            const int base = s_offU[s0];
-            int e1 = base;
-#pragma unroll
-            for (int ss = 0; ss < CH; ++ss) {
-                const int s = s0 + ss;
-                if (s >= s1) break;
-                const int j = n - 1 - s;
-                const int e0 = e1;
-                e1 = s_offU[s + 1];
-                const TF yj = y[j];
-                __syncwarp();
-                const CompB<TF> bq = comp_b(yj, c);
-                for (int e = e0 + es; e < e1; e += 16) {
-                    const int i = j - s_Udist[e];
-                    T* yi = reinterpret_cast<T*>(&y[i]) + c;
-                    const T vc = e == e0 ? T(0) : *yi;
-                    *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], bq);
-                }
-                __syncwarp();
-            }
-        }
-    }
+    if (ix.maxUcol <= 16) split_backward<TF, CH, ST, 1>(sw);
+    else if (ix.maxUcol <= 32) split_backward<TF, CH, ST, 2>(sw);
+    else split_backward<TF, CH, ST, 0>(sw);
     if (r > 0) {
         const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
         TF* sl = zb + r;
@@ -2125,6 +2186,8 @@ static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     ix.wgroups = h.cWg; ix.batch = h.batch; ix.gs = h.cG; ix.wg0 = 0;
     ix.maxLc = h.cMaxLk[chunk_index(chunk)];
     ix.maxUc = h.cMaxUk[chunk_index(chunk)];
+    ix.maxLcol = h.cMaxLcol;
+    ix.maxUcol = h.cMaxUcol;
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
     ix.offV = h.c_offV; ix.Vcol = h.c_Vcol;
     return ix;
@@ -2191,6 +2254,9 @@ static void compact(Banded& h, cudaStream_t st) {
         h.cMaxLk[k] = ml;
         h.cMaxUk[k] = mu;
     }
+    h.cMaxLcol = h.cMaxUcol = 0;
+    for (int j = 0; j + 1 < n; ++j) h.cMaxLcol = std::max(h.cMaxLcol, offL[j + 1] - offL[j]);
+    for (int s2 = 0; s2 < n; ++s2) h.cMaxUcol = std::max(h.cMaxUcol, offU[s2 + 1] - offU[s2]);
     h.cL = (int)Lrow.size();
     h.cU = (int)Udist.size();
     h.cV = (int)Vcol.size();
