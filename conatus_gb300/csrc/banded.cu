@@ -1621,16 +1621,10 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 const int e0 = e1;
                 e1 = s_offL[j + 1];
                 __syncwarp();
-                auto upd = [&](int e) {
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j + 1 + s_Lrow[e];
                     const TF v = (i == l) ? yj0 : y[i];
                     y[i] = cfms(v, Lc[(e - base) * gs + gsel], bj);
-                };
-                // one predicated pass where every column fits the 16 lanes (the same updates)
-                if (ix.maxLcol <= kLanesPer) {
-                    if (e0 + lg < e1) upd(e0 + lg);
-                } else {
-                    for (int e = e0 + lg; e < e1; e += kLanesPer) upd(e);
                 }
                 if (lg == 0) {
                     y[j] = bj;
@@ -1671,16 +1665,9 @@ __device__ __forceinline__ void solve_compact_body(const CompactIdx& ix, const C
                 __syncwarp();
                 // the column's first entry is the diagonal, held as -1/u_jj: it takes a lane of the
                 // same pass (y_j = 0 - (-1/u_jj) y_j) instead of a pass of its own
-                auto upd = [&](int e) {
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
                     const int i = j - s_Udist[e];
                     y[i] = cfms(e == e0 ? TF(0.0) : y[i], Uc[(e - base) * gs + gsel], yj);
-                };
-                // two predicated passes where every column fits 32 entries (the same updates)
-                if (ix.maxUcol <= 2 * kLanesPer) {
-                    if (e0 + lg < e1) upd(e0 + lg);
-                    if (e0 + lg + kLanesPer < e1) upd(e0 + lg + kLanesPer);
-                } else {
-                    for (int e = e0 + lg; e < e1; e += kLanesPer) upd(e);
                 }
                 __syncwarp();
             }
