@@ -2,8 +2,11 @@
 
 Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_set_schedule(h,
 -1)``) and the compact-stream schedules of ``cng_banded_schedules`` (two systems per warp over the
-union pattern of the factors, with different staging chunks and ring depths, and one system per
-warp with the lanes split over entries and components for small batches). Each candidate solves
+union pattern of the factors, with different staging chunks and ring depths; one system per warp
+with the lanes split over entries and components for small batches; and the partitioned solve of
+small FP64 batches, one block of warps per system sweeping its blocks of 32 columns at once).
+Candidates a factor set cannot take (a shared pair, the FP32 form, a batch too large for the
+partitioned solve's responses) are refused by the library and skipped. Each candidate solves
 the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
 few times on the factors at hand; the fastest is kept for every handle of the factor set. Results
 are cached per process by the shapes of the buckets (batch, n, border, band) and the precision, so
@@ -23,7 +26,7 @@ import os
 
 from ._lib import call
 
-__all__ = ["schedules", "split_schedules", "tune_solve", "tune_rhs", "cache"]
+__all__ = ["schedules", "split_schedules", "partitioned_schedules", "tune_solve", "tune_rhs", "cache"]
 
 _CACHE: dict = {}
 
@@ -44,6 +47,17 @@ def split_schedules() -> set:
     flags = (ctypes.c_int32 * n.value)()
     call("cng_banded_schedules", ctypes.byref(n), None, None, flags)
     return {k for k in range(n.value) if flags[k]}
+
+
+def partitioned_schedules() -> set:
+    """Schedules of the partitioned solve (small batches, FP64: blocks of 32 columns swept at once
+    with their responses to the blocks before them); refused for the FP32 form, shared pairs,
+    system ranges and large batches."""
+    n = ctypes.c_int32()
+    call("cng_banded_schedules", ctypes.byref(n), None, None, None)
+    flags = (ctypes.c_int32 * n.value)()
+    call("cng_banded_schedules", ctypes.byref(n), None, None, flags)
+    return {k for k in range(n.value) if flags[k] == 2}
 
 
 def cache() -> dict:

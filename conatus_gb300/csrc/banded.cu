@@ -747,6 +747,12 @@ struct Banded {
     int cL = 0, cU = 0, cV = 0, cWg = 0;
     int cMaxLk[4] = {0, 0, 0, 0}, cMaxUk[4] = {0, 0, 0, 0};   // largest stream chunk per chunk size 2, 4, 8, 16
     int cMaxLcol = 0, cMaxUcol = 0;                            // most entries of one column (L, U)
+    // partitioned solve (kPartSchedule): per system and block of 32 columns, the responses of the
+    // block's forward and backward sweeps to unit boundary values (built by build_part)
+    bool part_ready = false;
+    int p_nbf = 0, p_nbb = 0, p_kwf = 0, p_kwb = 0, p_maxLc = 0, p_maxUc = 0;
+    void* p_Rf = nullptr;           // [batch][nbf][32 + kwf][kwf] complex128
+    void* p_Rb = nullptr;           // [batch][nbb][32 + kwb][kwb] complex128
     int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
     int cG = 2;                     // systems per warp group of the compact streams (1: shared pair)
     bool shared = false;            // factors shared with a sign-similar partner bucket
@@ -785,7 +791,7 @@ struct Banded {
                         (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32,
                         (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
                         (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
-                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c})
+                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c, p_Rf, p_Rb})
             dev_free(p);
     }
 
@@ -1456,11 +1462,14 @@ constexpr int kCChunk = 8;              // columns per staged chunk (the default
 // autotuner (conatus_gb300.autotune) times them on the factors at hand. Schedule 0 is the default.
 // Schedules 8-10 run one system per warp with the lanes split over entries and components (the
 // latency variant for small batches, k_solve_split_multi).
+// Schedule 11 (split = 2) is the partitioned solve of small batches (k_solve_part: one block of
+// warps per system, blocks of 32 columns swept at once; FP64 only).
 struct CompactSchedule { int chunk, stages, split; };
-constexpr int kNumSchedules = 11;
+constexpr int kNumSchedules = 12;
+constexpr int kPartSchedule = 11;
 constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
-                                                       {8, 2, 1}, {16, 2, 1}, {4, 3, 1}};
+                                                       {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1841,6 +1850,8 @@ struct SplitSweep {
     const TF* Ug;
     const int* Pg;
     int n, maxLc, maxUc, gs, es, c, lane;
+    // a block of the partitioned solve (PART sweeps): columns [c0, c1), y holds rows base ..
+    int c0 = 0, c1 = 0, base = 0;
 };
 
 // One pass of a column's entries (slots es, es + 16, ...): NP > 0 unrolls NP predicated passes
@@ -1859,17 +1870,20 @@ __device__ __forceinline__ void column_passes(int e0, int e1, int es, F&& f) {
     }
 }
 
-// forward: L with the row interchanges
-template <class TF, int CH, int ST, int NP>
+// forward: L with the row interchanges (PART: the columns [c0, c1) of a block, on the rows held
+// from w.base; else every column)
+template <class TF, int CH, int ST, int NP, bool PART = false>
 __device__ __forceinline__ void split_forward(const SplitSweep<TF>& w) {
     using T = typename CompT<TF>::T;
     TF* y = w.y;
     const int n = w.n, gs = w.gs, c = w.c;
-    const int nch = (n - 1 + CH - 1) / CH;
+    const int cb = PART ? w.c0 : 0, ce = PART ? w.c1 : n - 1;
+    const int yb = PART ? w.base : 0;
+    const int nch = (ce - cb + CH - 1) / CH;
     auto issue = [&](int ch) {
         if (ch < nch) {
             const int buf = ch % ST;
-            const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+            const int j0 = cb + ch * CH, j1 = min(j0 + CH, ce);
             warp_stage(w.Lb + (size_t)buf * w.maxLc * 2, w.Lg + (size_t)w.s_offL[j0] * 2,
                        (w.s_offL[j1] - w.s_offL[j0]) * 2);
             warp_stage(w.Pb + (size_t)buf * CH * 2, w.Pg + (size_t)j0 * 2, (j1 - j0) * 2);
@@ -1883,7 +1897,7 @@ __device__ __forceinline__ void split_forward(const SplitSweep<TF>& w) {
         __syncwarp();
         const TF* Lc = w.Lb + (size_t)(ch % ST) * w.maxLc * 2;
         const int* Pc = w.Pb + (size_t)(ch % ST) * CH * 2;
-        const int j0 = ch * CH, j1 = min(j0 + CH, n - 1);
+        const int j0 = cb + ch * CH, j1 = min(j0 + CH, ce);
         const int base = w.s_offL[j0];
         int e1 = base;
 #pragma unroll
@@ -1891,8 +1905,8 @@ __device__ __forceinline__ void split_forward(const SplitSweep<TF>& w) {
             const int j = j0 + jj;
             if (j >= j1) break;
             const int l = Pc[jj * 2 + gs];
-            const TF bj = y[l];
-            const TF yj0 = y[j];
+            const TF bj = y[l - yb];
+            const TF yj0 = y[j - yb];
             const int e0 = e1;
             e1 = w.s_offL[j + 1];
             __syncwarp();
@@ -1900,29 +1914,31 @@ __device__ __forceinline__ void split_forward(const SplitSweep<TF>& w) {
             const T yj0c = comp(yj0, c);
             column_passes<NP>(e0, e1, w.es, [&](int e) {
                 const int i = j + 1 + w.s_Lrow[e];
-                T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                T* yi = reinterpret_cast<T*>(&y[i - yb]) + c;
                 const T vc = (i == l) ? yj0c : *yi;
                 *yi = cfms_comp<TF>(vc, Lc[(e - base) * 2 + gs], bq);
             });
             if (w.lane == 0) {
-                y[j] = bj;
-                if (l != j && !((w.s_Lmask[j] >> (l - j - 1)) & 1u)) y[l] = yj0;
+                y[j - yb] = bj;
+                if (l != j && !((w.s_Lmask[j] >> (l - j - 1)) & 1u)) y[l - yb] = yj0;
             }
             __syncwarp();
         }
     }
 }
 
-// backward: U (each column's first entry is its diagonal, held as -1/u_jj)
-template <class TF, int CH, int ST, int NP>
+// backward: U (each column's first entry is its diagonal, held as -1/u_jj); PART as split_forward
+template <class TF, int CH, int ST, int NP, bool PART = false>
 __device__ __forceinline__ void split_backward(const SplitSweep<TF>& w) {
     using T = typename CompT<TF>::T;
     TF* y = w.y;
     const int n = w.n, gs = w.gs, c = w.c;
-    const int nch = (n + CH - 1) / CH;
+    const int sb = PART ? n - w.c1 : 0, se = PART ? n - w.c0 : n;     // sweep index s = n - 1 - j
+    const int yb = PART ? w.base : 0;
+    const int nch = (se - sb + CH - 1) / CH;
     auto issue = [&](int ch) {
         if (ch < nch) {
-            const int s0 = ch * CH, s1 = min(s0 + CH, n);
+            const int s0 = sb + ch * CH, s1 = min(s0 + CH, se);
             warp_stage(w.Ub + (size_t)(ch % ST) * w.maxUc * 2, w.Ug + (size_t)w.s_offU[s0] * 2,
                        (w.s_offU[s1] - w.s_offU[s0]) * 2);
         }
@@ -1934,7 +1950,7 @@ __device__ __forceinline__ void split_backward(const SplitSweep<TF>& w) {
         cp_async_wait<ST - 1>();
         __syncwarp();
         const TF* Uc = w.Ub + (size_t)(ch % ST) * w.maxUc * 2;
-        const int s0 = ch * CH, s1 = min(s0 + CH, n);
+        const int s0 = sb + ch * CH, s1 = min(s0 + CH, se);
         const int base = w.s_offU[s0];
         int e1 = base;
 #pragma unroll
@@ -1944,12 +1960,12 @@ __device__ __forceinline__ void split_backward(const SplitSweep<TF>& w) {
             const int j = n - 1 - s;
             const int e0 = e1;
             e1 = w.s_offU[s + 1];
-            const TF yj = y[j];
+            const TF yj = y[j - yb];
             __syncwarp();
             const CompB<TF> bq = comp_b(yj, c);
             column_passes<NP>(e0, e1, w.es, [&](int e) {
                 const int i = j - w.s_Udist[e];
-                T* yi = reinterpret_cast<T*>(&y[i]) + c;
+                T* yi = reinterpret_cast<T*>(&y[i - yb]) + c;
                 const T vc = e == e0 ? T(0) : *yi;
                 *yi = cfms_comp<TF>(vc, Uc[(e - base) * 2 + gs], bq);
             });
@@ -2102,6 +2118,262 @@ k_solve_split_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
     solve_split_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], blockIdx.x - ms.block_start[b]);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Partitioned solve (small batches, FP64): the latency of one warp's column chain bounds the sweeps
+// of a small batch (one warp per system, the SMs mostly idle). The columns of a system are split in
+// blocks of kPartM; block k's forward sweep maps the values on its first kwf rows (the window the
+// previous blocks leave) and the right-hand side on its other rows linearly to its final rows and
+// to the window it leaves the next block, so
+//     out_k = sweep_k(b) + R_k delta_k,   delta_{k+1} = (window part of out_k) - b on those rows,
+// where sweep_k(b) is the block's sweep of the right-hand side alone (all blocks at once, one warp
+// each), R_k the block's responses to unit window values (built once per factorization by the same
+// sweep), and the kwf-vectors delta_k the only sequential part. The backward sweep is split the same
+// way, from the last block up, with windows of kwb = kl + ku rows (the reach of a U column). The
+// same operations as the sequential sweeps, grouped otherwise: the results agree to rounding. This
+// is the partitioned ("SPIKE") solve of banded systems (Polizzi and Sameh, 2006) applied to the
+// sweeps of the factored system.
+constexpr int kPartM = 32;              // columns per block
+constexpr int kPartCH = 8, kPartST = 2; // staging of the blocks' factor streams
+constexpr int kPartMaxWarps = 32;       // blocks per system: n <= 1024
+
+struct PartArgs {
+    CompactIdx ix;
+    CompactData<zd> cd;
+    SolveIo io;
+    const zd* Rf;                       // [batch][nbf][32 + kwf][kwf]
+    const zd* Rb;                       // [batch][nbb][32 + kwb][kwb]
+    int nbf, nbb, kwf, kwb, maxLc, maxUc;
+};
+
+// shared memory of one warp's block sweep: its block buffer and the staging ring
+__host__ __device__ inline size_t part_warp_elems(int maxLc, int maxUc) {
+    return 64 + (size_t)kPartST * (maxLc + maxUc) * 2 + ((size_t)kPartST * kPartCH * 2 * sizeof(int) + 15) / 16;
+}
+__host__ __device__ inline size_t part_index_bytes(int n, int nL, int nU) {
+    return (((size_t)(n + 1) * 8 + (size_t)n * 4 + nL + nU) + 15) & ~(size_t)15;
+}
+
+// load the stream index lists of a bucket into shared memory (every thread of the block)
+__device__ __forceinline__ void part_load_index(const CompactIdx& ix, unsigned char* sm, int** offL, int** offU,
+                                                unsigned** Lmask, unsigned char** Lrow, unsigned char** Udist) {
+    const int n = ix.n;
+    *offL = reinterpret_cast<int*>(sm);
+    *offU = *offL + (n + 1);
+    *Lmask = reinterpret_cast<unsigned*>(*offU + (n + 1));
+    *Lrow = reinterpret_cast<unsigned char*>(*Lmask + n);
+    *Udist = *Lrow + ix.nL;
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) {
+        (*offL)[i] = ix.offL[i];
+        (*offU)[i] = ix.offU[i];
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) (*Lmask)[i] = ix.Lmask[i];
+    for (int i = threadIdx.x; i < ix.nL; i += blockDim.x) (*Lrow)[i] = ix.Lrow[i];
+    for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) (*Udist)[i] = ix.Udist[i];
+}
+
+template <int NPF, int NPB>
+__device__ __forceinline__ void part_sweep(const SplitSweep<zd>& w, bool forward) {
+    if (forward) split_forward<zd, kPartCH, kPartST, NPF, true>(w);
+    else split_backward<zd, kPartCH, kPartST, NPB, true>(w);
+}
+
+// The responses: one warp per (system, direction, block, unit position u). Forward: the unit at the
+// block's window row u (row c0 + u); backward: at row c1 - kwb + u (the rows the blocks below
+// update), the last block's (never used: nothing lies below it) written as zeros.
+template <int NPF, int NPB>
+__global__ void __launch_bounds__(256) k_part_build(PartArgs pa, zd* Rf, zd* Rb) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const CompactIdx& ix = pa.ix;
+    int *s_offL, *s_offU;
+    unsigned* s_Lmask;
+    unsigned char *s_Lrow, *s_Udist;
+    part_load_index(ix, sm, &s_offL, &s_offU, &s_Lmask, &s_Lrow, &s_Udist);
+    __syncthreads();
+    const int n = ix.n, lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const long long per_sys = (long long)pa.nbf * pa.kwf + (long long)pa.nbb * pa.kwb;
+    const long long task = (long long)blockIdx.x * nw + wib;
+    if (task >= per_sys * ix.batch) return;
+    const int sys = (int)(task / per_sys);
+    long long rem = task - (long long)sys * per_sys;
+    const bool fwd = rem < (long long)pa.nbf * pa.kwf;
+    if (!fwd) rem -= (long long)pa.nbf * pa.kwf;
+    const int kw = fwd ? pa.kwf : pa.kwb;
+    const int k = (int)(rem / kw), u = (int)(rem - (long long)k * kw);
+    const int c0 = k * kPartM;
+    const int c1 = fwd ? min(c0 + kPartM, n - 1) : min(c0 + kPartM, n);
+    const int len = kPartM + kw;
+    zd* buf = reinterpret_cast<zd*>(sm + part_index_bytes(n, ix.nL, ix.nU)) +
+              (size_t)wib * part_warp_elems(pa.maxLc, pa.maxUc);
+    for (int i = lane; i < 64; i += 32) buf[i] = zd(0.0, 0.0);
+    __syncwarp();
+    const bool last_b = !fwd && k == pa.nbb - 1;
+    if (!last_b) {
+        if (lane == 0) buf[fwd ? u : kPartM + u] = zd(1.0, 0.0);
+        __syncwarp();
+        const int gs = sys & 1, wgs = sys >> 1;
+        SplitSweep<zd> w{buf, s_offL, s_offU, s_Lmask, s_Lrow, s_Udist, buf + 64,
+                         buf + 64 + (size_t)kPartST * pa.maxLc * 2,
+                         reinterpret_cast<int*>(buf + 64 + (size_t)kPartST * (pa.maxLc + pa.maxUc) * 2),
+                         pa.cd.L + (size_t)wgs * ix.nL * 2, pa.cd.U + (size_t)wgs * ix.nU * 2,
+                         pa.cd.piv + (size_t)wgs * n * 2, n, pa.maxLc, pa.maxUc, gs, lane >> 1, lane & 1, lane};
+        w.c0 = c0;
+        w.c1 = c1;
+        w.base = fwd ? c0 : c0 - pa.kwb;
+        if (c1 > c0) part_sweep<NPF, NPB>(w, fwd);
+    }
+    zd* R = fwd ? Rf + (((size_t)sys * pa.nbf + k) * len) * kw : Rb + (((size_t)sys * pa.nbb + k) * len) * kw;
+    for (int i = lane; i < len; i += 32) R[(size_t)i * kw + u] = buf[i];
+}
+
+// complex c = a b (component by component, for the responses' sums)
+__device__ __forceinline__ zd part_cmac(zd acc, zd a, zd b) {
+    return zd(fma(-a.im, b.im, fma(a.re, b.re, acc.re)), fma(a.im, b.re, fma(a.re, b.im, acc.im)));
+}
+
+// The solve: one block per system, one warp per column block.
+struct MultiPart {
+    int nb;
+    int block_start[kMaxMulti + 1];
+    PartArgs a[kMaxMulti];
+};
+
+template <int NPF, int NPB>
+__global__ void __launch_bounds__(32 * kPartMaxWarps) k_solve_part(const __grid_constant__ MultiPart mp) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    int b = 0;
+    while (b + 1 < mp.nb && (int)blockIdx.x >= mp.block_start[b + 1]) ++b;
+    const PartArgs& pa = mp.a[b];
+    const CompactIdx& ix = pa.ix;
+    const CompactData<zd>& cd = pa.cd;
+    const int sys = blockIdx.x - mp.block_start[b];
+    const int n = ix.n, r = ix.r, lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int kwf = pa.kwf, kwb = pa.kwb, nbf = pa.nbf, nbb = pa.nbb;
+    int *s_offL, *s_offU;
+    unsigned* s_Lmask;
+    unsigned char *s_Lrow, *s_Udist;
+    part_load_index(ix, sm, &s_offL, &s_offU, &s_Lmask, &s_Lrow, &s_Udist);
+    zd* y = reinterpret_cast<zd*>(sm + part_index_bytes(n, ix.nL, ix.nU));      // n (+ 64: z, S)
+    zd* df = y + n + 64;                                                       // (nbf + 1) x kwf
+    zd* db = df + (size_t)(nbf + 1) * kwf;                                     // (nbb + 1) x kwb
+    zd* wk = db + (size_t)(nbb + 1) * kwb;
+    zd* buf = wk + (size_t)wib * part_warp_elems(pa.maxLc, pa.maxUc);
+    // the right-hand side, rows in solver order
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = io_load<zd, IO_MAPPED>(pa.io, sys, n, cd.perm[i]);
+    for (int i = threadIdx.x; i < (nbf + 1) * kwf; i += blockDim.x) df[i] = zd(0.0, 0.0);
+    for (int i = threadIdx.x; i < (nbb + 1) * kwb; i += blockDim.x) db[i] = zd(0.0, 0.0);
+    __syncthreads();
+    const int gs = sys & 1, wgs = sys >> 1;
+    SplitSweep<zd> w{buf, s_offL, s_offU, s_Lmask, s_Lrow, s_Udist, buf + 64,
+                     buf + 64 + (size_t)kPartST * pa.maxLc * 2,
+                     reinterpret_cast<int*>(buf + 64 + (size_t)kPartST * (pa.maxLc + pa.maxUc) * 2),
+                     cd.L + (size_t)wgs * ix.nL * 2, cd.U + (size_t)wgs * ix.nU * 2, cd.piv + (size_t)wgs * n * 2,
+                     n, pa.maxLc, pa.maxUc, gs, lane >> 1, lane & 1, lane};
+    const int lenf = kPartM + kwf, lenb = kPartM + kwb;
+    // ---- forward: every block's sweep of the right-hand side (rows c0 .. c1 + kwf)
+    const int kf = wib, c0f = kf * kPartM, c1f = min(c0f + kPartM, n - 1);
+    if (kf < nbf) {
+        for (int i = lane; i < 64; i += 32) buf[i] = (i < lenf && c0f + i < n) ? y[c0f + i] : zd(0.0, 0.0);
+        __syncwarp();
+        w.c0 = c0f;
+        w.c1 = c1f;
+        w.base = c0f;
+        if (c1f > c0f) part_sweep<NPF, NPB>(w, true);
+    }
+    __syncthreads();
+    // the windows, block after block (one warp; lanes over window row and component)
+    if (wib == 0) {
+        const int t = lane >> 1, cc = lane & 1;
+        for (int k = 0; k + 1 < nbf; ++k) {
+            const int c1 = (k + 1) * kPartM;
+            const zd* bk = wk + (size_t)k * part_warp_elems(pa.maxLc, pa.maxUc);
+            if (t < kwf && c1 + t < n) {
+                const zd* Rk = pa.Rf + (((size_t)sys * nbf + k) * lenf + kPartM + t) * kwf;
+                const zd* dk = df + (size_t)k * kwf;
+                zd acc = bk[kPartM + t] - y[c1 + t];
+                for (int v = 0; v < kwf; ++v) acc = part_cmac(acc, Rk[v], dk[v]);
+                if (cc == 0) df[(size_t)(k + 1) * kwf + t] = acc;
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    // final rows of the forward sweep: out = sweep(b) + R delta
+    if (kf < nbf) {
+        const int rows = (kf == nbf - 1) ? n - c0f : kPartM;
+        const zd* dk = df + (size_t)kf * kwf;
+        const zd* Rk = pa.Rf + ((size_t)sys * nbf + kf) * lenf * kwf;
+        for (int i = lane; i < rows; i += 32) {
+            zd acc = buf[i];
+            for (int v = 0; v < kwf; ++v) acc = part_cmac(acc, Rk[(size_t)i * kwf + v], dk[v]);
+            y[c0f + i] = acc;
+        }
+    }
+    __syncthreads();
+    // ---- backward: every block's sweep of the forward result (rows c0 - kwb .. c1)
+    const int kb = wib, c0b = kb * kPartM, c1b = min(c0b + kPartM, n);
+    if (kb < nbb) {
+        for (int i = lane; i < 64; i += 32) {
+            const int g = c0b - kwb + i;
+            buf[i] = (i < lenb && g >= 0 && g < c1b) ? y[g] : zd(0.0, 0.0);
+        }
+        __syncwarp();
+        w.c0 = c0b;
+        w.c1 = c1b;
+        w.base = c0b - kwb;
+        part_sweep<NPF, NPB>(w, false);
+    }
+    __syncthreads();
+    // the windows from the last block up (warps 0 and 1: lanes over window row and component; every
+    // warp takes part in the block barrier of each step)
+    for (int k = nbb - 1; k >= 1; --k) {
+        const int t = 16 * wib + (lane >> 1), cc = lane & 1;
+        const int c0 = k * kPartM;
+        if (wib < 2 && t < kwb && c0 - kwb + t >= 0) {
+            const zd* bk = wk + (size_t)k * part_warp_elems(pa.maxLc, pa.maxUc);
+            const zd* Rk = pa.Rb + (((size_t)sys * nbb + k) * lenb + t) * kwb;
+            const zd* dk = db + (size_t)k * kwb;
+            zd acc = bk[t] - y[c0 - kwb + t];
+            for (int v = 0; v < kwb; ++v) acc = part_cmac(acc, Rk[v], dk[v]);
+            if (cc == 0) db[(size_t)(k - 1) * kwb + t] = acc;
+        }
+        __syncthreads();
+    }
+    if (kb < nbb) {
+        const int rows = c1b - c0b;
+        const zd* dk = db + (size_t)kb * kwb;
+        const zd* Rk = pa.Rb + ((size_t)sys * nbb + kb) * lenb * kwb;
+        for (int i = lane; i < rows; i += 32) {
+            zd acc = buf[kwb + i];
+            for (int v = 0; v < kwb; ++v) acc = part_cmac(acc, Rk[(size_t)(kwb + i) * kwb + v], dk[v]);
+            y[c0b + i] = acc;
+        }
+    }
+    __syncthreads();
+    // ---- Woodbury: z = S^{-1} V^T y (warp a % nw takes border row a), y -= W z
+    zd* zb = y + n;
+    if (r > 0) {
+        const zd* Vg = cd.V + (size_t)wgs * ix.nV * 2;
+        for (int a = wib; a < r; a += nw) {
+            zd acc(0.0, 0.0);
+            for (int e = ix.offV[a] + lane; e < ix.offV[a + 1]; e += 32)
+                acc = cfma(acc, Vg[(size_t)e * 2 + gs], y[ix.Vcol[e]]);
+            for (int m = 16; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
+            if (lane == 0) zb[a] = acc;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        __syncthreads();
+        const zd* Ws = cd.W + (size_t)sys * r * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            zd acc = y[i];
+            for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
+            y[i] = acc;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) io_store<zd, IO_MAPPED>(pa.io, sys, n, i, y[i]);
 }
 
 }  // namespace cng
@@ -2257,6 +2529,24 @@ static void compact(Banded& h, cudaStream_t st) {
     h.cMaxLcol = h.cMaxUcol = 0;
     for (int j = 0; j + 1 < n; ++j) h.cMaxLcol = std::max(h.cMaxLcol, offL[j + 1] - offL[j]);
     for (int s2 = 0; s2 < n; ++s2) h.cMaxUcol = std::max(h.cMaxUcol, offU[s2 + 1] - offU[s2]);
+    // the partitioned solve stages each block's streams in chunks of kPartCH columns from the
+    // block's first column (forward) or from its last (backward): the largest such chunk
+    h.p_maxLc = h.p_maxUc = 1;
+    for (int c0 = 0; c0 < n - 1; c0 += kPartM) {
+        const int c1 = std::min(c0 + kPartM, n - 1);
+        for (int j0 = c0; j0 < c1; j0 += kPartCH)
+            h.p_maxLc = std::max(h.p_maxLc, offL[std::min(j0 + kPartCH, c1)] - offL[j0]);
+    }
+    for (int c0 = 0; c0 < n; c0 += kPartM) {
+        const int c1 = std::min(c0 + kPartM, n), sb = n - c1, se = n - c0;
+        for (int s0 = sb; s0 < se; s0 += kPartCH)
+            h.p_maxUc = std::max(h.p_maxUc, offU[std::min(s0 + kPartCH, se)] - offU[s0]);
+    }
+    // responses of an earlier factor set are stale
+    dev_free(h.p_Rf);
+    dev_free(h.p_Rb);
+    h.p_Rf = h.p_Rb = nullptr;
+    h.part_ready = false;
     h.cL = (int)Lrow.size();
     h.cU = (int)Udist.size();
     h.cV = (int)Vcol.size();
@@ -2334,6 +2624,113 @@ static bool launch_solve_compact(const Banded& h, int io_kind, const SolveIo& io
 }  // namespace cng
 
 namespace cng {
+
+// ---- the partitioned solve: arguments, responses, launch
+static PartArgs part_args(const Banded& h, const SolveIo& io) {
+    PartArgs pa{};
+    pa.ix = compact_idx(h, kPartCH);
+    pa.cd = CompactData<zd>{static_cast<const zd*>(h.c_L), static_cast<const zd*>(h.c_U), h.c_piv,
+                            static_cast<const zd*>(h.c_V), static_cast<const zd*>(h.w),
+                            static_cast<const zd*>(h.slu), h.spiv, h.perm, h.flip_r, h.flip_c};
+    pa.io = io;
+    pa.Rf = static_cast<const zd*>(h.p_Rf);
+    pa.Rb = static_cast<const zd*>(h.p_Rb);
+    pa.nbf = h.p_nbf;
+    pa.nbb = h.p_nbb;
+    pa.kwf = h.p_kwf;
+    pa.kwb = h.p_kwb;
+    pa.maxLc = h.p_maxLc;
+    pa.maxUc = h.p_maxUc;
+    return pa;
+}
+
+// unrolled column passes: 1 or 2 where every column fits 16 or 32 entry slots, 0 (a loop) else
+static int part_passes(int maxcol) { return maxcol <= 16 ? 1 : (maxcol <= 32 ? 2 : 0); }
+
+template <class F>
+static void part_dispatch(int npf, int npb, F&& f) {
+    auto b = [&](auto pf) {
+        if (npb == 1) f(pf, std::integral_constant<int, 1>{});
+        else if (npb == 2) f(pf, std::integral_constant<int, 2>{});
+        else f(pf, std::integral_constant<int, 0>{});
+    };
+    if (npf == 1) b(std::integral_constant<int, 1>{});
+    else if (npf == 2) b(std::integral_constant<int, 2>{});
+    else b(std::integral_constant<int, 0>{});
+}
+
+// The responses of every block of every system (once per factor set; the legacy stream, waited
+// for). Refused where the partitioned solve does not apply or would hold too much memory: shared
+// pairs, kl > 16, kl + ku > 32, n > 1024, or more than 256 MB of responses (it is meant for the
+// small batches whose sweeps one warp per system leaves latency-bound).
+static void build_part(Banded& h) {
+    if (h.part_ready) return;
+    if (!h.compact_ready || h.dtype != 1) throw InvalidArgument("the partitioned solve needs a compact complex128 handle");
+    if (h.shared) throw InvalidArgument("the partitioned solve does not solve shared pairs: a compact two-system schedule");
+    const int n = h.n, kwf = h.kl, kwb = h.kl + h.ku;
+    if (kwf < 1 || kwf > 16 || kwb > kPartM)
+        throw InvalidArgument("partitioned solve: band outside kl <= 16, kl + ku <= 32");
+    const int nbf = ceil_div(n - 1, kPartM), nbb = ceil_div(n, kPartM);
+    if (n < 2 || std::max(nbf, nbb) > kPartMaxWarps) throw InvalidArgument("partitioned solve: 2 <= n <= 1024");
+    const size_t ef = (size_t)h.batch * nbf * (kPartM + kwf) * kwf, eb = (size_t)h.batch * nbb * (kPartM + kwb) * kwb;
+    if ((ef + eb) * sizeof(zd) > ((size_t)256 << 20))
+        throw InvalidArgument("partitioned solve: a small-batch schedule (its responses would exceed 256 MB)");
+    const int nw = 8;
+    const size_t smem = part_index_bytes(n, h.cL, h.cU) + (size_t)nw * part_warp_elems(h.p_maxLc, h.p_maxUc) * sizeof(zd);
+    if (smem > 220 * 1024) throw InvalidArgument("partitioned solve: streams too large for shared memory");
+    dalloc(&h.p_Rf, ef, sizeof(zd));
+    dalloc(&h.p_Rb, eb, sizeof(zd));
+    h.p_nbf = nbf;
+    h.p_nbb = nbb;
+    h.p_kwf = kwf;
+    h.p_kwb = kwb;
+    const PartArgs pa = part_args(h, SolveIo{});
+    const long long tasks = (long long)h.batch * ((long long)nbf * kwf + (long long)nbb * kwb);
+    part_dispatch(part_passes(h.cMaxLcol), part_passes(h.cMaxUcol), [&](auto pf, auto pb) {
+        constexpr int PF = decltype(pf)::value, PB = decltype(pb)::value;
+        ensure_smem_attr((const void*)k_part_build<PF, PB>, 220 * 1024);
+        k_part_build<PF, PB><<<ceil_div(tasks, nw), 32 * nw, smem, nullptr>>>(pa, static_cast<zd*>(h.p_Rf),
+                                                                            static_cast<zd*>(h.p_Rb));
+        CNG_LAUNCH("k_part_build");
+    });
+    CNG_CUDA(cudaStreamSynchronize(nullptr));
+    h.part_ready = true;
+}
+
+static void launch_part(const std::vector<const Banded*>& hs, const std::vector<SolveIo>& ios,
+                        const std::vector<SolveIo>& ios2, const std::vector<int>& rng, cudaStream_t st) {
+    MultiPart mp{};
+    mp.nb = (int)hs.size();
+    int nw = 2, npf = 1, npb = 1, blocks = 0;
+    size_t smem = 0;
+    for (size_t i = 0; i < hs.size(); ++i) {
+        const Banded& h = *hs[i];
+        if (!h.part_ready) throw InvalidArgument("the partitioned solve's responses are not built (cng_banded_set_schedule)");
+        if (rng[2 * i + 1] >= 0) throw InvalidArgument("the partitioned solve solves whole batches (no system range)");
+        if (ios2[i].rhs) throw InvalidArgument("the partitioned solve does not solve shared pairs");
+        nw = std::max(nw, std::max(h.p_nbf, h.p_nbb));
+        const int pf = part_passes(h.cMaxLcol), pb = part_passes(h.cMaxUcol);
+        npf = (pf == 0 || npf == 0) ? 0 : std::max(npf, pf);
+        npb = (pb == 0 || npb == 0) ? 0 : std::max(npb, pb);
+    }
+    for (size_t i = 0; i < hs.size(); ++i) {
+        const Banded& h = *hs[i];
+        mp.block_start[i] = blocks;
+        mp.a[i] = part_args(h, ios[i]);
+        blocks += h.batch;
+        const size_t vec = (size_t)h.n + 64 + (size_t)(h.p_nbf + 1) * h.p_kwf + (size_t)(h.p_nbb + 1) * h.p_kwb;
+        smem = std::max(smem, part_index_bytes(h.n, h.cL, h.cU) +
+                                  (vec + (size_t)nw * part_warp_elems(h.p_maxLc, h.p_maxUc)) * sizeof(zd));
+    }
+    mp.block_start[mp.nb] = blocks;
+    if (smem > 220 * 1024) throw InvalidArgument("partitioned solve: streams too large for shared memory");
+    part_dispatch(npf, npb, [&](auto pf, auto pb) {
+        constexpr int PF = decltype(pf)::value, PB = decltype(pb)::value;
+        ensure_smem_attr((const void*)k_solve_part<PF, PB>, 220 * 1024);
+        k_solve_part<PF, PB><<<blocks, 32 * nw, smem, st>>>(mp);
+        CNG_LAUNCH("k_solve_part");
+    });
+}
 
 // warp groups [first, end) of handle h that solve systems [s0, s1) (s1 < 0: all)
 static void group_range(const Banded& h, int s0, int s1, int& first, int& end) {
@@ -2487,6 +2884,10 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 8: launch_split_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
         case 9: launch_split_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, rng, sched, st); break;
         case 10: launch_split_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, rng, sched, st); break;
+        case kPartSchedule:
+            if constexpr (std::is_same<TF, zd>::value) launch_part(hs, ios, ios2, rng, st);
+            else throw InvalidArgument("the partitioned solve is FP64 only: another schedule for the FP32 form");
+            break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }
@@ -2636,6 +3037,14 @@ int cng_banded_set_schedule(cng_banded* hh, int sched) {
         if (!h) throw InvalidArgument("null handle");
         if (sched < -1 || sched >= kNumSchedules) throw InvalidArgument("schedule out of range");
         if (sched >= 0 && !h->compact_ready) throw InvalidArgument("compact schedules need cng_banded_compact first");
+        if (sched == cng::kPartSchedule) {
+            cng::build_part(*h);                   // the responses (refused where it does not apply)
+        } else if (h->part_ready) {                // another schedule: the responses are not kept
+            dev_free(h->p_Rf);
+            dev_free(h->p_Rb);
+            h->p_Rf = h->p_Rb = nullptr;
+            h->part_ready = false;
+        }
         h->sched = sched;
     })
 }

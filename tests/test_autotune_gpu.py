@@ -38,12 +38,20 @@ def test_every_schedule_solves_alike(tname, sizes, share, precision, rng, cuda_l
     tol = 1e-10 if precision == "fp64" else 1e-5
     r = dev.zeros()
     split = autotune.split_schedules()
+    part = autotune.partitioned_schedules()
     refused = set()
     for sched in autotune.schedules():
         out = dev.zeros()
-        autotune.apply(fs, sched)
         if dev.shared and (sched < 0 or sched in split):
-            # a shared pair needs a compact two-system schedule: refused, never run otherwise
+            # a shared pair needs a compact two-system schedule: refused, never run otherwise (the
+            # partitioned schedule already when it is set)
+            with pytest.raises(ValueError):
+                autotune.apply(fs, sched)
+                dev.solve(a, b, rhs, out)
+            refused.add(sched)
+            continue
+        autotune.apply(fs, sched)
+        if precision == "fp32" and sched in part:       # the partitioned solve is FP64 only
             with pytest.raises(ValueError):
                 dev.solve(a, b, rhs, out)
             refused.add(sched)
