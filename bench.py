@@ -295,11 +295,13 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from conatus_gb300 import workloads as W
-    from conatus_gb300.ivp import IVPSolver
+    from conatus_gb300.ivp import DeviceProblem, IVPSolver
     cfg = args.cfg
     P = W.problem(args.config, args.fourier)
     C0 = W.initial_state(args.config, P, seed=rank)
-    solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=args.precision)
+    dp = DeviceProblem(P, args.precision)
+    dp.partitioned = dp.partitioned or args.partitioned
+    solver = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], precision=args.precision, device_problem=dp)
     dev = solver.dev
     solver.set_state(C0)
     solver.run_graph(max(args.warmup, solver.ring))            # start-up, capture, warm-up
@@ -383,7 +385,8 @@ def run_gpu(args):
     e2e_s = (time.perf_counter() - t0) / ke
     nbytes = dev.n_total * 16
     out = {
-        "metric": METRIC[args.config] + (" FP32 form" if args.precision == "fp32" else " plain FP64"),
+        "metric": METRIC[args.config] + (" FP32 form" if args.precision == "fp32" else " plain FP64") +
+                  (", partitioned solve allowed" if args.partitioned else ""),
         "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
@@ -425,8 +428,9 @@ def run_gpu(args):
 def subrecords(args):
     """The other configurations, compact and time-bounded, beside the default line: the serving
     stream (100 requests at 200/s, steps U[1000, 20000]; FP64 and the FP32 form under the 150 GB
-    budget, FP64 under a 1.5 GB budget that binds), the KS ensemble (4096 members, 500 steps) and the
-    RB ensemble (1024 cases of three Nz, 50 steps) in the FP32 form."""
+    budget, FP64 under a 1.5 GB budget that binds), RB 256x64 and Burgers in FP64 with and without
+    the partitioned solve, the KS ensemble (4096 members, 500 steps) and the RB ensemble (1024 cases
+    of three Nz, 50 steps) in the FP32 form."""
     import copy
     import torch
     out = {}
@@ -447,6 +451,8 @@ def subrecords(args):
                      "peak_planned_gb": st["peak_planned_bytes"] / 1e9, "budget_gb": budget / 1e9,
                      "workload": rec["config"]["workload"]}
         torch.cuda.empty_cache()
+    out["small_fp64_partitioned"] = partitioned_record()
+    torch.cuda.empty_cache()
     for name, fn, members, steps in (("ks_ensemble", ks_ensemble_record, 4096, 500),
                                      ("rb_ensemble", rb_ensemble_record, 1024, 50)):
         a = copy.copy(args)
@@ -457,6 +463,47 @@ def subrecords(args):
         out[name]["workload"] = rec["config"]["workload"]
         if "launches_per_step" in rec["config"]:
             out[name]["launches_per_step"] = rec["config"]["launches_per_step"]
+        torch.cuda.empty_cache()
+    return out
+
+
+def partitioned_record(steps=100, warmup=5):
+    """RB 256x64 (SBDF2 and RK443) and Burgers N=128 in FP64, graph-replayed steps with the tuner's
+    sequential-sweep schedules and with the partitioned solve allowed, from the same state: steps/s
+    of each and the relative difference of the two final states (the partitioned solve's rounding).
+    100 steps: RB's configured state grows too fast to stay finite past about 200 steps at dt=1e-4."""
+    import torch
+    from conatus_gb300 import workloads as W
+    from conatus_gb300.ivp import DeviceProblem, IVPSolver
+    out = {}
+    for name, config, scheme in (("rayleigh_benard_sbdf2", "rayleigh_benard", None),
+                                 ("rayleigh_benard_rk443", "rayleigh_benard", "RK443"),
+                                 ("burgers_sbdf2", "burgers", None)):
+        cfg = W.CONFIGS[config]
+        P = W.problem(config)
+        C0 = W.initial_state(config, P, seed=0)
+        rec, X = {}, []
+        for part in (False, True):
+            dev = DeviceProblem(P, "fp64")
+            dev.partitioned = part
+            s = IVPSolver(P, scheme=scheme or cfg["scheme"], dt=cfg["dt"], device_problem=dev)
+            s.set_state(C0)
+            s.run_graph(max(warmup, s.ring))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s.stream)
+            s.run_graph(steps)
+            e1.record(s.stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            key = "partitioned" if part else "sequential"
+            rec[key] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "solve_schedule": _schedule_summary(dev)}
+            X.append(s.X.clone())
+            del s, dev
+        rec["state_rel_diff"] = float(torch.linalg.vector_norm(X[1] - X[0]) / torch.linalg.vector_norm(X[0]))
+        rec["speedup"] = rec["sequential"]["ms_per_step"] / rec["partitioned"]["ms_per_step"]
+        rec["steps"] = steps
+        out[name] = rec
         torch.cuda.empty_cache()
     return out
 
@@ -491,8 +538,11 @@ def _schedule_summary(dev):
     """The solve schedule the autotuner kept (-1: band kernel; k >= 0: compact schedule k) and the
     time per solve it measured for each candidate."""
     from conatus_gb300 import autotune
-    for (prec, _), (best, times) in autotune.cache().items():
-        if prec == dev.precision:
+    cache = autotune.cache()
+    for fs in reversed(list(dev._factors.values())):          # the problem's own factor sets
+        hit = cache.get(autotune._signature(dev, fs))
+        if hit:
+            best, times = hit
             return {"chosen": best, "ms_per_solve": {str(k): round(v, 4) for k, v in times.items()}}
     return None
 
@@ -752,6 +802,9 @@ def main():
                     help="IMEX scheme instead of the configuration's (e.g. RK443: the reference's published "
                          "Rayleigh-Benard case); the CPU baseline times SBDF schemes only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--partitioned", action="store_true",
+                    help="FP64: let the solve tuner take the partitioned solve of small batches (faster "
+                         "on RB 256x64 and Burgers; residuals up to about 15x the sequential sweeps')")
     ap.add_argument("--no-forms", action="store_true", help="channel FP64: skip the FP32 form's line")
     ap.add_argument("--error-steps", type=int, default=None,
                     help="steps of the FP32 form's error run (default: the configuration's length)")

@@ -4,7 +4,9 @@ Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_
 -1)``) and the compact-stream schedules of ``cng_banded_schedules`` (two systems per warp over the
 union pattern of the factors, with different staging chunks and ring depths; one system per warp
 with the lanes split over entries and components for small batches; and the partitioned solve of
-small FP64 batches, one block of warps per system sweeping its blocks of 32 columns at once).
+small FP64 batches, one block of warps per system sweeping its blocks of 32 columns at once). The
+partitioned solve is a candidate only where the DeviceProblem opts into it (``dev.partitioned``,
+or CONATUS_GB300_PARTITIONED=1): its residuals run up to about 15x those of the sequential sweeps.
 Candidates a factor set cannot take (a shared pair, the FP32 form, a batch too large for the
 partitioned solve's responses) are refused by the library and skipped. Each candidate solves
 the step's systems (all buckets, one batched call, the FP32 form with its refinement residual) a
@@ -65,7 +67,8 @@ def cache() -> dict:
 
 
 def _signature(dev, fs):
-    return (dev.precision, tuple((h.batch, h.n, h.rank, h.kl, h.ku, getattr(h, "primary", -1)) for h in fs))
+    return (dev.precision, bool(getattr(dev, "partitioned", False)),
+            tuple((h.batch, h.n, h.rank, h.kl, h.ku, getattr(h, "primary", -1)) for h in fs))
 
 
 def apply(fs, sched: int) -> None:
@@ -90,6 +93,11 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
     if sig in _CACHE:
         apply(fs, _CACHE[sig][0])
         return _CACHE[sig][1]
+    if candidates is None:
+        candidates = schedules()
+        if not getattr(dev, "partitioned", False):       # opted into (its residuals run larger)
+            part = partitioned_schedules()
+            candidates = [c for c in candidates if c not in part]
     if stream is None:
         st = torch.cuda.current_stream()
     elif isinstance(stream, int):
@@ -101,7 +109,7 @@ def tune_solve(dev, key, fs, stream=None, reps: int = 3, candidates=None) -> dic
     with torch.cuda.stream(st):
         rhs.fill_(1.0)
     times = {}
-    for sched in (candidates if candidates is not None else schedules()):
+    for sched in candidates:
         try:
             apply(fs, sched)
             dev._solve_with(fs, key[0], key[1], rhs, out, st)          # warm-up (and first-use set-up)

@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 
 import numpy as np
 
@@ -104,6 +105,10 @@ class DeviceProblem:
         _lib.lib()
         self.factor_sets = factor_sets      # None: keep every (a, b) factorization, else at most this many
         self.autotune = True                # time the solve schedules on each new factor set
+        # let the tuner pick the partitioned solve of small FP64 batches (blocks of 32 columns swept
+        # at once): faster on small batches, but its residuals run up to about 15x those of the
+        # sequential sweeps (the blocks' separate responses cancel), so it is opted into
+        self.partitioned = os.environ.get("CONATUS_GB300_PARTITIONED", "0") == "1"
         self.refine = 1                     # FP32 form: refinement passes (FP64 residual + FP32 solve)
         self.overlap_refine = True          # FP32 form: two bucket groups refined on two streams
         self._aux = None

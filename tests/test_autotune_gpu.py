@@ -67,5 +67,5 @@ def test_every_schedule_solves_alike(tname, sizes, share, precision, rng, cuda_l
             assert np.array_equal(out.cpu().numpy(), ref_h), sched
     assert bool(dev.shared) == (share and tname.startswith("channel"))
     times = autotune.tune_solve(dev, (a, b), fs, reps=2)
-    assert set(times) == set(autotune.schedules()) - refused
+    assert set(times) == set(autotune.schedules()) - refused - part     # partitioned: opted into
     assert autotune.cache()[autotune._signature(dev, fs)][0] == min(times, key=times.get)

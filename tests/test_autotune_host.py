@@ -77,6 +77,7 @@ def fake(monkeypatch):
             h.schedule = int(sched)
     monkeypatch.setattr(autotune, "apply", apply)
     monkeypatch.setattr(autotune, "schedules", lambda: sorted(COST))
+    monkeypatch.setattr(autotune, "partitioned_schedules", lambda: set())
     monkeypatch.setattr(autotune, "_CACHE", {})
     monkeypatch.delenv("CONATUS_GB300_SOLVE_SCHEDULE", raising=False)
     return clock
@@ -95,6 +96,21 @@ def test_candidates_that_do_not_fit_are_skipped(fake):
     fs = [_Handle(100, 74)]
     times = autotune.tune_solve(_Dev(fake, refuse={1, 2}), (1.0, 0.5), fs)
     assert set(times) == {-1, 0, 3} and fs[0].schedule == 0
+
+
+def test_partitioned_schedule_only_when_opted_into(fake, monkeypatch):
+    """The partitioned solve (here the fastest, schedule 1) is timed only for a DeviceProblem that
+    opts into it; the two choices are cached apart."""
+    monkeypatch.setattr(autotune, "partitioned_schedules", lambda: {1})
+    fs = [_Handle(127, 262)]
+    times = autotune.tune_solve(_Dev(fake), (1.0, 0.5), fs)
+    assert 1 not in times and fs[0].schedule == 2
+    dev = _Dev(fake)
+    dev.partitioned = True
+    fs2 = [_Handle(127, 262)]
+    times = autotune.tune_solve(dev, (1.0, 0.5), fs2)
+    assert 1 in times and fs2[0].schedule == 1
+    assert len(autotune.cache()) == 2
 
 
 def test_no_fitting_candidate_is_an_error(fake):

@@ -92,16 +92,19 @@ def test_shared_solve_matches_the_compiled_reference(cuda_lib):
 
 def test_band_kernel_and_split_schedules_refuse_partners(cuda_lib):
     """A shared pair needs a compact two-system schedule: the band kernel and the split-lane
-    schedules refuse it (the autotuner skips them)."""
+    schedules refuse it at the solve, the partitioned solve already when it is set (the autotuner
+    skips them all)."""
     from conatus_gb300 import autotune
     P = template("channel_ny17").instantiate([8, 8])
     sh, _ = _devices(P, "fp64")
     a, b = 11 / 6 / 5e-3, 1.0
     fs = sh.factor(a, b)
     rhs, x = sh.zeros(), sh.zeros()
+    part = autotune.partitioned_schedules()
     for sched in [-1] + sorted(autotune.split_schedules()):
-        autotune.apply(fs, sched)
         with pytest.raises(ValueError):
+            autotune.apply(fs, sched)
+            assert sched not in part                     # refused where it is set
             sh.solve(a, b, rhs, x)
     autotune.apply(fs, 0)
     sh.solve(a, b, rhs, x)
