@@ -28,7 +28,8 @@ import os
 
 from ._lib import call
 
-__all__ = ["schedules", "split_schedules", "partitioned_schedules", "tune_solve", "tune_rhs", "cache"]
+__all__ = ["schedules", "split_schedules", "partitioned_schedules", "windowed_schedules", "tune_solve", "tune_rhs",
+           "cache"]
 
 _CACHE: dict = {}
 
@@ -40,26 +41,34 @@ def schedules() -> list:
     return [-1] + list(range(int(n.value)))
 
 
-def split_schedules() -> set:
-    """Compact schedules that run one system per warp with the lanes split over entries and
-    components (the latency variant: the same sweeps, another order of sums in the border
-    correction)."""
+def _flags() -> list:
     n = ctypes.c_int32()
     call("cng_banded_schedules", ctypes.byref(n), None, None, None)
     flags = (ctypes.c_int32 * n.value)()
     call("cng_banded_schedules", ctypes.byref(n), None, None, flags)
-    return {k for k in range(n.value) if flags[k]}
+    return list(flags)
+
+
+def split_schedules() -> set:
+    """Compact schedules that do not sweep two systems per warp over whole vectors and refuse
+    shared pairs: one system per warp with the lanes split over entries and components (the
+    latency variant: the same sweeps, another order of sums in the border correction), and the
+    partitioned solve."""
+    return {k for k, f in enumerate(_flags()) if f in (1, 2)}
 
 
 def partitioned_schedules() -> set:
     """Schedules of the partitioned solve (small batches, FP64: blocks of 32 columns swept at once
     with their responses to the blocks before them); refused for the FP32 form, shared pairs,
     system ranges and large batches."""
-    n = ctypes.c_int32()
-    call("cng_banded_schedules", ctypes.byref(n), None, None, None)
-    flags = (ctypes.c_int32 * n.value)()
-    call("cng_banded_schedules", ctypes.byref(n), None, None, flags)
-    return {k for k in range(n.value) if flags[k] == 2}
+    return {k for k, f in enumerate(_flags()) if f == 2}
+
+
+def windowed_schedules() -> set:
+    """Schedules of the windowed compact solve: the two-systems sweeps with a window of each vector
+    in shared memory and the rest in a per-handle scratch (more resident warps; the same bits as
+    schedule 0)."""
+    return {k for k, f in enumerate(_flags()) if f == 3}
 
 
 def cache() -> dict:

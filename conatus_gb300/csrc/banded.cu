@@ -753,7 +753,11 @@ struct Banded {
     int p_nbf = 0, p_nbb = 0, p_kwf = 0, p_kwb = 0, p_maxLc = 0, p_maxUc = 0;
     void* p_Rf = nullptr;           // [batch][nbf][32 + kwf][kwf] complex128
     void* p_Rb = nullptr;           // [batch][nbb][32 + kwb][kwb] complex128
-    int sched = 0;                  // compact solve schedule (index into kSchedules); -1: band kernel
+    // windowed schedules: the scratch the sweeps spill finished rows to ([cWg][kGroup][n], room
+    // for complex128; allocated by cng_banded_set_schedule)
+    void* w_scr = nullptr;
+    size_t w_cap = 0;               // entries
+    int sched = 0;                 // compact solve schedule (index into kSchedules); -1: band kernel
     int cG = 2;                     // systems per warp group of the compact streams (1: shared pair)
     bool shared = false;            // factors shared with a sign-similar partner bucket
     unsigned char* flip_r = nullptr;    // partner = diag(dr) A diag(dc): 1 where dr_i = -1
@@ -791,7 +795,7 @@ struct Banded {
                         (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32,
                         (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
                         (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
-                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c, p_Rf, p_Rb})
+                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c, p_Rf, p_Rb, w_scr})
             dev_free(p);
     }
 
@@ -1464,12 +1468,17 @@ constexpr int kCChunk = 8;              // columns per staged chunk (the default
 // latency variant for small batches, k_solve_split_multi).
 // Schedule 11 (split = 2) is the partitioned solve of small batches (k_solve_part: one block of
 // warps per system, blocks of 32 columns swept at once; FP64 only).
+// Schedules 12-15 (split = 3) are the windowed compact solve (k_solve_window_multi: the two-systems
+// sweeps with a window of each vector in shared memory and the rest in a global scratch, for more
+// resident warps per SM; the same bits as schedule 0).
 struct CompactSchedule { int chunk, stages, split; };
-constexpr int kNumSchedules = 12;
+constexpr int kNumSchedules = 16;
 constexpr int kPartSchedule = 11;
+constexpr int kWindowFlag = 3;
 constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
-                                                       {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2}};
+                                                       {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2},
+                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {4, 2, 3}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1480,6 +1489,8 @@ struct CompactIdx {
     int wg0;                            // first warp group solved (wgroups: one past the last)
     int maxLc, maxUc;                   // largest chunk of the L / U streams (entries)
     int maxLcol, maxUcol;               // most entries of one column of the L / U streams
+    int wmask;                          // windowed schedules: window slots - 1 (a power of two)
+    void* scratch;                      // windowed schedules: [warp group][kGroup][n] TF
     const int* offL;                    // n + 1
     const unsigned char* Lrow;          // nL: t (row kv + 1 + t of the column)
     const unsigned* Lmask;              // n: bit t set if row t is in the union
@@ -1803,6 +1814,270 @@ k_solve_compact_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
     solve_compact_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
+}
+
+// ---- windowed compact solve: the sweeps of solve_compact_body with a window of each vector -------
+// In the compact solve a system's vector y (n entries) takes most of a warp's shared memory, which
+// bounds the warps resident per SM, and the sweeps are latency-bound chains: more resident warps
+// is more throughput. A column touches rows j .. j + kl (forward) or j - kv .. j (backward) only,
+// so a ring of WS >= CH + kv + 1 rows (a power of two, ix.wmask = WS - 1) holds every row a chunk of
+// CH columns needs. The rows the next chunk brings in are loaded into registers one chunk ahead
+// (forward: the permuted right-hand side; backward: the forward result); the rows a chunk finishes
+// go to a per-handle scratch in global memory ([warp group][kGroup][n], ix.scratch: the forward
+// result, then the solution before the border correction), which the Woodbury pass and the output
+// read back. The operations and their order are those of the compact solve: the same bits.
+template <class TF, class TD, int IO, int CH, int ST>
+__device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const CompactData<TF>& cd,
+                                                  const SolveIo& io0, const SolveIo& io2, int block) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int g = lane / kLanesPer, lg = lane % kLanesPer;
+    const int wg = ix.wg0 + block * nw + wib;
+    const int gs = ix.gs;
+    const bool pair = gs == 1;
+    const bool partner = pair && g == 1;
+    const int gsel = pair ? 0 : g;
+    const int sys = pair ? wg : wg * kGroup + g;
+    const SolveIo& io = partner ? io2 : io0;
+    const bool live = sys < ix.batch && (!partner || io2.rhs != nullptr);
+    const bool wlive = wg < ix.wgroups;
+    const int n = ix.n, r = ix.r, M = ix.wmask, WS = ix.wmask + 1;
+    // shared memory: index lists, then per warp the windows win[G][WS + 64] (z and S after each
+    // window), then the staging buffers
+    int* s_offL = reinterpret_cast<int*>(sm);
+    int* s_offU = s_offL + (n + 1);
+    unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
+    unsigned char* s_Lrow = reinterpret_cast<unsigned char*>(s_Lmask + n);
+    unsigned char* s_Udist = s_Lrow + ix.nL;
+    size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
+    off = (off + 15) & ~(size_t)15;
+    const size_t per_warp = (size_t)kGroup * (WS + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * gs +
+                            (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
+    TF* win = y0 + (size_t)g * (WS + 64);
+    TF* zb = win + WS;
+    TF* Lb = y0 + (size_t)kGroup * (WS + 64);
+    TF* Ub = Lb + ST * (size_t)ix.maxLc * gs;
+    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * gs);
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) {
+        s_offL[i] = ix.offL[i];
+        s_offU[i] = ix.offU[i];
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_Lmask[i] = ix.Lmask[i];
+    for (int i = threadIdx.x; i < ix.nL; i += blockDim.x) s_Lrow[i] = ix.Lrow[i];
+    for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) s_Udist[i] = ix.Udist[i];
+    __syncthreads();
+    if (!wlive) return;
+    TF* scr = static_cast<TF*>(ix.scratch) + ((size_t)wg * kGroup + g) * n;
+    // row i (solver order) of this half's right-hand side
+    auto rhs_row = [&](int i) -> TF {
+        TF v = TF(0.0);
+        if (live) {
+            const int p = cd.perm[i];
+            if constexpr (IO == IO_MIXED) {
+                v = to_zf(static_cast<const zd*>(io.rhs)[(size_t)sys * n + p]);
+            } else {
+                v = io_load<TF, IO>(io, sys, n, p);
+            }
+            if (partner && cd.flip_r[p]) v = -v;
+        }
+        return v;
+    };
+    const TF* Lg = cd.L + (size_t)wg * ix.nL * gs;
+    const TF* Ug = cd.U + (size_t)wg * (ix.nU) * gs;
+    const int* Pg = cd.piv + (size_t)wg * n * gs;
+    // ---------------- forward: L with the row interchanges (rows [0, hi) have entered the window)
+    if (ix.kl > 0 && n > 1) {
+        const int nch = (n - 1 + CH - 1) / CH;
+        int hi = min(n, min(CH, n - 1) + ix.kl);
+        for (int i = lg; i < hi; i += kLanesPer) win[i & M] = rhs_row(i);
+        auto issue = [&](int c) {
+            if (c < nch) {
+                const int buf = c % ST;
+                const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
+                warp_stage(Lb + (size_t)buf * ix.maxLc * gs, Lg + (size_t)s_offL[j0] * gs,
+                           (s_offL[j1] - s_offL[j0]) * gs);
+                warp_stage(Pb + (size_t)buf * CH * gs, Pg + (size_t)j0 * gs, (j1 - j0) * gs);
+            }
+            cp_async_commit();
+        };
+        for (int c = 0; c < ST - 1; ++c) issue(c);
+        for (int c = 0; c < nch; ++c) {
+            issue(c + ST - 1);
+            // the rows chunk c + 1 brings in (at most CH: one per lane), loaded while c is swept
+            const int hin = (c + 1 < nch) ? min(n, min((c + 2) * CH, n - 1) + ix.kl) : hi;
+            TF pf = TF(0.0);
+            if (hi + lg < hin) pf = rhs_row(hi + lg);
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * gs;
+            const int* Pc = Pb + (size_t)(c % ST) * CH * gs;
+            const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
+            const int base = s_offL[j0];
+            int e1 = base;
+#pragma unroll
+            for (int jj = 0; jj < CH; ++jj) {
+                const int j = j0 + jj;
+                if (j >= j1) break;
+                const int l = Pc[jj * gs + gsel];
+                const TF bj = win[l & M];
+                const TF yj0 = win[j & M];
+                const int e0 = e1;
+                e1 = s_offL[j + 1];
+                __syncwarp();
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
+                    const int i = j + 1 + s_Lrow[e];
+                    const TF v = (i == l) ? yj0 : win[i & M];
+                    win[i & M] = cfms(v, Lc[(e - base) * gs + gsel], bj);
+                }
+                if (lg == 0) {
+                    win[j & M] = bj;
+                    if (l != j && !((s_Lmask[j] >> (l - j - 1)) & 1u)) win[l & M] = yj0;
+                }
+                __syncwarp();
+            }
+            // rows j0 .. j1 - 1 are final: out to the scratch, then chunk c + 1's rows in (rows
+            // j1 .. hin - 1 span at most CH + kl < WS slots)
+            for (int i = j0 + lg; i < j1; i += kLanesPer) scr[i] = win[i & M];
+            __syncwarp();
+            if (hi + lg < hin) win[(hi + lg) & M] = pf;
+            hi = hin;
+        }
+        __syncwarp();
+        if (lg == 0) scr[n - 1] = win[(n - 1) & M];      // the last row has no column of its own
+    } else {
+        for (int i = lg; i < n; i += kLanesPer) scr[i] = rhs_row(i);
+    }
+    __syncwarp();
+    // ---------------- backward: U (diagonal holds -1/u_jj); rows [lo, n) have entered the window
+    {
+        const int nch = (n + CH - 1) / CH;
+        int lo = max(0, n - min(CH, n) - ix.kv);
+        for (int i = lo + lg; i < n; i += kLanesPer) win[i & M] = scr[i];
+        auto issue = [&](int c) {
+            if (c < nch) {
+                const int s0 = c * CH, s1 = min(s0 + CH, n);
+                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * gs, Ug + (size_t)s_offU[s0] * gs,
+                           (s_offU[s1] - s_offU[s0]) * gs);
+            }
+            cp_async_commit();
+        };
+        for (int c = 0; c < ST - 1; ++c) issue(c);
+        for (int c = 0; c < nch; ++c) {
+            issue(c + ST - 1);
+            const int lon = (c + 1 < nch) ? max(0, n - min((c + 2) * CH, n) - ix.kv) : lo;
+            TF pf = TF(0.0);
+            if (lon + lg < lo) pf = scr[lon + lg];
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * gs;
+            const int s0 = c * CH, s1 = min(s0 + CH, n);
+            const int base = s_offU[s0];
+            int e1 = base;
+#pragma unroll
+            for (int ss = 0; ss < CH; ++ss) {
+                const int s = s0 + ss;
+                if (s >= s1) break;
+                const int j = n - 1 - s;
+                const int e0 = e1;
+                e1 = s_offU[s + 1];
+                const TF yj = win[j & M];
+                __syncwarp();
+                for (int e = e0 + lg; e < e1; e += kLanesPer) {
+                    const int i = j - s_Udist[e];
+                    win[i & M] = cfms(e == e0 ? TF(0.0) : win[i & M], Uc[(e - base) * gs + gsel], yj);
+                }
+                __syncwarp();
+            }
+            // rows n - s1 .. n - s0 - 1 are final (before the border correction): out to the
+            // scratch over their forward values (read when they entered), then chunk c + 1's rows
+            for (int i = n - s1 + lg; i < n - s0; i += kLanesPer) scr[i] = win[i & M];
+            __syncwarp();
+            if (lon + lg < lo) win[(lon + lg) & M] = pf;
+            lo = lon;
+        }
+    }
+    __syncwarp();
+    // ---------------- Woodbury: z = S^{-1} V^T y, x = y - W z (y from the scratch)
+    constexpr int kU = 2;
+    if (r > 0) {
+        const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
+        TF* sl = zb + r;
+        if (staged && live)
+            for (int q = lg; q < r * r; q += kLanesPer) sl[q] = cd.slu[(size_t)sys * r * r + q];
+        const TF* Vg = cd.V + (size_t)wg * ix.nV * gs;
+        for (int a = 0; a < r; ++a) {
+            TF acc = TF(0.0);
+            const int ea = ix.offV[a], eb = ix.offV[a + 1];
+            for (int e0 = ea + lg; e0 < eb; e0 += kU * kLanesPer) {
+                int c[kU];
+                TF v[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int e = e0 + u * kLanesPer;
+                    c[u] = e < eb ? ix.Vcol[e] : -1;
+                    v[u] = e < eb ? Vg[(size_t)e * gs + gsel] : TF(0.0);
+                }
+                TF yc[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) yc[u] = c[u] >= 0 ? scr[c[u]] : TF(0.0);
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                    if (c[u] >= 0) acc = cfma(acc, v[u], yc[u]);
+            }
+            for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
+            if (lg == 0) zb[a] = acc;
+        }
+        __syncwarp();
+        if (lg == 0 && live) {
+            if (staged) small_getrs_staged(sl, cd.spiv + (size_t)sys * r, zb, r);
+            else small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
+        }
+        __syncwarp();
+    }
+    if (!live) return;
+    const TF* Ws = cd.W + (size_t)sys * r * n;
+    // the solution's row i: y_i - sum_k W_ki z_k (the compact solve's order), x = dc y for a partner
+    auto fin = [&](int i) -> TF {
+        TF acc = scr[i];
+        if (r > 0) {
+            if (r <= kMaxRUnroll) {
+                TF w[kMaxRUnroll];
+#pragma unroll
+                for (int k = 0; k < kMaxRUnroll; ++k)
+                    if (k < r) w[k] = Ws[(size_t)k * n + i];
+#pragma unroll
+                for (int k = 0; k < kMaxRUnroll; ++k)
+                    if (k < r) acc = cfms(acc, w[k], zb[k]);
+            } else {
+                for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
+            }
+        }
+        if (partner && cd.flip_c[i]) acc = -acc;
+        return acc;
+    };
+    if constexpr (IO == IO_MIXED) {
+        zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
+        zd* xt = static_cast<zd*>(io.xT);
+        const size_t nb = (size_t)ix.batch;
+        for (int i = lg; i < n; i += kLanesPer) {
+            const TF f = fin(i);
+            const zd v = io.accumulate ? xs[i] + zd(f.re, f.im) : zd(f.re, f.im);
+            xs[i] = v;
+            if (xt) xt[(size_t)i * nb + sys] = v;
+        }
+    } else {
+        for (int i = lg; i < n; i += kLanesPer) io_store<TF, IO>(io, sys, n, i, fin(i));
+    }
+}
+
+template <class TF, class TD, int IO, int CH, int ST>
+__global__ void __launch_bounds__(256)
+k_solve_window_multi(MultiSolve<TF> ms) {
+    int b = 0;
+    while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
+    solve_window_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
 }
 
 // ---- one system per warp, lanes split over (entry, real/imaginary part) -------------------------
@@ -2452,6 +2727,14 @@ static void demote_compact(Banded& h, cudaStream_t st) {
     dem(h.c_V, h.c_V32, (long long)(W * std::max(h.cV, 1) * G));
 }
 
+// rows of the windowed sweeps' ring: a power of two >= chunk + kl + ku + 1 (every row a chunk of
+// columns touches, with the next chunk's rows)
+static int window_slots(const Banded& h, int chunk) {
+    int p = 1;
+    while (p < chunk + h.kl + h.ku + 1) p <<= 1;
+    return p;
+}
+
 static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     CompactIdx ix;
     ix.n = h.n; ix.r = h.r; ix.kl = h.kl; ix.kv = h.kl + h.ku; ix.nL = h.cL; ix.nU = h.cU; ix.nV = h.cV;
@@ -2462,6 +2745,8 @@ static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     ix.maxUcol = h.cMaxUcol;
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
     ix.offV = h.c_offV; ix.Vcol = h.c_Vcol;
+    ix.wmask = window_slots(h, chunk) - 1;
+    ix.scratch = h.w_scr;
     return ix;
 }
 
@@ -2586,11 +2871,16 @@ static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
     const int k = chunk_index(sc.chunk);
     size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
     off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)kGroup * (h.n + 64) +
+    // a system's vector (n rows), or its window in the windowed schedules
+    const int rows = sc.split == kWindowFlag ? window_slots(h, sc.chunk) : h.n;
+    const size_t per_warp = (size_t)kGroup * (rows + 64) +
                             (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG +
                             ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     return off + sizeof(TF) * per_warp * nwarps;
 }
+
+// entries of the windowed schedules' scratch for handle h
+static size_t window_scratch_entries(const Banded& h) { return (size_t)h.cWg * kGroup * h.n; }
 
 template <class TF, class TD, int IO>
 static void launch_compact(const Banded& h, const CompactData<TF>& cd, const SolveIo& io, cudaStream_t st) {
@@ -2739,11 +3029,21 @@ static void group_range(const Banded& h, int s0, int s1, int& first, int& end) {
     end = std::min(h.cWg, (s1 + h.cG - 1) / h.cG);
 }
 
-template <class TF, class TD, int IO, int CH, int ST>
+template <class TF, class TD, int IO, int CH, int ST, bool WIN = false>
 static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
                            const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2,
                            const std::vector<int>& rng, int sched, cudaStream_t st) {
-    ensure_smem_attr((const void*)k_solve_compact_multi<TF, TD, IO, CH, ST>, 220 * 1024);
+    // the two-systems sweeps, over whole vectors or (WIN) windows of them
+    auto kern = [] {
+        if constexpr (WIN) return k_solve_window_multi<TF, TD, IO, CH, ST>;
+        else return k_solve_compact_multi<TF, TD, IO, CH, ST>;
+    }();
+    if (WIN)
+        for (const Banded* h : hs)
+            if (!h->w_scr || h->w_cap < window_scratch_entries(*h))
+                throw InvalidArgument("windowed solve: the scratch is not allocated (cng_banded_set_schedule "
+                                      "after cng_banded_compact)");
+    ensure_smem_attr((const void*)kern, 220 * 1024);
     // one warp count for all blocks: the one that keeps the most warps resident per SM (blocks per
     // SM are bounded by their shared memory: eight warps in one block can lose to seven in two),
     // and no more than it takes to give every SM a block (a small batch spreads over the SMs: each
@@ -2764,8 +3064,7 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         const size_t m = smem_of(w);
         if (m > 220 * 1024) break;
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_compact_multi<TF, TD, IO, CH, ST>, 32 * w,
-                                                          m) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, m) != cudaSuccess)
             per_sm = 1;
         if (per_sm * w >= resident) { resident = per_sm * w; nw = w; }
     }
@@ -2792,8 +3091,8 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         blocks += ceil_div(end[i] - first[i], nw);
     }
     ms.block_start[ms.nb] = blocks;
-    k_solve_compact_multi<TF, TD, IO, CH, ST><<<blocks, 32 * nw, smem, st>>>(ms);
-    CNG_LAUNCH("k_solve_compact_multi");
+    kern<<<blocks, 32 * nw, smem, st>>>(ms);
+    CNG_LAUNCH(WIN ? "k_solve_window_multi" : "k_solve_compact_multi");
 }
 
 template <class TF>
@@ -2888,6 +3187,10 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
             if constexpr (std::is_same<TF, zd>::value) launch_part(hs, ios, ios2, rng, st);
             else throw InvalidArgument("the partitioned solve is FP64 only: another schedule for the FP32 form");
             break;
+        case 12: launch_multi_t<TF, TD, IO, 8, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 13: launch_multi_t<TF, TD, IO, 4, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 14: launch_multi_t<TF, TD, IO, 16, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 15: launch_multi_t<TF, TD, IO, 4, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }
@@ -3044,6 +3347,20 @@ int cng_banded_set_schedule(cng_banded* hh, int sched) {
             dev_free(h->p_Rb);
             h->p_Rf = h->p_Rb = nullptr;
             h->part_ready = false;
+        }
+        if (sched >= 0 && cng::kSchedules[sched].split == cng::kWindowFlag) {
+            const size_t need = cng::window_scratch_entries(*h);     // the windowed sweeps' scratch
+            if (h->w_cap < need) {
+                dev_free(h->w_scr);
+                h->w_scr = nullptr;
+                h->w_cap = 0;
+                dalloc(&h->w_scr, need, sizeof(zd));
+                h->w_cap = need;
+            }
+        } else if (h->w_scr) {                     // another schedule: the scratch is not kept
+            dev_free(h->w_scr);
+            h->w_scr = nullptr;
+            h->w_cap = 0;
         }
         h->sched = sched;
     })

@@ -13,7 +13,8 @@ one by one:
   factor set, plus one for -L X), and the factor set of ``cng_banded_create_shared`` (band LU ldab x n, pivots, the
   border blocks V^T and W (r x n each), the capacitance LU (r x r)), its FP32 copies in the FP32
   form, and the compact factor streams (bounded above by the band: at most kl entries of L and
-  kl + ku + 1 of U per column, r x n of V); one transient copy of a M + b L while factoring;
+  kl + ku + 1 of U per column, r x n of V) with the windowed schedules' scratch (one complex128
+  vector per system slot); one transient copy of a M + b L while factoring;
 * the F pipeline's work buffers (``cng_rhs_create``: the spectra S and two grid buffers).
 
 A shared pair's partner (the (kx, -kz) systems solved with the (kx, +kz) factors) holds no factors;
@@ -63,6 +64,8 @@ def _factor_bytes(b, nsys, precision, compact, shared=False):
         out += slots * (per * _Z + n * 4) + 6 * (n + 1) * 4 + per * 5
         if precision == "fp32":
             out += slots * per * _C
+        # the windowed schedules' scratch (two vectors per warp group), held when the tuner picks one
+        out += (2 * nsys if shared else slots) * n * _Z
     return out
 
 
