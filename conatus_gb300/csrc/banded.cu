@@ -1478,7 +1478,7 @@ constexpr int kWindowFlag = 3;
 constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
                                                        {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2},
-                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {4, 2, 3}};
+                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1843,8 +1843,9 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     const bool live = sys < ix.batch && (!partner || io2.rhs != nullptr);
     const bool wlive = wg < ix.wgroups;
     const int n = ix.n, r = ix.r, M = ix.wmask, WS = ix.wmask + 1;
-    // shared memory: index lists, then per warp the windows win[G][WS + 64] (z and S after each
-    // window), then the staging buffers
+    // shared memory: index lists, then per warp the windows win[G][WS], the staging ring of the
+    // factor streams (at least G x 64 entries: z and S of each half take it over after the sweeps),
+    // and the pivots' ring
     int* s_offL = reinterpret_cast<int*>(sm);
     int* s_offU = s_offL + (n + 1);
     unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
@@ -1852,14 +1853,18 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     unsigned char* s_Udist = s_Lrow + ix.nL;
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)kGroup * (WS + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * gs +
+    const size_t ring = max(ST * (size_t)(ix.maxLc + ix.maxUc) * gs, (size_t)kGroup * 64);
+    // the second half's window 64 bytes further on: the halves touch the same rows in lockstep, and
+    // windows a power of two apart would put those rows in the same banks
+    constexpr int PAD = 64 / sizeof(TF);
+    const size_t per_warp = (size_t)kGroup * WS + PAD + ring +
                             (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
-    TF* win = y0 + (size_t)g * (WS + 64);
-    TF* zb = win + WS;
-    TF* Lb = y0 + (size_t)kGroup * (WS + 64);
+    TF* win = y0 + (size_t)g * (WS + PAD);
+    TF* Lb = y0 + (size_t)kGroup * WS + PAD;
     TF* Ub = Lb + ST * (size_t)ix.maxLc * gs;
-    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * gs);
+    TF* zb = Lb + (size_t)g * 64;
+    int* Pb = reinterpret_cast<int*>(Lb + ring);
     for (int i = threadIdx.x; i <= n; i += blockDim.x) {
         s_offL[i] = ix.offL[i];
         s_offU[i] = ix.offU[i];
@@ -1998,6 +2003,7 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
             lo = lon;
         }
     }
+    cp_async_wait<0>();                          // the ring is free for z and S
     __syncwarp();
     // ---------------- Woodbury: z = S^{-1} V^T y, x = y - W z (y from the scratch)
     constexpr int kU = 2;
@@ -2072,8 +2078,13 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     }
 }
 
+// warps per block of the windowed solve: FP32 16 (the index lists shared by more warps; measured on
+// the channel's FP32 solve 2.36 ms against 2.47 with 8), FP64 8 (the register budget of 8-warp
+// blocks keeps it at 48 registers: 3.05 ms against 3.20 with 16)
+template <class TF>
+constexpr int window_max_warps() { return sizeof(TF) == 8 ? 16 : 8; }
 template <class TF, class TD, int IO, int CH, int ST>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * window_max_warps<TF>())
 k_solve_window_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
@@ -2871,11 +2882,14 @@ static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
     const int k = chunk_index(sc.chunk);
     size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 4 + h.cL + h.cU;
     off = (off + 15) & ~(size_t)15;
-    // a system's vector (n rows), or its window in the windowed schedules
-    const int rows = sc.split == kWindowFlag ? window_slots(h, sc.chunk) : h.n;
-    const size_t per_warp = (size_t)kGroup * (rows + 64) +
-                            (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG +
-                            ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    const size_t ring = (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG;
+    const size_t pivots = ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    // the windowed schedules: a window of each vector, z and S in the ring after the sweeps
+    if (sc.split == kWindowFlag)
+        return off + sizeof(TF) * nwarps *
+                         ((size_t)kGroup * window_slots(h, sc.chunk) + 64 / sizeof(TF) +
+                          std::max(ring, (size_t)kGroup * 64) + pivots);
+    const size_t per_warp = (size_t)kGroup * (h.n + 64) + ring + pivots;
     return off + sizeof(TF) * per_warp * nwarps;
 }
 
@@ -3060,7 +3074,7 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         total += end[i] - first[i];
     }
     int nw = 1, resident = 0;
-    for (int w = 1; w <= 8; ++w) {
+    for (int w = 1; w <= (WIN ? window_max_warps<TF>() : 8); ++w) {
         const size_t m = smem_of(w);
         if (m > 220 * 1024) break;
         int per_sm = 0;
@@ -3190,7 +3204,7 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 12: launch_multi_t<TF, TD, IO, 8, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 13: launch_multi_t<TF, TD, IO, 4, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 14: launch_multi_t<TF, TD, IO, 16, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
-        case 15: launch_multi_t<TF, TD, IO, 4, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 15: launch_multi_t<TF, TD, IO, 8, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }
