@@ -152,14 +152,33 @@ def step_bytes(dev, solver):
 # DRAM bytes per system of one batched solve launch, from the ncu captures of the channel solve
 # (64x129x64; dram__bytes_read.sum + dram__bytes_write.sum): the compact solve reads the union pattern
 # of the factors, not the band, and a shared pair's factors once for both systems, so its traffic is
-# below the band-equivalent bytes
+# below the band-equivalent bytes. Per solve kernel: the windowed solve adds its scratch round trip
+# (mostly absorbed by L2)
 TRAFFIC_PER_SYSTEM = {
-    ("channel", "fp64"): ((174.600192 + 3.016192) * 1e6 / 1985,
-                          "profiles/k_solve_compact_multi_channel64x129x64_fp64.md"),
+    ("channel", "fp64", "k_solve_compact_multi"): ((174.600192 + 3.016192) * 1e6 / 1985,
+                                                   "profiles/k_solve_compact_multi_channel64x129x64_fp64.md"),
+    ("channel", "fp64", "k_solve_window_multi"): ((178.431232 + 16.321792) * 1e6 / 1985,
+                                                  "profiles/k_solve_window_multi_channel64x129x64_fp64.md"),
     # the FP32 form solves in two groups: the captured launch is the group of 1024 paired systems
-    ("channel", "fp32"): ((47.700736 + 0.423936) * 1e6 / 1024,
-                          "profiles/k_solve_compact_multi_channel64x129x64_fp32.md"),
+    ("channel", "fp32", "k_solve_compact_multi"): ((47.700736 + 0.423936) * 1e6 / 1024,
+                                                   "profiles/k_solve_compact_multi_channel64x129x64_fp32.md"),
+    ("channel", "fp32", "k_solve_window_multi"): ((47.577856 + 0.329984) * 1e6 / 1024,
+                                                  "profiles/k_solve_window_multi_channel64x129x64_fp32.md"),
 }
+
+
+def solve_kernel(sched: int) -> str:
+    """The kernel that runs solve schedule ``sched`` (-1: the band kernel)."""
+    from conatus_gb300 import autotune
+    if sched is None or sched < 0:
+        return "k_solve"
+    if sched in autotune.windowed_schedules():
+        return "k_solve_window_multi"
+    if sched in autotune.partitioned_schedules():
+        return "k_solve_part"
+    if sched in autotune.split_schedules():
+        return "k_solve_split_multi"
+    return "k_solve_compact_multi"
 
 
 # DRAM bytes of the F pipeline's x backward real transform on the channel 64x129x64 (ncu: read +
@@ -351,8 +370,9 @@ def run_gpu(args):
     hbm_peak, peak_kind = measured_peaks()
     sb = solve_bytes(dev, fs)
     nsys = sum(h.batch for h in fs)
-    tr = TRAFFIC_PER_SYSTEM.get((args.config, args.precision)) if args.fourier is None else None
-    solve_roof = {"kernel": "k_solve_compact_multi (batched bordered-banded solve, all buckets in one launch)",
+    kname = solve_kernel(getattr(next(h for h in fs if h.h is not None), "schedule", 0))
+    tr = TRAFFIC_PER_SYSTEM.get((args.config, args.precision, kname)) if args.fourier is None else None
+    solve_roof = {"kernel": kname + " (batched bordered-banded solve, all buckets in one launch)",
             "bound": "hbm", "achieved": sb / (solve_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
             "frac": sb / (solve_ms / 1e3) / 1e9 / hbm_peak,
             "traffic": tr[0] * nsys if tr else None,
@@ -527,6 +547,13 @@ def form_fp32(P, C0, cfg, args):
     res = {"metric": METRIC[args.config] + " FP32 form", "value": args.steps / (ms / 1e3), "unit": "steps/s",
            "ms_per_step": ms / args.steps, "steps": args.steps, "dtype": "f32+f64",
            "gpu_launches": s.launches_per_step() * args.steps}
+    # the whole step's algorithmic bytes against the measured HBM rate
+    hbm_peak, peak_kind = measured_peaks()
+    sbytes = step_bytes(s.dev, s)
+    gbs = sbytes["total"] / (ms / args.steps / 1e3) / 1e9
+    res["step_roofline"] = {"bytes_per_step": sbytes, "achieved": gbs, "unit": "GB/s", "peak": hbm_peak,
+                            "frac": gbs / hbm_peak, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    res["solve_schedule"] = _schedule_summary(s.dev)
     del s
     torch.cuda.empty_cache()
     if args.error_steps > 0:
