@@ -2,9 +2,11 @@
 
 Candidates: the band kernel (one warp per system over the LU band, ``cng_banded_set_schedule(h,
 -1)``) and the compact-stream schedules of ``cng_banded_schedules`` (two systems per warp over the
-union pattern of the factors, with different staging chunks and ring depths; one system per warp
-with the lanes split over entries and components for small batches; and the partitioned solve of
-small FP64 batches, one block of warps per system sweeping its blocks of 32 columns at once). The
+union pattern of the factors, with different staging chunks and ring depths, over whole vectors
+or over windows of them with the rest in a scratch (more resident warps, the same bits); one
+system per warp with the lanes split over entries and components for small batches; and the
+partitioned solve of small FP64 batches, one block of warps per system sweeping its blocks of 32
+columns at once). The
 partitioned solve is a candidate only where the DeviceProblem opts into it (``dev.partitioned``,
 or CONATUS_GB300_PARTITIONED=1): its residuals run up to about 15x those of the sequential sweeps.
 Candidates a factor set cannot take (a shared pair, the FP32 form, a batch too large for the

@@ -150,8 +150,9 @@ int cng_banded_solve_batch2(int nh, cng_banded* const* h, const void* const* b, 
  * the columns per staged chunk of the factor streams, the depth of the staging ring and whether it
  * runs one system per warp with the lanes split over entries and real/imaginary parts (split = 1:
  * the latency variant for small batches; split = 2: the partitioned solve of small FP64 batches,
- * one block of warps per system sweeping its blocks of 32 columns at once; else two systems per
- * warp). Any output may be NULL. No
+ * one block of warps per system sweeping its blocks of 32 columns at once; split = 3: the windowed
+ * two-systems sweeps, a window of each vector in shared memory and the rest in a scratch, the
+ * same bits as schedule 0; else two systems per warp). Any output may be NULL. No
  * reference counterpart: the reference picks its solve kernel (level-scheduled streams or the band
  * kernel) by constructor flags (python/conatus/runtime/cuda.py:140-152); here the choice is timed
  * (conatus_gb300.autotune). */
@@ -163,7 +164,9 @@ int cng_banded_schedules(int32_t* count, int32_t* chunk, int32_t* stages, int32_
  * the legacy default stream and waits for it) and refuses (status 1) shared pairs, kl > 16,
  * kl + ku > 32, n > 1024 and responses above 256 MB; its solves refuse the FP32 factors and
  * system ranges. Its residuals run up to about 15x the sequential sweeps' (the blocks' separate
- * responses cancel). Setting another schedule frees the responses. */
+ * responses cancel). Setting another schedule frees the responses. Setting a windowed schedule
+ * allocates its scratch (16 bytes x 2 x n per warp group of systems; freed when another schedule
+ * is set): two solves of the same systems of h must then not run at the same time. */
 int cng_banded_set_schedule(cng_banded* h, int sched);
 
 /* Mixed precision: keep FP32 (complex64) copies of the FP64 factors (allocates; refreshed by
