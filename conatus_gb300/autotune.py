@@ -30,8 +30,8 @@ import os
 
 from ._lib import call
 
-__all__ = ["schedules", "split_schedules", "partitioned_schedules", "windowed_schedules", "register_schedules",
-           "tune_solve", "tune_rhs", "cache"]
+__all__ = ["schedules", "split_schedules", "partitioned_schedules", "windowed_schedules", "tune_solve", "tune_rhs",
+           "cache"]
 
 _CACHE: dict = {}
 
@@ -71,12 +71,6 @@ def windowed_schedules() -> set:
     in shared memory and the rest in a per-handle scratch (more resident warps; the same bits as
     schedule 0)."""
     return {k for k, f in enumerate(_flags()) if f == 3}
-
-
-def register_schedules() -> set:
-    """Schedules of the register-window solve: one system per warp, the rows a column touches held
-    one per lane in registers and joined by shuffles (kl + ku <= 31; the same bits as schedule 0)."""
-    return {k for k, f in enumerate(_flags()) if f == 4}
 
 
 def cache() -> dict:

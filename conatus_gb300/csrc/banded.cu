@@ -767,7 +767,6 @@ struct Banded {
     unsigned* c_Lmask = nullptr;
     int* c_offU = nullptr;
     unsigned char* c_Udist = nullptr;
-    unsigned* c_Umask = nullptr;    // sweep order: bit d set where distance d is in the column (kl + ku <= 31)
     int* c_offV = nullptr;
     int* c_Vcol = nullptr;
     void* c_L = nullptr;
@@ -796,8 +795,7 @@ struct Banded {
                         (void*)bp, (void*)bcol, (void*)ab32, (void*)vt32, (void*)w32, (void*)slu32,
                         (void*)c_offL, (void*)c_Lrow, (void*)c_Lmask, (void*)c_offU, (void*)c_Udist,
                         (void*)c_offV, (void*)c_Vcol, c_L, c_U, c_V, (void*)c_piv, (void*)c_L32,
-                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c, p_Rf, p_Rb, w_scr,
-                        (void*)c_Umask})
+                        (void*)c_U32, (void*)c_V32, (void*)flip_r, (void*)flip_c, p_Rf, p_Rb, w_scr})
             dev_free(p);
     }
 
@@ -1473,18 +1471,14 @@ constexpr int kCChunk = 8;              // columns per staged chunk (the default
 // Schedules 12-15 (split = 3) are the windowed compact solve (k_solve_window_multi: the two-systems
 // sweeps with a window of each vector in shared memory and the rest in a global scratch, for more
 // resident warps per SM; the same bits as schedule 0).
-// Schedules 16-18 (split = 4) are the register-window solve (k_solve_reg_multi: one system per
-// warp, the rows a column touches one per lane in registers, columns joined by shuffles; kl + ku <=
-// 31; the same bits as schedule 0).
 struct CompactSchedule { int chunk, stages, split; };
-constexpr int kNumSchedules = 19;
+constexpr int kNumSchedules = 16;
 constexpr int kPartSchedule = 11;
 constexpr int kWindowFlag = 3;
 constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
                                                        {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2},
-                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3},
-                                                       {8, 2, 4}, {16, 2, 4}, {4, 3, 4}};
+                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1502,7 +1496,6 @@ struct CompactIdx {
     const unsigned* Lmask;              // n: bit t set if row t is in the union
     const int* offU;                    // n + 1, sweep order s = n - 1 - j, entries incl. diagonal
     const unsigned char* Udist;         // per U stream entry: distance d >= 1 above the diagonal (0 = diagonal)
-    const unsigned* Umask;              // n, sweep order: bit d set if distance d is in the column
     const int* offV;                    // r + 1
     const int* Vcol;                    // nV
 };
@@ -2096,232 +2089,6 @@ k_solve_window_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
     solve_window_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
-}
-
-// ---- register-window compact solve: one system per warp, the rows a column touches in registers --
-// With kl + ku <= 31 a column touches rows of the window [j, j + 31] (forward) or [j - 31, j]
-// (backward) only, one per lane: lane t holds the window's row that is t mod 32. A column is then
-// two shuffles (the pivot row and row j; backward: row j) and one update per lane instead of a
-// chain of shared-memory loads and stores. The row a column finishes goes to shared memory and its
-// lane takes the row 32 further on (forward: the right-hand side, loaded 32 columns ahead;
-// backward: the forward result). A lane finds its entry of the column in the staged streams from
-// the column's row mask (Lmask; Umask in sweep order). The updates are the compact solve's, value
-// for value, and the border correction sums in its order (16 lanes per system): the same bits as
-// schedule 0. A shared pair's partner is a warp of its own on the same factors. ix.wg0 / ix.wgroups
-// count warps here: one per system (a pair: two per system, the primary's then the partner's).
-template <class TF, class TD, int IO, int CH, int ST>
-__device__ __forceinline__ void solve_reg_body(const CompactIdx& ix, const CompactData<TF>& cd,
-                                               const SolveIo& io0, const SolveIo& io2, int block) {
-    extern __shared__ __align__(16) unsigned char sm[];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int gs = ix.gs;
-    const bool pair = gs == 1;
-    const int q = ix.wg0 + block * nw + wib;
-    const int sys = pair ? (q >> 1) : q;
-    const bool partner = pair && (q & 1);
-    const int wg = pair ? sys : (sys >> 1);
-    const int gsel = pair ? 0 : (sys & 1);
-    const SolveIo& io = partner ? io2 : io0;
-    const bool live = q < ix.wgroups && sys < ix.batch && (!partner || io2.rhs != nullptr);
-    const int n = ix.n, r = ix.r;
-    // shared memory: offL, offU, Lmask, Umask, then per warp y[n + 64] (z and S after the vector)
-    // and the staging ring of the warp group's streams
-    int* s_offL = reinterpret_cast<int*>(sm);
-    int* s_offU = s_offL + (n + 1);
-    unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
-    unsigned* s_Umask = s_Lmask + n;
-    size_t off = (size_t)(n + 1) * 8 + (size_t)n * 8;
-    off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)(n + 64) + ST * (size_t)(ix.maxLc + ix.maxUc) * gs +
-                            (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
-    TF* y = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
-    TF* zb = y + n;
-    TF* Lb = y + (n + 64);
-    TF* Ub = Lb + ST * (size_t)ix.maxLc * gs;
-    int* Pb = reinterpret_cast<int*>(Ub + ST * (size_t)ix.maxUc * gs);
-    for (int i = threadIdx.x; i <= n; i += blockDim.x) {
-        s_offL[i] = ix.offL[i];
-        s_offU[i] = ix.offU[i];
-    }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        s_Lmask[i] = ix.Lmask[i];
-        s_Umask[i] = ix.Umask[i];
-    }
-    __syncthreads();
-    if (!live) return;                           // no block barrier below: the warp may leave
-    auto rhs_row = [&](int i) -> TF {
-        const int p = cd.perm[i];
-        TF v;
-        if constexpr (IO == IO_MIXED) {
-            v = to_zf(static_cast<const zd*>(io.rhs)[(size_t)sys * n + p]);
-        } else {
-            v = io_load<TF, IO>(io, sys, n, p);
-        }
-        if (partner && cd.flip_r[p]) v = -v;
-        return v;
-    };
-    const TF* Lg = cd.L + (size_t)wg * ix.nL * gs;
-    const TF* Ug = cd.U + (size_t)wg * ix.nU * gs;
-    const int* Pg = cd.piv + (size_t)wg * n * gs;
-    // ---------------- forward: L with the row interchanges; lane t holds row j + ((t - j) & 31)
-    TF val = lane < n ? rhs_row(lane) : TF(0.0);
-    if (ix.kl > 0 && n > 1) {
-        TF nxt = lane + 32 < n ? rhs_row(lane + 32) : TF(0.0);
-        const int nch = (n - 1 + CH - 1) / CH;
-        auto issue = [&](int c) {
-            if (c < nch) {
-                const int buf = c % ST;
-                const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
-                warp_stage(Lb + (size_t)buf * ix.maxLc * gs, Lg + (size_t)s_offL[j0] * gs,
-                           (s_offL[j1] - s_offL[j0]) * gs);
-                warp_stage(Pb + (size_t)buf * CH * gs, Pg + (size_t)j0 * gs, (j1 - j0) * gs);
-            }
-            cp_async_commit();
-        };
-        for (int c = 0; c < ST - 1; ++c) issue(c);
-        for (int c = 0; c < nch; ++c) {
-            issue(c + ST - 1);
-            cp_async_wait<ST - 1>();
-            __syncwarp();
-            const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * gs;
-            const int* Pc = Pb + (size_t)(c % ST) * CH * gs;
-            const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
-            const int base = s_offL[j0];
-#pragma unroll
-            for (int jj = 0; jj < CH; ++jj) {
-                const int j = j0 + jj;
-                if (j >= j1) break;
-                const int l = Pc[jj * gs + gsel];
-                const int t = ((lane - j) & 31) - 1;            // this lane's row: j + 1 + t
-                const unsigned m = s_Lmask[j];
-                const bool has = t >= 0 && ((m >> t) & 1u);
-                TF a = TF(0.0);
-                if (has) a = Lc[(s_offL[j] - base + __popc(m & ((1u << t) - 1u))) * gs + gsel];
-                const TF bj = shfl(val, l & 31);
-                const TF yj0 = shfl(val, j & 31);
-                TF v = (j + 1 + t == l) ? yj0 : val;
-                if (has) v = cfms(v, a, bj);
-                if (t < 0) {                                     // row j is final: out; take row j + 32
-                    y[j] = bj;
-                    v = nxt;
-                    nxt = j + 64 < n ? rhs_row(j + 64) : TF(0.0);
-                }
-                val = v;
-            }
-        }
-        if (lane == ((n - 1) & 31)) y[n - 1] = val;              // the last row has no column
-    } else {
-        for (int i = lane; i < n; i += 32) y[i] = rhs_row(i);
-    }
-    __syncwarp();
-    // ---------------- backward: U (diagonal holds -1/u_jj); lane t holds row j - ((j - t) & 31)
-    {
-        const int nch = (n + CH - 1) / CH;
-        {
-            const int row = (n - 1) - (((n - 1) - lane) & 31);
-            val = row >= 0 ? y[row] : TF(0.0);
-        }
-        auto issue = [&](int c) {
-            if (c < nch) {
-                const int s0 = c * CH, s1 = min(s0 + CH, n);
-                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * gs, Ug + (size_t)s_offU[s0] * gs,
-                           (s_offU[s1] - s_offU[s0]) * gs);
-            }
-            cp_async_commit();
-        };
-        for (int c = 0; c < ST - 1; ++c) issue(c);
-        for (int c = 0; c < nch; ++c) {
-            issue(c + ST - 1);
-            cp_async_wait<ST - 1>();
-            __syncwarp();
-            const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * gs;
-            const int s0 = c * CH, s1 = min(s0 + CH, n);
-            const int base = s_offU[s0];
-#pragma unroll
-            for (int ss = 0; ss < CH; ++ss) {
-                const int s = s0 + ss;
-                if (s >= s1) break;
-                const int j = n - 1 - s;
-                const int d = (j - lane) & 31;                   // this lane's row: j - d
-                const unsigned m = s_Umask[s];
-                const bool has = (m >> d) & 1u;
-                TF a = TF(0.0);
-                if (has) a = Uc[(s_offU[s] - base + __popc(m & ((1u << d) - 1u))) * gs + gsel];
-                const TF yj = shfl(val, j & 31);
-                if (has) val = cfms(d == 0 ? TF(0.0) : val, a, yj);
-                if (d == 0) {                                    // row j is final: out; take row j - 32
-                    y[j] = val;
-                    val = j >= 32 ? y[j - 32] : TF(0.0);
-                }
-            }
-        }
-    }
-    __syncwarp();
-    // ---------------- Woodbury: z = S^{-1} V^T y, y -= W z (the compact solve's sums: 16 lanes)
-    if (r > 0) {
-        const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
-        TF* sl = zb + r;
-        if (staged)
-            for (int k = lane; k < r * r; k += 32) sl[k] = cd.slu[(size_t)sys * r * r + k];
-        const TF* Vg = cd.V + (size_t)wg * ix.nV * gs;
-        for (int a = 0; a < r; ++a) {
-            TF acc = TF(0.0);
-            if (lane < kLanesPer) {
-                const int ea = ix.offV[a], eb = ix.offV[a + 1];
-                for (int e = ea + lane; e < eb; e += kLanesPer)
-                    acc = cfma(acc, Vg[(size_t)e * gs + gsel], y[ix.Vcol[e]]);
-            }
-            for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
-            if (lane == 0) zb[a] = acc;
-        }
-        __syncwarp();
-        if (lane == 0) {
-            if (staged) small_getrs_staged(sl, cd.spiv + (size_t)sys * r, zb, r);
-            else small_getrs(cd.slu + (size_t)sys * r * r, cd.spiv + (size_t)sys * r, zb, r);
-        }
-        __syncwarp();
-        const TF* Ws = cd.W + (size_t)sys * r * n;
-        for (int i = lane; i < n; i += 32) {
-            TF acc = y[i];
-            if (r <= kMaxRUnroll) {
-                TF w[kMaxRUnroll];
-#pragma unroll
-                for (int k = 0; k < kMaxRUnroll; ++k)
-                    if (k < r) w[k] = Ws[(size_t)k * n + i];
-#pragma unroll
-                for (int k = 0; k < kMaxRUnroll; ++k)
-                    if (k < r) acc = cfms(acc, w[k], zb[k]);
-            } else {
-                for (int k = 0; k < r; ++k) acc = cfms(acc, Ws[(size_t)k * n + i], zb[k]);
-            }
-            y[i] = acc;
-        }
-        __syncwarp();
-    }
-    if (partner)
-        for (int i = lane; i < n; i += 32)
-            if (cd.flip_c[i]) y[i] = -y[i];
-    if constexpr (IO == IO_MIXED) {
-        zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
-        zd* xt = static_cast<zd*>(io.xT);
-        const size_t nb = (size_t)ix.batch;
-        for (int i = lane; i < n; i += 32) {
-            const zd v = io.accumulate ? xs[i] + zd(y[i].re, y[i].im) : zd(y[i].re, y[i].im);
-            xs[i] = v;
-            if (xt) xt[(size_t)i * nb + sys] = v;
-        }
-    } else {
-        for (int i = lane; i < n; i += 32) io_store<TF, IO>(io, sys, n, i, y[i]);
-    }
-}
-
-template <class TF, class TD, int IO, int CH, int ST>
-__global__ void __launch_bounds__(256)
-k_solve_reg_multi(MultiSolve<TF> ms) {
-    int b = 0;
-    while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
-    solve_reg_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
 }
 
 // ---- one system per warp, lanes split over (entry, real/imaginary part) -------------------------
@@ -2988,7 +2755,6 @@ static CompactIdx compact_idx(const Banded& h, int chunk = kCChunk) {
     ix.maxLcol = h.cMaxLcol;
     ix.maxUcol = h.cMaxUcol;
     ix.offL = h.c_offL; ix.Lrow = h.c_Lrow; ix.Lmask = h.c_Lmask; ix.offU = h.c_offU; ix.Udist = h.c_Udist;
-    ix.Umask = h.c_Umask;
     ix.offV = h.c_offV; ix.Vcol = h.c_Vcol;
     ix.wmask = window_slots(h, chunk) - 1;
     ix.scratch = h.w_scr;
@@ -3036,16 +2802,11 @@ static void compact(Banded& h, cudaStream_t st) {
         }
         offL[j + 1] = (int)Lrow.size();
     }
-    std::vector<unsigned> Umask(n, 0u);
     for (int s2 = 0; s2 < n; ++s2) {
         const int j = n - 1 - s2;
         Udist.push_back(0);                                  // 1 / u_jj
-        Umask[s2] = 1u;
         for (int d = 1; d <= std::min(kv, j); ++d)
-            if (mab[(size_t)j * h.ldab + kv - d]) {
-                Udist.push_back((unsigned char)d);
-                if (d < 32) Umask[s2] |= 1u << d;
-            }
+            if (mab[(size_t)j * h.ldab + kv - d]) Udist.push_back((unsigned char)d);
         offU[s2 + 1] = (int)Udist.size();
     }
     for (int a = 0; a < r; ++a) {
@@ -3094,7 +2855,7 @@ static void compact(Banded& h, cudaStream_t st) {
     };
     if (!h.c_offL) {
         up(&h.c_offL, offL); up(&h.c_Lrow, Lrow); up(&h.c_Lmask, Lmask); up(&h.c_offU, offU);
-        up(&h.c_Udist, Udist); up(&h.c_offV, offV); up(&h.c_Vcol, Vcol); up(&h.c_Umask, Umask);
+        up(&h.c_Udist, Udist); up(&h.c_offV, offV); up(&h.c_Vcol, Vcol);
         const size_t G = h.cG, W = h.cWg;
         dalloc(&h.c_L, W * std::max(h.cL, 1) * G, sizeof(zd));
         dalloc(&h.c_U, W * std::max(h.cU, 1) * G, sizeof(zd));
@@ -3348,75 +3109,6 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
     CNG_LAUNCH(WIN ? "k_solve_window_multi" : "k_solve_compact_multi");
 }
 
-// shared memory of the register-window solve: offL, offU, Lmask, Umask, then per warp y[n + 64] and
-// the ring of the warp group's streams
-template <class TF>
-static size_t reg_smem(const Banded& h, int nwarps, int sched) {
-    const CompactSchedule sc = kSchedules[sched];
-    const int k = chunk_index(sc.chunk);
-    size_t off = (size_t)(h.n + 1) * 8 + (size_t)h.n * 8;
-    off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = (size_t)(h.n + 64) + (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG +
-                            ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
-    return off + sizeof(TF) * per_warp * nwarps;
-}
-
-template <class TF, class TD, int IO, int CH, int ST>
-static void launch_reg_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
-                         const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2,
-                         const std::vector<int>& rng, int sched, cudaStream_t st) {
-    for (const Banded* h : hs)
-        if (h->kl + h->ku > 31)
-            throw InvalidArgument("the register-window schedules need kl + ku <= 31: another schedule");
-    const auto kern = k_solve_reg_multi<TF, TD, IO, CH, ST>;
-    ensure_smem_attr((const void*)kern, 220 * 1024);
-    // warps: one per system, a shared pair's two per system (primary, partner)
-    std::vector<int> first(hs.size()), end(hs.size());
-    int total = 0;
-    for (size_t i = 0; i < hs.size(); ++i) {
-        const int per = hs[i]->cG == 1 ? 2 : 1;
-        first[i] = per * (rng[2 * i + 1] < 0 ? 0 : rng[2 * i]);
-        end[i] = per * (rng[2 * i + 1] < 0 ? hs[i]->batch : rng[2 * i + 1]);
-        total += end[i] - first[i];
-    }
-    auto smem_of = [&](int w) {
-        size_t m = 0;
-        for (const Banded* h : hs) m = std::max(m, reg_smem<TF>(*h, w, sched));
-        return m;
-    };
-    int nw = 1, resident = 0;
-    for (int w = 1; w <= 8; ++w) {
-        const size_t m = smem_of(w);
-        if (m > 220 * 1024) break;
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, m) != cudaSuccess) per_sm = 1;
-        if (per_sm * w >= resident) { resident = per_sm * w; nw = w; }
-    }
-    nw = std::min(nw, std::max(1, ceil_div(total, sm_count())));
-    const size_t smem = smem_of(nw);
-    if (smem > 220 * 1024) throw InvalidArgument("compact solve: system too large for shared memory");
-    MultiSolve<TF> ms{};
-    ms.nb = (int)hs.size();
-    std::vector<int> order(hs.size());
-    for (size_t i = 0; i < hs.size(); ++i) order[i] = (int)i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return end[a] - first[a] > end[b] - first[b]; });
-    int blocks = 0;
-    for (int k = 0; k < ms.nb; ++k) {
-        const int i = order[k];
-        ms.block_start[k] = blocks;
-        ms.ix[k] = compact_idx(*hs[i], CH);
-        ms.ix[k].wg0 = first[i];              // in warps
-        ms.ix[k].wgroups = end[i];
-        ms.cd[k] = cds[i];
-        ms.io[k] = ios[i];
-        ms.io2[k] = ios2[i];
-        blocks += ceil_div(end[i] - first[i], nw);
-    }
-    ms.block_start[ms.nb] = blocks;
-    kern<<<blocks, 32 * nw, smem, st>>>(ms);
-    CNG_LAUNCH("k_solve_reg_multi");
-}
-
 template <class TF>
 static size_t split_smem(const Banded& h, int nwarps, int sched) {
     const CompactSchedule sc = kSchedules[sched];
@@ -3513,9 +3205,6 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 13: launch_multi_t<TF, TD, IO, 4, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 14: launch_multi_t<TF, TD, IO, 16, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 15: launch_multi_t<TF, TD, IO, 8, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
-        case 16: launch_reg_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
-        case 17: launch_reg_t<TF, TD, IO, 16, 2>(hs, cds, ios, ios2, rng, sched, st); break;
-        case 18: launch_reg_t<TF, TD, IO, 4, 3>(hs, cds, ios, ios2, rng, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }

@@ -188,9 +188,6 @@ __host__ __device__ inline bool is_zero(zf x) { return x.re == 0.0f && x.im == 0
 __device__ inline zf shfl_xor(zf v, int m) {
     return zf(__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m));
 }
-__device__ inline zf shfl(zf v, int src) {
-    return zf(__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src));
-}
 __host__ __device__ inline zf to_zf(zd a) { return zf((float)a.re, (float)a.im); }
 
 // Magnitudes: |.| of LAPACK's pivot search (i?amax: |re| + |im| for complex) and the modulus.

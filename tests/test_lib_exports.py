@@ -38,8 +38,7 @@ def test_library_reports_no_device_on_cpu_host():
 
 def test_solve_schedule_table():
     """The schedules the autotuner times: chunks of 2-16 columns, rings 2-4 deep, the split-lane
-    (flag 1), partitioned (2), windowed (3) and register-window (4) variants flagged (a host-only
-    query)."""
+    (flag 1), partitioned (2) and windowed (3) variants flagged (a host-only query)."""
     from conatus_gb300 import autotune
     n = ctypes.c_int32()
     from conatus_gb300._lib import call
@@ -49,11 +48,10 @@ def test_solve_schedule_table():
     assert n.value >= 8
     assert all(chunk[k] in (2, 4, 8, 16) and 2 <= stages[k] <= 4 for k in range(n.value))
     assert autotune.schedules() == [-1] + list(range(n.value))
-    assert all(split[k] in (0, 1, 2, 3, 4) for k in range(n.value))
+    assert all(split[k] in (0, 1, 2, 3) for k in range(n.value))
     assert autotune.split_schedules() == {k for k in range(n.value) if split[k] in (1, 2)}
     assert autotune.partitioned_schedules() == {k for k in range(n.value) if split[k] == 2}
     assert autotune.windowed_schedules() == {k for k in range(n.value) if split[k] == 3}
-    assert autotune.register_schedules() == {k for k in range(n.value) if split[k] == 4}
     assert autotune.split_schedules()                     # the latency variant is offered
     assert autotune.windowed_schedules()
 

@@ -1,9 +1,8 @@
 """GPU: the windowed compact solve (schedules ``autotune.windowed_schedules()``: the two-systems
 sweeps with only a window of each vector in shared memory, the finished rows in a per-handle
-scratch) and the register-window solve (``autotune.register_schedules()``: one system per warp,
-the rows a column touches in registers) give the bits of schedule 0: single solves in FP64 and in
-the FP32 form with its refinement (shared pairs, the row-major copy of x, two refinement groups on
-two streams), system ranges, and whole graph-replayed steps."""
+scratch) gives the bits of schedule 0: single solves in FP64 and in the FP32 form with its
+refinement (shared pairs, the row-major copy of x, two refinement groups on two streams), system
+ranges, and whole graph-replayed steps."""
 from __future__ import annotations
 
 import numpy as np
@@ -40,8 +39,8 @@ def test_windowed_solves_give_the_compact_bits(tname, sizes, precision, rng, cud
     dev.solve(a, b, rhs, ref)
     dev._batch_call(fs, [(big, 2 if hi > 2 else 0, hi)], rhs, ref_r, None, fp32, 0, 0)
     torch.cuda.synchronize()
-    wins = sorted(autotune.windowed_schedules() | autotune.register_schedules())
-    assert autotune.windowed_schedules() and autotune.register_schedules()
+    wins = sorted(autotune.windowed_schedules())
+    assert wins
     for s in wins:
         out, out_r = dev.zeros(), dev.zeros()
         autotune.apply(fs, s)
@@ -52,15 +51,12 @@ def test_windowed_solves_give_the_compact_bits(tname, sizes, precision, rng, cud
         assert torch.equal(out_r, ref_r), s
 
 
-@pytest.mark.parametrize("config,fourier,precision,family", [("rayleigh_benard", None, "fp64", "windowed"),
-                                                             ("rayleigh_benard", None, "fp32", "windowed"),
-                                                             ("channel", [24, 24], "fp32", "windowed"),
-                                                             ("rayleigh_benard", None, "fp64", "register"),
-                                                             ("burgers", None, "fp64", "register"),
-                                                             ("channel", [24, 24], "fp32", "register")])
-def test_windowed_steps_give_the_compact_bits(config, fourier, precision, family, cuda_lib):
-    """Graph-replayed steps with a windowed or register-window schedule against schedule 0 from
-    the same state: the same bits."""
+@pytest.mark.parametrize("config,fourier,precision", [("rayleigh_benard", None, "fp64"),
+                                                      ("rayleigh_benard", None, "fp32"),
+                                                      ("channel", [24, 24], "fp32")])
+def test_windowed_steps_give_the_compact_bits(config, fourier, precision, cuda_lib):
+    """Graph-replayed steps with a windowed schedule against schedule 0 from the same state: the
+    same bits."""
     import torch
     from conatus_gb300 import autotune, workloads as W
     from conatus_gb300.ivp import DeviceProblem, IVPSolver
@@ -68,8 +64,7 @@ def test_windowed_steps_give_the_compact_bits(config, fourier, precision, family
     cfg = W.CONFIGS[config]
     C0 = W.initial_state(config, P, seed=0)
     out = []
-    fam = autotune.windowed_schedules() if family == "windowed" else autotune.register_schedules()
-    for sched in (0, min(fam)):
+    for sched in (0, min(autotune.windowed_schedules())):
         dev = DeviceProblem(P, precision)
         dev.autotune = False
         s = IVPSolver(P, scheme=cfg["scheme"], dt=cfg["dt"], device_problem=dev)
