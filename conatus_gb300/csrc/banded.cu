@@ -1470,15 +1470,17 @@ constexpr int kCChunk = 8;              // columns per staged chunk (the default
 // warps per system, blocks of 32 columns swept at once; FP64 only).
 // Schedules 12-15 (split = 3) are the windowed compact solve (k_solve_window_multi: the two-systems
 // sweeps with a window of each vector in shared memory and the rest in a global scratch, for more
-// resident warps per SM; the same bits as schedule 0).
-struct CompactSchedule { int chunk, stages, split; };
-constexpr int kNumSchedules = 16;
+// resident warps per SM; the same bits as schedule 0); 16-18 the same with 8 lanes per system
+// (four systems, two warp groups of the streams per warp: fewer instructions per system).
+struct CompactSchedule { int chunk, stages, split, lanes = 16; };
+constexpr int kNumSchedules = 19;
 constexpr int kPartSchedule = 11;
 constexpr int kWindowFlag = 3;
 constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4, 3, 0}, {16, 2, 0},
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
                                                        {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2},
-                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3}};
+                                                       {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3},
+                                                       {8, 2, 3, 8}, {16, 2, 3, 8}, {8, 3, 3, 8}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -1529,6 +1531,11 @@ template <class T>
 __device__ __forceinline__ void warp_stage(T* dst, const T* src, int cnt) {
     const int lane = threadIdx.x & 31;
     for (int e = lane; e < cnt; e += 32) cp_async_bytes<T>(dst + e, src + e, (int)sizeof(T));
+}
+// the same by `stride` lanes of a warp, this thread being lane l0 of them
+template <class T>
+__device__ __forceinline__ void lanes_stage(T* dst, const T* src, int cnt, int l0, int stride) {
+    for (int e = l0; e < cnt; e += stride) cp_async_bytes<T>(dst + e, src + e, (int)sizeof(T));
 }
 
 // The solve: TF = factor type, IO as k_solve (IO_MIXED: TF = zf, data complex128 with accumulate).
@@ -1826,22 +1833,30 @@ k_solve_compact_multi(MultiSolve<TF> ms) {
 // go to a per-handle scratch in global memory ([warp group][kGroup][n], ix.scratch: the forward
 // result, then the solution before the border correction), which the Woodbury pass and the output
 // read back. The operations and their order are those of the compact solve: the same bits.
-template <class TF, class TD, int IO, int CH, int ST>
+template <class TF, class TD, int IO, int CH, int ST, int LP>
 __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const CompactData<TF>& cd,
                                                   const SolveIo& io0, const SolveIo& io2, int block) {
     extern __shared__ __align__(16) unsigned char sm[];
+    // LP lanes per system: 16 (a warp sweeps one warp group of the streams: two systems, or a shared
+    // pair), or 8 (two warp groups, four systems: a column's entries fill more of each FP64
+    // instruction's lanes; each half of the warp stages its own group's streams)
+    constexpr int NS = 32 / LP, NH = NS / kGroup, HL = 32 / NH;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int g = lane / kLanesPer, lg = lane % kLanesPer;
-    const int wg = ix.wg0 + block * nw + wib;
+    const int gq = lane / LP, lg = lane % LP;
+    const int half = gq / kGroup, g = gq % kGroup, hl = lane % HL;
+    const int wg0w = ix.wg0 + (block * nw + wib) * NH;
+    const int wg = wg0w + half;
+    const bool hlive = wg < ix.wgroups;          // this half's warp group is solved by this launch
+    const int wgc = hlive ? wg : wg0w;           // the streams a half without a group reads (unused)
     const int gs = ix.gs;
     const bool pair = gs == 1;
     const bool partner = pair && g == 1;
     const int gsel = pair ? 0 : g;
     const int sys = pair ? wg : wg * kGroup + g;
     const SolveIo& io = partner ? io2 : io0;
-    const bool live = sys < ix.batch && (!partner || io2.rhs != nullptr);
-    const bool wlive = wg < ix.wgroups;
+    const bool live = hlive && sys < ix.batch && (!partner || io2.rhs != nullptr);
+    const bool wlive = wg0w < ix.wgroups;
     const int n = ix.n, r = ix.r, M = ix.wmask, WS = ix.wmask + 1;
     // shared memory: index lists, then per warp the windows win[G][WS], the staging ring of the
     // factor streams (at least G x 64 entries: z and S of each half take it over after the sweeps),
@@ -1854,17 +1869,18 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
     const size_t ring = max(ST * (size_t)(ix.maxLc + ix.maxUc) * gs, (size_t)kGroup * 64);
-    // the second half's window 64 bytes further on: the halves touch the same rows in lockstep, and
-    // windows a power of two apart would put those rows in the same banks
-    constexpr int PAD = 64 / sizeof(TF);
-    const size_t per_warp = (size_t)kGroup * WS + PAD + ring +
-                            (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    // each system's window PAD bytes after the previous one: the systems touch the same rows in
+    // lockstep, and windows a power of two apart would put those rows in the same banks
+    constexpr int PAD = (LP == 16 ? 64 : 32) / sizeof(TF);
+    const size_t pivw = (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
+    const size_t wins = (size_t)NS * WS + (NS - 1) * PAD;
+    const size_t per_warp = wins + NH * ring + NH * pivw;
     TF* y0 = reinterpret_cast<TF*>(sm + off) + (size_t)wib * per_warp;
-    TF* win = y0 + (size_t)g * (WS + PAD);
-    TF* Lb = y0 + (size_t)kGroup * WS + PAD;
+    TF* win = y0 + (size_t)gq * (WS + PAD);
+    TF* Lb = y0 + wins + (size_t)half * ring;
     TF* Ub = Lb + ST * (size_t)ix.maxLc * gs;
-    TF* zb = Lb + (size_t)g * 64;
-    int* Pb = reinterpret_cast<int*>(Lb + ring);
+    TF* zb = y0 + wins + (size_t)gq * 64;
+    int* Pb = reinterpret_cast<int*>(y0 + wins + NH * ring + (size_t)half * pivw);
     for (int i = threadIdx.x; i <= n; i += blockDim.x) {
         s_offL[i] = ix.offL[i];
         s_offU[i] = ix.offU[i];
@@ -1874,7 +1890,13 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     for (int i = threadIdx.x; i < ix.nU; i += blockDim.x) s_Udist[i] = ix.Udist[i];
     __syncthreads();
     if (!wlive) return;
-    TF* scr = static_cast<TF*>(ix.scratch) + ((size_t)wg * kGroup + g) * n;
+    TF* scr = static_cast<TF*>(ix.scratch) + ((size_t)wgc * kGroup + g) * n;
+    // the scratch of a half without a group is neither read nor written
+    auto sget = [&](int i) -> TF { return hlive ? scr[i] : TF(0.0); };
+    auto sput = [&](int i, TF v) {
+        if (hlive) scr[i] = v;
+    };
+
     // row i (solver order) of this half's right-hand side
     auto rhs_row = [&](int i) -> TF {
         TF v = TF(0.0);
@@ -1889,31 +1911,33 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
         }
         return v;
     };
-    const TF* Lg = cd.L + (size_t)wg * ix.nL * gs;
-    const TF* Ug = cd.U + (size_t)wg * (ix.nU) * gs;
-    const int* Pg = cd.piv + (size_t)wg * n * gs;
+    const TF* Lg = cd.L + (size_t)wgc * ix.nL * gs;
+    const TF* Ug = cd.U + (size_t)wgc * (ix.nU) * gs;
+    const int* Pg = cd.piv + (size_t)wgc * n * gs;
+    constexpr int PF = (CH + LP - 1) / LP;        // rows a chunk brings in, per lane
     // ---------------- forward: L with the row interchanges (rows [0, hi) have entered the window)
     if (ix.kl > 0 && n > 1) {
         const int nch = (n - 1 + CH - 1) / CH;
         int hi = min(n, min(CH, n - 1) + ix.kl);
-        for (int i = lg; i < hi; i += kLanesPer) win[i & M] = rhs_row(i);
+        for (int i = lg; i < hi; i += LP) win[i & M] = rhs_row(i);
         auto issue = [&](int c) {
             if (c < nch) {
                 const int buf = c % ST;
                 const int j0 = c * CH, j1 = min(j0 + CH, n - 1);
-                warp_stage(Lb + (size_t)buf * ix.maxLc * gs, Lg + (size_t)s_offL[j0] * gs,
-                           (s_offL[j1] - s_offL[j0]) * gs);
-                warp_stage(Pb + (size_t)buf * CH * gs, Pg + (size_t)j0 * gs, (j1 - j0) * gs);
+                lanes_stage(Lb + (size_t)buf * ix.maxLc * gs, Lg + (size_t)s_offL[j0] * gs,
+                            (s_offL[j1] - s_offL[j0]) * gs, hl, HL);
+                lanes_stage(Pb + (size_t)buf * CH * gs, Pg + (size_t)j0 * gs, (j1 - j0) * gs, hl, HL);
             }
             cp_async_commit();
         };
         for (int c = 0; c < ST - 1; ++c) issue(c);
         for (int c = 0; c < nch; ++c) {
             issue(c + ST - 1);
-            // the rows chunk c + 1 brings in (at most CH: one per lane), loaded while c is swept
+            // the rows chunk c + 1 brings in (at most CH), loaded while c is swept
             const int hin = (c + 1 < nch) ? min(n, min((c + 2) * CH, n - 1) + ix.kl) : hi;
-            TF pf = TF(0.0);
-            if (hi + lg < hin) pf = rhs_row(hi + lg);
+            TF pf[PF];
+#pragma unroll
+            for (int u = 0; u < PF; ++u) pf[u] = hi + lg + u * LP < hin ? rhs_row(hi + lg + u * LP) : TF(0.0);
             cp_async_wait<ST - 1>();
             __syncwarp();
             const TF* Lc = Lb + (size_t)(c % ST) * ix.maxLc * gs;
@@ -1931,7 +1955,7 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
                 const int e0 = e1;
                 e1 = s_offL[j + 1];
                 __syncwarp();
-                for (int e = e0 + lg; e < e1; e += kLanesPer) {
+                for (int e = e0 + lg; e < e1; e += LP) {
                     const int i = j + 1 + s_Lrow[e];
                     const TF v = (i == l) ? yj0 : win[i & M];
                     win[i & M] = cfms(v, Lc[(e - base) * gs + gsel], bj);
@@ -1944,27 +1968,29 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
             }
             // rows j0 .. j1 - 1 are final: out to the scratch, then chunk c + 1's rows in (rows
             // j1 .. hin - 1 span at most CH + kl < WS slots)
-            for (int i = j0 + lg; i < j1; i += kLanesPer) scr[i] = win[i & M];
+            for (int i = j0 + lg; i < j1; i += LP) sput(i, win[i & M]);
             __syncwarp();
-            if (hi + lg < hin) win[(hi + lg) & M] = pf;
+#pragma unroll
+            for (int u = 0; u < PF; ++u)
+                if (hi + lg + u * LP < hin) win[(hi + lg + u * LP) & M] = pf[u];
             hi = hin;
         }
         __syncwarp();
-        if (lg == 0) scr[n - 1] = win[(n - 1) & M];      // the last row has no column of its own
+        if (lg == 0) sput(n - 1, win[(n - 1) & M]);      // the last row has no column of its own
     } else {
-        for (int i = lg; i < n; i += kLanesPer) scr[i] = rhs_row(i);
+        for (int i = lg; i < n; i += LP) sput(i, rhs_row(i));
     }
     __syncwarp();
     // ---------------- backward: U (diagonal holds -1/u_jj); rows [lo, n) have entered the window
     {
         const int nch = (n + CH - 1) / CH;
         int lo = max(0, n - min(CH, n) - ix.kv);
-        for (int i = lo + lg; i < n; i += kLanesPer) win[i & M] = scr[i];
+        for (int i = lo + lg; i < n; i += LP) win[i & M] = sget(i);
         auto issue = [&](int c) {
             if (c < nch) {
                 const int s0 = c * CH, s1 = min(s0 + CH, n);
-                warp_stage(Ub + (size_t)(c % ST) * ix.maxUc * gs, Ug + (size_t)s_offU[s0] * gs,
-                           (s_offU[s1] - s_offU[s0]) * gs);
+                lanes_stage(Ub + (size_t)(c % ST) * ix.maxUc * gs, Ug + (size_t)s_offU[s0] * gs,
+                            (s_offU[s1] - s_offU[s0]) * gs, hl, HL);
             }
             cp_async_commit();
         };
@@ -1972,8 +1998,9 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
         for (int c = 0; c < nch; ++c) {
             issue(c + ST - 1);
             const int lon = (c + 1 < nch) ? max(0, n - min((c + 2) * CH, n) - ix.kv) : lo;
-            TF pf = TF(0.0);
-            if (lon + lg < lo) pf = scr[lon + lg];
+            TF pf[PF];
+#pragma unroll
+            for (int u = 0; u < PF; ++u) pf[u] = lon + lg + u * LP < lo ? sget(lon + lg + u * LP) : TF(0.0);
             cp_async_wait<ST - 1>();
             __syncwarp();
             const TF* Uc = Ub + (size_t)(c % ST) * ix.maxUc * gs;
@@ -1989,7 +2016,7 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
                 e1 = s_offU[s + 1];
                 const TF yj = win[j & M];
                 __syncwarp();
-                for (int e = e0 + lg; e < e1; e += kLanesPer) {
+                for (int e = e0 + lg; e < e1; e += LP) {
                     const int i = j - s_Udist[e];
                     win[i & M] = cfms(e == e0 ? TF(0.0) : win[i & M], Uc[(e - base) * gs + gsel], yj);
                 }
@@ -1997,9 +2024,11 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
             }
             // rows n - s1 .. n - s0 - 1 are final (before the border correction): out to the
             // scratch over their forward values (read when they entered), then chunk c + 1's rows
-            for (int i = n - s1 + lg; i < n - s0; i += kLanesPer) scr[i] = win[i & M];
+            for (int i = n - s1 + lg; i < n - s0; i += LP) sput(i, win[i & M]);
             __syncwarp();
-            if (lon + lg < lo) win[(lon + lg) & M] = pf;
+#pragma unroll
+            for (int u = 0; u < PF; ++u)
+                if (lon + lg + u * LP < lo) win[(lon + lg + u * LP) & M] = pf[u];
             lo = lon;
         }
     }
@@ -2011,28 +2040,44 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
         const bool staged = r + r * r <= 64 && r <= kMaxRUnroll;
         TF* sl = zb + r;
         if (staged && live)
-            for (int q = lg; q < r * r; q += kLanesPer) sl[q] = cd.slu[(size_t)sys * r * r + q];
-        const TF* Vg = cd.V + (size_t)wg * ix.nV * gs;
+            for (int q = lg; q < r * r; q += LP) sl[q] = cd.slu[(size_t)sys * r * r + q];
+        const TF* Vg = cd.V + (size_t)wgc * ix.nV * gs;
         for (int a = 0; a < r; ++a) {
             TF acc = TF(0.0);
             const int ea = ix.offV[a], eb = ix.offV[a + 1];
-            for (int e0 = ea + lg; e0 < eb; e0 += kU * kLanesPer) {
-                int c[kU];
-                TF v[kU];
+            if constexpr (LP == kLanesPer) {
+                for (int e0 = ea + lg; e0 < eb; e0 += kU * kLanesPer) {
+                    int c[kU];
+                    TF v[kU];
 #pragma unroll
-                for (int u = 0; u < kU; ++u) {
-                    const int e = e0 + u * kLanesPer;
-                    c[u] = e < eb ? ix.Vcol[e] : -1;
-                    v[u] = e < eb ? Vg[(size_t)e * gs + gsel] : TF(0.0);
+                    for (int u = 0; u < kU; ++u) {
+                        const int e = e0 + u * kLanesPer;
+                        c[u] = e < eb ? ix.Vcol[e] : -1;
+                        v[u] = e < eb ? Vg[(size_t)e * gs + gsel] : TF(0.0);
+                    }
+                    TF yc[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; ++u) yc[u] = c[u] >= 0 ? sget(c[u]) : TF(0.0);
+#pragma unroll
+                    for (int u = 0; u < kU; ++u)
+                        if (c[u] >= 0) acc = cfma(acc, v[u], yc[u]);
                 }
-                TF yc[kU];
-#pragma unroll
-                for (int u = 0; u < kU; ++u) yc[u] = c[u] >= 0 ? scr[c[u]] : TF(0.0);
-#pragma unroll
-                for (int u = 0; u < kU; ++u)
-                    if (c[u] >= 0) acc = cfma(acc, v[u], yc[u]);
+            } else {
+                // each lane sums the entries of two of the 16-lane solve's lanes (lg and lg + 8) and
+                // adds the two sums as that solve's first reduction level does: the same bits
+                TF a0 = TF(0.0), a1 = TF(0.0);
+                for (int e0 = ea + lg; e0 < eb; e0 += kLanesPer) {
+                    const int e1 = e0 + LP;
+                    const int c0 = ix.Vcol[e0], c1 = e1 < eb ? ix.Vcol[e1] : -1;
+                    const TF v0 = Vg[(size_t)e0 * gs + gsel];
+                    const TF v1 = c1 >= 0 ? Vg[(size_t)e1 * gs + gsel] : TF(0.0);
+                    const TF y0v = sget(c0), y1v = c1 >= 0 ? sget(c1) : TF(0.0);
+                    a0 = cfma(a0, v0, y0v);
+                    if (c1 >= 0) a1 = cfma(a1, v1, y1v);
+                }
+                acc = a0 + a1;
             }
-            for (int m = kLanesPer / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
+            for (int m = LP / 2; m > 0; m >>= 1) acc = acc + shfl_xor(acc, m);
             if (lg == 0) zb[a] = acc;
         }
         __syncwarp();
@@ -2067,14 +2112,14 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
         zd* xs = static_cast<zd*>(io.x) + (size_t)sys * n;
         zd* xt = static_cast<zd*>(io.xT);
         const size_t nb = (size_t)ix.batch;
-        for (int i = lg; i < n; i += kLanesPer) {
+        for (int i = lg; i < n; i += LP) {
             const TF f = fin(i);
             const zd v = io.accumulate ? xs[i] + zd(f.re, f.im) : zd(f.re, f.im);
             xs[i] = v;
             if (xt) xt[(size_t)i * nb + sys] = v;
         }
     } else {
-        for (int i = lg; i < n; i += kLanesPer) io_store<TF, IO>(io, sys, n, i, fin(i));
+        for (int i = lg; i < n; i += LP) io_store<TF, IO>(io, sys, n, i, fin(i));
     }
 }
 
@@ -2083,12 +2128,12 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
 // blocks keeps it at 48 registers: 3.05 ms against 3.20 with 16)
 template <class TF>
 constexpr int window_max_warps() { return sizeof(TF) == 8 ? 16 : 8; }
-template <class TF, class TD, int IO, int CH, int ST>
+template <class TF, class TD, int IO, int CH, int ST, int LP>
 __global__ void __launch_bounds__(32 * window_max_warps<TF>())
 k_solve_window_multi(MultiSolve<TF> ms) {
     int b = 0;
     while (b + 1 < ms.nb && (int)blockIdx.x >= ms.block_start[b + 1]) ++b;
-    solve_window_body<TF, TD, IO, CH, ST>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
+    solve_window_body<TF, TD, IO, CH, ST, LP>(ms.ix[b], ms.cd[b], ms.io[b], ms.io2[b], blockIdx.x - ms.block_start[b]);
 }
 
 // ---- one system per warp, lanes split over (entry, real/imaginary part) -------------------------
@@ -2884,11 +2929,14 @@ static size_t compact_smem(const Banded& h, int nwarps, int sched = 0) {
     off = (off + 15) & ~(size_t)15;
     const size_t ring = (size_t)sc.stages * (size_t)(h.cMaxLk[k] + h.cMaxUk[k]) * h.cG;
     const size_t pivots = ((size_t)sc.stages * sc.chunk * h.cG * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
-    // the windowed schedules: a window of each vector, z and S in the ring after the sweeps
-    if (sc.split == kWindowFlag)
+    // the windowed schedules: a window of each vector, z and S in the ring after the sweeps; with
+    // 8 lanes per system four windows and two warp groups' rings
+    if (sc.split == kWindowFlag) {
+        const size_t ns = 32 / sc.lanes, nh = ns / kGroup, pad = (sc.lanes == 16 ? 64 : 32) / sizeof(TF);
         return off + sizeof(TF) * nwarps *
-                         ((size_t)kGroup * window_slots(h, sc.chunk) + 64 / sizeof(TF) +
-                          std::max(ring, (size_t)kGroup * 64) + pivots);
+                         (ns * window_slots(h, sc.chunk) + (ns - 1) * pad +
+                          nh * (std::max(ring, (size_t)kGroup * 64) + pivots));
+    }
     const size_t per_warp = (size_t)kGroup * (h.n + 64) + ring + pivots;
     return off + sizeof(TF) * per_warp * nwarps;
 }
@@ -3043,13 +3091,15 @@ static void group_range(const Banded& h, int s0, int s1, int& first, int& end) {
     end = std::min(h.cWg, (s1 + h.cG - 1) / h.cG);
 }
 
-template <class TF, class TD, int IO, int CH, int ST, bool WIN = false>
+template <class TF, class TD, int IO, int CH, int ST, bool WIN = false, int LP = kLanesPer>
 static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vector<CompactData<TF>>& cds,
                            const std::vector<SolveIo>& ios, const std::vector<SolveIo>& ios2,
                            const std::vector<int>& rng, int sched, cudaStream_t st) {
-    // the two-systems sweeps, over whole vectors or (WIN) windows of them
+    // the two-systems sweeps, over whole vectors or (WIN) windows of them, LP lanes per system
+    // (8: a warp sweeps two warp groups)
+    constexpr int NH = 32 / LP / kGroup;
     auto kern = [] {
-        if constexpr (WIN) return k_solve_window_multi<TF, TD, IO, CH, ST>;
+        if constexpr (WIN) return k_solve_window_multi<TF, TD, IO, CH, ST, LP>;
         else return k_solve_compact_multi<TF, TD, IO, CH, ST>;
     }();
     if (WIN)
@@ -3068,10 +3118,10 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         return m;
     };
     std::vector<int> first(hs.size()), end(hs.size());
-    int total = 0;
+    int total = 0;                                   // warps
     for (size_t i = 0; i < hs.size(); ++i) {
         group_range(*hs[i], rng[2 * i], rng[2 * i + 1], first[i], end[i]);
-        total += end[i] - first[i];
+        total += ceil_div(end[i] - first[i], NH);
     }
     int nw = 1, resident = 0;
     for (int w = 1; w <= (WIN ? window_max_warps<TF>() : 8); ++w) {
@@ -3102,7 +3152,7 @@ static void launch_multi_t(const std::vector<const Banded*>& hs, const std::vect
         ms.cd[k] = cds[i];
         ms.io[k] = ios[i];
         ms.io2[k] = ios2[i];
-        blocks += ceil_div(end[i] - first[i], nw);
+        blocks += ceil_div(ceil_div(end[i] - first[i], NH), nw);
     }
     ms.block_start[ms.nb] = blocks;
     kern<<<blocks, 32 * nw, smem, st>>>(ms);
@@ -3205,6 +3255,9 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 13: launch_multi_t<TF, TD, IO, 4, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 14: launch_multi_t<TF, TD, IO, 16, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 15: launch_multi_t<TF, TD, IO, 8, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 16: launch_multi_t<TF, TD, IO, 8, 2, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 17: launch_multi_t<TF, TD, IO, 16, 2, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 18: launch_multi_t<TF, TD, IO, 8, 3, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
 }
