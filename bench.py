@@ -157,8 +157,8 @@ def step_bytes(dev, solver):
 TRAFFIC_PER_SYSTEM = {
     ("channel", "fp64", "k_solve_compact_multi"): ((174.600192 + 3.016192) * 1e6 / 1985,
                                                    "profiles/k_solve_compact_multi_channel64x129x64_fp64.md"),
-    ("channel", "fp64", "k_solve_window_multi"): ((178.431232 + 16.321792) * 1e6 / 1985,
-                                                  "profiles/k_solve_window_multi_channel64x129x64_fp64.md"),
+    ("channel", "fp64", "k_solve_window_multi"): ((177.924352 + 15.470848) * 1e6 / 1985,
+                                                  "profiles/k_solve_window_multi_lanes8_channel64x129x64_fp64.md"),
     # the FP32 form solves in two groups: the captured launch is the group of 1024 paired systems
     ("channel", "fp32", "k_solve_compact_multi"): ((47.700736 + 0.423936) * 1e6 / 1024,
                                                    "profiles/k_solve_compact_multi_channel64x129x64_fp32.md"),
