@@ -34,21 +34,29 @@ def test_windowed_solves_give_the_compact_bits(tname, sizes, precision, rng, cud
         big = dev.shared[big]
     hi = min(dev.nsys[big], 6)
     fp32 = 1 if precision == "fp32" else 0
-    ref, ref_r = dev.zeros(), dev.zeros()
+    # system ranges: several warp groups, and a single one (with 8 lanes per system a warp sweeps
+    # two groups: the second half of its warp then has none)
+    ranges = [(big, 2 if hi > 2 else 0, hi), (big, 2 if hi > 4 else 0, 4 if hi > 4 else hi)]
+    ref = dev.zeros()
+    ref_r = [dev.zeros() for _ in ranges]
     autotune.apply(fs, 0)
     dev.solve(a, b, rhs, ref)
-    dev._batch_call(fs, [(big, 2 if hi > 2 else 0, hi)], rhs, ref_r, None, fp32, 0, 0)
+    for rg, o in zip(ranges, ref_r):
+        dev._batch_call(fs, [rg], rhs, o, None, fp32, 0, 0)
     torch.cuda.synchronize()
     wins = sorted(autotune.windowed_schedules())
     assert wins
     for s in wins:
-        out, out_r = dev.zeros(), dev.zeros()
+        out = dev.zeros()
         autotune.apply(fs, s)
         dev.solve(a, b, rhs, out)
-        dev._batch_call(fs, [(big, 2 if hi > 2 else 0, hi)], rhs, out_r, None, fp32, 0, 0)
         torch.cuda.synchronize()
         assert torch.equal(out, ref), s
-        assert torch.equal(out_r, ref_r), s
+        for rg, o_ref in zip(ranges, ref_r):
+            o = dev.zeros()
+            dev._batch_call(fs, [rg], rhs, o, None, fp32, 0, 0)
+            torch.cuda.synchronize()
+            assert torch.equal(o, o_ref), (s, rg)
 
 
 @pytest.mark.parametrize("config,fourier,precision", [("rayleigh_benard", None, "fp64"),
