@@ -151,8 +151,8 @@ int cng_banded_solve_batch2(int nh, cng_banded* const* h, const void* const* b, 
  * runs one system per warp with the lanes split over entries and real/imaginary parts (split = 1:
  * the latency variant for small batches; split = 2: the partitioned solve of small FP64 batches,
  * one block of warps per system sweeping its blocks of 32 columns at once; split = 3: the windowed
- * two-systems sweeps, a window of each vector in shared memory and the rest in a scratch, the
- * same bits as schedule 0; else two systems per warp). Any output may be NULL. No
+ * sweeps of two or four systems per warp, a window of each vector in shared memory and the rest in
+ * a scratch, the same bits as schedule 0; else two systems per warp). Any output may be NULL. No
  * reference counterpart: the reference picks its solve kernel (level-scheduled streams or the band
  * kernel) by constructor flags (python/conatus/runtime/cuda.py:140-152); here the choice is timed
  * (conatus_gb300.autotune). */
