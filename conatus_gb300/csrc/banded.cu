@@ -1480,7 +1480,7 @@ constexpr CompactSchedule kSchedules[kNumSchedules] = {{8, 2, 0}, {8, 3, 0}, {4,
                                                        {16, 3, 0}, {4, 4, 0}, {2, 4, 0}, {16, 4, 0},
                                                        {8, 2, 1}, {16, 2, 1}, {4, 3, 1}, {8, 2, 2},
                                                        {8, 2, 3}, {4, 3, 3}, {16, 2, 3}, {8, 3, 3},
-                                                       {8, 2, 3, 8}, {16, 2, 3, 8}, {8, 3, 3, 8}};
+                                                       {8, 2, 3, 8}, {4, 3, 3, 8}, {8, 3, 3, 8}};
 constexpr int kChunkSizes[4] = {2, 4, 8, 16};
 __host__ __device__ constexpr int chunk_index(int ch) { return ch == 2 ? 0 : (ch == 4 ? 1 : (ch == 8 ? 2 : 3)); }
 
@@ -3256,7 +3256,7 @@ static void launch_multi(const std::vector<const Banded*>& hs, const std::vector
         case 14: launch_multi_t<TF, TD, IO, 16, 2, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 15: launch_multi_t<TF, TD, IO, 8, 3, true>(hs, cds, ios, ios2, rng, sched, st); break;
         case 16: launch_multi_t<TF, TD, IO, 8, 2, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
-        case 17: launch_multi_t<TF, TD, IO, 16, 2, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
+        case 17: launch_multi_t<TF, TD, IO, 4, 3, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
         case 18: launch_multi_t<TF, TD, IO, 8, 3, true, 8>(hs, cds, ios, ios2, rng, sched, st); break;
         default: launch_multi_t<TF, TD, IO, 8, 2>(hs, cds, ios, ios2, rng, sched, st); break;
     }
