@@ -563,15 +563,18 @@ struct BucketArgs {
     BucketDev b;
     const void* in;
     void* out;
+    int split = 1;          // warps per system (unpack: over the y-groups; pack: over the rows)
 };
 
 template <class R>
 __device__ __forceinline__ void unpack_body(unsigned bid, const RhsDev& d, const BucketDev& b,
-                                            const double2* __restrict__ state, c2<R>* __restrict__ S) {
+                                            const double2* __restrict__ state, c2<R>* __restrict__ S,
+                                            int split) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
-    const int m = bid * nw + wib;
+    const int q = bid * nw + wib;
+    const int m = q / split, part = q - m * split;      // system, and its y-groups part, part + split, ...
     if (m >= b.nsys) return;
     const int Ny = d.Ny;
     // the system's state, rounded once to the transform precision R
@@ -591,7 +594,7 @@ __device__ __forceinline__ void unpack_body(unsigned bid, const RhsDev& d, const
     const double w = b.dact == 0 ? 1.0 : (b.dact == 1 ? 0.5 : 0.25);
     const int slot = zslot(jz, b.sign, d.Nzc);
     const int cbase = (b.case_of ? b.case_of[m] : 0) * d.ngy;
-    for (int gy = 0; gy < d.ngy; ++gy) {
+    for (int gy = part; gy < d.ngy; gy += split) {
         const int f = d.yg_rep[gy];
         const int* fd = d.factors + 5 * f;
         const int oy = fd[3];
@@ -651,7 +654,8 @@ template <class R>
 __global__ void k_unpack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
     const int k = g.find(blockIdx.x);
     const BucketArgs<R>& a = g.a[k];
-    unpack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const double2*>(a.in), static_cast<c2<R>*>(a.out));
+    unpack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const double2*>(a.in), static_cast<c2<R>*>(a.out),
+                   a.split);
 }
 
 // products on the grid: out_o = sum_m c_m prod_j G_j. The monomial tables are staged in shared
@@ -792,12 +796,14 @@ __global__ void k_products_grp(const __grid_constant__ Grp<ProductArgs<R>> g) {
 // one warp per system: output spectra -> rows (C^(lambda) conversion, 2^d_act, real buckets real)
 template <class R>
 __device__ __forceinline__ void pack_body(unsigned bid, const RhsDev& d, const BucketDev& b,
-                                          const c2<R>* __restrict__ H, double2* __restrict__ rows) {
+                                          const c2<R>* __restrict__ H, double2* __restrict__ rows, int split) {
     // the system's output spectra are staged in shared memory (coalesced), then gathered by row
+    // (split warps per system: each stages the spectra and takes every split-th run of 32 rows)
     extern __shared__ __align__(16) unsigned char sm[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
-    const int m = bid * nw + wib;
+    const int q = bid * nw + wib;
+    const int m = q / split, part = q - m * split;
     if (m >= b.nsys) return;
     const int Ny = d.Ny;
     const int jx = b.modes[2 * m], jz = b.modes[2 * m + 1];
@@ -820,7 +826,7 @@ __device__ __forceinline__ void pack_body(unsigned bid, const RhsDev& d, const B
     }
     __syncwarp();
 #pragma unroll 2
-    for (int i = lane; i < b.n; i += 32) {
+    for (int i = 32 * part + lane; i < b.n; i += 32 * split) {
         const int o = b.rowmap[2 * i], nn = b.rowmap[2 * i + 1];
         double2 v = make_double2(0.0, 0.0);
         if (o >= 0) {
@@ -854,7 +860,8 @@ template <class R>
 __global__ void k_pack_grp(const __grid_constant__ Grp<BucketArgs<R>> g) {
     const int k = g.find(blockIdx.x);
     const BucketArgs<R>& a = g.a[k];
-    pack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const c2<R>*>(a.in), static_cast<double2*>(a.out));
+    pack_body<R>(blockIdx.x - g.start[k], a.d, a.b, static_cast<const c2<R>*>(a.in), static_cast<double2*>(a.out),
+                 a.split);
 }
 
 // constant part of F: rows[idx] += value
@@ -1075,15 +1082,27 @@ struct Rhs {
 // system; buckets of different lengths run side by side instead of one after the other).
 constexpr int kBucketWarps = 4;
 
+// warps per system of unpack and pack: one where the systems fill the SMs, else up to `most` (a
+// small problem's few systems: RB 256x64 has 129, Burgers one)
+static int bucket_split(Rhs* const* hs, int n, int most) {
+    long long systems = 0;
+    for (int i = 0; i < n; ++i)
+        for (const auto& b : hs[i]->buckets) systems += b.nsys;
+    return systems < 2LL * sm_count() * kBucketWarps ? most : 1;
+}
+
 template <class R>
 static void launch_unpack(Rhs* const* hs, int n, const double2* state, cudaStream_t st) {
     std::vector<BucketArgs<R>> args;
     std::vector<unsigned> blocks;
     size_t smem = 0;
+    int ngy = 1;
+    for (int i = 0; i < n; ++i) ngy = std::max(ngy, hs[i]->dev.ngy);
+    const int split = bucket_split(hs, n, std::min(ngy, 8));
     for (int i = 0; i < n; ++i)
         for (const auto& b : hs[i]->buckets) {
-            args.push_back(BucketArgs<R>{hs[i]->dev, b, state, hs[i]->S});
-            blocks.push_back((unsigned)ceil_div(b.nsys, kBucketWarps));
+            args.push_back(BucketArgs<R>{hs[i]->dev, b, state, hs[i]->S, split});
+            blocks.push_back((unsigned)ceil_div(b.nsys * split, kBucketWarps));
             if (b.nsys) smem = std::max(smem, (size_t)kBucketWarps * (b.n + 2 * hs[i]->ny) * sizeof(c2<R>));
         }
     ensure_smem_attr((const void*)k_unpack_grp<R>, 200 * 1024);
@@ -1098,10 +1117,11 @@ static void launch_pack(Rhs* const* hs, int n, double2* rows, cudaStream_t st) {
     std::vector<BucketArgs<R>> args;
     std::vector<unsigned> blocks;
     size_t smem = 0;
+    const int split = bucket_split(hs, n, 4);
     for (int i = 0; i < n; ++i)
         for (const auto& b : hs[i]->buckets) {
-            args.push_back(BucketArgs<R>{hs[i]->dev, b, hs[i]->S, rows});
-            blocks.push_back((unsigned)ceil_div(b.nsys, kBucketWarps));
+            args.push_back(BucketArgs<R>{hs[i]->dev, b, hs[i]->S, rows, split});
+            blocks.push_back((unsigned)ceil_div(b.nsys * split, kBucketWarps));
             if (b.nsys) smem = std::max(smem, (size_t)kBucketWarps * hs[i]->noutputs * hs[i]->ny * sizeof(double2));
         }
     ensure_smem_attr((const void*)k_pack_grp<R>, 200 * 1024);
