@@ -1858,9 +1858,9 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     const bool live = hlive && sys < ix.batch && (!partner || io2.rhs != nullptr);
     const bool wlive = wg0w < ix.wgroups;
     const int n = ix.n, r = ix.r, M = ix.wmask, WS = ix.wmask + 1;
-    // shared memory: index lists, then per warp the windows win[G][WS], the staging ring of the
-    // factor streams (at least G x 64 entries: z and S of each half take it over after the sweeps),
-    // and the pivots' ring
+    // shared memory: index lists, then per warp the NS windows of WS rows, the staging rings of the
+    // factor streams (one per warp group, at least kGroup x 64 entries each: z and S of every system
+    // take them over after the sweeps), and the pivots' rings
     int* s_offL = reinterpret_cast<int*>(sm);
     int* s_offU = s_offL + (n + 1);
     unsigned* s_Lmask = reinterpret_cast<unsigned*>(s_offU + (n + 1));
@@ -1869,8 +1869,9 @@ __device__ __forceinline__ void solve_window_body(const CompactIdx& ix, const Co
     size_t off = (size_t)(n + 1) * 8 + (size_t)n * 4 + ix.nL + ix.nU;
     off = (off + 15) & ~(size_t)15;
     const size_t ring = max(ST * (size_t)(ix.maxLc + ix.maxUc) * gs, (size_t)kGroup * 64);
-    // each system's window PAD bytes after the previous one: the systems touch the same rows in
-    // lockstep, and windows a power of two apart would put those rows in the same banks
+    // each system's window 64 (16 lanes) or 32 (8 lanes) bytes after the previous one (PAD
+    // elements): the systems touch the same rows in lockstep, and windows a power of two apart
+    // would put those rows in the same banks
     constexpr int PAD = (LP == 16 ? 64 : 32) / sizeof(TF);
     const size_t pivw = (ST * (size_t)CH * gs * sizeof(int) + sizeof(TF) - 1) / sizeof(TF);
     const size_t wins = (size_t)NS * WS + (NS - 1) * PAD;
